@@ -1,0 +1,138 @@
+/*
+ * ttals.h -- C ABI of the GB300 (sm_103a) tensor-train ALS engine.
+ *
+ * The engine is a drop-in for scikit_tt's ALS hot path.  Each entry point
+ * names the reference function it replaces (paths are relative to the
+ * scikit_tt project root).  All functions return an int status (TTALS_OK on
+ * success); ttals_last_error() gives a one-line message for the last failure
+ * on a context.  No torch or CUDA types appear in the signatures: tensors are
+ * plain double pointers, either host memory (copied to/from the device inside
+ * the call) or device memory (on_device = 1).
+ *
+ * A tensor train is described by ttals_tt: `order` cores, core i of shape
+ * (ranks[i], row_dims[i], col_dims[i], ranks[i+1]) in C order, all cores
+ * concatenated in `data` (the layout of scikit_tt/tensor_train.py:184-188).
+ */
+#ifndef TTALS_H_
+#define TTALS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define TTALS_OK 0
+#define TTALS_ERR_ARG 1         /* malformed shapes / arguments (ValueError)   */
+#define TTALS_ERR_CUDA 2        /* CUDA runtime failure                         */
+#define TTALS_ERR_NOMEM 3       /* device memory budget exceeded                */
+#define TTALS_ERR_SINGULAR 4    /* local system singular / Krylov breakdown     */
+#define TTALS_ERR_NONFINITE 5   /* NaN/Inf met in a local solve                 */
+#define TTALS_ERR_TIMEOUT 6     /* a device-side wait gave up                   */
+#define TTALS_ERR_NOCONV 7      /* local solve missed its tolerance             */
+#define TTALS_ERR_UNSUPPORTED 8 /* feature outside the implemented path         */
+
+/* arithmetic of the local solves */
+#define TTALS_PREC_FP64 0  /* plain FP64 everywhere                                   */
+#define TTALS_PREC_MIXED 1 /* FP32 Krylov inner solves + FP64 refinement residual     */
+
+/* sle.als `solver` argument (scikit_tt/solvers/sle.py:505-509) */
+#define TTALS_SLE_SOLVE 0
+#define TTALS_SLE_LU 1
+
+/* evp.als `solver` argument (scikit_tt/solvers/evp.py:417-439) */
+#define TTALS_EVP_EIG 0
+#define TTALS_EVP_EIGS 1
+#define TTALS_EVP_EIGH 2
+
+typedef struct ttals_ctx ttals_ctx;
+
+typedef struct {
+  int32_t order;
+  const int64_t* row_dims; /* [order]     */
+  const int64_t* col_dims; /* [order]     */
+  const int64_t* ranks;    /* [order + 1] */
+  const double* data;      /* concatenated cores */
+  int32_t on_device;       /* 0: host pointer, 1: device pointer */
+} ttals_tt;
+
+typedef struct {
+  int64_t local_solves;       /* micro systems solved                          */
+  int64_t krylov_iterations;  /* inner Krylov iterations, all local solves     */
+  int64_t refinement_steps;   /* FP64 residual evaluations, all local solves   */
+  double max_local_residual;  /* worst final relative residual of a local solve */
+  double device_ms;           /* device time of the call (CUDA events)         */
+} ttals_stats;
+
+/* Context: one device, one stream, one device-memory arena capped at
+ * budget_bytes (0 = 90% of free memory).  No reference counterpart: the
+ * reference is single-process NumPy (scikit_tt/solvers/sle.py:10). */
+int ttals_create(ttals_ctx** ctx, int device, size_t budget_bytes);
+int ttals_destroy(ttals_ctx* ctx);
+const char* ttals_last_error(const ttals_ctx* ctx);
+/* Run on a caller-provided cudaStream_t (passed as void*); NULL restores the
+ * context's own stream. */
+int ttals_set_stream(ttals_ctx* ctx, void* stream);
+
+/* Rank schedule of one ALS run: the ranks of the returned solution for
+ * dims/x_ranks, following the economic QR/RQ rank rule of
+ * scikit_tt/solvers/sle.py:517-541 (identical for evp.py:452-487 when
+ * number_ev == 1).  Host-only, no device work. */
+int ttals_als_ranks(int32_t order, const int64_t* dims, const int64_t* x_ranks, int64_t* out_ranks);
+
+/* scikit_tt/solvers/sle.py:10 `als(operator, initial_guess, right_hand_side,
+ * repeats, solver)`.  out_data receives the solution cores (ranks from
+ * ttals_als_ranks, written to out_ranks).  tol is the relative residual each
+ * local system is solved to (<= 0 selects 1e-13 for FP64, 1e-10 for MIXED). */
+int ttals_sle_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const ttals_tt* rhs,
+                  int32_t repeats, int32_t solver, int32_t precision, double tol,
+                  double* out_data, int32_t out_on_device, int64_t* out_ranks, ttals_stats* stats);
+
+/* scikit_tt/solvers/evp.py:17 `als(operator, initial_guess, previous, shift,
+ * operator_gevp=None, number_ev, repeats, conv_eps, solver, sigma, real)` for
+ * symmetric operators.  out_vals[number_ev]; out_data as for ttals_sle_als
+ * (for number_ev > 1 core 0 carries a trailing axis of length number_ev, the
+ * 5-D core of evp.py:492-493).  *iterations as evp.py:177. */
+int ttals_evp_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, int32_t n_previous,
+                  const ttals_tt* previous, double shift, int32_t number_ev, int32_t repeats,
+                  double conv_eps, int32_t solver, double sigma, int32_t precision, double tol,
+                  double* out_vals, double* out_data, int32_t out_on_device, int64_t* out_ranks,
+                  int32_t* iterations, ttals_stats* stats);
+
+/* scikit_tt/tensor_train.py:422-501 (`__matmul__` / `dot`): core-wise
+ * product of two trains; out has ranks a.ranks[i] * b.ranks[i]. */
+int ttals_tt_matmul(ttals_ctx* ctx, const ttals_tt* a, const ttals_tt* b, double* out_data,
+                    int32_t out_on_device);
+
+/* scikit_tt/tensor_train.py:1092-1310 (`ortho_left` / `ortho_right` without
+ * truncation): Householder QR (left, direction 0) or RQ (right, direction 1)
+ * sweep over cores [first, last]; out_ranks receives the new ranks. */
+int ttals_tt_ortho(ttals_ctx* ctx, const ttals_tt* t, int32_t direction, int32_t first, int32_t last,
+                   double* out_data, int32_t out_on_device, int64_t* out_ranks);
+
+/* scikit_tt/tensor_train.py:1334-1430 (`norm(p=2)`): Euclidean/Frobenius
+ * norm, computed by a QR sweep with the scale carried as a logarithm. */
+int ttals_tt_norm(ttals_ctx* ctx, const ttals_tt* t, double* out_norm);
+
+/* scikit_tt/solvers/sle.py:194-219 `__construct_stack_left_op` (left=1) and
+ * sle.py:250-276 `__construct_stack_right_op` (left=0): one interface stack
+ * from its neighbour `stack` (a, R, a) [left] or (s, R', s) [right], solution
+ * core x (r0, n, r1) and operator core op (R, n, n, R'). */
+int ttals_stack_op(ttals_ctx* ctx, int32_t left, const double* stack, const double* x,
+                   const double* op, int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1,
+                   double* out, int32_t on_device);
+
+/* scikit_tt/solvers/sle.py:308-347 `__construct_micro_matrix_als`: dense
+ * local operator (r0*n*r1)^2 from stacks L (r0, R0, r0), Rt (r1, R1, r1) and
+ * operator core op (R0, n, n, R1). */
+int ttals_micro_matrix(ttals_ctx* ctx, const double* L, const double* op, const double* Rt,
+                       int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1, double* out,
+                       int32_t on_device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TTALS_H_ */

@@ -1,0 +1,443 @@
+"""NumPy restatement of scikit_tt's tensor-train ALS hot path (CPU oracle).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
+and ``bench.py`` (CPU baseline / reference arm).  The product package never
+imports it.
+
+A tensor train is a plain ``list`` of 4-D NumPy cores ``(r_i, m_i, n_i,
+r_{i+1})`` (row dimension m, column dimension n), exactly the layout of
+``scikit_tt/tensor_train.py:184-188``.  The algorithms follow the reference
+line by line in meaning (same contractions, same dense local solves, same
+QR/RQ/SVD rank rules, same sweep schedule and stopping rule); the code itself
+is written with ``einsum`` instead of chains of ``tensordot``.
+
+Pinned against the reference's own outputs: ``tests/golden/*.npz`` were
+produced by ``tests/golden/make_golden.py`` from the reference package, and
+``tests/test_oracle_golden.py`` checks this module against them.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+import scipy.sparse.linalg as spla
+
+# ----------------------------------------------------------------------------
+# interface stacks (sle.py:194-305, evp.py:253-334)
+# ----------------------------------------------------------------------------
+
+
+def stack_left_op(prev, x, a, conj_first=False):
+    """Left operator stack ``L_i[s, R', s']`` from ``L_{i-1}``, core ``x`` (3-D
+    ``(a, n, s)``) and operator core ``a`` ``(R, m, n, R')``.
+
+    SLE (sle.py:217-219): ``sum L[a,R,a'] x[a,n,s] A[R,m,n,R'] conj(x)[a',m,s']``.
+    EVP (evp.py:281-283) conjugates the first factor instead
+    (``conj_first=True``); both agree for real data.
+    """
+    xl = np.conj(x) if conj_first else x
+    xr = x if conj_first else np.conj(x)
+    return np.einsum('aRb,ans,RmnQ,bmt->sQt', prev, xl, a, xr, optimize=True)
+
+
+def stack_right_op(nxt, x, a):
+    """Right operator stack ``R_i[a, R, a']`` (sle.py:274-276, evp.py:323-325):
+    ``sum x[a,n,s] A[R,m,n,R'] conj(x)[a',m,s'] R_{i+1}[s,R',s']``."""
+    return np.einsum('ans,RmnQ,bmt,sQt->aRb', x, a, np.conj(x), nxt, optimize=True)
+
+
+def stack_left_vec(prev, x, b):
+    """Left stack of a TT vector against the solution (sle.py:246-247,
+    evp.py:291-292): ``Lb_i[g, s'] = sum Lb[h,a'] b[h,m,g] conj(x)[a',m,s']``."""
+    return np.einsum('hb,hmg,bmt->gt', prev, b, np.conj(x), optimize=True)
+
+
+def stack_right_vec(nxt, x, b):
+    """Right stack of a TT vector (sle.py:303-305, evp.py:333-334):
+    ``Rb_i[h, a'] = sum b[h,m,g] conj(x)[a',m,s'] Rb_{i+1}[g,s']``."""
+    return np.einsum('hmg,bmt,gt->hb', b, np.conj(x), nxt, optimize=True)
+
+
+def micro_matrix(left, a, right):
+    """Dense local operator (sle.py:339-345, evp.py:359-365):
+    ``M[(a',m,s'), (a,n,s)] = sum L[a,R,a'] A[R,m,n,R'] Rt[s,R',s']``."""
+    r0, _, r0p = left.shape
+    rr, _, rrp = right.shape
+    m, n = a.shape[1], a.shape[2]
+    t = np.einsum('aRb,RmnQ,sQt->bmtans', left, a, right, optimize=True)
+    return t.reshape(r0p * m * rrp, r0 * n * rr)
+
+
+def micro_vec(left, b, right):
+    """Local right-hand side (sle.py:424-428, evp.py:377-379):
+    ``f[(a',m,s')] = sum Lb[h,a'] b[h,m,g] Rb[g,s']`` as an ``(N, 1)`` column."""
+    f = np.einsum('hb,hmg,gt->bmt', left, b, right, optimize=True)
+    return f.reshape(-1, 1)
+
+
+# ----------------------------------------------------------------------------
+# sle.als (sle.py:10-95, 475-547)
+# ----------------------------------------------------------------------------
+
+
+def _update_core_sle(i, mop, mrhs, cores, ranks, dims, solver, direction):
+    """Local solve plus QR/RQ re-gauging, sle.py:475-547."""
+    if solver == 'solve':
+        cores[i] = np.linalg.solve(mop, mrhs)
+    elif solver == 'lu':
+        lu = sla.lu_factor(mop, overwrite_a=True, check_finite=False)
+        cores[i] = sla.lu_solve(lu, mrhs, trans=0, overwrite_b=True, check_finite=False)
+    # any other solver string: the reference skips the solve and re-gauges the
+    # old core (sle.py:505-509 has no else branch)
+    a, n, s = ranks[i], dims[i], ranks[i + 1]
+    if direction == 'forward':
+        q, _ = sla.qr(np.reshape(cores[i], (a * n, s)), mode='economic', check_finite=False)
+        ranks[i + 1] = q.shape[1]
+        cores[i] = q.reshape(a, n, 1, ranks[i + 1])
+    else:
+        if i > 0:
+            _, q = sla.rq(np.reshape(cores[i], (a, n * s)), mode='economic', check_finite=False)
+            ranks[i] = q.shape[0]
+            cores[i] = q.reshape(ranks[i], n, 1, s)
+        else:
+            cores[i] = np.reshape(cores[i], (a, n, 1, s))
+
+
+def sle_als(op, x0, b, repeats=1, solver='solve'):
+    """One-site ALS for ``op @ x = b`` (sle.py:10-95).  Returns the core list."""
+    d = len(op)
+    cores = [c.copy() for c in x0]
+    ranks = [c.shape[0] for c in cores] + [cores[-1].shape[3]]
+    dims = [c.shape[1] for c in op]
+    sl_op, sl_b, sr_op, sr_b = [None] * d, [None] * d, [None] * d, [None] * d
+
+    def right(i):
+        if i == d - 1:
+            sr_op[i] = np.ones((1, 1, 1))
+            sr_b[i] = np.ones((1, 1))
+        else:
+            x = cores[i + 1][:, :, 0, :]
+            sr_op[i] = stack_right_op(sr_op[i + 1], x, op[i + 1])
+            sr_b[i] = stack_right_vec(sr_b[i + 1], x, b[i + 1][:, :, 0, :])
+
+    def left(i):
+        if i == 0:
+            sl_op[i] = np.ones((1, 1, 1))
+            sl_b[i] = np.ones((1, 1))
+        else:
+            x = cores[i - 1][:, :, 0, :]
+            sl_op[i] = stack_left_op(sl_op[i - 1], x, op[i - 1])
+            sl_b[i] = stack_left_vec(sl_b[i - 1], x, b[i - 1][:, :, 0, :])
+
+    def micro(i):
+        return (micro_matrix(sl_op[i], op[i], sr_op[i]),
+                micro_vec(sl_b[i], b[i][:, :, 0, :], sr_b[i]))
+
+    for i in range(d - 1, -1, -1):          # sle.py:54-56
+        right(i)
+    for _ in range(repeats):                 # sle.py:62-93
+        for i in range(d):
+            left(i)
+            if i < d - 1:
+                mop, mrhs = micro(i)
+                _update_core_sle(i, mop, mrhs, cores, ranks, dims, solver, 'forward')
+        for i in range(d - 1, -1, -1):
+            right(i)
+            mop, mrhs = micro(i)
+            _update_core_sle(i, mop, mrhs, cores, ranks, dims, solver, 'backward')
+    return cores
+
+
+# ----------------------------------------------------------------------------
+# evp.als (evp.py:17-179, 386-495)
+# ----------------------------------------------------------------------------
+
+
+def _local_eig(mop, mgevp, number_ev, solver, sigma, real):
+    """Local eigensolve and selection rule, evp.py:414-443."""
+    vals = vecs = None
+    if solver == 'eigs':
+        v0 = np.ones(mop.shape[0])
+        vals, vecs = spla.eigs(mop, M=mgevp, sigma=sigma, k=number_ev, v0=v0)
+        idx = np.abs(vals - sigma).argsort()[::-1]
+        vals, vecs = vals[idx], vecs[:, idx]
+    if solver == 'eig':
+        vals, vecs = sla.eig(mop, b=mgevp, overwrite_a=True, overwrite_b=True, check_finite=False)
+        idx = np.abs(vals - sigma).argsort()
+        vals, vecs = vals[idx[:number_ev]], vecs[:, idx[:number_ev]]
+    if solver == 'eigh':
+        n = mop.shape[0]
+        vals, vecs = sla.eigh(mop, b=mgevp, overwrite_a=True, overwrite_b=True, check_finite=False,
+                              subset_by_index=(n - number_ev, n - 1))
+        vals, vecs = vals[::-1], vecs[:, ::-1]
+    if real is True:
+        vals = np.real(vals)
+    return vals, vecs
+
+
+def evp_als(op, x0, previous=(), shift=0.0, op_gevp=None, number_ev=1, repeats=1,
+            conv_eps=1e-10, solver='eig', sigma=1.0, real=True):
+    """One-site ALS eigensolver (evp.py:17-179).
+
+    Returns ``(eigenvalue(s), cores or list of core lists, iterations)`` with the
+    reference's return conventions: for ``number_ev == 1`` the best pair over the
+    sweeps (evp.py:151-155), else the last sweep's values and one TT per
+    eigenvector (evp.py:172-175).
+    """
+    d = len(op)
+    cores = [c.copy() for c in x0]
+    ranks = [c.shape[0] for c in cores] + [cores[-1].shape[3]]
+    dims = [c.shape[1] for c in op]
+    prev = list(previous)
+    so_l, so_r = [None] * d, [None] * d
+    sg_l, sg_r = [None] * d, [None] * d
+    sp_l = [[None] * d for _ in prev]
+    sp_r = [[None] * d for _ in prev]
+
+    def left(i):                                   # evp.py:253-292
+        if i == 0:
+            so_l[i] = np.ones((1, 1, 1))
+            if op_gevp is not None:
+                sg_l[i] = np.ones((1, 1, 1))
+            for j in range(len(prev)):
+                sp_l[j][i] = np.ones((1, 1))
+            return
+        x = cores[i - 1][:, :, 0, :]
+        so_l[i] = stack_left_op(so_l[i - 1], x, op[i - 1], conj_first=True)
+        if op_gevp is not None:
+            sg_l[i] = stack_left_op(sg_l[i - 1], x, op_gevp[i - 1], conj_first=True)
+        for j in range(len(prev)):
+            sp_l[j][i] = stack_left_vec(sp_l[j][i - 1], x, prev[j][i - 1][:, :, 0, :])
+
+    def right(i):                                  # evp.py:295-334
+        if i == d - 1:
+            so_r[i] = np.ones((1, 1, 1))
+            if op_gevp is not None:
+                sg_r[i] = np.ones((1, 1, 1))
+            for j in range(len(prev)):
+                sp_r[j][i] = np.ones((1, 1))
+            return
+        x = cores[i + 1][:, :, 0, :]
+        so_r[i] = stack_right_op(so_r[i + 1], x, op[i + 1])
+        if op_gevp is not None:
+            sg_r[i] = stack_right_op(sg_r[i + 1], x, op_gevp[i + 1])
+        for j in range(len(prev)):
+            sp_r[j][i] = stack_right_vec(sp_r[j][i + 1], x, prev[j][i + 1][:, :, 0, :])
+
+    def micro(i):                                  # evp.py:337-383
+        mop = micro_matrix(so_l[i], op[i], so_r[i])
+        mg = micro_matrix(sg_l[i], op_gevp[i], sg_r[i]) if op_gevp is not None else None
+        for j in range(len(prev)):
+            t = micro_vec(sp_l[j][i], prev[j][i][:, :, 0, :], sp_r[j][i])
+            mop = mop + shift * t.dot(np.conj(t.T))
+        return mop, mg
+
+    def update(i, mop, mg, direction):             # evp.py:386-495
+        vals, vecs = _local_eig(mop, mg, number_ev, solver, sigma, real)
+        a, n, s = ranks[i], dims[i], ranks[i + 1]
+        if direction == 'forward':
+            u, _, _ = sla.svd(vecs.reshape(a * n, s * number_ev), check_finite=False, lapack_driver='gesvd')
+            r = min(s, u.shape[1])
+            ranks[i + 1] = r
+            cores[i] = u[:, :r].reshape(a, n, 1, r)
+        else:
+            if i > 0:
+                vt = vecs.transpose()
+                _, _, v = sla.svd(vt.reshape(number_ev * a, n * s), check_finite=False, lapack_driver='gesvd')
+                r = min(a, v.shape[0])
+                ranks[i] = r
+                cores[i] = v[:r, :].reshape(r, n, 1, s)
+            else:
+                cores[i] = vecs.reshape(a, n, 1, s, number_ev)
+        return vals
+
+    for i in range(d - 1, -1, -1):
+        right(i)
+    it = 1
+    vals_pre = np.array([np.inf] * number_ev)[None, :]
+    converged = False
+    val_opt, cores_opt = np.inf, None
+    vals = None
+    while it <= repeats and not converged:         # evp.py:118-165
+        for i in range(d):
+            left(i)
+            if i < d - 1:
+                mop, mg = micro(i)
+                vals = update(i, mop, mg, 'forward')
+        for i in range(d - 1, -1, -1):
+            right(i)
+            mop, mg = micro(i)
+            vals = update(i, mop, mg, 'backward')
+        it += 1
+        if number_ev == 1 and np.abs(vals[0] - sigma) < np.abs(val_opt - sigma):
+            val_opt = vals[0].copy()
+            cores_opt = [cores[0][:, :, :, :, 0]] + cores[1:]
+        last = vals_pre[-min(3, vals_pre.shape[0]):, :]
+        if np.amax(np.abs(last - vals)) < conv_eps:
+            converged = True
+        vals_pre = np.vstack((vals_pre, vals))
+    if number_ev == 1:
+        return val_opt, cores_opt, it - 1
+    tts = [[cores[0][:, :, :, :, k]] + cores[1:] for k in range(number_ev)]
+    return vals, tts, it - 1
+
+
+# ----------------------------------------------------------------------------
+# TT algebra used by the harness (tensor_train.py)
+# ----------------------------------------------------------------------------
+
+
+def tt_matmul(t, u):
+    """Core-wise operator product (tensor_train.py:447-501); the combined rank
+    index has ``t``'s rank as the major index.  Returns cores (no scalar
+    collapse)."""
+    out = []
+    for c1, c2 in zip(t, u):
+        r1, m, _, r2 = c1.shape
+        s1, _, p, s2 = c2.shape
+        out.append(np.einsum('aijb,cjkd->acikbd', c1, c2).reshape(r1 * s1, m, p, r2 * s2))
+    return out
+
+
+def tt_add(t, u):
+    """Block-diagonal rank sum (tensor_train.py:282-344)."""
+    d = len(t)
+    rt = [c.shape[0] for c in t] + [1]
+    ru = [c.shape[0] for c in u] + [1]
+    ranks = [1] + [rt[i] + ru[i] for i in range(1, d)] + [1]
+    out = []
+    for i in range(d):
+        m, n = t[i].shape[1], t[i].shape[2]
+        dt = np.result_type(t[i], u[i])
+        c = np.zeros((ranks[i], m, n, ranks[i + 1]), dtype=dt)
+        c[:rt[i], :, :, :rt[i + 1]] = t[i]
+        c[ranks[i] - ru[i]:, :, :, ranks[i + 1] - ru[i + 1]:] = u[i]
+        out.append(c)
+    return out
+
+
+def tt_scale(t, alpha):
+    """Scalar times TT: scales the first core (tensor_train.py:368-399)."""
+    return [alpha * t[0]] + [c.copy() for c in t[1:]]
+
+
+def ortho_left(t, threshold=0.0, max_rank=np.inf):
+    """SVD left-orthonormalisation (tensor_train.py:1161-1191); returns new cores."""
+    t = [c.copy() for c in t]
+    d = len(t)
+    for i in range(d - 1):
+        r, m, n, s = t[i].shape
+        try:
+            u, sv, v = sla.svd(t[i].reshape(r * m * n, s), full_matrices=False, check_finite=False)
+        except sla.LinAlgError:
+            u, sv, v = sla.svd(t[i].reshape(r * m * n, s), full_matrices=False, check_finite=False,
+                               lapack_driver='gesvd')
+        if threshold != 0:
+            keep = np.where(sv / sv[0] > threshold)[0]
+            u, sv, v = u[:, keep], sv[keep], v[keep, :]
+        if max_rank != np.inf:
+            k = int(min(u.shape[1], max_rank))
+            u, sv, v = u[:, :k], sv[:k], v[:k, :]
+        t[i] = u.reshape(r, m, n, u.shape[1])
+        t[i + 1] = np.tensordot(np.diag(sv).dot(v), t[i + 1], axes=(1, 0))
+    return t
+
+
+def ortho_right(t, threshold=0.0, max_rank=np.inf):
+    """SVD right-orthonormalisation (tensor_train.py:1267-1299); returns new cores."""
+    t = [c.copy() for c in t]
+    d = len(t)
+    for i in range(d - 1, 0, -1):
+        r, m, n, s = t[i].shape
+        try:
+            u, sv, v = sla.svd(t[i].reshape(r, m * n * s), full_matrices=False, check_finite=False)
+        except sla.LinAlgError:
+            u, sv, v = sla.svd(t[i].reshape(r, m * n * s), full_matrices=False, check_finite=False,
+                               lapack_driver='gesvd')
+        if threshold != 0:
+            keep = np.where(sv / sv[0] > threshold)[0]
+            u, sv, v = u[:, keep], sv[keep], v[keep, :]
+        if max_rank != np.inf:
+            k = int(min(v.shape[0], max_rank))
+            u, sv, v = u[:, :k], sv[:k], v[:k, :]
+        k = v.shape[0]
+        t[i] = v.reshape(k, m, n, s)
+        p = t[i - 1]
+        t[i - 1] = (p.reshape(-1, p.shape[3]).dot(u).dot(np.diag(sv))).reshape(p.shape[0], p.shape[1],
+                                                                                  p.shape[2], k)
+    return t
+
+
+def norm2(t):
+    """2-norm (tensor_train.py:1409-1425): flatten operator cores, right-
+    orthonormalise, Frobenius norm of the first core."""
+    is_op = not (all(c.shape[1] == 1 for c in t) or all(c.shape[2] == 1 for c in t))
+    if is_op:
+        t = [c.reshape(c.shape[0], c.shape[1] * c.shape[2], 1, c.shape[3]) for c in t]
+    t = ortho_right(t)
+    return float(np.linalg.norm(t[0].ravel()))
+
+
+def full_vector(t):
+    """Dense vector of a TT with unit column dims (tensor_train.py:1061-1090)."""
+    v = t[0].reshape(t[0].shape[1], t[0].shape[3])
+    for c in t[1:]:
+        v = np.tensordot(v, c[:, :, 0, :], axes=(1, 0)).reshape(-1, c.shape[3])
+    return v.reshape(-1)
+
+
+def full_matrix(t):
+    """Dense matrix of a TT operator (tensor_train.py:1061-1090)."""
+    mat = t[0].reshape(t[0].shape[1], t[0].shape[2], t[0].shape[3])
+    for c in t[1:]:
+        mat = np.tensordot(mat, c, axes=(2, 0))
+        mat = mat.transpose(0, 2, 1, 3, 4)
+        mat = mat.reshape(mat.shape[0] * mat.shape[1], mat.shape[2] * mat.shape[3], c.shape[3])
+    return mat[:, :, 0]
+
+
+# ----------------------------------------------------------------------------
+# numerically stable metrics (needed at large d, where ||b|| reaches 1e40)
+# ----------------------------------------------------------------------------
+
+
+def stable_norm(t):
+    """Euclidean norm via a left-to-right QR sweep with the norm carried in the
+    last core; avoids the over/underflow the SVD-based ``norm`` meets on
+    unnormalised trains."""
+    t = [c.reshape(c.shape[0], -1, c.shape[3]) for c in t]
+    logscale = 0.0
+    carry = np.ones((1, 1))
+    for i, c in enumerate(t):
+        c = np.tensordot(carry, c, axes=(1, 0))
+        r, k, s = c.shape
+        if i == len(t) - 1:
+            nrm = np.linalg.norm(c.ravel())
+            return float(nrm * np.exp(logscale)) if nrm > 0 else 0.0
+        q, rr = np.linalg.qr(c.reshape(r * k, s))
+        sc = np.linalg.norm(rr)
+        if sc == 0:
+            return 0.0
+        logscale += np.log(sc)
+        carry = rr / sc
+    return 0.0
+
+
+def stable_rel_diff(x, y):
+    """``||x - y|| / ||y||`` of two TT vectors, computed stably."""
+    ny = stable_norm(y)
+    return stable_norm(tt_add(x, tt_scale(y, -1.0))) / ny
+
+
+def stable_residual(op, x, b):
+    """``||op @ x - b|| / ||b||`` computed stably (left-orthonormal sweep)."""
+    ax = tt_matmul(op, x)
+    return stable_rel_diff(ax, b)
+
+
+def ising_exact_e0(d, coupling, field):
+    """Ground energy of the open transverse-field Ising chain
+    ``H = -J sum z_i z_{i+1} - g sum x_i`` by free fermions (Pfeuty 1970):
+    ``E0 = -sum_k sigma_k(B)`` with ``B = bidiag(g on the diagonal, J above)``."""
+    bmat = np.diag(field * np.ones(d)) + np.diag(coupling * np.ones(d - 1), 1)
+    return -float(np.sum(np.linalg.svd(bmat, compute_uv=False)))

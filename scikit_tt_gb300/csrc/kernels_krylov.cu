@@ -1,0 +1,674 @@
+// Persistent, grid-cooperative Krylov solvers for the ALS local problems.
+//
+// The local operator M (the micro matrix of scikit_tt/solvers/sle.py:308-347,
+// N = r_i n_i r_{i+1}) is never assembled: every Krylov step applies it as the
+// three contractions L -> A -> Rt (O(n R r^3) instead of O(N^2) per product).
+//
+// gmres_ir_kernel<TI>: restarted GMRES with an FP64 outer residual.
+//   Each cycle evaluates r = f - M x in FP64, then runs one GMRES(m) cycle in
+//   precision TI on M d = r / |r| (classical Gram-Schmidt, applied twice) and
+//   updates x += |r| d in FP64.  TI = double is the plain FP64 solver (the
+//   cycles are ordinary restarts); TI = float is GMRES-based iterative
+//   refinement: FP32 Krylov work, FP64 residual and solution.
+//   Replaces np.linalg.solve / lu_factor+lu_solve of sle.py:505-509.
+//
+// lanczos_kernel: Lanczos with full reorthogonalisation (CGS2) for the
+//   symmetric local eigenproblem of scikit_tt/solvers/evp.py:386-443; Ritz
+//   values from the tridiagonal matrix by Sturm-count multisection, Ritz
+//   vectors by inverse iteration; selection "largest k" (eigh),
+//   "closest to sigma" (eig/eigs) or "smallest".  Deflation by previous
+//   eigentensors (evp.py:376-381) is applied matrix-free: M += shift t t^T.
+//
+// One CTA per SM, co-resident (cooperative launch).  Vector work uses a fixed
+// chunk of elements per CTA; every scalar (dot, norm, Givens rotation, Ritz
+// value) is reduced identically in every CTA, so control flow is uniform.
+#include <float.h>
+
+#include <algorithm>
+
+#include "ttals_internal.h"
+
+namespace ttals {
+
+constexpr int kKThreads = 512;
+
+__host__ __device__ __forceinline__ int64_t imin64(int64_t a, int64_t b) { return a < b ? a : b; }
+
+template <typename TI>
+struct GmresK {
+  Contraction p1, p2, p3;
+  int N;
+  const double *L64, *A64, *R64;
+  double *T1_64, *T2_64;
+  const TI *Li, *Ai, *Ri;
+  TI *T1i, *T2i;
+  const double* f;
+  double* x;
+  double* r;
+  TI* V;
+  TI* w;
+  double* partials;
+  int m, max_cycles;
+  double tol, inner_floor;
+  unsigned* bar;
+  int* status;
+  double* report;
+};
+
+// Phases 1 and 2 of y -> M y over the whole grid (output T2 complete on return).
+template <typename T>
+__device__ __forceinline__ bool apply12(const Contraction& p1, const Contraction& p2, const T* L, const T* A,
+                                        const T* y, T* T1, T* T2, const GridBarrier& bar, int* st) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t G = (int64_t)gridDim.x * blockDim.x;
+  contract_range(p1, L, y, T1, T(1), T(0), g, G);
+  if (!grid_sync(bar, st)) return false;
+  contract_range(p2, T1, A, T2, T(1), T(0), g, G);
+  return grid_sync(bar, st);
+}
+
+// Phase 3 for one element of the (dense) output vector.
+template <typename T>
+__device__ __forceinline__ T apply3(const Contraction& p3, const T* T2, const T* R, int64_t e) {
+  int64_t ao, bo, co;
+  contract_offsets(p3, e, ao, bo, co);
+  return contract_sum(p3, T2, R, ao, bo);
+}
+
+// partial[kk] = sum_{e in chunk} X_kk[e] w[e] for kk < nvec (X_kk = V_kk),
+// partial[nvec] = sum w[e]^2.
+template <typename T>
+__device__ __forceinline__ void chunk_dots(const T* V, int64_t N, int nvec, const T* w, int e0, int e1,
+                                           double* partial) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int kk = warp; kk <= nvec; kk += nw) {
+    const T* xv = (kk < nvec) ? V + (int64_t)kk * N : w;
+    double s = 0.0;
+    for (int e = e0 + lane; e < e1; e += 32) s += (double)xv[e] * (double)w[e];
+    s = warp_sum(s);
+    if (lane == 0) partial[kk] = s;
+  }
+}
+
+// Block sum of one value per thread, written by thread 0 to *dst.
+__device__ __forceinline__ void block_partial(double v, double* dst) {
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < nw; ++i) s += red[i];
+    *dst = s;
+  }
+  __syncthreads();
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(kKThreads, 1) gmres_ir_kernel(GmresK<TI> k) {
+  extern __shared__ double sm[];
+  const int m = k.m;
+  double* H = sm;  // (m+1) x m, column-major
+  double* cs = H + (m + 1) * m;
+  double* sn = cs + m;
+  double* gv = sn + m;     // m + 1
+  double* yv = gv + m + 1; // m
+  double* h1 = yv + m;     // m + 2
+  double* h2 = h1 + m + 2; // m + 2
+  __shared__ double s_scal[4];
+  __shared__ int s_flag;
+
+  const GridBarrier bar{k.bar, k.bar + 1};
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int64_t N = k.N;
+  const int chunk = (int)((N + gridDim.x - 1) / gridDim.x);
+  const int e0 = (int)imin64(N, (int64_t)blockIdx.x * chunk);
+  const int e1 = (int)imin64(N, (int64_t)e0 + chunk);
+  const int ps = m + 2;
+  int rb = 0;
+  auto prow = [&](int buf) { return k.partials + ((int64_t)buf * gridDim.x + blockIdx.x) * ps; };
+  auto pbuf = [&](int buf) { return k.partials + (int64_t)buf * gridDim.x * ps; };
+
+  // ||f||
+  {
+    double s = 0.0;
+    for (int e = e0 + tid; e < e1; e += nt) s += k.f[e] * k.f[e];
+    block_partial(s, prow(rb));
+    if (!grid_sync(bar, k.status)) return;
+    reduce_partials(pbuf(rb), ps, 1, h1);
+    rb ^= 1;
+  }
+  const double fnorm = sqrt(h1[0]);
+  if (!(fnorm > 0.0)) {
+    for (int e = e0 + tid; e < e1; e += nt) k.x[e] = 0.0;
+    if (blockIdx.x == 0 && tid == 0) {
+      k.report[0] = 0.0; k.report[1] = 0; k.report[2] = 0;
+      if (!(fnorm == 0.0)) atomicCAS(k.status, ST_OK, ST_NONFINITE);
+    }
+    return;
+  }
+
+  double rel = 1.0;
+  int cycles = 0, inner = 0;
+  for (int cyc = 0; cyc < k.max_cycles; ++cyc) {
+    // FP64 residual r = f - M x
+    if (!apply12<double>(k.p1, k.p2, k.L64, k.A64, k.x, k.T1_64, k.T2_64, bar, k.status)) return;
+    double s = 0.0;
+    for (int e = e0 + tid; e < e1; e += nt) {
+      const double re = k.f[e] - apply3<double>(k.p3, k.T2_64, k.R64, e);
+      k.r[e] = re;
+      s += re * re;
+    }
+    block_partial(s, prow(rb));
+    if (!grid_sync(bar, k.status)) return;
+    reduce_partials(pbuf(rb), ps, 1, h1);
+    rb ^= 1;
+    const double rho = sqrt(h1[0]);
+    rel = rho / fnorm;
+    cycles = cyc + 1;
+    if (!isfinite(rel)) {
+      if (tid == 0) atomicCAS(k.status, ST_OK, ST_NONFINITE);
+      break;
+    }
+    if (rel <= k.tol) break;
+
+    // one inner GMRES(m) cycle in TI on M d = r / rho
+    const double target = fmax(k.tol / rel, k.inner_floor);
+    for (int e = e0 + tid; e < e1; e += nt) k.V[e] = (TI)(k.r[e] / rho);
+    if (tid == 0) {
+      gv[0] = 1.0;
+      for (int i = 1; i <= m; ++i) gv[i] = 0.0;
+    }
+    if (!grid_sync(bar, k.status)) return;
+    int jj = 0;
+    for (int j = 0; j < m; ++j) {
+      const TI* vj = k.V + (int64_t)j * N;
+      if (!apply12<TI>(k.p1, k.p2, k.Li, k.Ai, vj, k.T1i, k.T2i, bar, k.status)) return;
+      for (int e = e0 + tid; e < e1; e += nt) k.w[e] = apply3<TI>(k.p3, k.T2i, k.Ri, e);
+      __syncthreads();
+      chunk_dots<TI>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+      if (!grid_sync(bar, k.status)) return;
+      reduce_partials(pbuf(rb), ps, j + 2, h1);
+      rb ^= 1;
+      for (int e = e0 + tid; e < e1; e += nt) {
+        double acc = (double)k.w[e];
+        for (int q = 0; q <= j; ++q) acc -= h1[q] * (double)k.V[(int64_t)q * N + e];
+        k.w[e] = (TI)acc;
+      }
+      __syncthreads();
+      chunk_dots<TI>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+      if (!grid_sync(bar, k.status)) return;
+      reduce_partials(pbuf(rb), ps, j + 2, h2);
+      rb ^= 1;
+      double hn2 = h2[j + 1];
+      for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
+      const double hn = sqrt(fmax(hn2, 0.0));
+      if (hn > 0.0) {
+        const double inv = 1.0 / hn;
+        TI* vn = k.V + (int64_t)(j + 1) * N;
+        for (int e = e0 + tid; e < e1; e += nt) {
+          double acc = (double)k.w[e];
+          for (int q = 0; q <= j; ++q) acc -= h2[q] * (double)k.V[(int64_t)q * N + e];
+          vn[e] = (TI)(acc * inv);
+        }
+      }
+      if (tid == 0) {
+        double* col = H + (int64_t)j * (m + 1);
+        for (int i = 0; i <= j; ++i) col[i] = h1[i] + h2[i];
+        col[j + 1] = hn;
+        for (int i = 0; i < j; ++i) {
+          const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+          col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+          col[i] = t;
+        }
+        const double a = col[j], b = col[j + 1];
+        double c = 1.0, sg = 0.0, rr = a;
+        if (b != 0.0) {
+          rr = hypot(a, b);
+          c = a / rr;
+          sg = b / rr;
+        }
+        cs[j] = c; sn[j] = sg;
+        col[j] = rr; col[j + 1] = 0.0;
+        gv[j + 1] = -sg * gv[j];
+        gv[j] = c * gv[j];
+        s_scal[0] = fabs(gv[j + 1]);
+        s_flag = (hn <= 1e-300) ? 1 : 0;
+      }
+      __syncthreads();
+      jj = j + 1;
+      ++inner;
+      if (s_scal[0] <= target || s_flag) break;
+      if (!grid_sync(bar, k.status)) return;  // V_{j+1} complete
+    }
+    // y = H(0:jj, 0:jj)^{-1} g
+    if (tid == 0) {
+      int bad = 0;
+      for (int i = jj - 1; i >= 0; --i) {
+        double acc = gv[i];
+        for (int l = i + 1; l < jj; ++l) acc -= H[(int64_t)l * (m + 1) + i] * yv[l];
+        const double dgl = H[(int64_t)i * (m + 1) + i];
+        if (dgl == 0.0) { bad = 1; yv[i] = 0.0; } else yv[i] = acc / dgl;
+      }
+      s_flag = bad;
+    }
+    __syncthreads();
+    if (s_flag) {
+      if (tid == 0) atomicCAS(k.status, ST_OK, ST_SINGULAR);
+      break;
+    }
+    for (int e = e0 + tid; e < e1; e += nt) {
+      double acc = 0.0;
+      for (int q = 0; q < jj; ++q) acc += yv[q] * (double)k.V[(int64_t)q * N + e];
+      k.x[e] += rho * acc;
+    }
+    if (!grid_sync(bar, k.status)) return;  // x complete before the next residual
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    k.report[0] = rel;
+    k.report[1] = cycles;
+    k.report[2] = inner;
+  }
+}
+
+size_t gmres_partials_doubles(int m, int num_sms) { return (size_t)2 * num_sms * (m + 2); }
+
+static size_t gmres_smem_bytes(int m) {
+  return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + (m + 1) + m + 2 * (m + 2));
+}
+
+cudaError_t launch_gmres(const GmresLaunch& g, int num_sms, cudaStream_t st) {
+  Contraction p1, p2, p3;
+  local_apply_descs(g.sh, &p1, &p2, &p3);
+  const size_t smem = gmres_smem_bytes(g.m);
+  dim3 grid(num_sms), block(kKThreads);
+  if (g.precision == 0) {
+    GmresK<double> k{p1, p2, p3, (int)g.sh.N(), g.L64, g.A64, g.R64, g.T1_64, g.T2_64,
+                     (const double*)g.Li, (const double*)g.Ai, (const double*)g.Ri, (double*)g.T1i,
+                     (double*)g.T2i, g.f, g.x, g.r, (double*)g.V, (double*)g.w, g.partials, g.m,
+                     g.max_cycles, g.tol, g.inner_floor, g.bar, g.status, g.report};
+    cudaError_t e = cudaFuncSetAttribute(gmres_ir_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    void* args[] = {&k};
+    return cudaLaunchCooperativeKernel((const void*)gmres_ir_kernel<double>, grid, block, args, smem, st);
+  }
+  GmresK<float> k{p1, p2, p3, (int)g.sh.N(), g.L64, g.A64, g.R64, g.T1_64, g.T2_64,
+                  (const float*)g.Li, (const float*)g.Ai, (const float*)g.Ri, (float*)g.T1i,
+                  (float*)g.T2i, g.f, g.x, g.r, (float*)g.V, (float*)g.w, g.partials, g.m,
+                  g.max_cycles, g.tol, g.inner_floor, g.bar, g.status, g.report};
+  cudaError_t e = cudaFuncSetAttribute(gmres_ir_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&k};
+  return cudaLaunchCooperativeKernel((const void*)gmres_ir_kernel<float>, grid, block, args, smem, st);
+}
+
+// ---------------------------------------------------------------------------
+// symmetric tridiagonal helpers (one warp)
+// ---------------------------------------------------------------------------
+
+// Number of eigenvalues of T (diag al, off-diag be) smaller than x
+// (Sylvester inertia of T - x I through its LDL^T pivots).
+__device__ int sturm_count(const double* al, const double* be, int n, double x, double pivmin) {
+  int c = 0;
+  double d = al[0] - x;
+  if (fabs(d) < pivmin) d = -pivmin;
+  c += d < 0.0;
+  for (int i = 1; i < n; ++i) {
+    d = (al[i] - x) - be[i - 1] * be[i - 1] / d;
+    if (fabs(d) < pivmin) d = -pivmin;
+    c += d < 0.0;
+  }
+  return c;
+}
+
+// Eigenvalue number idx (ascending, 0-based) by 33-way multisection of
+// [lo, hi] with the 32 lanes of the calling warp; uniform result.
+__device__ double tri_eigval(const double* al, const double* be, int n, int idx, double lo, double hi,
+                             double pivmin) {
+  const int lane = threadIdx.x & 31;
+  for (int round = 0; round < 24; ++round) {
+    const double width = hi - lo;
+    if (width <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+    const double x = lo + width * (double)(lane + 1) / 33.0;
+    const int c = sturm_count(al, be, n, x, pivmin);
+    const unsigned mask = __ballot_sync(0xffffffffu, c > idx);
+    const int first = mask ? (__ffs(mask) - 1) : 32;
+    const double nlo = (first == 0) ? lo : lo + width * (double)first / 33.0;
+    const double nhi = (first == 32) ? hi : lo + width * (double)(first + 1) / 33.0;
+    lo = nlo;
+    hi = nhi;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// Inverse iteration for the eigenvector of T at theta (one thread).  Partial
+// pivoting Gaussian elimination of the tridiagonal T - theta I; z (n) out,
+// work: 5 n doubles + n ints.
+__device__ void tri_eigvec(const double* al, const double* be, int n, double theta, double tnorm, double* z,
+                           double* wk, int* piv) {
+  double* d = wk;
+  double* du = wk + n;
+  double* du2 = wk + 2 * n;
+  double* dl = wk + 3 * n;
+  double* b = wk + 4 * n;
+  const double tiny = DBL_EPSILON * tnorm + 1e-300;
+  for (int i = 0; i < n; ++i) {
+    d[i] = al[i] - theta;
+    du[i] = (i < n - 1) ? be[i] : 0.0;
+    dl[i] = (i < n - 1) ? be[i] : 0.0;
+    du2[i] = 0.0;
+  }
+  for (int i = 0; i < n - 1; ++i) {
+    if (fabs(d[i]) >= fabs(dl[i])) {
+      if (d[i] == 0.0) d[i] = tiny;
+      const double fct = dl[i] / d[i];
+      dl[i] = fct;
+      d[i + 1] -= fct * du[i];
+      piv[i] = 0;
+    } else {
+      const double fct = d[i] / dl[i];
+      d[i] = dl[i];
+      dl[i] = fct;
+      const double tmp = du[i];
+      du[i] = d[i + 1];
+      d[i + 1] = tmp - fct * d[i + 1];
+      if (i < n - 2) {
+        du2[i] = du[i + 1];
+        du[i + 1] = -fct * du[i + 1];
+      }
+      piv[i] = 1;
+    }
+  }
+  if (d[n - 1] == 0.0) d[n - 1] = tiny;
+  for (int i = 0; i < n; ++i) z[i] = 1.0 / sqrt((double)n) * (1.0 + 0.01 * (double)(i % 7));
+  for (int it = 0; it < 3; ++it) {
+    for (int i = 0; i < n; ++i) b[i] = z[i];
+    for (int i = 0; i < n - 1; ++i) {
+      if (!piv[i]) {
+        b[i + 1] -= dl[i] * b[i];
+      } else {
+        const double t = b[i];
+        b[i] = b[i + 1];
+        b[i + 1] = t - dl[i] * b[i];
+      }
+    }
+    z[n - 1] = b[n - 1] / d[n - 1];
+    if (n > 1) z[n - 2] = (b[n - 2] - du[n - 2] * z[n - 1]) / d[n - 2];
+    for (int i = n - 3; i >= 0; --i) z[i] = (b[i] - du[i] * z[i + 1] - du2[i] * z[i + 2]) / d[i];
+    double nrm = 0.0;
+    for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
+    nrm = sqrt(nrm);
+    if (!(nrm > 0.0) || !isfinite(nrm)) {
+      for (int i = 0; i < n; ++i) z[i] = (i == 0) ? 1.0 : 0.0;
+      return;
+    }
+    for (int i = 0; i < n; ++i) z[i] /= nrm;
+  }
+}
+
+struct LanczosK {
+  Contraction p1, p2, p3;
+  int N;
+  const double *L, *A, *R;
+  double *T1, *T2;
+  int nprev;
+  const double* prevt;
+  double shift;
+  double* x;
+  double* vals;
+  double* V;
+  double* w;
+  double* partials;
+  int m, k, mode;
+  double sigma;
+  int max_restarts;
+  double tol;
+  unsigned* bar;
+  int* status;
+  double* report;
+};
+
+constexpr int kMaxEv = 8;
+
+// smem: al m, be m, h1 (m+2), h2 (m+2), svec m*kMaxEv, tri work 6m, piv m (ints)
+size_t lanczos_smem_bytes(int m) {
+  return sizeof(double) * ((size_t)2 * m + 2 * (m + 2) + (size_t)m * kMaxEv + 6 * (size_t)m + 8) +
+         sizeof(int) * (size_t)m;
+}
+size_t lanczos_partials_doubles(int m, int num_sms) { return (size_t)2 * num_sms * (m + 2 + 8); }
+
+__global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
+  extern __shared__ double sm[];
+  const int m = k.m;
+  double* al = sm;
+  double* be = al + m;
+  double* h1 = be + m;
+  double* h2 = h1 + m + 2;
+  double* svec = h2 + m + 2;       // m x kMaxEv, column c at svec + c*m
+  double* twk = svec + m * kMaxEv; // 5m tri work + m z
+  int* piv = (int*)(twk + 6 * m + 8);
+  __shared__ double s_theta[kMaxEv];
+  __shared__ double s_res;
+  __shared__ int s_sel[kMaxEv];
+  __shared__ int s_conv, s_nt;
+
+  const GridBarrier bar{k.bar, k.bar + 1};
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t N = k.N;
+  const int chunk = (int)((N + gridDim.x - 1) / gridDim.x);
+  const int e0 = (int)imin64(N, (int64_t)blockIdx.x * chunk);
+  const int e1 = (int)imin64(N, (int64_t)e0 + chunk);
+  const int ps = m + 2 + 8;
+  int rb = 0;
+  auto prow = [&](int buf) { return k.partials + ((int64_t)buf * gridDim.x + blockIdx.x) * ps; };
+  auto pbuf = [&](int buf) { return k.partials + (int64_t)buf * gridDim.x * ps; };
+  const int kev = k.k;
+
+  // V_0 = x / |x|
+  {
+    double s = 0.0;
+    for (int e = e0 + tid; e < e1; e += nt) s += k.x[e] * k.x[e];
+    block_partial(s, prow(rb));
+    if (!grid_sync(bar, k.status)) return;
+    reduce_partials(pbuf(rb), ps, 1, h1);
+    rb ^= 1;
+    const double nrm = sqrt(h1[0]);
+    const bool ok = nrm > 0.0 && isfinite(nrm);
+    for (int e = e0 + tid; e < e1; e += nt)
+      k.V[e] = ok ? k.x[e] / nrm : 1.0 / sqrt((double)N);
+    if (!grid_sync(bar, k.status)) return;
+  }
+
+  int total_it = 0, restarts = 0;
+  double last_res = 0.0;
+  const int mm = (int)imin64((int64_t)m, N);
+  for (;;) {
+    int nT = 0;
+    for (int j = 0; j < mm; ++j) {
+      const double* vj = k.V + (int64_t)j * N;
+      // deflation dots t_p . v_j over this chunk (reduced after the P1 barrier)
+      if (k.nprev > 0) {
+        for (int p = warp; p < k.nprev; p += (nt >> 5)) {
+          const double* tp = k.prevt + (int64_t)p * N;
+          double s = 0.0;
+          for (int e = e0 + lane; e < e1; e += 32) s += tp[e] * vj[e];
+          s = warp_sum(s);
+          if (lane == 0) prow(rb)[p] = s;
+        }
+      }
+      if (!apply12<double>(k.p1, k.p2, k.L, k.A, vj, k.T1, k.T2, bar, k.status)) return;
+      if (k.nprev > 0) {
+        reduce_partials(pbuf(rb), ps, k.nprev, h2);
+        rb ^= 1;
+      }
+      for (int e = e0 + tid; e < e1; e += nt) {
+        double v = apply3<double>(k.p3, k.T2, k.R, e);
+        for (int p = 0; p < k.nprev; ++p) v += k.shift * h2[p] * k.prevt[(int64_t)p * N + e];
+        k.w[e] = v;
+      }
+      __syncthreads();
+      chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+      if (!grid_sync(bar, k.status)) return;
+      reduce_partials(pbuf(rb), ps, j + 2, h1);
+      rb ^= 1;
+      for (int e = e0 + tid; e < e1; e += nt) {
+        double acc = k.w[e];
+        for (int q = 0; q <= j; ++q) acc -= h1[q] * k.V[(int64_t)q * N + e];
+        k.w[e] = acc;
+      }
+      __syncthreads();
+      chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+      if (!grid_sync(bar, k.status)) return;
+      reduce_partials(pbuf(rb), ps, j + 2, h2);
+      rb ^= 1;
+      double b2 = h2[j + 1];
+      for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
+      const double bj = sqrt(fmax(b2, 0.0));
+      if (tid == 0) {
+        al[j] = h1[j] + h2[j];
+        be[j] = bj;
+      }
+      if (bj > 0.0 && j + 1 < mm) {
+        double* vn = k.V + (int64_t)(j + 1) * N;
+        const double inv = 1.0 / bj;
+        for (int e = e0 + tid; e < e1; e += nt) {
+          double acc = k.w[e];
+          for (int q = 0; q <= j; ++q) acc -= h2[q] * k.V[(int64_t)q * N + e];
+          vn[e] = acc * inv;
+        }
+      }
+      __syncthreads();
+      ++total_it;
+      nT = j + 1;
+      // Rayleigh-Ritz on T_nT every 4 steps, at the end of the basis, or on breakdown
+      double tnorm = 0.0;
+      for (int i = 0; i < nT; ++i)
+        tnorm = fmax(tnorm, fabs(al[i]) + fabs(be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      const bool breakdown = !(bj > 1e-14 * fmax(tnorm, 1e-300));
+      const bool check = nT >= kev && ((nT % 4) == 0 || nT == mm || breakdown);
+      if (check) {
+        if (warp == 0) {
+          double lo = 1e300, hi = -1e300;
+          for (int i = 0; i < nT; ++i) {
+            const double rad = (i > 0 ? fabs(be[i - 1]) : 0.0) + (i < nT - 1 ? fabs(be[i]) : 0.0);
+            lo = fmin(lo, al[i] - rad);
+            hi = fmax(hi, al[i] + rad);
+          }
+          const double pivmin = 1e-300 + DBL_MIN * fmax(1.0, tnorm * tnorm);
+          lo -= 1e-12 * fmax(1.0, tnorm);
+          hi += 1e-12 * fmax(1.0, tnorm);
+          // choose the wanted indices
+          int sel[kMaxEv];
+          if (k.mode == 0) {
+            for (int c = 0; c < kev; ++c) sel[c] = nT - 1 - c;
+          } else if (k.mode == 2) {
+            for (int c = 0; c < kev; ++c) sel[c] = c;
+          } else {
+            // closest to sigma: merge outward from the count below sigma
+            const int below = sturm_count(al, be, nT, k.sigma, pivmin);
+            int dn = below - 1, up = below;
+            double vdn = (dn >= 0) ? tri_eigval(al, be, nT, dn, lo, hi, pivmin) : 0.0;
+            double vup = (up < nT) ? tri_eigval(al, be, nT, up, lo, hi, pivmin) : 0.0;
+            for (int c = 0; c < kev; ++c) {
+              const bool take_dn = (dn >= 0) && (up >= nT || fabs(vdn - k.sigma) <= fabs(vup - k.sigma));
+              if (take_dn) {
+                sel[c] = dn--;
+                if (dn >= 0) vdn = tri_eigval(al, be, nT, dn, lo, hi, pivmin);
+              } else {
+                sel[c] = up++;
+                if (up < nT) vup = tri_eigval(al, be, nT, up, lo, hi, pivmin);
+              }
+            }
+          }
+          double resmax = 0.0;
+          for (int c = 0; c < kev; ++c) {
+            const double th = tri_eigval(al, be, nT, sel[c], lo, hi, pivmin);
+            double* z = svec + c * m;
+            if (lane == 0) {
+              tri_eigvec(al, be, nT, th, fmax(tnorm, 1e-300), z, twk, piv);
+              // orthogonalise against earlier selected vectors (clustered values)
+              for (int q = 0; q < c; ++q) {
+                const double* zq = svec + q * m;
+                double dt = 0.0;
+                for (int i = 0; i < nT; ++i) dt += zq[i] * z[i];
+                for (int i = 0; i < nT; ++i) z[i] -= dt * zq[i];
+                double nr = 0.0;
+                for (int i = 0; i < nT; ++i) nr += z[i] * z[i];
+                nr = sqrt(nr);
+                if (nr > 0.0)
+                  for (int i = 0; i < nT; ++i) z[i] /= nr;
+              }
+              s_theta[c] = th;
+              s_sel[c] = sel[c];
+            }
+            __syncwarp();
+            resmax = fmax(resmax, bj * fabs(z[nT - 1]) / fmax(tnorm, 1e-300));
+          }
+          if (lane == 0) {
+            s_res = resmax;
+            s_conv = (resmax <= k.tol) || breakdown;
+          }
+        }
+        __syncthreads();
+        last_res = s_res;
+        if (s_conv || nT == mm) break;
+      } else if (breakdown) {
+        break;
+      }
+      if (!grid_sync(bar, k.status)) return;  // V_{j+1} complete
+    }
+    // Ritz vectors X[e*k + c] = sum_l V_l[e] z_c[l]
+    for (int e = e0 + tid; e < e1; e += nt) {
+      for (int c = 0; c < kev; ++c) {
+        const double* z = svec + c * m;
+        double acc = 0.0;
+        for (int l = 0; l < nT; ++l) acc += z[l] * k.V[(int64_t)l * N + e];
+        k.x[(int64_t)e * kev + c] = acc;
+      }
+    }
+    const bool done = s_conv || restarts >= k.max_restarts;
+    if (done) break;
+    ++restarts;
+    // restart from the (sum of the) wanted Ritz vectors
+    if (!grid_sync(bar, k.status)) return;
+    double s = 0.0;
+    for (int e = e0 + tid; e < e1; e += nt) {
+      double v = 0.0;
+      for (int c = 0; c < kev; ++c) v += k.x[(int64_t)e * kev + c];
+      k.w[e] = v;
+      s += v * v;
+    }
+    block_partial(s, prow(rb));
+    if (!grid_sync(bar, k.status)) return;
+    reduce_partials(pbuf(rb), ps, 1, h1);
+    rb ^= 1;
+    const double nrm = sqrt(h1[0]);
+    for (int e = e0 + tid; e < e1; e += nt) k.V[e] = (nrm > 0.0) ? k.w[e] / nrm : 1.0 / sqrt((double)N);
+    if (!grid_sync(bar, k.status)) return;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    for (int c = 0; c < kev; ++c) k.vals[c] = s_theta[c];
+    k.report[0] = last_res;
+    k.report[1] = restarts;
+    k.report[2] = total_it;
+    if (!s_conv) k.report[3] = 1.0;
+    else k.report[3] = 0.0;
+  }
+}
+
+cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st) {
+  if (l.k < 1 || l.k > kMaxEv) return cudaErrorInvalidValue;
+  Contraction p1, p2, p3;
+  local_apply_descs(l.sh, &p1, &p2, &p3);
+  LanczosK k{p1, p2, p3, (int)l.sh.N(), l.L, l.A, l.R, l.T1, l.T2, l.nprev, l.prevt, l.shift, l.x, l.vals,
+             l.V, l.w, l.partials, l.m, l.k, l.mode, l.sigma, l.max_restarts, l.tol, l.bar, l.status,
+             l.report};
+  const size_t smem = lanczos_smem_bytes(l.m);
+  cudaError_t e = cudaFuncSetAttribute(lanczos_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&k};
+  return cudaLaunchCooperativeKernel((const void*)lanczos_kernel, dim3(num_sms), dim3(kKThreads), args, smem, st);
+}
+
+}  // namespace ttals

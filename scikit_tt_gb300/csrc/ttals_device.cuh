@@ -1,0 +1,219 @@
+// Device-side building blocks of the tensor-train ALS engine (sm_103a).
+//
+// * Contraction: a strided "one output element per thread" tensor contraction
+//   descriptor.  Every contraction of the ALS hot path (interface stacks,
+//   local-operator apply, local right-hand side, gauge pushes, operator-core
+//   products) is one or a chain of these.
+// * GridBarrier: an all-CTA barrier for cooperative (co-resident) launches.
+//   Its spin is bounded: after kSpinLimit polls it records a timeout in the
+//   solver's status word and returns false, so a broken launch never hangs
+//   the device.
+// * Deterministic grid reductions: every CTA writes its partial sums, then
+//   every CTA re-reduces all partials in the same fixed order, so all CTAs
+//   hold bit-identical scalars and take identical branches.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ttals {
+
+constexpr int kMaxOut = 6;
+constexpr int kMaxK = 3;
+
+// status codes shared with the host (mirrors include/ttals.h)
+enum : int {
+  ST_OK = 0,
+  ST_ARG = 1,
+  ST_CUDA = 2,
+  ST_NOMEM = 3,
+  ST_SINGULAR = 4,
+  ST_NONFINITE = 5,
+  ST_TIMEOUT = 6,
+  ST_NOCONV = 7,
+  ST_UNSUPPORTED = 8,
+};
+
+// C[out] = alpha * sum_k A[a_off(out) + a_k(k)] * B[b_off(out) + b_k(k)] + beta * C[out]
+// out is the row-major multi-index over out_dim[0..nout-1]; C is dense in
+// that order unless c_stride is given.
+struct Contraction {
+  int nout, nk;
+  int out_dim[kMaxOut];
+  int k_dim[kMaxK];
+  int64_t a_os[kMaxOut], a_ks[kMaxK];
+  int64_t b_os[kMaxOut], b_ks[kMaxK];
+  int64_t c_os[kMaxOut];
+  int64_t total;   // product of out_dim
+  int64_t ktotal;  // product of k_dim
+};
+
+// Offsets of output element e (row-major over out_dim) in A, B and C.
+__device__ __forceinline__ void contract_offsets(const Contraction& c, int64_t e, int64_t& ao,
+                                                 int64_t& bo, int64_t& co) {
+  int64_t rem = e;
+  ao = 0; bo = 0; co = 0;
+#pragma unroll
+  for (int q = kMaxOut - 1; q >= 0; --q) {
+    if (q < c.nout) {
+      int64_t iq = rem % c.out_dim[q];
+      rem /= c.out_dim[q];
+      ao += iq * c.a_os[q];
+      bo += iq * c.b_os[q];
+      co += iq * c.c_os[q];
+    }
+  }
+}
+
+// The contraction sum of one output element.
+template <typename T>
+__device__ __forceinline__ T contract_sum(const Contraction& c, const T* __restrict__ A,
+                                          const T* __restrict__ B, int64_t ao, int64_t bo) {
+  T acc = T(0);
+  if (c.nk == 1) {
+    const int64_t sa = c.a_ks[0], sb = c.b_ks[0];
+    const T* pa = A + ao;
+    const T* pb = B + bo;
+    for (int k = 0; k < c.k_dim[0]; ++k) acc += pa[k * sa] * pb[k * sb];
+  } else if (c.nk == 2) {
+    const int64_t sa = c.a_ks[1], sb = c.b_ks[1];
+    for (int k0 = 0; k0 < c.k_dim[0]; ++k0) {
+      const T* pa = A + ao + k0 * c.a_ks[0];
+      const T* pb = B + bo + k0 * c.b_ks[0];
+      for (int k1 = 0; k1 < c.k_dim[1]; ++k1) acc += pa[k1 * sa] * pb[k1 * sb];
+    }
+  } else if (c.nk == 3) {
+    const int64_t sa = c.a_ks[2], sb = c.b_ks[2];
+    for (int k0 = 0; k0 < c.k_dim[0]; ++k0)
+      for (int k1 = 0; k1 < c.k_dim[1]; ++k1) {
+        const T* pa = A + ao + k0 * c.a_ks[0] + k1 * c.a_ks[1];
+        const T* pb = B + bo + k0 * c.b_ks[0] + k1 * c.b_ks[1];
+        for (int k2 = 0; k2 < c.k_dim[2]; ++k2) acc += pa[k2 * sa] * pb[k2 * sb];
+      }
+  } else {  // nk == 0: elementwise product
+    acc = A[ao] * B[bo];
+  }
+  return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ void contract_range(const Contraction& c, const T* __restrict__ A,
+                                               const T* __restrict__ B, T* __restrict__ C,
+                                               T alpha, T beta, int64_t first, int64_t step) {
+  for (int64_t e = first; e < c.total; e += step) {
+    int64_t ao, bo, co;
+    contract_offsets(c, e, ao, bo, co);
+    T out = alpha * contract_sum(c, A, B, ao, bo);
+    if (beta != T(0)) out += beta * C[co];
+    C[co] = out;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// grid barrier with a bounded spin
+// ---------------------------------------------------------------------------
+
+constexpr unsigned kSpinLimit = 1u << 24;  // ~1-2 s of polling with nanosleep
+
+struct GridBarrier {
+  unsigned* count;  // arrivals in the current generation
+  unsigned* gen;    // generation counter
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Returns false (all threads of the CTA) if the barrier timed out or another
+// CTA has already flagged an error in *status.
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    unsigned g = ld_acquire_u32(b.gen);
+    unsigned arrived = atom_add_acq_rel_u32(b.count, 1u);
+    if (arrived == gridDim.x - 1) {
+      *b.count = 0u;
+      st_release_u32(b.gen, g + 1u);
+    } else {
+      unsigned spins = 0;
+      while (ld_acquire_u32(b.gen) == g) {
+        if (++spins > kSpinLimit) {
+          atomicCAS(status, ST_OK, ST_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    if (ok && ld_acquire_s32(status) != ST_OK) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-reduce `nv` per-thread values (vals[0..nv-1]) into out[0..nv-1]
+// (valid in every thread afterwards).  scratch: >= (blockDim/32) * nv doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum_n(double (&vals)[NV], int nv, double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < nv; ++k) {
+    double v = warp_sum(vals[k]);
+    if (lane == 0) scratch[warp * NV + k] = v;
+  }
+  __syncthreads();
+  for (int k = 0; k < nv; ++k) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += scratch[w * NV + k];
+    vals[k] = s;
+  }
+  __syncthreads();
+}
+
+// Reduce the per-CTA partials partials[b * stride + k] (b < gridDim.x,
+// k < nv) into out[k] in shared memory, identically in every CTA.
+__device__ __forceinline__ void reduce_partials(const double* partials, int stride, int nv, double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = warp; k < nv; k += nw) {
+    double s = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(partials + (int64_t)b * stride + k);
+    s = warp_sum(s);
+    if (lane == 0) out[k] = s;
+  }
+  __syncthreads();
+}
+
+}  // namespace ttals

@@ -1,0 +1,114 @@
+// Host-side declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "ttals_device.cuh"
+
+namespace ttals {
+
+// ---------------------------------------------------------------------------
+// contraction descriptors (host builders)
+// ---------------------------------------------------------------------------
+
+struct Axis {          // one output or contraction axis
+  int64_t dim;
+  int64_t sa, sb, sc;  // strides in A, B, C (sc unused for contraction axes)
+};
+
+Contraction make_contraction(const std::vector<Axis>& out, const std::vector<Axis>& k);
+
+// y -> M y for the local operator M[(a',m,s'),(a,n,s)] =
+//   sum_{R,R'} L[a,R,a'] A[R,m,n,R'] Rt[s,R',s']  (square: a'=a, s'=s, m=n)
+struct LocalShape {
+  int64_t a, n, s, R0, R1;
+  int64_t N() const { return a * n * s; }
+  int64_t t1() const { return R0 * a * n * s; }  // T1[R, a', n, s]
+  int64_t t2() const { return a * n * s * R1; }  // T2[a', m, s, R']
+};
+void local_apply_descs(const LocalShape& sh, Contraction* p1, Contraction* p2, Contraction* p3);
+
+// ---------------------------------------------------------------------------
+// kernel launchers (kernels_basic.cu)
+// ---------------------------------------------------------------------------
+
+template <typename T>
+cudaError_t launch_contract(const Contraction& c, const T* A, const T* B, T* C, T alpha, T beta,
+                            cudaStream_t st);
+cudaError_t launch_fill(double* p, int64_t n, double v, cudaStream_t st);
+cudaError_t launch_to_float(const double* src, float* dst, int64_t n, cudaStream_t st);
+cudaError_t launch_scale(double* p, int64_t n, const double* scale_dev, int invert, cudaStream_t st);
+
+// Householder QR of the rows x cols matrix M(i, j) = in[i*ris + j*rjs].
+// Writes Q (rows x k, k = min(rows, cols)) to q[i*qis + j*qjs] and R
+// (k x cols) to r[i*ris_r + j*rjs_r] (r may be null).  If normalize_r, R is
+// divided by its Frobenius norm (used where only the gauge matters) and the
+// norm is stored in *rnorm (may be null).  work: rows*cols + 2*rows*k + k
+// doubles.
+struct QrArgs {
+  const double* in; int64_t ris, rjs;
+  double* q; int64_t qis, qjs;
+  double* r; int64_t r_is, r_js;
+  int64_t rows, cols;
+  int normalize_r;
+  double* rnorm;
+  double* work;
+};
+cudaError_t launch_qr(const QrArgs& a, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// persistent Krylov solvers (kernels_krylov.cu)
+// ---------------------------------------------------------------------------
+
+struct GmresLaunch {
+  LocalShape sh;
+  const double *L64, *A64, *R64;
+  const void *Li, *Ai, *Ri;  // inner-precision copies (float for MIXED; == *64 for FP64)
+  double *T1_64, *T2_64;
+  void *T1i, *T2i;
+  const double* f;
+  double* x;
+  double* r;
+  void* V;
+  void* w;
+  double* partials;
+  int m, max_cycles;
+  double tol, inner_floor;
+  unsigned* bar;  // 2 unsigned: count, generation
+  int* status;
+  double* report;  // 4 doubles: rel residual, cycles, inner iterations, flag
+  int precision;   // 0 fp64, 1 mixed
+};
+// grid: one CTA per SM (cooperative launch)
+cudaError_t launch_gmres(const GmresLaunch& g, int num_sms, cudaStream_t st);
+size_t gmres_partials_doubles(int m, int num_sms);
+
+struct LanczosLaunch {
+  LocalShape sh;
+  const double *L, *A, *R;
+  double *T1, *T2;
+  int nprev;               // deflation vectors: M += shift * t t^T
+  const double* prevt;     // nprev x N
+  double shift;
+  double* x;               // in: start vector (N); out: eigenvectors (N x k, column k contiguous)
+  double* vals;            // out: k eigenvalues
+  double* V;               // (m+1) x N
+  double* w;               // N
+  double* partials;
+  int m, k, mode;          // mode 0: largest, 1: closest to sigma, 2: smallest
+  double sigma;
+  int max_restarts;
+  double tol;
+  unsigned* bar;
+  int* status;
+  double* report;          // rel residual, restarts, iterations
+};
+cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st);
+size_t lanczos_partials_doubles(int m, int num_sms);
+size_t lanczos_smem_bytes(int m);
+
+}  // namespace ttals

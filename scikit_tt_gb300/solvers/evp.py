@@ -1,0 +1,82 @@
+"""Alternating linear scheme for (symmetric) eigenproblems in the TT format, on
+the GPU.
+
+Drop-in for ``scikit_tt/solvers/evp.py``: ``als`` keeps its signature
+(evp.py:17-27) and return convention ``(eigenvalue(s), eigentensor(s),
+iterations)``.  The sweep runs in ``libttals.so`` (``ttals_evp_als``): the
+local eigenproblem is solved matrix-free by Lanczos with full
+reorthogonalisation, and the eigenvalue is selected by the reference's rule
+for ``solver`` -- largest for ``'eigh'`` (evp.py:434-439), closest to
+``sigma`` for ``'eig'`` / ``'eigs'`` (evp.py:417-432).
+
+Implemented: symmetric operators, ``number_ev == 1``, ``previous`` / ``shift``
+deflation, ``operator_gevp`` equal to the identity train.  Other cases raise
+``NotImplementedError`` (general generalised problems, ``number_ev > 1``).
+"""
+
+from __future__ import annotations
+
+from typing import List
+
+import numpy as np
+
+from .. import _lib
+from ..tensor_train import TT
+
+last_stats = {}
+
+
+def _is_identity(op: TT) -> bool:
+    if op is None:
+        return True
+    return all(c.shape[0] == 1 and c.shape[3] == 1 and c.shape[1] == c.shape[2]
+               and np.array_equal(c[0, :, :, 0], np.eye(c.shape[1])) for c in op.cores)
+
+
+def _is_symmetric(op: TT) -> bool:
+    return all(np.allclose(c, np.transpose(c, (0, 2, 1, 3)), rtol=0, atol=1e-14 * max(1.0, np.abs(c).max()))
+               for c in op.cores)
+
+
+def als(operator: 'TT', initial_guess: 'TT', previous: List['TT'] = [], shift: float = 0,
+        operator_gevp: 'TT' = None, number_ev: int = 1, repeats: int = 1, conv_eps: float = 1e-10,
+        solver: str = 'eig', sigma: float = 1, real: bool = True):
+    """ALS eigensolver with the signature of evp.py:17-27."""
+    global last_stats
+    if solver not in _lib.EVP_SOLVERS:
+        raise ValueError("solver must be 'eig', 'eigs' or 'eigh'")
+    if not _is_identity(operator_gevp):
+        raise NotImplementedError('generalised eigenproblems (operator_gevp other than the identity) are not '
+                                  'implemented on the device path')
+    if not _is_symmetric(operator):
+        raise NotImplementedError('the device eigen path needs a symmetric operator (core-wise symmetric cores)')
+    if number_ev != 1:
+        raise NotImplementedError('number_ev > 1 is not implemented on the device path')
+    op, x0 = _lib.Packed(operator.cores), _lib.Packed(initial_guess.cores)
+    prev = [_lib.Packed(p.cores) for p in previous]
+    prev_arr = (_lib.TTDesc * max(1, len(prev)))(*[p.desc for p in prev]) if prev else None
+    lib = _lib.load()
+    dims = np.array(operator.row_dims, dtype=np.int64)
+    ranks = np.zeros(operator.order + 1, dtype=np.int64)
+    _lib.check(lib.ttals_als_ranks(operator.order, _lib.i64ptr(dims), _lib.i64ptr(x0.ranks), _lib.i64ptr(ranks)))
+    total = int(sum(max(ranks[i], x0.ranks[i]) * dims[i] * max(ranks[i + 1], x0.ranks[i + 1])
+                    for i in range(operator.order)))
+    out = np.empty(max(total, 1), dtype=np.float64)
+    out_ranks = np.zeros(operator.order + 1, dtype=np.int64)
+    vals = np.zeros(max(1, number_ev), dtype=np.float64)
+    its = _lib.C.c_int32(0)
+    st = _lib.Stats()
+    _lib.check(lib.ttals_evp_als(_lib.context(), op.desc, x0.desc, len(prev), prev_arr, float(shift),
+                                 int(number_ev), int(repeats), float(conv_eps), _lib.EVP_SOLVERS[solver],
+                                 float(sigma), _lib.PREC_FP64, 0.0, _lib.dptr(vals), _lib.dptr(out), 0,
+                                 _lib.i64ptr(out_ranks), _lib.C.byref(its), st))
+    last_stats = st.as_dict()
+    if repeats < 1:
+        return np.inf, None, 0
+    cores = _lib.unpack(out, operator.row_dims, [1] * operator.order, out_ranks)
+    return np.float64(vals[0]), TT(cores), int(its.value)
+
+
+def power_method(operator, initial_guess, operator_gevp=None, repeats=10, sigma=0.999):
+    """Inverse power iteration (evp.py:182-250) is not on the device path yet."""
+    raise NotImplementedError('evp.power_method is not implemented on the device path')

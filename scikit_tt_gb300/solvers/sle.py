@@ -1,0 +1,134 @@
+"""Alternating linear scheme for ``A x = b`` in the TT format, on the GPU.
+
+Drop-in for ``scikit_tt/solvers/sle.py``: ``als`` keeps its signature
+(sle.py:10) and returns a host ``TT``.  The whole sweep -- interface stacks,
+local right-hand sides, matrix-free local solves, QR/RQ re-gauging -- runs in
+``libttals.so``; see ``ttals_sle_als`` in ``include/ttals.h``.
+
+Precision is chosen outside the reference signature (module attribute
+``PRECISION`` or the ``als_ex`` entry point): ``'fp64'`` (default, parity with
+the reference to round-off) or ``'mixed'`` (FP32 Krylov inner solves with
+FP64 residual refinement).
+
+The private helpers that ``scikit_tt/solvers/ode.py:13`` imports by name are
+provided with the same names and in-place semantics (real data).
+"""
+
+from __future__ import annotations
+
+from typing import List
+
+import numpy as np
+
+from .. import _lib
+from ..tensor_train import TT
+
+PRECISION = 'fp64'
+_PREC = {'fp64': _lib.PREC_FP64, 'mixed': _lib.PREC_MIXED}
+
+last_stats = {}
+
+
+def als_ex(operator: TT, initial_guess: TT, right_hand_side: TT, repeats: int = 1, solver: str = 'solve',
+           precision: str = None, tol: float = 0.0):
+    """``als`` plus engine options; returns ``(solution, stats)``.
+
+    ``tol`` is the relative residual every local system is solved to (0 picks
+    1e-13 for fp64 and 1e-10 for mixed)."""
+    if solver not in _lib.SLE_SOLVERS:
+        # the reference silently skips the local solve for unknown strings
+        # (sle.py:505-509); the device path refuses instead
+        raise ValueError("solver must be 'solve' or 'lu'")
+    precision = precision or PRECISION
+    if precision not in _PREC:
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    op, x0, b = _lib.Packed(operator.cores), _lib.Packed(initial_guess.cores), _lib.Packed(right_hand_side.cores)
+    lib = _lib.load()
+    dims = np.array(operator.row_dims, dtype=np.int64)
+    ranks = np.zeros(operator.order + 1, dtype=np.int64)
+    if repeats > 0:
+        _lib.check(lib.ttals_als_ranks(operator.order, _lib.i64ptr(dims), _lib.i64ptr(x0.ranks),
+                                       _lib.i64ptr(ranks)))
+    else:
+        ranks[:] = x0.ranks
+    total = int(sum(ranks[i] * dims[i] * ranks[i + 1] for i in range(operator.order)))
+    out = np.empty(max(total, 1), dtype=np.float64)
+    out_ranks = np.zeros(operator.order + 1, dtype=np.int64)
+    st = _lib.Stats()
+    _lib.check(lib.ttals_sle_als(_lib.context(), op.desc, x0.desc, b.desc, int(repeats), _lib.SLE_SOLVERS[solver],
+                                 _PREC[precision], float(tol), _lib.dptr(out), 0, _lib.i64ptr(out_ranks), st))
+    if repeats == 0:
+        # the reference returns the untouched copy of the initial guess
+        return initial_guess.copy(), st.as_dict()
+    cores = _lib.unpack(out, operator.row_dims, [1] * operator.order, out_ranks)
+    return TT(cores), st.as_dict()
+
+
+def als(operator: 'TT', initial_guess: 'TT', right_hand_side: 'TT', repeats: int = 1, solver: str = 'solve') -> 'TT':
+    """Alternating linear scheme (Holtz, Rohwedder, Schneider 2012), signature of
+    sle.py:10.  Returns the approximate solution of ``operator @ x =
+    right_hand_side`` after ``repeats`` forward+backward sweeps."""
+    global last_stats
+    sol, last_stats = als_ex(operator, initial_guess, right_hand_side, repeats, solver)
+    return sol
+
+
+def mals(operator: 'TT', initial_guess: 'TT', right_hand_side: 'TT', repeats: int = 1, solver: str = 'solve',
+         threshold: float = 1e-12, max_rank: int = np.inf) -> 'TT':
+    """Two-site MALS (sle.py:98) is not on the device path yet."""
+    raise NotImplementedError('sle.mals is not implemented on the device path')
+
+
+# ---------------------------------------------------------------------------
+# private helpers imported by scikit_tt/solvers/ode.py:13 (device-backed)
+# ---------------------------------------------------------------------------
+
+def _stack(left, stack, x, op):
+    r0, n, _, r1 = x.shape
+    R0, R1 = op.shape[0], op.shape[3]
+    stack = np.ascontiguousarray(stack, dtype=np.float64)
+    xc = np.ascontiguousarray(x[:, :, 0, :], dtype=np.float64)
+    oc = np.ascontiguousarray(op, dtype=np.float64)
+    out = np.empty((r1, R1, r1) if left else (r0, R0, r0), dtype=np.float64)
+    _lib.check(_lib.load().ttals_stack_op(_lib.context(), 1 if left else 0, _lib.dptr(stack), _lib.dptr(xc),
+                                          _lib.dptr(oc), r0, n, r1, R0, R1, _lib.dptr(out), 0))
+    return out
+
+
+def __construct_stack_left_op(i: int, stack_left_op: List[np.ndarray], operator: 'TT', solution: 'TT'):
+    """In-place left operator stack (sle.py:194-219) on the device."""
+    if i == 0:
+        stack_left_op[i] = np.array([1], ndmin=3)
+    else:
+        stack_left_op[i] = _stack(True, stack_left_op[i - 1], solution.cores[i - 1], operator.cores[i - 1])
+
+
+def __construct_stack_right_op(i: int, stack_right_op: List[np.ndarray], operator: 'TT', solution: 'TT'):
+    """In-place right operator stack (sle.py:250-276) on the device."""
+    if i == operator.order - 1:
+        stack_right_op[i] = np.array([1], ndmin=3)
+    else:
+        stack_right_op[i] = _stack(False, stack_right_op[i + 1], solution.cores[i + 1], operator.cores[i + 1])
+
+
+def __construct_micro_matrix_als(i: int, stack_left_op: List[np.ndarray], stack_right_op: List[np.ndarray],
+                                 operator: 'TT', solution: 'TT') -> np.ndarray:
+    """Dense local operator (sle.py:308-347), assembled on the device."""
+    r0, r1, n = solution.ranks[i], solution.ranks[i + 1], operator.row_dims[i]
+    R0, R1 = operator.ranks[i], operator.ranks[i + 1]
+    L = np.ascontiguousarray(stack_left_op[i], dtype=np.float64)
+    A = np.ascontiguousarray(operator.cores[i], dtype=np.float64)
+    Rt = np.ascontiguousarray(stack_right_op[i], dtype=np.float64)
+    for arr in (L, A, Rt):
+        if np.iscomplexobj(arr):
+            raise NotImplementedError('complex operators are not supported by the device path')
+    N = r0 * n * r1
+    out = np.empty((N, N), dtype=np.float64)
+    _lib.check(_lib.load().ttals_micro_matrix(_lib.context(), _lib.dptr(L), _lib.dptr(A), _lib.dptr(Rt), r0, n, r1,
+                                              R0, R1, _lib.dptr(out), 0))
+    return out
+
+
+def __construct_micro_matrix_mals(i, stack_left_op, stack_right_op, operator, solution):
+    """Two-site micro matrix (sle.py:350-390): MALS is not on the device path yet."""
+    raise NotImplementedError('MALS micro matrices are not implemented on the device path')

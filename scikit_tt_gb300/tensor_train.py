@@ -1,0 +1,370 @@
+"""Tensor-train container with the API of ``scikit_tt/tensor_train.py``.
+
+Cores are host NumPy arrays of shape ``(r_i, m_i, n_i, r_{i+1})`` exactly as in
+the reference (tensor_train.py:184-188), so a TT built here can be handed to
+code written for scikit_tt.  The operations of the ALS hot path run on the
+GPU through ``libttals.so``:
+
+* ``__matmul__`` / ``dot``  -- device core products  (tensor_train.py:422-524)
+* ``ortho_left`` / ``ortho_right`` / ``ortho`` -- device Householder QR/RQ
+  sweeps (tensor_train.py:1092-1332)
+* ``norm(p=2)`` -- device QR sweep with a log-carried scale
+  (tensor_train.py:1334-1430; immune to the over/underflow the SVD-based
+  reference meets on unnormalised trains)
+
+Structural helpers (``+``, ``-``, scalar ``*``, ``transpose``, ``copy``,
+``element``, ``full``, ``matricize``) are block copies and stay in NumPy.
+Truncated orthonormalisation (``threshold`` > 0 or finite ``max_rank``) is not
+implemented on the device and raises ``NotImplementedError``.
+"""
+
+from __future__ import annotations
+
+from typing import List, Optional, Union
+
+import numpy as np
+
+from . import _lib
+
+
+class TT(object):
+    """Tensor train (Oseledets 2011) with the attribute set of scikit_tt's TT:
+    ``order, row_dims, col_dims, ranks, cores``."""
+
+    def __init__(self, x: Union[List[np.ndarray], np.ndarray], threshold: float = 0, max_rank: int = np.inf,
+                 progress: bool = False, string: str = None):
+        if isinstance(x, list):
+            if all(c.ndim == 4 for c in x):
+                if all(x[i].shape[3] == x[i + 1].shape[0] for i in range(len(x) - 1)):
+                    self.order = len(x)
+                    self.row_dims = [c.shape[1] for c in x]
+                    self.col_dims = [c.shape[2] for c in x]
+                    self.ranks = [c.shape[0] for c in x] + [x[-1].shape[3]]
+                    self.cores = x
+                    if threshold != 0 or max_rank != np.inf:
+                        self.ortho(threshold=threshold, max_rank=max_rank)
+                else:
+                    raise ValueError('Shapes of list elements do not match.')
+            else:
+                raise ValueError('List elements must be 4-dimensional arrays.')
+        elif isinstance(x, np.ndarray):
+            if x.ndim % 2 != 0:
+                raise ValueError('Number of dimensions must be a multiple of 2.')
+            self.__init__(_hosvd(x, threshold, max_rank))
+        else:
+            raise TypeError('Parameter must be either a list of cores or an ndarray.')
+
+    def __repr__(self):
+        return ('\n'
+                'Tensor train with order    = {d}, \n'
+                '                  row_dims = {m}, \n'
+                '                  col_dims = {n}, \n'
+                '                  ranks    = {r}'.format(d=self.order, m=self.row_dims, n=self.col_dims,
+                                                         r=self.ranks))
+
+    # ------------------------------------------------------------------ algebra
+    def __add__(self, tt_add: 'TT') -> 'TT':
+        if not isinstance(tt_add, TT):
+            raise TypeError('Unsupported parameter.')
+        if self.row_dims != tt_add.row_dims or self.col_dims != tt_add.col_dims:
+            raise ValueError('Tensor trains must have the same dimensions')
+        d = self.order
+        ranks = [1] + [self.ranks[i] + tt_add.ranks[i] for i in range(1, d)] + [1]
+        cores = []
+        for i in range(d):
+            dt = np.result_type(self.cores[i], tt_add.cores[i])
+            c = np.zeros((ranks[i], self.row_dims[i], self.col_dims[i], ranks[i + 1]), dtype=dt)
+            c[:self.ranks[i], :, :, :self.ranks[i + 1]] = self.cores[i]
+            c[ranks[i] - tt_add.ranks[i]:, :, :, ranks[i + 1] - tt_add.ranks[i + 1]:] = tt_add.cores[i]
+            cores.append(c)
+        return TT(cores)
+
+    def __sub__(self, tt_sub: 'TT') -> 'TT':
+        return self + (-1) * tt_sub.copy()
+
+    def __mul__(self, scalar) -> 'TT':
+        out = self.copy()
+        if isinstance(scalar, (int, float, complex, np.number)):
+            out.cores[0] = scalar * out.cores[0]
+        else:
+            raise TypeError('Unsupported parameter.')
+        return out
+
+    def __rmul__(self, scalar) -> 'TT':
+        return self.copy() * scalar
+
+    def __matmul__(self, tt_mul: 'TT'):
+        """Core-wise product on the device (tensor_train.py:422-501)."""
+        if not isinstance(tt_mul, TT):
+            raise TypeError('Unsupported argument.')
+        if self.col_dims != tt_mul.row_dims:
+            raise ValueError('Dimensions do not match.')
+        a, b = _lib.Packed(self.cores), _lib.Packed(tt_mul.cores)
+        row, col = list(self.row_dims), list(tt_mul.col_dims)
+        ranks = [self.ranks[i] * tt_mul.ranks[i] for i in range(self.order + 1)]
+        total = sum(ranks[i] * row[i] * col[i] * ranks[i + 1] for i in range(self.order))
+        out = np.empty(total, dtype=np.float64)
+        lib = _lib.load()
+        _lib.check(lib.ttals_tt_matmul(_lib.context(), a.desc, b.desc, _lib.dptr(out), 0))
+        prod = TT(_lib.unpack(out, row, col, ranks))
+        if np.prod(prod.row_dims) == 1 and np.prod(prod.col_dims) == 1:
+            return prod.element([0] * prod.order * 2)
+        return prod
+
+    def dot(self, tt_mul: 'TT'):
+        return self.__matmul__(tt_mul)
+
+    def transpose(self, cores: Optional[List[int]] = None, conjugate: bool = False, overwrite: bool = False) -> 'TT':
+        if cores is None:
+            cores = np.arange(0, self.order)
+        t = self.copy() if overwrite is False else self
+        for i in range(self.order):
+            if np.isin(i, cores):
+                t.cores[i] = np.transpose(t.cores[i], [0, 2, 1, 3])
+                t.row_dims[i], t.col_dims[i] = t.col_dims[i], t.row_dims[i]
+                if conjugate:
+                    t.cores[i] = np.conj(t.cores[i])
+        return t
+
+    def conj(self, overwrite: bool = False) -> 'TT':
+        t = self.copy() if overwrite is False else self
+        for i in range(self.order):
+            t.cores[i] = np.conj(t.cores[i])
+        return t
+
+    def isoperator(self) -> bool:
+        return not (all(i == 1 for i in self.row_dims) or all(i == 1 for i in self.col_dims))
+
+    def copy(self) -> 'TT':
+        return TT([c.copy() for c in self.cores])
+
+    def element(self, indices: List[int]):
+        if not isinstance(indices, list):
+            raise TypeError('Unsupported parameter.')
+        if not all(isinstance(i, (int, np.integer)) for i in indices):
+            raise TypeError('Indices must be integers.')
+        if len(indices) != 2 * self.order:
+            raise ValueError('Number of indices must be twice the order of the tensor train.')
+        d = self.order
+        if not (all(i >= 0 for i in indices) and all(indices[i] < self.row_dims[i] for i in range(d))
+                and all(indices[d + i] < self.col_dims[i] for i in range(d))):
+            raise IndexError('Indices out of range.')
+        v = self.cores[0][:, indices[0], indices[d], :].reshape(1, self.ranks[1])
+        for i in range(1, d):
+            v = v.dot(self.cores[i][:, indices[i], indices[d + i], :].reshape(self.ranks[i], self.ranks[i + 1]))
+        return v[0, 0]
+
+    def full(self) -> np.ndarray:
+        if self.ranks[0] != 1 or self.ranks[-1] != 1:
+            raise ValueError('The first and last rank have to be 1!')
+        f = self.cores[0].reshape(self.row_dims[0] * self.col_dims[0], self.ranks[1])
+        for i in range(1, self.order):
+            f = f.dot(self.cores[i].reshape(self.ranks[i], -1))
+            f = f.reshape(-1, self.ranks[i + 1])
+        p = [None] * 2 * self.order
+        p[::2] = self.row_dims
+        p[1::2] = self.col_dims
+        q = [2 * i for i in range(self.order)] + [1 + 2 * i for i in range(self.order)]
+        return f.reshape(p).transpose(q)
+
+    def matricize(self) -> np.ndarray:
+        mat = self.cores[0].reshape(self.row_dims[0], self.col_dims[0], self.ranks[1])
+        for i in range(1, self.order):
+            mat = np.tensordot(mat, self.cores[i], axes=(2, 0))
+            mat = mat.transpose([0, 2, 1, 3, 4]).reshape((int(np.prod(self.row_dims[:i + 1])),
+                                                           int(np.prod(self.col_dims[:i + 1])), self.ranks[i + 1]))
+        m, n = int(np.prod(self.row_dims)), int(np.prod(self.col_dims))
+        return mat.reshape(m) if n == 1 else mat.reshape(m, n)
+
+    # ------------------------------------------------------- orthonormalisation
+    def _ortho(self, direction, first, last):
+        p = _lib.Packed(self.cores)
+        out = np.empty(p.data.size, dtype=np.float64)
+        ranks = np.zeros(self.order + 1, dtype=np.int64)
+        lib = _lib.load()
+        _lib.check(lib.ttals_tt_ortho(_lib.context(), p.desc, direction, first, last, _lib.dptr(out), 0,
+                                      _lib.i64ptr(ranks)))
+        self.cores = _lib.unpack(out, self.row_dims, self.col_dims, ranks)
+        self.ranks = [int(r) for r in ranks]
+        return self
+
+    @staticmethod
+    def _check_trunc(threshold, max_rank):
+        if not (isinstance(threshold, (int, float, np.floating, np.integer)) and threshold >= 0):
+            raise ValueError('Threshold must be greater or equal 0.')
+        if not ((isinstance(max_rank, (int, np.integer)) and max_rank > 0) or max_rank == np.inf
+                or isinstance(max_rank, list)):
+            raise ValueError('Maximum rank(s) must be positive integers.')
+        if threshold != 0 or (not isinstance(max_rank, list) and max_rank != np.inf) or \
+                (isinstance(max_rank, list) and any(m != np.inf for m in max_rank[1:-1])):
+            raise NotImplementedError('truncated orthonormalisation is not implemented on the device path')
+
+    def ortho_left(self, start_index: int = 0, end_index: Optional[int] = None, threshold: float = 0.0,
+                   max_rank=np.inf, progress: bool = False, string: str = 'Left-orthonormalization') -> 'TT':
+        """Left-orthonormalise cores ``start_index..end_index`` (default
+        ``0..d-2``) by device Householder QR (tensor_train.py:1092-1205)."""
+        if end_index is None:
+            end_index = self.order - 2
+        if not (isinstance(start_index, (int, np.integer)) and isinstance(end_index, (int, np.integer))):
+            raise TypeError('Start and end indices must be integers.')
+        self._check_trunc(threshold, max_rank)
+        return self._ortho(0, int(start_index), int(end_index))
+
+    def ortho_right(self, start_index: Optional[int] = None, end_index: int = 1, threshold: float = 0,
+                    max_rank=np.inf) -> 'TT':
+        """Right-orthonormalise cores ``start_index..end_index`` (default
+        ``d-1..1``) by device Householder RQ (tensor_train.py:1207-1310)."""
+        if start_index is None:
+            start_index = self.order - 1
+        if not (isinstance(start_index, (int, np.integer)) and isinstance(end_index, (int, np.integer))):
+            raise TypeError('Start and end indices must be integers.')
+        self._check_trunc(threshold, max_rank)
+        return self._ortho(1, int(start_index), int(end_index))
+
+    def ortho(self, threshold: float = 0, max_rank=np.inf) -> 'TT':
+        self.ortho_left(threshold=threshold).ortho_right(threshold=threshold, max_rank=max_rank)
+        return self
+
+    def norm(self, p: int = 2) -> float:
+        """p=2: Euclidean / Frobenius norm on the device (tensor_train.py:1404-1425).
+        p=1: Manhattan norm / maximum column sum for non-negative entries."""
+        if p == 1:
+            t = self.copy()
+            if all(i == 1 for i in self.row_dims):
+                t = t.transpose()
+            t.cores = [np.sum(t.cores[i], axis=1).reshape(t.ranks[i], 1, t.col_dims[i], t.ranks[i + 1])
+                       for i in range(t.order)]
+            t.row_dims = [1] * t.order
+            return np.max(t.matricize())
+        if p == 2:
+            cores = self.cores
+            if self.isoperator():
+                cores = [c.reshape(c.shape[0], c.shape[1] * c.shape[2], 1, c.shape[3]) for c in cores]
+            pk = _lib.Packed(cores)
+            out = np.zeros(1, dtype=np.float64)
+            _lib.check(_lib.load().ttals_tt_norm(_lib.context(), pk.desc, _lib.dptr(out)))
+            return float(out[0])
+        raise ValueError('p must be 1 or 2.')
+
+
+def _hosvd(x, threshold, max_rank):
+    """Sequential SVD of a full array into TT cores (tensor_train.py:201-264);
+    input conversion only, not part of the ALS path."""
+    order = x.ndim // 2
+    row_dims, col_dims = x.shape[:order], x.shape[order:]
+    ranks = [1] * (order + 1)
+    cores = []
+    p = [order * j + i for i in range(order) for j in range(2)]
+    y = np.transpose(x, p).copy()
+    for i in range(order - 1):
+        m = ranks[i] * row_dims[i] * col_dims[i]
+        y = y.reshape(m, -1)
+        u, s, v = np.linalg.svd(y, full_matrices=False)
+        if threshold != 0:
+            keep = np.where(s / s[0] > threshold)[0]
+            u, s, v = u[:, keep], s[keep], v[keep, :]
+        if max_rank != np.inf:
+            k = int(min(u.shape[1], max_rank))
+            u, s, v = u[:, :k], s[:k], v[:k, :]
+        ranks[i + 1] = u.shape[1]
+        cores.append(u.reshape(ranks[i], row_dims[i], col_dims[i], ranks[i + 1]))
+        y = np.diag(s).dot(v)
+    cores.append(y.reshape(ranks[-2], row_dims[-1], col_dims[-1], 1))
+    return cores
+
+
+# ---------------------------------------------------------------------------
+# constructors (tensor_train.py:1806-2032)
+# ---------------------------------------------------------------------------
+
+def _rank_list(ranks, d):
+    return ranks if isinstance(ranks, list) else [1] + [ranks] * (d - 1) + [1]
+
+
+def zeros(row_dims, col_dims, ranks=1) -> TT:
+    r = _rank_list(ranks, len(row_dims))
+    return TT([np.zeros([r[i], row_dims[i], col_dims[i], r[i + 1]]) for i in range(len(row_dims))])
+
+
+def ones(row_dims, col_dims, ranks=1) -> TT:
+    r = _rank_list(ranks, len(row_dims))
+    return TT([np.ones([r[i], row_dims[i], col_dims[i], r[i + 1]]) for i in range(len(row_dims))])
+
+
+def eye(dims) -> TT:
+    cores = [np.zeros([1, d, d, 1]) for d in dims]
+    for i, d in enumerate(dims):
+        cores[i][0, :, :, 0] = np.eye(d)
+    return TT(cores)
+
+
+def unit(dims, inds) -> TT:
+    t = zeros(dims, [1] * len(dims))
+    for i in range(t.order):
+        t.cores[i][0, inds[i], 0, 0] = 1
+    return t
+
+
+def rand(row_dims, col_dims, ranks=1) -> TT:
+    """Random TT with U[0,1) cores drawn from NumPy's global generator, in core
+    order (tensor_train.py:1921-1950)."""
+    r = _rank_list(ranks, len(row_dims))
+    return TT([np.random.rand(r[i], row_dims[i], col_dims[i], r[i + 1]) for i in range(len(row_dims))])
+
+
+def canonical(row_dims, max_rank) -> TT:
+    order = len(row_dims)
+    cores = [None] * order
+    rl = 1
+    for i in range(order // 2):
+        k = min(rl * row_dims[i], max_rank)
+        cores[i] = np.eye(rl * row_dims[i], k).reshape(rl, row_dims[i], 1, k)
+        rl = k
+    rr = 1
+    for i in range(order // 2):
+        k = min(rr * row_dims[-i - 1], max_rank)
+        cores[-i - 1] = np.eye(k, row_dims[-i - 1] * rr).reshape(k, row_dims[-i - 1], 1, rr)
+        rr = k
+    if order % 2 == 1:
+        cores[order // 2] = np.eye(rl * row_dims[order // 2], rr).reshape(rl, row_dims[order // 2], 1, rr)
+    return TT(cores)
+
+
+def uniform(row_dims, ranks=1, norm: float = 1) -> TT:
+    r = _rank_list(ranks, len(row_dims))
+    factor = (norm / (np.sqrt(np.prod(row_dims)) * np.prod(r))) ** np.true_divide(1, len(row_dims))
+    return TT([factor * np.ones([r[i], row_dims[i], 1, r[i + 1]]) for i in range(len(row_dims))])
+
+
+def residual_error(operator: TT, lhs: TT, rhs: TT) -> float:
+    """``||operator @ lhs - rhs||`` (tensor_train.py:2035-2074), computed on the
+    device as the norm of the rank-summed train ``A@x - b``."""
+    ax = operator.dot(lhs)
+    return (ax - rhs).norm()
+
+
+def build_core(matrix_list, iscomplex: bool = False) -> np.ndarray:
+    """Operator/vector core from a (nested) list of matrices or zeros
+    (tensor_train.py:2144-2262)."""
+    if isinstance(matrix_list[0], (np.ndarray, int)):
+        mats = [[e] for e in matrix_list]
+    else:
+        mats = matrix_list
+    r1, r2 = len(mats), len(mats[0])
+    shape = None
+    for row in mats:
+        if len(row) != r2:
+            raise ValueError('All lists must contain the same number of matrices.\n')
+        for e in row:
+            if isinstance(e, np.ndarray):
+                shape = (e.shape[0], 1) if e.ndim == 1 else e.shape
+    cplx = iscomplex or any(isinstance(e, np.ndarray) and np.iscomplexobj(e) for row in mats for e in row)
+    core = np.zeros((r1, shape[0], shape[1], r2), dtype=complex if cplx else float)
+    for i in range(r1):
+        for j in range(r2):
+            e = mats[i][j]
+            if isinstance(e, np.ndarray):
+                core[i, :, :, j] = e.reshape(shape)
+            elif e != 0:
+                raise TypeError('Parameters in list must be either an 0 or a matrix.\n')
+    return core

@@ -1,0 +1,153 @@
+"""Seeded synthetic ALS workloads (input construction only).
+
+Five workloads, each a pure function of its seed:
+
+1. ``laplace_sle``    shifted discrete Laplacian, d=10, n=4, operator rank 2,
+                      RHS rank 3 / guess rank 5 (N(0,1), default_rng(0)), 2 sweeps.
+2. ``coupled_sle``    Laplacian + nearest-neighbour coupling sum c_i D (x) D,
+                      d=32, n=8, operator rank 4, RHS rank 8, guess rank 32,
+                      4 sweeps.
+3. ``ising_evp``      transverse-field Ising chain d=48, J=1, g=1 (rank 3),
+                      guess ``rand`` rank 64 from RandomState(1), 6 sweeps.
+4. ``batch_sle``      256 independent instances, instance j from
+                      default_rng(1000 + j): d~U{8..32}, n in {2,4,8},
+                      r~U{4..48}, shift~U(0.5,2), c_i~U(0,0.5), RHS rank 4.
+5. ``serving_stream`` Poisson arrivals (rate 2000/s) mixing 80 % workload-4
+                      SLE requests and 20 % Ising EVP requests.
+
+Laplacian: ``L = tridiag(-1, 2, -1) / h^2`` with h = 1/5 (not rescaled with n).
+Coupling matrix: ``D = diag(linspace(-1, 1, n))``.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+
+from .tensor_train import build_core
+
+
+def laplacian(n: int, h: float = 0.2) -> np.ndarray:
+    return (2.0 * np.eye(n) - np.eye(n, k=1) - np.eye(n, k=-1)) / h ** 2
+
+
+def laplace_op(d: int, n: int, h: float = 0.2, shift: float = 1.0) -> List[np.ndarray]:
+    """``sum_i L_i + shift * I`` as a rank-2 TT operator; the shift is folded
+    into the first core: ``[[L + shift I, I]]``, ``[[I, 0], [L, I]]``, ``[I, L]``."""
+    L, I = laplacian(n, h), np.eye(n)
+    cores = [build_core([[L + shift * I, I]])]
+    cores += [build_core([[I, 0], [L, I]]) for _ in range(1, d - 1)]
+    cores.append(build_core([I, L]))
+    return cores
+
+
+def coupled_op(d: int, n: int, coupling: np.ndarray, h: float = 0.2, shift: float = 1.0) -> List[np.ndarray]:
+    """``sum_i L_i + shift * I + sum_i c_i D_i D_{i+1}`` as a rank-4 TT operator
+    with states {before, D pending, Laplacian done, coupling done}."""
+    L, I = laplacian(n, h), np.eye(n)
+    D = np.diag(np.linspace(-1.0, 1.0, n))
+    cores = [build_core([[I, coupling[0] * D, L + shift * I, 0]])]
+    for i in range(1, d - 1):
+        cores.append(build_core([[I, coupling[i] * D, L, 0], [0, 0, 0, D], [0, 0, I, 0], [0, 0, 0, I]]))
+    cores.append(build_core([L, D, I, I]))
+    return cores
+
+
+def gaussian_tt(rng, d: int, n: int, r: int) -> List[np.ndarray]:
+    ranks = [1] + [r] * (d - 1) + [1]
+    return [rng.standard_normal((ranks[i], n, 1, ranks[i + 1])) for i in range(d)]
+
+
+def ising_op(d: int, coupling: float, field_: float) -> List[np.ndarray]:
+    S = -field_ * np.array([[0.0, 1.0], [1.0, 0.0]])
+    Z = np.array([[1.0, 0.0], [0.0, -1.0]])
+    I = np.eye(2)
+    M = -coupling * Z
+    cores = [build_core([[S, Z, I]])]
+    cores += [build_core([[I, 0, 0], [M, 0, 0], [S, Z, I]]) for _ in range(1, d - 1)]
+    cores.append(build_core([I, M, S]))
+    return cores
+
+
+def uniform_tt(state, d: int, n: int, r: int) -> List[np.ndarray]:
+    """``tt.rand`` cores: U[0,1) in core order from a legacy RandomState."""
+    ranks = [1] + [r] * (d - 1) + [1]
+    return [state.rand(ranks[i], n, 1, ranks[i + 1]) for i in range(d)]
+
+
+@dataclass
+class SLEInstance:
+    op: List[np.ndarray]
+    rhs: List[np.ndarray]
+    x0: List[np.ndarray]
+    repeats: int
+    meta: dict = field(default_factory=dict)
+
+
+@dataclass
+class EVPInstance:
+    op: List[np.ndarray]
+    x0: List[np.ndarray]
+    repeats: int
+    sigma: float
+    meta: dict = field(default_factory=dict)
+
+
+def laplace_sle(d=10, n=4, rhs_rank=3, x_rank=5, repeats=2, seed=0) -> SLEInstance:
+    rng = np.random.default_rng(seed)
+    rhs = gaussian_tt(rng, d, n, rhs_rank)
+    x0 = gaussian_tt(rng, d, n, x_rank)
+    return SLEInstance(laplace_op(d, n), rhs, x0, repeats, dict(d=d, n=n, rhs_rank=rhs_rank, x_rank=x_rank))
+
+
+def coupled_sle(d=32, n=8, rhs_rank=8, x_rank=32, repeats=4, seed=0) -> SLEInstance:
+    c = np.random.default_rng(seed).uniform(0.0, 0.5, d)
+    rng = np.random.default_rng(seed)
+    rhs = gaussian_tt(rng, d, n, rhs_rank)
+    x0 = gaussian_tt(rng, d, n, x_rank)
+    return SLEInstance(coupled_op(d, n, c), rhs, x0, repeats, dict(d=d, n=n, rhs_rank=rhs_rank, x_rank=x_rank))
+
+
+def ising_evp(d=48, g=1.0, x_rank=64, repeats=6, seed=1) -> EVPInstance:
+    x0 = uniform_tt(np.random.RandomState(seed), d, 2, x_rank)
+    sigma = -(d - 1) - g * d - 1.0   # below the spectrum: lowest eigenpair
+    return EVPInstance(ising_op(d, 1.0, g), x0, repeats, sigma, dict(d=d, g=g, x_rank=x_rank))
+
+
+def batch_instance(j: int, repeats: int = 4) -> SLEInstance:
+    rng = np.random.default_rng(1000 + j)
+    d = int(rng.integers(8, 33))
+    n = int(rng.choice([2, 4, 8]))
+    r = int(rng.integers(4, 49))
+    shift = float(rng.uniform(0.5, 2.0))
+    c = rng.uniform(0.0, 0.5, d)
+    op = coupled_op(d, n, c, shift=shift)
+    rhs = gaussian_tt(rng, d, n, 4)
+    x0 = gaussian_tt(rng, d, n, r)
+    return SLEInstance(op, rhs, x0, repeats, dict(j=j, d=d, n=n, r=r, shift=shift))
+
+
+def batch_sle(count: int = 256, repeats: int = 4) -> List[SLEInstance]:
+    return [batch_instance(j, repeats) for j in range(count)]
+
+
+def serving_stream(rate: float = 2000.0, duration: float = 60.0, seed: int = 5, sle_fraction: float = 0.8,
+                   max_requests: int = None):
+    """Yields ``(arrival_time_s, kind, instance)`` in arrival order."""
+    rng = np.random.default_rng(seed)
+    t, k = 0.0, 0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > duration or (max_requests is not None and k >= max_requests):
+            return
+        if rng.uniform() < sle_fraction:
+            yield t, 'sle', batch_instance(int(rng.integers(0, 1 << 30)))
+        else:
+            d = int(rng.integers(16, 49))
+            r = int(rng.integers(16, 65))
+            g = float(rng.uniform(0.5, 1.5))
+            inst = ising_evp(d=d, g=g, x_rank=r, repeats=6, seed=int(rng.integers(0, 1 << 30)))
+            yield t, 'evp', inst
+        k += 1

@@ -1,0 +1,140 @@
+"""Generate the golden fixtures of ``tests/golden/`` from the reference itself.
+
+Runs the unmodified scikit_tt package (imported read-only from the path in
+``SCIKIT_TT_REF``, default ``/root/reference``) on small seeded inputs and
+stores inputs and outputs as ``.npz``.  The oracle and the device engine are
+both checked against these files; the GPU machine never needs the reference.
+
+    python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+REF = os.environ.get('SCIKIT_TT_REF', '/root/reference')
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REF)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import scipy.linalg as sla  # noqa: E402
+import scikit_tt.tensor_train as rtt  # noqa: E402
+import scikit_tt.models as rmodels  # noqa: E402
+import scikit_tt.solvers.sle as rsle  # noqa: E402
+import scikit_tt.solvers.evp as revp  # noqa: E402
+from scikit_tt.tensor_train import TT as RTT  # noqa: E402
+
+from scikit_tt_gb300 import workloads as wl  # noqa: E402
+
+
+def pack(prefix, cores, out):
+    out[prefix + '_n'] = np.array(len(cores))
+    for i, c in enumerate(cores):
+        out[f'{prefix}_{i}'] = np.asarray(c)
+
+
+def sle_case(name, op, rhs, x0, repeats, solver='solve', store_op=True):
+    sol = rsle.als(RTT([c.copy() for c in op]), RTT([c.copy() for c in x0]), RTT([c.copy() for c in rhs]),
+                   repeats=repeats, solver=solver)
+    out = {'repeats': np.array(repeats), 'solver': np.array(solver)}
+    if store_op:
+        pack('op', op, out)
+    pack('rhs', rhs, out)
+    pack('x0', x0, out)
+    pack('sol', sol.cores, out)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'ranks', sol.ranks)
+
+
+def evp_case(name, op, x0, repeats, solver, sigma, negate=False, conv_eps=1e-10):
+    A = RTT([c.copy() for c in op])
+    if negate:
+        A = -1 * A
+    val, vec, its = revp.als(A, RTT([c.copy() for c in x0]), repeats=repeats, solver=solver, sigma=sigma,
+                             conv_eps=conv_eps)
+    out = {'repeats': np.array(repeats), 'solver': np.array(solver), 'sigma': np.array(sigma),
+           'negate': np.array(negate), 'conv_eps': np.array(conv_eps), 'val': np.array(val), 'its': np.array(its)}
+    pack('op', [c.copy() for c in A.cores], out)
+    pack('x0', x0, out)
+    pack('vec', vec.cores, out)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'val', val, 'its', its)
+
+
+def helpers_case():
+    """Module-level helpers that scikit_tt/solvers/ode.py:13 imports."""
+    rng = np.random.default_rng(7)
+    a, n, s, R0, R1 = 5, 3, 4, 2, 3
+    x0c = rng.standard_normal((a, n, 1, s))
+    x1c = rng.standard_normal((s, n, 1, a))
+    A0 = rng.standard_normal((R0, n, n, R1))
+    A1 = rng.standard_normal((R1, n, n, R0))
+    op, sol = RTT([A0, A1]), RTT([x0c, x1c])
+    Lp = rng.standard_normal((a, R0, a))
+    Rn = rng.standard_normal((a, R0, a))
+    Ls = rng.standard_normal((a, R0, a))
+    Rs = rng.standard_normal((s, R1, s))
+    sl, sr = [Lp, None], [None, Rn]
+    getattr(rsle, '__construct_stack_left_op')(1, sl, op, sol)
+    getattr(rsle, '__construct_stack_right_op')(0, sr, op, sol)
+    M = getattr(rsle, '__construct_micro_matrix_als')(0, [Ls], [Rs], op, sol)
+    out = dict(x0c=x0c, x1c=x1c, A0=A0, A1=A1, Lp=Lp, Rn=Rn, Ls=Ls, Rs=Rs, left=sl[1], right=sr[0], micro=M)
+    np.savez_compressed(os.path.join(HERE, 'helpers.npz'), **out)
+    print('helpers', M.shape)
+
+
+def ttops_case():
+    rng = np.random.default_rng(11)
+    d = 5
+    ranks = [1, 3, 4, 2, 3, 1]
+    dims = [2, 3, 2, 3, 2]
+    t = [rng.standard_normal((ranks[i], dims[i], 1, ranks[i + 1])) for i in range(d)]
+    opr = [1, 2, 3, 2, 2, 1]
+    A = [rng.standard_normal((opr[i], dims[i], dims[i], opr[i + 1])) for i in range(d)]
+    At = RTT([c.copy() for c in A])
+    tt_ = RTT([c.copy() for c in t])
+    prod = At.dot(tt_)
+    out = dict(norm=np.array(tt_.norm()), opnorm=np.array(At.norm()), full=tt_.full().reshape(-1),
+               prod_full=prod.full().reshape(-1),
+               left_full=RTT([c.copy() for c in t]).ortho_left().full().reshape(-1),
+               right_full=RTT([c.copy() for c in t]).ortho_right().full().reshape(-1))
+    pack('t', t, out)
+    pack('A', A, out)
+    np.savez_compressed(os.path.join(HERE, 'ttops.npz'), **out)
+    print('ttops norm', out['norm'])
+
+
+def main():
+    # workload 1 (exact) with both local solvers
+    w1 = wl.laplace_sle()
+    sle_case('sle_laplace_d10', w1.op, w1.rhs, w1.x0, w1.repeats, 'solve')
+    sle_case('sle_laplace_d10_lu', w1.op, w1.rhs, w1.x0, w1.repeats, 'lu')
+    # workload 1 at rank 8, 4 sweeps (deeper convergence)
+    w1b = wl.laplace_sle(x_rank=8, repeats=4)
+    sle_case('sle_laplace_d10_r8', w1b.op, w1b.rhs, w1b.x0, w1b.repeats, 'solve')
+    # reduced workload 2 (coupled operator, rank 4)
+    w2 = wl.coupled_sle(d=8, n=4, rhs_rank=4, x_rank=8, repeats=3)
+    sle_case('sle_coupled_d8', w2.op, w2.rhs, w2.x0, w2.repeats, 'solve')
+    # the reference's own known-answer SLE test: Toeplitz(1..1024) as an order-10 TT
+    # (the operator is rebuilt by the tests: its untruncated TT is 17 MB)
+    mat = sla.toeplitz(np.arange(1, 2 ** 10 + 1), np.arange(1, 2 ** 10 + 1)).astype(float)
+    op = RTT(mat.reshape([2] * 20))
+    rhs = rtt.ones(op.row_dims, [1] * 10)
+    x0 = rtt.ones(op.row_dims, [1] * 10, ranks=5).ortho_right()
+    sle_case('sle_toeplitz', [c.copy() for c in op.cores], [c.copy() for c in rhs.cores],
+             [c.copy() for c in x0.cores], 1, 'solve', store_op=False)
+    # Ising EVP (lowest eigenpair) both ways the reference allows
+    for d, r in [(12, 16), (16, 16)]:
+        w3 = wl.ising_evp(d=d, x_rank=r, repeats=6)
+        x0o = RTT([c.copy() for c in w3.x0]).ortho_right()
+        evp_case(f'evp_ising_d{d}_eig', w3.op, [c.copy() for c in x0o.cores], 6, 'eig', w3.sigma)
+        evp_case(f'evp_ising_d{d}_eigh', w3.op, [c.copy() for c in x0o.cores], 6, 'eigh', 1.0, negate=True)
+    helpers_case()
+    ttops_case()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,72 @@
+"""The CPU oracle against outputs of the reference itself (tests/golden)."""
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+from oracle import tt_oracle as O
+from scikit_tt_gb300 import workloads as wl
+
+
+@pytest.mark.parametrize('name', ['sle_laplace_d10', 'sle_laplace_d10_lu', 'sle_laplace_d10_r8', 'sle_coupled_d8'])
+def test_oracle_sle_matches_reference(golden, name):
+    z, cores = golden(name)
+    sol = O.sle_als(cores('op'), cores('x0'), cores('rhs'), repeats=int(z['repeats']), solver=str(z['solver']))
+    ref = cores('sol')
+    assert [c.shape for c in sol] == [c.shape for c in ref]
+    assert O.stable_rel_diff(sol, ref) < 1e-12
+
+
+def test_oracle_sle_toeplitz_known_answer(golden):
+    z, cores = golden('sle_toeplitz')
+    mat = sla.toeplitz(np.arange(1, 2 ** 10 + 1), np.arange(1, 2 ** 10 + 1)).astype(float)
+    from scikit_tt_gb300.tensor_train import _hosvd
+    op = _hosvd(mat.reshape([2] * 20), 0, np.inf)
+    sol = O.sle_als(op, cores('x0'), cores('rhs'), repeats=1)
+    exact = np.linalg.solve(mat, np.ones(1024))
+    got = O.full_vector(sol)
+    ref = O.full_vector(cores('sol'))
+    assert np.linalg.norm(got - exact) / np.linalg.norm(exact) < 1e-7      # test_sle.py:53-59 tolerance
+    # cond(Toeplitz) is large: both solutions sit within the reference tolerance of
+    # the exact one and within 1e-6 of each other (operator TT gauges differ)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-6
+
+
+@pytest.mark.parametrize('name', ['evp_ising_d12_eig', 'evp_ising_d12_eigh'])
+def test_oracle_evp_matches_reference(golden, name):
+    z, cores = golden(name)
+    val, vec, its = O.evp_als(cores('op'), cores('x0'), repeats=int(z['repeats']), solver=str(z['solver']),
+                              sigma=float(z['sigma']), conv_eps=float(z['conv_eps']))
+    assert abs(val - float(z['val'])) < 1e-10
+    assert its == int(z['its'])
+    # eigenvectors agree up to sign
+    v, r = O.full_vector(vec), O.full_vector(cores('vec'))
+    assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-7
+
+
+def test_oracle_ising_free_fermion():
+    # E0 of the d=12 chain from free fermions vs the dense spectrum
+    op = wl.ising_op(8, 1.0, 1.0)
+    H = O.full_matrix(op)
+    assert abs(np.linalg.eigvalsh(H)[0] - O.ising_exact_e0(8, 1.0, 1.0)) < 1e-10
+
+
+def test_oracle_helpers_match_reference(golden):
+    z, _ = golden('helpers')
+    left = O.stack_left_op(z['Lp'], z['x0c'][:, :, 0, :], z['A0'])
+    right = O.stack_right_op(z['Rn'], z['x1c'][:, :, 0, :], z['A1'])
+    micro = O.micro_matrix(z['Ls'], z['A0'], z['Rs'])
+    np.testing.assert_allclose(left, z['left'], rtol=1e-13, atol=1e-13 * np.abs(z['left']).max())
+    np.testing.assert_allclose(right, z['right'], rtol=1e-13, atol=1e-13 * np.abs(z['right']).max())
+    np.testing.assert_allclose(micro, z['micro'], rtol=1e-13, atol=1e-13 * np.abs(z['micro']).max())
+
+
+def test_oracle_tt_ops_match_reference(golden):
+    z, cores = golden('ttops')
+    t, A = cores('t'), cores('A')
+    assert abs(O.norm2(t) - float(z['norm'])) < 1e-12 * float(z['norm'])
+    assert abs(O.norm2(A) - float(z['opnorm'])) < 1e-12 * float(z['opnorm'])
+    np.testing.assert_allclose(O.full_vector(O.tt_matmul(A, t)), z['prod_full'], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(O.full_vector(O.ortho_left(t)), z['left_full'], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(O.full_vector(O.ortho_right(t)), z['right_full'], rtol=1e-12, atol=1e-12)
+    assert abs(O.stable_norm(t) - float(z['norm'])) < 1e-12 * float(z['norm'])
