@@ -64,6 +64,12 @@ typedef struct {
   int64_t refinement_steps;   /* FP64 residual evaluations, all local solves   */
   double max_local_residual;  /* worst final relative residual of a local solve */
   double device_ms;           /* device time of the call (CUDA events)         */
+  int64_t kernel_launches;    /* kernels the call launched                      */
+  /* filled only while profiling is on (ttals_set_profiling):                  */
+  int64_t solver_launches;    /* local-solve kernel launches                    */
+  double solver_ms;           /* their summed duration (CUDA events)            */
+  double solver_flops64;      /* algorithmic FP64 flops of the local solves     */
+  double solver_flops32;      /* algorithmic FP32 flops of the local solves     */
 } ttals_stats;
 
 /* Context: one device, one stream, one device-memory arena capped at
@@ -75,6 +81,14 @@ const char* ttals_last_error(const ttals_ctx* ctx);
 /* Run on a caller-provided cudaStream_t (passed as void*); NULL restores the
  * context's own stream. */
 int ttals_set_stream(ttals_ctx* ctx, void* stream);
+
+/* Time every local-solve launch with CUDA events (adds two event records
+ * per launch) and report it in ttals_stats.  No reference counterpart. */
+int ttals_set_profiling(ttals_ctx* ctx, int32_t enable);
+
+/* Measured arithmetic peaks of this device (FMA-chain microbenchmarks), in
+ * GFLOP/s.  Used to state roofline fractions.  No reference counterpart. */
+int ttals_measure_peaks(ttals_ctx* ctx, double* fp64_gflops, double* fp32_gflops);
 
 /* Rank schedule of one ALS run: the ranks of the returned solution for
  * dims/x_ranks, following the economic QR/RQ rank rule of

@@ -36,7 +36,7 @@ EVP_SOLVERS = {'eig': 0, 'eigs': 1, 'eigh': 2}
 EXPORTS = (
     'ttals_create', 'ttals_destroy', 'ttals_last_error', 'ttals_set_stream', 'ttals_als_ranks',
     'ttals_sle_als', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_norm',
-    'ttals_stack_op', 'ttals_micro_matrix',
+    'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
 )
 
 
@@ -47,7 +47,9 @@ class TTDesc(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [('local_solves', C.c_int64), ('krylov_iterations', C.c_int64), ('refinement_steps', C.c_int64),
-                ('max_local_residual', C.c_double), ('device_ms', C.c_double)]
+                ('max_local_residual', C.c_double), ('device_ms', C.c_double), ('kernel_launches', C.c_int64),
+                ('solver_launches', C.c_int64), ('solver_ms', C.c_double), ('solver_flops64', C.c_double),
+                ('solver_flops32', C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -88,6 +90,8 @@ def load():
         lib.ttals_tt_norm.argtypes = [vp, P(TTDesc), pd]
         lib.ttals_stack_op.argtypes = [vp, i32, pd, pd, pd, i64, i64, i64, i64, i64, pd, i32]
         lib.ttals_micro_matrix.argtypes = [vp, pd, pd, pd, i64, i64, i64, i64, i64, pd, i32]
+        lib.ttals_set_profiling.argtypes = [vp, i32]
+        lib.ttals_measure_peaks.argtypes = [vp, pd, pd]
         for name in EXPORTS:
             if name not in ('ttals_last_error',):
                 getattr(lib, name).restype = C.c_int

@@ -42,6 +42,8 @@ struct ttals_ctx {
   size_t arena_cap = 0;
   std::string err;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool profiling = false;
+  std::vector<cudaEvent_t> evpool;  // event pairs around local-solve launches
 };
 
 namespace {
@@ -257,6 +259,11 @@ struct Engine {
   unsigned* bar = nullptr;
   int* status = nullptr;
   int m = 40;
+  struct SolveRec {
+    LocalShape sh;
+    int prec;
+  };
+  std::vector<SolveRec> recs;
   int64_t maxN = 1, maxT = 1, maxCore = 1, maxStackOp = 1, maxStackVec = 1, maxQr = 1, maxR = 1, maxU = 1;
   int nsolve = 0, solve_cap = 0;
 };
@@ -295,6 +302,30 @@ void ortho_initial(Engine& E, const std::vector<int64_t>& x0_off) {
 // ---------------------------------------------------------------------------
 // local solves
 // ---------------------------------------------------------------------------
+
+cudaEvent_t pool_event(ttals_ctx* c, size_t i) {
+  while (c->evpool.size() <= i) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->evpool.push_back(e);
+  }
+  return c->evpool[i];
+}
+
+// bracket one local-solve launch with events when profiling
+template <typename F>
+void timed_solve(Engine& E, const LocalShape& sh, int prec, F&& launch) {
+  const size_t q = E.recs.size();
+  if (E.c->profiling) CK(cudaEventRecord(pool_event(E.c, 2 * q), E.c->stream));
+  launch();
+  if (E.c->profiling) CK(cudaEventRecord(pool_event(E.c, 2 * q + 1), E.c->stream));
+  E.recs.push_back({sh, prec});
+}
+
+double apply_flops(const LocalShape& sh) {
+  const double a = sh.a, n = sh.n, s = sh.s, R0 = sh.R0, R1 = sh.R1;
+  return 2 * a * a * R0 * n * s + 2 * a * s * n * n * R0 * R1 + 2 * a * n * s * s * R1;
+}
 
 void solve_sle_site(Engine& E, int i, double tol) {
   auto& P = E.P;
@@ -344,7 +375,7 @@ void solve_sle_site(Engine& E, int i, double tol) {
     g.inner_floor = 0.0;
     g.precision = 0;
   }
-  CK(launch_gmres(g, E.c->num_sms, E.c->stream));
+  timed_solve(E, sh, E.prec, [&] { CK(launch_gmres(g, E.c->num_sms, E.c->stream)); });
 }
 
 // ---------------------------------------------------------------------------
@@ -362,12 +393,36 @@ void fill_stats(Engine& E, ttals_stats* st, float ms) {
   st->krylov_iterations = 0;
   st->refinement_steps = 0;
   st->max_local_residual = 0.0;
+  st->solver_launches = 0;
+  st->solver_ms = 0.0;
+  st->solver_flops64 = 0.0;
+  st->solver_flops32 = 0.0;
   for (int q = 0; q < cnt; ++q) {
     st->max_local_residual = std::max(st->max_local_residual, rep[4 * q]);
     st->refinement_steps += (int64_t)rep[4 * q + 1];
     st->krylov_iterations += (int64_t)rep[4 * q + 2];
   }
   st->device_ms = ms;
+  st->kernel_launches = launch_counter();
+  if (E.c->profiling && cnt == (int)E.recs.size()) {
+    for (int q = 0; q < cnt; ++q) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, E.c->evpool[2 * q], E.c->evpool[2 * q + 1]));
+      st->solver_ms += t;
+      const double N = (double)E.recs[q].sh.N(), fa = apply_flops(E.recs[q].sh) + 2 * N;
+      const double cycles = rep[4 * q + 1], its = rep[4 * q + 2];
+      // Gram-Schmidt (two passes of dots + updates) over j = 0..it-1 per cycle
+      const double per = cycles > 0 ? its / cycles : its;
+      const double cgs = cycles * 8.0 * N * per * (per + 1) / 2.0;
+      const double inner = its * fa + cgs;
+      st->solver_flops64 += cycles * fa;
+      if (E.recs[q].prec == TTALS_PREC_MIXED)
+        st->solver_flops32 += inner;
+      else
+        st->solver_flops64 += inner;
+    }
+    st->solver_launches = cnt;
+  }
 }
 
 void alloc_common(Engine& E, Bump& B, int64_t op_total, int64_t rhs_total, int64_t x0_total, int n_vec_tt) {
@@ -473,6 +528,7 @@ void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttal
   require(out != nullptr, TTALS_ERR_ARG, "output buffer is null");
   if (tol <= 0) tol = (prec == TTALS_PREC_FP64) ? 1e-13 : 1e-10;
 
+  launch_counter() = 0;
   Engine E;
   E.c = c;
   E.prec = prec;
@@ -606,6 +662,7 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
     validate_vec(prev.back(), op, "previous");
   }
 
+  launch_counter() = 0;
   Engine E;
   E.c = c;
   E.m = 64;
@@ -705,7 +762,7 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
     l.status = E.status;
     l.report = E.reports + 4 * (int64_t)(E.nsolve % E.solve_cap);
     ++E.nsolve;
-    CK(launch_lanczos(l, c->num_sms, c->stream));
+    timed_solve(E, sh, 0, [&] { CK(launch_lanczos(l, c->num_sms, c->stream)); });
   };
 
   for (int i = d - 1; i >= 0; --i) right(i);
@@ -846,6 +903,7 @@ int ttals_destroy(ttals_ctx* c) {
   if (c->arena) cudaFree(c->arena);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (auto e : c->evpool) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return TTALS_OK;
@@ -857,6 +915,19 @@ int ttals_set_stream(ttals_ctx* c, void* stream) {
   if (!c) return TTALS_ERR_ARG;
   c->stream = stream ? (cudaStream_t)stream : c->own;
   return TTALS_OK;
+}
+
+int ttals_set_profiling(ttals_ctx* c, int32_t enable) {
+  if (!c) return TTALS_ERR_ARG;
+  c->profiling = enable != 0;
+  return TTALS_OK;
+}
+
+int ttals_measure_peaks(ttals_ctx* c, double* fp64, double* fp32) {
+  return guarded(c, [&] {
+    require(fp64 && fp32, TTALS_ERR_ARG, "null pointer");
+    CK(measure_fma_peaks(c->stream, c->num_sms, fp64, fp32));
+  });
 }
 
 int ttals_als_ranks(int32_t order, const int64_t* dims, const int64_t* x_ranks, int64_t* out_ranks) {

@@ -8,6 +8,11 @@
 
 namespace ttals {
 
+int64_t& launch_counter() {
+  static thread_local int64_t n = 0;
+  return n;
+}
+
 Contraction make_contraction(const std::vector<Axis>& out, const std::vector<Axis>& k) {
   Contraction c{};
   c.nout = (int)out.size();
@@ -64,6 +69,7 @@ cudaError_t launch_contract(const Contraction& c, const T* A, const T* B, T* C, 
   int64_t blocks = (c.total + 255) / 256;
   blocks = std::min<int64_t>(blocks, 65535);
   contract_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(c, A, B, C, alpha, beta);
+  ++launch_counter();
   return cudaGetLastError();
 }
 template cudaError_t launch_contract<double>(const Contraction&, const double*, const double*, double*,
@@ -79,6 +85,7 @@ cudaError_t launch_fill(double* p, int64_t n, double v, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
   fill_kernel<<<blocks, 256, 0, st>>>(p, n, v);
+  ++launch_counter();
   return cudaGetLastError();
 }
 
@@ -90,6 +97,7 @@ cudaError_t launch_to_float(const double* src, float* dst, int64_t n, cudaStream
   if (n <= 0) return cudaSuccess;
   unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
   to_float_kernel<<<blocks, 256, 0, st>>>(src, dst, n);
+  ++launch_counter();
   return cudaGetLastError();
 }
 
@@ -103,6 +111,7 @@ cudaError_t launch_scale(double* p, int64_t n, const double* scale_dev, int inve
   if (n <= 0) return cudaSuccess;
   unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
   scale_kernel<<<blocks, 256, 0, st>>>(p, n, scale_dev, invert);
+  ++launch_counter();
   return cudaGetLastError();
 }
 
@@ -224,6 +233,52 @@ __global__ void __launch_bounds__(kQrThreads) qr_kernel(QrArgs a) {
 cudaError_t launch_qr(const QrArgs& a, cudaStream_t st) {
   if (a.rows <= 0 || a.cols <= 0) return cudaSuccess;
   qr_kernel<<<1, kQrThreads, 0, st>>>(a);
+  ++launch_counter();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// arithmetic peak microbenchmark: 8 independent FMA chains per thread
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(512) fma_chain_kernel(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3);
+  T x4 = x0 + T(4), x5 = x0 + T(5), x6 = x0 + T(6), x7 = x0 + T(7);
+  for (int i = 0; i < iters; ++i) {
+    x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+    x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+  }
+  out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t measure_fma_peaks(cudaStream_t st, int num_sms, double* fp64, double* fp32) {
+  const int blocks = num_sms * 4, threads = 512;
+  void* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, (size_t)blocks * threads * sizeof(double));
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto run = [&](bool dbl, int iters) -> double {
+    cudaEventRecord(e0, st);
+    if (dbl)
+      fma_chain_kernel<double><<<blocks, threads, 0, st>>>((double*)buf, iters, 0.999, 0.001);
+    else
+      fma_chain_kernel<float><<<blocks, threads, 0, st>>>((float*)buf, iters, 0.999f, 0.001f);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e9;
+  };
+  run(true, 200);
+  *fp64 = std::max(run(true, 4000), run(true, 4000));
+  run(false, 200);
+  *fp32 = std::max(run(false, 40000), run(false, 40000));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
   return cudaGetLastError();
 }
 

@@ -291,6 +291,7 @@ cudaError_t launch_gmres(const GmresLaunch& g, int num_sms, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(gmres_ir_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     void* args[] = {&k};
+    ++launch_counter();
     return cudaLaunchCooperativeKernel((const void*)gmres_ir_kernel<double>, grid, block, args, smem, st);
   }
   GmresK<float> k{p1, p2, p3, (int)g.sh.N(), g.L64, g.A64, g.R64, g.T1_64, g.T2_64,
@@ -300,6 +301,7 @@ cudaError_t launch_gmres(const GmresLaunch& g, int num_sms, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(gmres_ir_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {&k};
+  ++launch_counter();
   return cudaLaunchCooperativeKernel((const void*)gmres_ir_kernel<float>, grid, block, args, smem, st);
 }
 
@@ -668,6 +670,7 @@ cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st)
   cudaError_t e = cudaFuncSetAttribute(lanczos_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {&k};
+  ++launch_counter();
   return cudaLaunchCooperativeKernel((const void*)lanczos_kernel, dim3(num_sms), dim3(kKThreads), args, smem, st);
 }
 

@@ -36,6 +36,13 @@ void local_apply_descs(const LocalShape& sh, Contraction* p1, Contraction* p2, C
 // kernel launchers (kernels_basic.cu)
 // ---------------------------------------------------------------------------
 
+// Kernels launched by this host thread since the last reset (every launch_*
+// wrapper counts itself).
+int64_t& launch_counter();
+
+// FMA-chain throughput of the device in GFLOP/s (FP64 and FP32).
+cudaError_t measure_fma_peaks(cudaStream_t st, int num_sms, double* fp64, double* fp32);
+
 template <typename T>
 cudaError_t launch_contract(const Contraction& c, const T* A, const T* B, T* C, T alpha, T beta,
                             cudaStream_t st);
