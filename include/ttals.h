@@ -138,6 +138,21 @@ int ttals_stack_op(ttals_ctx* ctx, int32_t left, const double* stack, const doub
                    const double* op, int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1,
                    double* out, int32_t on_device);
 
+/* Allocation-free ttals_stack_op, for callers that cannot allocate device
+ * memory (a process whose device memory is pre-reserved by its own pool, a
+ * serving loop that must avoid the synchronisation of cudaMalloc/cudaFree, a
+ * foreign host that only hands over buffers it owns).  No counterpart in the
+ * reference.  All pointers are device pointers; the work is enqueued on the
+ * context's stream and the call returns without waiting.  The intermediates
+ * live in a 16 MiB static device array (2 * max(R0,R1) * max(r0,r1)^2 * n
+ * doubles must fit, else TTALS_ERR_ARG).  The first call on a device looks up
+ * the array's address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race. */
+int ttals_stack_op_noalloc(ttals_ctx* ctx, int32_t left, const double* stack, const double* x,
+                           const double* op, int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1,
+                           double* out);
+
 /* scikit_tt/solvers/sle.py:308-347 `__construct_micro_matrix_als`: dense
  * local operator (r0*n*r1)^2 from stacks L (r0, R0, r0), Rt (r1, R1, r1) and
  * operator core op (R0, n, n, R1). */

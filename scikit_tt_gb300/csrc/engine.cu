@@ -856,6 +856,31 @@ int guarded(ttals_ctx* c, F&& f) {
 
 }  // namespace
 
+namespace ttals {
+
+// Helpers for entry points defined in other translation units.
+int ctx_device(const ttals_ctx* c) { return c->device; }
+void ctx_set_error(ttals_ctx* c, const std::string& msg) { c->err = msg; }
+
+// Enqueue one interface-stack update on the context's stream with the
+// caller's intermediates t1 and t2 (each >= max(R0,R1)*max(r0,r1)^2*n
+// doubles).  All pointers are device pointers; nothing is allocated and the
+// host does not wait for the result.
+int stack_op_on_stream(ttals_ctx* c, int32_t left, const double* stack, const double* x, const double* op,
+                       int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1, double* t1, double* t2,
+                       double* out) {
+  return guarded(c, [&] {
+    require(stack && x && op && out && t1 && t2, TTALS_ERR_ARG, "null pointer");
+    require(r0 > 0 && n > 0 && r1 > 0 && R0 > 0 && R1 > 0, TTALS_ERR_ARG, "dimensions must be positive");
+    if (left)
+      stack_left_op(c, stack, x, op, r0, n, r1, R0, R1, t1, t2, out);
+    else
+      stack_right_op(c, stack, x, op, r0, n, r1, R0, R1, t1, t2, out);
+  });
+}
+
+}  // namespace ttals
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------

@@ -118,4 +118,13 @@ cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st)
 size_t lanczos_partials_doubles(int m, int num_sms);
 size_t lanczos_smem_bytes(int m);
 
+// engine.cu helpers used by the allocation-free entry point (noalloc.cu)
+}  // namespace ttals
+struct ttals_ctx;
+namespace ttals {
+int ctx_device(const ttals_ctx* c);
+void ctx_set_error(ttals_ctx* c, const std::string& msg);
+int stack_op_on_stream(ttals_ctx* c, int32_t left, const double* stack, const double* x, const double* op,
+                       int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1, double* t1, double* t2,
+                       double* out);
 }  // namespace ttals
