@@ -3,16 +3,18 @@
 
 Workload: SLE ALS on the coupled Laplacian (d=32 sites, mode size n=8,
 operator rank 4, right-hand side rank 8, solution rank 32, 4 sweeps, seeded
-inputs).  A *step* is one full solve.
+inputs).  A *step* is one batch of independent solves of that workload (2 per
+SM by default) in one launch, one CTA per solve.
 
 * ``value``: solves/s of the mixed-precision engine (FP32 Krylov inner solves,
   FP64 refinement residual, FP64 stacks and QR) with the inputs resident in HBM,
   timed with CUDA events on the engine's stream, L2 flushed between steps.
-* ``e2e``: the same solve through the C ABI with host buffers (host->device
-  copies of the three trains and the device->host copy of the solution inside
-  the timed region), wall clock.
-* ``plain_fp64``: the plain FP64 engine on the same inputs (the drop-in
-  baseline the mixed path is compared with).
+* ``e2e``: the same batch through the C ABI with host buffers (host->device
+  copies of all trains and the device->host copy of the solutions inside the
+  timed region), wall clock.
+* ``plain_fp64``: the plain FP64 engine on the same batch; ``dropin_single_solve``:
+  one solve spread over the whole GPU (the drop-in for a single ``sle.als``
+  call), plain FP64 and mixed.
 * ``cpu_baseline``: the CPU oracle (a NumPy restatement of the reference's
   dense-LU ALS) on a bounded sample of the same workload, extrapolated.
 
@@ -203,6 +205,18 @@ class ClockSampler:
                 'samples': len(sm)}
 
 
+def _desc_array(lib_mod, packs, bufs=None):
+    C = lib_mod.C
+    arr = (lib_mod.TTDesc * len(packs))()
+    for k, p in enumerate(packs):
+        if bufs is None:
+            arr[k] = p.desc
+        else:
+            arr[k] = lib_mod.TTDesc(p.order, lib_mod.i64ptr(p.row), lib_mod.i64ptr(p.col), lib_mod.i64ptr(p.ranks),
+                                    C.cast(bufs[k].data_ptr(), C.POINTER(C.c_double)), 1)
+    return arr
+
+
 def main_gpu(args):
     import torch
     from scikit_tt_gb300 import _lib
@@ -219,143 +233,157 @@ def main_gpu(args):
     ctx = _lib.context()
     stream = torch.cuda.current_stream(dev)
     _lib.check(lib.ttals_set_stream(ctx, _lib.C.c_void_p(stream.cuda_stream)))
+    C = _lib.C
+    B = args.batch or 2 * torch.cuda.get_device_properties(dev).multi_processor_count
 
-    # each rank solves its own replica (independent seeded instance)
-    w = wl.coupled_sle(seed=rank, **WORKLOAD)
-    packs = [_lib.Packed(t) for t in (w.op, w.x0, w.rhs)]
-    dev_bufs = [torch.from_numpy(p.data).to(dev) for p in packs]
-    dev_descs = []
-    for p, b in zip(packs, dev_bufs):
-        dev_descs.append(_lib.TTDesc(p.order, _lib.i64ptr(p.row), _lib.i64ptr(p.col), _lib.i64ptr(p.ranks),
-                                     _lib.C.cast(b.data_ptr(), _lib.C.POINTER(_lib.C.c_double)), 1))
-    dims = np.array([c.shape[1] for c in w.op], dtype=np.int64)
-    out_ranks = np.zeros(len(w.op) + 1, dtype=np.int64)
-    _lib.check(lib.ttals_als_ranks(len(w.op), _lib.i64ptr(dims), _lib.i64ptr(packs[1].ranks), _lib.i64ptr(out_ranks)))
-    out_total = int(sum(out_ranks[i] * dims[i] * out_ranks[i + 1] for i in range(len(w.op))))
-    out_dev = torch.empty(out_total, dtype=torch.float64, device=dev)
-    out_host = np.empty(out_total, dtype=np.float64)
+    # B independent seeded instances per rank (weak scaling: each rank its own batch)
+    inst = [wl.coupled_sle(seed=rank * B + j, **WORKLOAD) for j in range(B)]
+    packs = [[_lib.Packed(t) for t in (w.op, w.x0, w.rhs)] for w in inst]
+    dbufs = [[torch.from_numpy(p.data).to(dev) for p in pk] for pk in packs]
+    dev_ops = _desc_array(_lib, [pk[0] for pk in packs], [b[0] for b in dbufs])
+    dev_x0s = _desc_array(_lib, [pk[1] for pk in packs], [b[1] for b in dbufs])
+    dev_rhs = _desc_array(_lib, [pk[2] for pk in packs], [b[2] for b in dbufs])
+    host_ops = _desc_array(_lib, [pk[0] for pk in packs])
+    host_x0s = _desc_array(_lib, [pk[1] for pk in packs])
+    host_rhs = _desc_array(_lib, [pk[2] for pk in packs])
+    dims = np.array([c.shape[1] for c in inst[0].op], dtype=np.int64)
+    out_ranks = np.zeros(len(dims) + 1, dtype=np.int64)
+    _lib.check(lib.ttals_als_ranks(len(dims), _lib.i64ptr(dims), _lib.i64ptr(packs[0][1].ranks),
+                                   _lib.i64ptr(out_ranks)))
+    out_n = int(sum(out_ranks[i] * dims[i] * out_ranks[i + 1] for i in range(len(dims))))
+    out_dev = torch.empty((B, out_n), dtype=torch.float64, device=dev)
+    out_host = np.empty((B, out_n), dtype=np.float64)
+    dev_ptrs = (C.POINTER(C.c_double) * B)(*[C.cast(out_dev[j].data_ptr(), C.POINTER(C.c_double))
+                                             for j in range(B)])
+    host_ptrs = (C.POINTER(C.c_double) * B)(*[_lib.dptr(out_host[j]) for j in range(B)])
+    reps = (C.c_int32 * B)(*([WORKLOAD['repeats']] * B))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def solve_dev(prec, tol, stats=None):
-        st = stats if stats is not None else _lib.Stats()
-        _lib.check(lib.ttals_sle_als(ctx, dev_descs[0], dev_descs[1], dev_descs[2], w.repeats, 0, prec, tol,
-                                     _lib.C.cast(out_dev.data_ptr(), _lib.C.POINTER(_lib.C.c_double)), 1,
-                                     _lib.i64ptr(out_ranks), st))
-        return st
-
-    def solve_host(prec, tol):
+    def batch(prec, tol, on_device=True):
         st = _lib.Stats()
-        _lib.check(lib.ttals_sle_als(ctx, packs[0].desc, packs[1].desc, packs[2].desc, w.repeats, 0, prec, tol,
-                                     _lib.dptr(out_host), 0, _lib.i64ptr(out_ranks), st))
+        if on_device:
+            _lib.check(lib.ttals_sle_als_batch(ctx, B, dev_ops, dev_x0s, dev_rhs, reps, prec, tol, dev_ptrs, 1, st))
+        else:
+            _lib.check(lib.ttals_sle_als_batch(ctx, B, host_ops, host_x0s, host_rhs, reps, prec, tol, host_ptrs, 0,
+                                               st))
         return st
 
-    def timed(prec, tol, steps, warmup):
+    def timed(fn, steps, warmup):
         for _ in range(warmup):
-            solve_dev(prec, tol)
+            fn()
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        launches, stats = 0, []
+        stats = []
         for k in range(steps):
             flush.zero_()
             ev[k][0].record(stream)
-            st = solve_dev(prec, tol)
+            stats.append(fn())
             ev[k][1].record(stream)
-            launches += st.kernel_launches
-            stats.append(st.as_dict())
         torch.cuda.synchronize()
-        ms = [a.elapsed_time(b) for a, b in ev]
-        return ms, launches, stats
+        return [a.elapsed_time(b) for a, b in ev], stats
 
-    # arithmetic peaks of this device (FMA chains), for the roofline fractions
-    p64, p32 = _lib.C.c_double(0), _lib.C.c_double(0)
-    _lib.check(lib.ttals_measure_peaks(ctx, _lib.C.byref(p64), _lib.C.byref(p32)))
+    p64, p32 = C.c_double(0), C.c_double(0)
+    _lib.check(lib.ttals_measure_peaks(ctx, C.byref(p64), C.byref(p32)))
 
+    # headline: mixed-precision batch, inputs resident in HBM
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        ms_mixed, launches, st_mixed = timed(_lib.PREC_MIXED, MIXED_TOL, args.steps, args.warmup)
+        ms_mixed, st_mixed = timed(lambda: batch(_lib.PREC_MIXED, MIXED_TOL), args.steps, args.warmup)
     torch.cuda.synchronize()
     total_ms = float(np.sum(ms_mixed))
     if world > 1:
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
-    value = world * args.steps / (total_ms / 1e3)
-    mixed_sol = out_dev.cpu().numpy().copy()
+    value = world * B * args.steps / (total_ms / 1e3)
+    mixed_sol = out_dev[0].cpu().numpy().copy()
+    launches = int(sum(s.kernel_launches for s in st_mixed))
 
-    # plain FP64 drop-in on the same inputs
-    plain_steps = max(1, min(args.steps, 3))
-    ms_plain, _, st_plain = timed(_lib.PREC_FP64, 0.0, plain_steps, 1)
-    plain_sol = out_dev.cpu().numpy().copy()
-    plain_value = 1e3 / float(np.mean(ms_plain))
+    # plain FP64 on the same batch
+    ms_plain_b, st_plain_b = timed(lambda: batch(_lib.PREC_FP64, 0.0), 1, 1)
+    plain_batch_value = B / (float(np.mean(ms_plain_b)) / 1e3)
+    plain_sol = out_dev[0].cpu().numpy().copy()
 
-    # agreement of the mixed and plain solutions (device TT norm)
+    # the single-instance drop-in (whole GPU on one solve), plain FP64 and mixed
+    w0 = packs[0]
+    out1 = torch.empty(out_n, dtype=torch.float64, device=dev)
+
+    def single(prec, tol):
+        st = _lib.Stats()
+        _lib.check(lib.ttals_sle_als(ctx, dev_ops[0], dev_x0s[0], dev_rhs[0], WORKLOAD['repeats'], 0, prec, tol,
+                                     C.cast(out1.data_ptr(), C.POINTER(C.c_double)), 1, _lib.i64ptr(out_ranks), st))
+        return st
+    ms_drop64, _ = timed(lambda: single(_lib.PREC_FP64, 0.0), 3, 1)
+    ms_dropmx, _ = timed(lambda: single(_lib.PREC_MIXED, MIXED_TOL), 3, 1)
+
+    # agreement of mixed and plain solutions of instance 0 (device TT norm)
     from scikit_tt_gb300.tensor_train import TT
     rk = [int(r) for r in out_ranks]
     tm = TT(_lib.unpack(mixed_sol, dims, [1] * len(dims), rk))
     tp = TT(_lib.unpack(plain_sol, dims, [1] * len(dims), rk))
     mixed_vs_plain = (tm - tp).norm() / tp.norm()
 
-    # end to end through the C ABI with host buffers
+    # end to end: the same batch through the C ABI with host buffers
     e2e_ms = []
-    for _ in range(2):
-        solve_host(_lib.PREC_MIXED, MIXED_TOL)
-    for _ in range(args.steps):
+    batch(_lib.PREC_MIXED, MIXED_TOL, on_device=False)
+    for _ in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
-        solve_host(_lib.PREC_MIXED, MIXED_TOL)
+        batch(_lib.PREC_MIXED, MIXED_TOL, on_device=False)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    h2d = sum(p.data.nbytes for p in packs)
-    d2h = out_host.nbytes + 8 * len(out_ranks)
+    h2d = sum(p.data.nbytes for pk in packs for p in pk)
+    d2h = out_host.nbytes
 
-    # roofline of the local-solve kernel: profiled pass, live CUDA events
-    _lib.check(lib.ttals_set_profiling(ctx, 1))
-    prof = solve_dev(_lib.PREC_MIXED, MIXED_TOL)
-    prof_plain = solve_dev(_lib.PREC_FP64, 0.0)
-    _lib.check(lib.ttals_set_profiling(ctx, 0))
-    torch.cuda.synchronize()
-    per_launch_s = prof.solver_ms / max(prof.solver_launches, 1) / 1e3
-    ach64 = prof.solver_flops64 / max(prof.solver_launches, 1) / per_launch_s / 1e9
-    ach32 = prof.solver_flops32 / max(prof.solver_launches, 1) / per_launch_s / 1e9
-    plain_per_launch_s = prof_plain.solver_ms / max(prof_plain.solver_launches, 1) / 1e3
-    plain_ach64 = prof_plain.solver_flops64 / max(prof_plain.solver_launches, 1) / plain_per_launch_s / 1e9
+    # roofline of the batch kernel (its CUDA-event duration, algorithmic flops from the kernel's own counters)
+    sm_ = st_mixed[-1]
+    kern_s = sm_.solver_ms / 1e3
+    ach64 = sm_.solver_flops64 / kern_s / 1e9
+    ach32 = sm_.solver_flops32 / kern_s / 1e9
+    sp_ = st_plain_b[-1]
+    plain_ach64 = sp_.solver_flops64 / (sp_.solver_ms / 1e3) / 1e9
     traffic = None
     tf = os.path.join(ROOT, 'profiles', 'traffic.json')
     if os.path.exists(tf):
-        traffic = json.load(open(tf)).get('gmres_ir_kernel<float>')
+        traffic = json.load(open(tf)).get('batch_sle_kernel')
 
     if rank != 0:
         return
-    cpu_est, nsamp, nmax = cpu_sample(w, nsites=2)
+    cpu_est, nsamp, nmax = cpu_sample(inst[0], nsites=2)
     lat = np.array(ms_mixed)
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': total_ms / args.steps, 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 Krylov + f64 refinement/stacks/QR',
         'data': 'synthetic (seeded N(0,1) trains)',
-        'config': {'workload': WORKLOAD_NAME, 'precision': 'mixed', 'local_tol': MIXED_TOL, 'batch': 1,
-                   'l2': 'flushed between steps (256 MiB write)', 'parallelism': f'replicas x{world}'},
+        'config': {'workload': WORKLOAD_NAME, 'precision': 'mixed', 'local_tol': MIXED_TOL,
+                   'batch_per_gpu': B, 'step': f'{B} independent solves in one launch (one CTA per solve)',
+                   'l2': 'flushed between steps (256 MiB write); batch working set > L2',
+                   'parallelism': f'instances sharded over {world} GPU(s)'},
         'latency_ms': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99)),
-                       'mean': float(lat.mean())},
-        'plain_fp64': {'value': plain_value, 'unit': UNIT, 'ms_per_solve': float(np.mean(ms_plain)),
-                       'max_local_residual': st_plain[-1]['max_local_residual'],
-                       'solver_achieved_fp64_gflops': plain_ach64},
-        'mixed_over_plain': value / world / plain_value,
+                       'note': 'per batch step; every solve of the batch completes within it'},
+        'plain_fp64': {'value': plain_batch_value, 'unit': UNIT, 'what': 'same batch, plain FP64 engine',
+                       'max_local_residual': st_plain_b[-1].max_local_residual,
+                       'achieved_fp64_gflops': plain_ach64},
+        'mixed_over_plain_batched': value / world / plain_batch_value,
+        'dropin_single_solve': {'fp64_ms': float(np.mean(ms_drop64)), 'mixed_ms': float(np.mean(ms_dropmx)),
+                                'fp64_solves_per_s': 1e3 / float(np.mean(ms_drop64)),
+                                'mixed_solves_per_s': 1e3 / float(np.mean(ms_dropmx)),
+                                'what': 'one solve spread over the whole GPU (cooperative kernels)'},
+        'mixed_over_plain_dropin': value / world / (1e3 / float(np.mean(ms_drop64))),
         'mixed_vs_plain_rel_diff': mixed_vs_plain,
-        'max_local_residual': max(s['max_local_residual'] for s in st_mixed),
-        'e2e': {'value': 1e3 / float(np.mean(e2e_ms)), 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
-                'd2h_bytes_per_step': int(d2h), 'p50_ms': float(np.percentile(e2e_ms, 50)),
-                'p99_ms': float(np.percentile(e2e_ms, 99))},
-        'gpu_launches': int(launches),
-        'roofline': {'kernel': 'gmres_ir_kernel<float> (local solve)', 'bound': 'fp64',
-                     'achieved': ach64, 'peak': p64.value, 'unit': 'GFLOP/s', 'frac': ach64 / p64.value,
-                     'traffic': traffic, 'peak_source': 'FP64 FMA-chain microbenchmark run in this process',
+        'max_local_residual': max(s.max_local_residual for s in st_mixed),
+        'e2e': {'value': B / (float(np.mean(e2e_ms)) / 1e3), 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
+                'd2h_bytes_per_step': int(d2h), 'ms_per_step': float(np.mean(e2e_ms))},
+        'gpu_launches': launches,
+        'roofline': {'kernel': 'batch_sle_kernel (mixed)', 'bound': 'fp64', 'achieved': ach64,
+                     'peak': p64.value, 'unit': 'GFLOP/s', 'frac': ach64 / p64.value, 'traffic': traffic,
+                     'peak_source': 'FP64 FMA-chain microbenchmark run in this process (ttals_measure_peaks)',
                      'achieved_fp32_gflops': ach32, 'fp32_peak_gflops': p32.value,
-                     'avg_launch_ms': per_launch_s * 1e3,
-                     'share_of_step': prof.solver_ms / max(prof.device_ms, 1e-9)},
+                     'avg_launch_ms': sm_.solver_ms, 'plain_fp64_frac': plain_ach64 / p64.value},
         'cpu_baseline': {'value': 1.0 / cpu_est, 'unit': UNIT, 'cores': cpu_threads(), 'kind': 'port',
                          'sample': f'{nsamp} oracle local steps at N={nmax} (stack, dense matrix, LU, QR), '
-                                   f'extrapolated by N^3 to all local solves of one run'},
+                                   f'extrapolated by N^3 to all local solves of one solve'},
         'clocks': clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -367,6 +395,7 @@ def main():
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--batch', type=int, default=0, help='solves per step and GPU (default 2 x SM count)')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

@@ -104,6 +104,14 @@ int ttals_sle_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const 
                   int32_t repeats, int32_t solver, int32_t precision, double tol,
                   double* out_data, int32_t out_on_device, int64_t* out_ranks, ttals_stats* stats);
 
+/* Batched scikit_tt/solvers/sle.py:10 `als`: `count` independent systems
+ * (each with its own order, mode sizes and ranks) solved in one launch, one
+ * CTA per system.  out_data[j] receives system j's cores with the ranks
+ * ttals_als_ranks gives; all systems use `precision` and `tol`. */
+int ttals_sle_als_batch(ttals_ctx* ctx, int32_t count, const ttals_tt* ops, const ttals_tt* x0s,
+                        const ttals_tt* rhss, const int32_t* repeats, int32_t precision, double tol,
+                        double* const* out_data, int32_t out_on_device, ttals_stats* stats);
+
 /* scikit_tt/solvers/evp.py:17 `als(operator, initial_guess, previous, shift,
  * operator_gevp=None, number_ev, repeats, conv_eps, solver, sigma, real)` for
  * symmetric operators.  out_vals[number_ev]; out_data as for ttals_sle_als

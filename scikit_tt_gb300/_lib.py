@@ -37,7 +37,7 @@ EXPORTS = (
     'ttals_create', 'ttals_destroy', 'ttals_last_error', 'ttals_set_stream', 'ttals_als_ranks',
     'ttals_sle_als', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_norm',
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
-    'ttals_stack_op_noalloc',
+    'ttals_stack_op_noalloc', 'ttals_sle_als_batch',
 )
 
 
@@ -93,6 +93,8 @@ def load():
         lib.ttals_micro_matrix.argtypes = [vp, pd, pd, pd, i64, i64, i64, i64, i64, pd, i32]
         lib.ttals_set_profiling.argtypes = [vp, i32]
         lib.ttals_measure_peaks.argtypes = [vp, pd, pd]
+        lib.ttals_sle_als_batch.argtypes = [vp, i32, P(TTDesc), P(TTDesc), P(TTDesc), P(i32), i32, dbl,
+                                            P(pd), i32, P(Stats)]
         lib.ttals_stack_op_noalloc.argtypes = [vp, i32, pd, pd, pd, i64, i64, i64, i64, i64, pd]
         for name in EXPORTS:
             if name not in ('ttals_last_error',):

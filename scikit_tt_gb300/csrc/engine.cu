@@ -28,6 +28,8 @@
 #include <vector>
 
 #include "../../include/ttals.h"
+#include "ttals_batch.h"
+#include "ttals_desc.cuh"
 #include "ttals_internal.h"
 
 using namespace ttals;
@@ -139,30 +141,18 @@ void upload(ttals_ctx* ctx, double* dst, const TTView& v) {
 // left operator stack: L_new[s,Q,s'] from L[a,R,a'], x[a,n,s], A[R,n,n,Q]
 void stack_left_op(ttals_ctx* c, const double* L, const double* x, const double* A, int64_t a, int64_t n,
                    int64_t s, int64_t R, int64_t Q, double* T1, double* T2, double* out) {
-  LocalShape sh{a, n, s, R, Q};
   Contraction p1, p2, p3;
-  local_apply_descs(sh, &p1, &p2, &p3);
+  desc_apply(a, n, s, R, Q, &p1, &p2, &p3);
   CK(launch_contract<double>(p1, L, x, T1, 1.0, 0.0, c->stream));
   CK(launch_contract<double>(p2, T1, A, T2, 1.0, 0.0, c->stream));
-  // L_new[s, Q, s'] = sum_{a', m} T2[a', m, s, Q] x[a', m, s']
-  Contraction p = make_contraction({{s, Q, 0, Q * s}, {Q, 1, 0, s}, {s, 0, 1, 1}},
-                                   {{a, n * s * Q, n * s, 0}, {n, s * Q, s, 0}});
-  CK(launch_contract<double>(p, T2, x, out, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_left_p3(a, n, s, Q), T2, x, out, 1.0, 0.0, c->stream));
 }
 
 // right operator stack: Rt_new[a,R,a'] from Rn[s,Q,s'], x[a,n,s], A[R,n,n,Q]
 void stack_right_op(ttals_ctx* c, const double* Rn, const double* x, const double* A, int64_t a, int64_t n,
                     int64_t s, int64_t R, int64_t Q, double* U1, double* U2, double* out) {
-  // U1[s, Q, a', m] = sum_s' Rn[s, Q, s'] x[a', m, s']
-  Contraction q1 = make_contraction(
-      {{s, Q * s, 0, Q * a * n}, {Q, s, 0, a * n}, {a, 0, n * s, n}, {n, 0, s, 1}}, {{s, 1, 1, 0}});
-  // U2[s, R, n, a'] = sum_{Q, m} U1[s, Q, a', m] A[R, m, n, Q]
-  Contraction q2 = make_contraction(
-      {{s, Q * a * n, 0, R * n * a}, {R, 0, n * n * Q, n * a}, {n, 0, Q, a}, {a, n, 0, 1}},
-      {{Q, a * n, 1, 0}, {n, 1, n * Q, 0}});
-  // Rt_new[a, R, a'] = sum_{n, s} x[a, n, s] U2[s, R, n, a']
-  Contraction q3 = make_contraction({{a, n * s, 0, R * a}, {R, 0, n * a, a}, {a, 0, 1, 1}},
-                                    {{n, s, a, 0}, {s, 1, R * n * a, 0}});
+  Contraction q1, q2, q3;
+  desc_right(a, n, s, R, Q, &q1, &q2, &q3);
   CK(launch_contract<double>(q1, Rn, x, U1, 1.0, 0.0, c->stream));
   CK(launch_contract<double>(q2, U1, A, U2, 1.0, 0.0, c->stream));
   CK(launch_contract<double>(q3, x, U2, out, 1.0, 0.0, c->stream));
@@ -171,39 +161,31 @@ void stack_right_op(ttals_ctx* c, const double* Rn, const double* x, const doubl
 // left vector stack: Lb_new[g, s'] from Lb[h, a'], b[h, n, g], x[a', n, s']
 void stack_left_vec(ttals_ctx* c, const double* Lb, const double* b, const double* x, int64_t a, int64_t n,
                     int64_t s, int64_t h, int64_t g, double* U, double* out) {
-  Contraction u = make_contraction({{a, 1, 0, n * g}, {n, 0, g, g}, {g, 0, 1, 1}}, {{h, a, n * g, 0}});
-  Contraction p = make_contraction({{g, 1, 0, s}, {s, 0, 1, 1}}, {{a, n * g, n * s, 0}, {n, g, s, 0}});
-  CK(launch_contract<double>(u, Lb, b, U, 1.0, 0.0, c->stream));
-  CK(launch_contract<double>(p, U, x, out, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_vec_u_left(a, n, h, g), Lb, b, U, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_vec_left(a, n, s, g), U, x, out, 1.0, 0.0, c->stream));
 }
 
 // right vector stack: Rb_new[h, a'] from Rb[g, s'], b[h, n, g], x[a', n, s']
 void stack_right_vec(ttals_ctx* c, const double* Rb, const double* b, const double* x, int64_t a, int64_t n,
                      int64_t s, int64_t h, int64_t g, double* U, double* out) {
-  Contraction u = make_contraction({{a, n * s, 0, n * g}, {n, s, 0, g}, {g, 0, s, 1}}, {{s, 1, 1, 0}});
-  Contraction p = make_contraction({{h, n * g, 0, a}, {a, 0, n * g, 1}}, {{n, g, g, 0}, {g, 1, 1, 0}});
-  CK(launch_contract<double>(u, x, Rb, U, 1.0, 0.0, c->stream));
-  CK(launch_contract<double>(p, b, U, out, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_vec_u_right(a, n, s, g), x, Rb, U, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_vec_right(a, n, h, g), b, U, out, 1.0, 0.0, c->stream));
 }
 
 // local vector f[a', m, s'] = sum Lb[h, a'] b[h, m, g] Rb[g, s']
 void micro_vec(ttals_ctx* c, const double* Lb, const double* b, const double* Rb, int64_t a, int64_t n, int64_t s,
                int64_t h, int64_t g, double* U, double* out) {
-  Contraction u = make_contraction({{a, 1, 0, n * g}, {n, 0, g, g}, {g, 0, 1, 1}}, {{h, a, n * g, 0}});
-  Contraction p = make_contraction({{a, n * g, 0, n * s}, {n, g, 0, s}, {s, 0, 1, 1}}, {{g, 1, s, 0}});
-  CK(launch_contract<double>(u, Lb, b, U, 1.0, 0.0, c->stream));
-  CK(launch_contract<double>(p, U, Rb, out, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_vec_u_left(a, n, h, g), Lb, b, U, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_micro_f(a, n, s, g), U, Rb, out, 1.0, 0.0, c->stream));
 }
 
 // C (p x k) = X (p x a) * R (a x k)
 void push_right(ttals_ctx* c, const double* X, const double* R, int64_t p, int64_t a, int64_t k, double* out) {
-  Contraction q = make_contraction({{p, a, 0, k}, {k, 0, 1, 1}}, {{a, 1, k, 0}});
-  CK(launch_contract<double>(q, X, R, out, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_push_right(p, a, k), X, R, out, 1.0, 0.0, c->stream));
 }
 // C (k x q) = R (k x s) * X (s x q)
 void push_left(ttals_ctx* c, const double* R, const double* X, int64_t k, int64_t s, int64_t q, double* out) {
-  Contraction p = make_contraction({{k, s, 0, q}, {q, 0, 1, 1}}, {{s, 1, q, 0}});
-  CK(launch_contract<double>(p, R, X, out, 1.0, 0.0, c->stream));
+  CK(launch_contract<double>(desc_push_left(k, s, q), R, X, out, 1.0, 0.0, c->stream));
 }
 
 int64_t qr_work(int64_t rows, int64_t cols) {
@@ -640,6 +622,203 @@ void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttal
 }
 
 // ---------------------------------------------------------------------------
+// batched SLE driver: one CTA per instance (kernels_batch.cu)
+// ---------------------------------------------------------------------------
+
+void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt* x0s, const ttals_tt* rhss,
+                   const int32_t* repeats, int prec, double tol, double* const* outs, int out_dev, ttals_stats* st) {
+  require(count >= 1, TTALS_ERR_ARG, "count must be >= 1");
+  require(ops && x0s && rhss && repeats && outs, TTALS_ERR_ARG, "null array argument");
+  require(prec == TTALS_PREC_FP64 || prec == TTALS_PREC_MIXED, TTALS_ERR_ARG, "unknown precision mode");
+  if (tol <= 0) tol = (prec == TTALS_PREC_FP64) ? 1e-13 : 1e-10;
+  launch_counter() = 0;
+  const int m = 40;
+  struct Inst {
+    TTView op, x0, b;
+    std::vector<int64_t> cap, fin;
+    int64_t region = 0, meta_off = 0;
+    std::vector<int64_t> off;  // op, rhs, x0, X, L, Rt, Lb, Rb, out, report (relative to region)
+  };
+  std::vector<Inst> in(count);
+  BatchSizes z{1, 1, 1, 1, 1, 1, 1, 1};
+  std::vector<int64_t> meta;
+  int64_t region_total = 0;
+  for (int j = 0; j < count; ++j) {
+    Inst& I = in[j];
+    I.op = view(ops + j, "operator");
+    I.x0 = view(x0s + j, "initial_guess");
+    I.b = view(rhss + j, "right_hand_side");
+    validate_square_op(I.op);
+    validate_vec(I.x0, I.op, "initial_guess");
+    validate_vec(I.b, I.op, "right_hand_side");
+    require(repeats[j] >= 1, TTALS_ERR_ARG, "repeats must be >= 1 in a batch");
+    const int d = I.op.d;
+    require(d <= 256, TTALS_ERR_UNSUPPORTED, "batched instances support order <= 256");
+    const std::vector<int64_t>& n = I.op.m;
+    const std::vector<int64_t>& R = I.op.r;
+    const std::vector<int64_t>& rb = I.b.r;
+    const std::vector<int64_t>& rx0 = I.x0.r;
+    I.cap = ro_ranks(n, rx0);
+    I.fin = final_ranks(n, rx0);
+    std::vector<int64_t> Xo(d), Lo(d), Rto(d), Lbo(d), Rbo(d);
+    int64_t xs = 0, ls = 0, rts = 0, lbs = 0, rbs = 0, outs_n = 0;
+    for (int i = 0; i < d; ++i) {
+      const int64_t a = I.cap[i], nn = n[i], s = I.cap[i + 1];
+      Xo[i] = xs;
+      xs += a * nn * s;
+      Lo[i] = ls;
+      ls += a * R[i] * a;
+      Rto[i] = rts;
+      rts += s * R[i + 1] * s;
+      Lbo[i] = lbs;
+      lbs += rb[i] * a;
+      Rbo[i] = rbs;
+      rbs += rb[i + 1] * s;
+      outs_n += I.fin[i] * nn * I.fin[i + 1];
+      z.N = std::max(z.N, a * nn * s);
+      z.T = std::max(z.T, std::max(R[i], R[i + 1]) * std::max(a, s) * std::max(a, s) * nn);
+      z.U = std::max(z.U, std::max(a, s) * nn * std::max(rb[i], rb[i + 1]));
+      z.R = std::max(z.R, std::max(std::max(a, s) * std::max(a, s), rx0[i] * rx0[i]));
+      z.Q = std::max(z.Q, std::max(std::max(qr_work(a * nn, s), qr_work(nn * s, a)), qr_work(nn * I.cap[i + 1], rx0[i])));
+      z.core = std::max(z.core, std::max(a * nn * s, rx0[i] * nn * std::max(I.cap[i + 1], rx0[i + 1])));
+      z.stack = std::max(z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
+      z.opcore = std::max(z.opcore, R[i] * nn * nn * R[i + 1]);
+    }
+    // instance region layout (doubles)
+    I.off.resize(10);
+    int64_t o = 0;
+    auto put = [&](int k, int64_t cnt) {
+      I.off[k] = o;
+      o += (cnt + 31) / 32 * 32;
+    };
+    put(0, I.op.total);
+    put(1, I.b.total);
+    put(2, I.x0.total);
+    put(3, xs);
+    put(4, ls);
+    put(5, rts);
+    put(6, lbs);
+    put(7, rbs);
+    put(8, outs_n);
+    put(9, 8 + d + 1);
+    I.region = region_total;
+    region_total += o;
+    // meta
+    I.meta_off = (int64_t)meta.size();
+    auto app = [&](const std::vector<int64_t>& v, int cnt) { meta.insert(meta.end(), v.begin(), v.begin() + cnt); };
+    app(n, d);
+    app(R, d + 1);
+    app(rb, d + 1);
+    app(rx0, d + 1);
+    app(I.cap, d + 1);
+    std::vector<int64_t> oo(I.op.off.begin(), I.op.off.begin() + d), bo(I.b.off.begin(), I.b.off.begin() + d),
+        xo(I.x0.off.begin(), I.x0.off.begin() + d);
+    app(oo, d);
+    app(bo, d);
+    app(xo, d);
+    app(Xo, d);
+    app(Lo, d);
+    app(Rto, d);
+    app(Lbo, d);
+    app(Rbo, d);
+  }
+  const int grid = std::min(count, c->num_sms * batch_blocks_per_sm(m));
+  const int64_t stride = batch_scratch_stride(z, m);
+  double* data = nullptr;
+  int64_t* dmeta = nullptr;
+  BatchInst* dinst = nullptr;
+  char* scratch = nullptr;
+  int* next = nullptr;
+  Bump B{c};
+  B.want(&data, region_total);
+  B.want(&dmeta, (int64_t)meta.size());
+  B.want((char**)&dinst, (int64_t)sizeof(BatchInst) * count);
+  B.want(&scratch, stride * grid);
+  B.want(&next, 4);
+  B.commit();
+  std::vector<BatchInst> hinst(count);
+  for (int j = 0; j < count; ++j) {
+    Inst& I = in[j];
+    double* base = data + I.region;
+    BatchInst& H = hinst[j];
+    H.d = I.op.d;
+    H.repeats = repeats[j];
+    H.meta_off = I.meta_off;
+    H.op = base + I.off[0];
+    H.rhs = base + I.off[1];
+    H.x0 = base + I.off[2];
+    H.X = base + I.off[3];
+    H.L = base + I.off[4];
+    H.Rt = base + I.off[5];
+    H.Lb = base + I.off[6];
+    H.Rb = base + I.off[7];
+    H.out = base + I.off[8];
+    H.report = base + I.off[9];
+  }
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(cudaMemcpyAsync(dmeta, meta.data(), sizeof(int64_t) * meta.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, c->stream));
+  for (int j = 0; j < count; ++j) {
+    upload(c, (double*)hinst[j].op, in[j].op);
+    upload(c, (double*)hinst[j].rhs, in[j].b);
+    upload(c, (double*)hinst[j].x0, in[j].x0);
+  }
+  CK(cudaMemsetAsync(next, 0, sizeof(int), c->stream));
+  BatchArgs args{dinst, count, dmeta, next, scratch, stride, z, m, prec == TTALS_PREC_MIXED ? 1 : 0, tol};
+  cudaEvent_t k0 = pool_event(c, 0), k1 = pool_event(c, 1);
+  CK(cudaEventRecord(k0, c->stream));
+  CK(launch_batch_sle(args, grid, c->stream));
+  CK(cudaEventRecord(k1, c->stream));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  // reports, then outputs
+  std::vector<std::vector<double>> rep(count);
+  for (int j = 0; j < count; ++j) {
+    const int d = in[j].op.d;
+    rep[j].resize(8 + d + 1);
+    CK(cudaMemcpyAsync(rep[j].data(), hinst[j].report, sizeof(double) * (8 + d + 1), cudaMemcpyDeviceToHost,
+                       c->stream));
+    int64_t cnt = 0;
+    for (int i = 0; i < d; ++i) cnt += in[j].fin[i] * in[j].op.m[i] * in[j].fin[i + 1];
+    CK(cudaMemcpyAsync(outs[j], hinst[j].out, sizeof(double) * cnt,
+                       out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
+  int64_t nsolve = 0, nits = 0, ncyc = 0;
+  for (int j = 0; j < count; ++j) {
+    fl64 += rep[j][5];
+    fl32 += rep[j][6];
+    const int st_j = (int)rep[j][4];
+    if (st_j == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in a local solve of instance " + std::to_string(j)};
+    if (st_j == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in instance " + std::to_string(j)};
+    if (st_j != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(st_j)};
+    for (int i = 0; i <= in[j].op.d; ++i)
+      require((int64_t)rep[j][8 + i] == in[j].fin[i], TTALS_ERR_CUDA, "rank schedule mismatch in batch instance");
+    maxres = std::max(maxres, rep[j][0]);
+    nsolve += (int64_t)rep[j][1];
+    nits += (int64_t)rep[j][2];
+    ncyc += (int64_t)rep[j][3];
+  }
+  if (st) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    st->local_solves = nsolve;
+    st->krylov_iterations = nits;
+    st->refinement_steps = ncyc;
+    st->max_local_residual = maxres;
+    st->device_ms = ms;
+    st->kernel_launches = launch_counter();
+    // the batch kernel is the only local-solve launch; always timed
+    float kms = 0.f;
+    CK(cudaEventElapsedTime(&kms, k0, k1));
+    st->solver_launches = 1;
+    st->solver_ms = kms;
+    st->solver_flops64 = fl64;
+    st->solver_flops32 = fl32;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // EVP driver (symmetric local problems, number_ev == 1 path plus k <= 8 values)
 // ---------------------------------------------------------------------------
 
@@ -968,6 +1147,14 @@ int ttals_sle_als(ttals_ctx* c, const ttals_tt* op, const ttals_tt* x0, const tt
                   int64_t* out_ranks, ttals_stats* stats) {
   return guarded(c, [&] {
     run_sle(c, op, x0, rhs, repeats, solver, precision, tol, out_data, out_on_device, out_ranks, stats);
+  });
+}
+
+int ttals_sle_als_batch(ttals_ctx* c, int32_t count, const ttals_tt* ops, const ttals_tt* x0s,
+                        const ttals_tt* rhss, const int32_t* repeats, int32_t precision, double tol,
+                        double* const* out_data, int32_t out_on_device, ttals_stats* stats) {
+  return guarded(c, [&] {
+    run_sle_batch(c, count, ops, x0s, rhss, repeats, precision, tol, out_data, out_on_device, stats);
   });
 }
 

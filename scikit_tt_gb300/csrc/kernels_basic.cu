@@ -4,7 +4,9 @@
 // re-gauging (scikit_tt/solvers/sle.py:514-547).
 #include <algorithm>
 
+#include "ttals_desc.cuh"
 #include "ttals_internal.h"
+#include "ttals_qr.cuh"
 
 namespace ttals {
 
@@ -14,43 +16,15 @@ int64_t& launch_counter() {
 }
 
 Contraction make_contraction(const std::vector<Axis>& out, const std::vector<Axis>& k) {
-  Contraction c{};
-  c.nout = (int)out.size();
-  c.nk = (int)k.size();
-  c.total = 1;
-  for (int q = 0; q < c.nout; ++q) {
-    c.out_dim[q] = (int)out[q].dim;
-    c.a_os[q] = out[q].sa;
-    c.b_os[q] = out[q].sb;
-    c.c_os[q] = out[q].sc;
-    c.total *= out[q].dim;
-  }
-  c.ktotal = 1;
-  for (int q = 0; q < c.nk; ++q) {
-    c.k_dim[q] = (int)k[q].dim;
-    c.a_ks[q] = k[q].sa;
-    c.b_ks[q] = k[q].sb;
-    c.ktotal *= k[q].dim;
-  }
-  return c;
+  Ax o[kMaxOut], kk[kMaxK];
+  for (size_t q = 0; q < out.size(); ++q) o[q] = {out[q].dim, out[q].sa, out[q].sb, out[q].sc};
+  for (size_t q = 0; q < k.size(); ++q) kk[q] = {k[q].dim, k[q].sa, k[q].sb, 0};
+  return desc_make((int)out.size(), o, (int)k.size(), kk);
 }
 
-// Three phases of y -> M y (see LocalShape):
-//   P1  T1[R, a', n, s]  = sum_a      L[a, R, a'] y[a, n, s]
-//   P2  T2[a', m, s, R'] = sum_{R,n}  T1[R, a', n, s] A[R, m, n, R']
-//   P3  out[a', m, s']   = sum_{s,R'} T2[a', m, s, R'] Rt[s, R', s']
+// Three phases of y -> M y (see LocalShape and desc_apply).
 void local_apply_descs(const LocalShape& sh, Contraction* p1, Contraction* p2, Contraction* p3) {
-  const int64_t a = sh.a, n = sh.n, s = sh.s, R0 = sh.R0, R1 = sh.R1;
-  // P1: A-operand L (strides a: R0*a, R: a, a': 1), B-operand y (a: n*s, n: s, s: 1)
-  *p1 = make_contraction({{R0, a, 0, a * n * s}, {a, 1, 0, n * s}, {n, 0, s, s}, {s, 0, 1, 1}},
-                         {{a, R0 * a, n * s, 0}});
-  // P2: A-operand T1 (R: a*n*s, a': n*s, n: s, s: 1), B-operand A (R: n*n*R1, m: n*R1, n: R1, R': 1)
-  *p2 = make_contraction(
-      {{a, n * s, 0, n * s * R1}, {n, 0, n * R1, s * R1}, {s, 1, 0, R1}, {R1, 0, 1, 1}},
-      {{R0, a * n * s, n * n * R1, 0}, {n, s, R1, 0}});
-  // P3: A-operand T2 (a': n*s*R1, m: s*R1, s: R1, R': 1), B-operand Rt (s: R1*s, R': s, s': 1)
-  *p3 = make_contraction({{a, n * s * R1, 0, n * s}, {n, s * R1, 0, s}, {s, 0, 1, 1}},
-                         {{s, R1, R1 * s, 0}, {R1, 1, s, 0}});
+  desc_apply(sh.a, sh.n, sh.s, sh.R0, sh.R1, p1, p2, p3);
 }
 
 template <typename T>
@@ -66,6 +40,7 @@ template <typename T>
 cudaError_t launch_contract(const Contraction& c, const T* A, const T* B, T* C, T alpha, T beta,
                             cudaStream_t st) {
   if (c.total <= 0) return cudaSuccess;
+  if (c.total >= (int64_t(1) << 31)) return cudaErrorInvalidValue;  // 32-bit index arithmetic
   int64_t blocks = (c.total + 255) / 256;
   blocks = std::min<int64_t>(blocks, 65535);
   contract_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(c, A, B, C, alpha, beta);
@@ -116,119 +91,12 @@ cudaError_t launch_scale(double* p, int64_t n, const double* scale_dev, int inve
 }
 
 // ---------------------------------------------------------------------------
-// Householder QR, one CTA.  Column-major working copy W (rows x cols) and
-// reflectors Vh (rows x k) live in global scratch (L2 resident at ALS sizes).
-// Reflector j: H_j = I - tau_j v_j v_j^T with v_j[j] = x_j - alpha_j,
-// alpha_j = -sign(x_j) ||x||, so R[j][j] = alpha_j (the LAPACK sign choice).
+// Householder QR, one CTA (body in ttals_qr.cuh, shared with the batch kernel)
 // ---------------------------------------------------------------------------
 
 constexpr int kQrThreads = 512;
 
-__global__ void __launch_bounds__(kQrThreads) qr_kernel(QrArgs a) {
-  const int64_t rows = a.rows, cols = a.cols;
-  const int64_t k = rows < cols ? rows : cols;
-  double* W = a.work;
-  double* Vh = W + rows * cols;
-  double* Qw = Vh + rows * k;
-  double* tau = Qw + rows * k;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  __shared__ double red[32];
-  __shared__ double s_alpha, s_tau, s_v0;
-
-  for (int64_t e = tid; e < rows * cols; e += nt) {
-    const int64_t i = e % rows, c = e / rows;
-    W[e] = a.in[i * a.ris + c * a.rjs];
-  }
-  __syncthreads();
-
-  for (int64_t j = 0; j < k; ++j) {
-    const double* col = W + j * rows;
-    double s = 0.0;
-    for (int64_t i = j + tid; i < rows; i += nt) s += col[i] * col[i];
-    s = warp_sum(s);
-    if (lane == 0) red[warp] = s;
-    __syncthreads();
-    if (tid == 0) {
-      double tot = 0.0;
-      for (int w = 0; w < nw; ++w) tot += red[w];
-      const double x0 = col[j];
-      const double nrm = sqrt(tot);
-      if (nrm == 0.0) {
-        s_alpha = 0.0; s_tau = 0.0; s_v0 = 1.0;
-      } else {
-        const double alpha = (x0 >= 0.0) ? -nrm : nrm;
-        const double v0 = x0 - alpha;
-        const double vn2 = tot - x0 * x0 + v0 * v0;
-        s_alpha = alpha; s_v0 = v0; s_tau = (vn2 > 0.0) ? 2.0 / vn2 : 0.0;
-      }
-      tau[j] = s_tau;
-    }
-    __syncthreads();
-    double* v = Vh + j * rows;
-    for (int64_t i = j + tid; i < rows; i += nt) v[i] = (i == j) ? s_v0 : col[i];
-    __syncthreads();
-    const double tj = s_tau;
-    for (int64_t c = j + 1 + warp; c < cols; c += nw) {
-      double* wc = W + c * rows;
-      double dot = 0.0;
-      for (int64_t i = j + lane; i < rows; i += 32) dot += v[i] * wc[i];
-      dot = warp_sum(dot) * tj;
-      for (int64_t i = j + lane; i < rows; i += 32) wc[i] -= dot * v[i];
-    }
-    __syncthreads();
-    if (tid == 0) W[j * rows + j] = s_alpha;
-    __syncthreads();
-  }
-
-  // R (k x cols, upper trapezoidal) and optional normalisation
-  double rscale = 1.0;
-  if (a.normalize_r) {
-    double s = 0.0;
-    for (int64_t e = tid; e < k * cols; e += nt) {
-      const int64_t i = e / cols, c = e % cols;
-      if (i <= c) { const double v = W[c * rows + i]; s += v * v; }
-    }
-    s = warp_sum(s);
-    if (lane == 0) red[warp] = s;
-    __syncthreads();
-    double tot = 0.0;
-    for (int w = 0; w < nw; ++w) tot += red[w];
-    __syncthreads();
-    const double nrm = sqrt(tot);
-    if (a.rnorm && tid == 0) *a.rnorm = nrm;
-    rscale = (nrm > 0.0) ? 1.0 / nrm : 1.0;
-  }
-  if (a.r) {
-    for (int64_t e = tid; e < k * cols; e += nt) {
-      const int64_t i = e / cols, c = e % cols;
-      a.r[i * a.r_is + c * a.r_js] = (i <= c) ? W[c * rows + i] * rscale : 0.0;
-    }
-  }
-
-  // Q = H_0 ... H_{k-1} [I_k; 0], accumulated backwards (column-major Qw)
-  for (int64_t e = tid; e < rows * k; e += nt) {
-    const int64_t i = e % rows, c = e / rows;
-    Qw[e] = (i == c) ? 1.0 : 0.0;
-  }
-  __syncthreads();
-  for (int64_t j = k - 1; j >= 0; --j) {
-    const double* v = Vh + j * rows;
-    const double tj = tau[j];
-    for (int64_t c = j + warp; c < k; c += nw) {
-      double* qc = Qw + c * rows;
-      double dot = 0.0;
-      for (int64_t i = j + lane; i < rows; i += 32) dot += v[i] * qc[i];
-      dot = warp_sum(dot) * tj;
-      for (int64_t i = j + lane; i < rows; i += 32) qc[i] -= dot * v[i];
-    }
-    __syncthreads();
-  }
-  for (int64_t e = tid; e < rows * k; e += nt) {
-    const int64_t i = e % rows, c = e / rows;
-    a.q[i * a.qis + c * a.qjs] = Qw[e];
-  }
-}
+__global__ void __launch_bounds__(kQrThreads) qr_kernel(QrArgs a) { cta_householder_qr(a); }
 
 cudaError_t launch_qr(const QrArgs& a, cudaStream_t st) {
   if (a.rows <= 0 || a.cols <= 0) return cudaSuccess;

@@ -1,0 +1,504 @@
+// Batched ALS: one CTA runs one complete ALS solve.
+//
+// Independent instances (uneven order d, mode sizes and ranks) are taken from
+// a device work counter by persistent CTAs; each CTA runs the whole program of
+// scikit_tt/solvers/sle.py:10-95 (or evp.py:17-179) for its instance --
+// right-orthonormalisation of the guess, initial right stacks, forward and
+// backward half-sweeps with matrix-free local solves and QR/RQ re-gauging --
+// with nothing but CTA barriers.  No grid-wide synchronisation exists, so the
+// GPU fills with instances and FP64 work runs at the device's FP64 rate.
+//
+// Local solves: GMRES with FP64 residual refinement (inner Krylov in FP32 for
+// PREC_MIXED, FP64 otherwise) and, for eigenproblems, Lanczos with full
+// reorthogonalisation.  Contractions use the descriptors of ttals_desc.cuh.
+#include <float.h>
+
+#include "ttals_batch.h"
+#include "ttals_desc.cuh"
+#include "ttals_internal.h"
+#include "ttals_qr.cuh"
+
+namespace ttals {
+
+constexpr int kMaxOrderB = 256;
+constexpr int kBatchThreads = 256;  // two CTAs per SM: FP32 and FP64 phases of different instances overlap
+
+// ---------------------------------------------------------------------------
+// CTA primitives
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ void cta_contract(const Contraction& c, const T* A, const T* B, T* C) {
+  for (int64_t e = threadIdx.x; e < c.total; e += blockDim.x) {
+    int64_t ao, bo, co;
+    contract_offsets(c, e, ao, bo, co);
+    C[co] = contract_sum(c, A, B, ao, bo);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void cta_fill(double* p, int64_t n, double v) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
+  __syncthreads();
+}
+__device__ __forceinline__ void cta_copy(double* d, const double* s, int64_t n) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+  __syncthreads();
+}
+__device__ __forceinline__ void cta_to_float(float* d, const double* s, int64_t n) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = (float)s[i];
+  __syncthreads();
+}
+
+// sum over the CTA, returned to every thread
+__device__ __forceinline__ double cta_sum(double v) {
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < nw; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+// out[kk] = <X_kk, w> for kk < nvec (X_kk = V + kk*N), out[nvec] = <w, w>
+template <typename T>
+__device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const T* w, double* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int kk = warp; kk <= nvec; kk += nw) {
+    const T* xv = (kk < nvec) ? V + (int64_t)kk * N : w;
+    double s = 0.0;
+    for (int64_t e = lane; e < N; e += 32) s += (double)xv[e] * (double)w[e];
+    s = warp_sum(s);
+    if (lane == 0) out[kk] = s;
+  }
+  __syncthreads();
+}
+
+// y -> out = M y (three contraction phases through T1, T2)
+template <typename T>
+__device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
+                                          const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out) {
+  cta_contract(p1, L, y, T1);
+  cta_contract(p2, T1, A, T2);
+  cta_contract(p3, T2, R, out);
+}
+
+// ---------------------------------------------------------------------------
+// CTA GMRES with FP64 residual refinement (see gmres_ir_kernel for the grid version)
+// ---------------------------------------------------------------------------
+
+struct CtaSolveStats {
+  double rel;
+  int cycles, inner, status;
+};
+
+template <typename TI>
+__device__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& p2, const Contraction& p3,
+                                      const double* L64, const double* A64, const double* R64, double* T1_64,
+                                      double* T2_64, const TI* Li, const TI* Ai, const TI* Ri, TI* T1i, TI* T2i,
+                                      const double* f, double* x, double* r, TI* V, TI* w, int64_t N, int m,
+                                      int max_cycles, double tol, double inner_floor, double* sm) {
+  double* H = sm;                // (m+1) x m
+  double* cs = H + (m + 1) * m;  // m
+  double* sn = cs + m;           // m
+  double* gv = sn + m;           // m+1
+  double* yv = gv + m + 1;       // m
+  double* h1 = yv + m;           // m+2
+  double* h2 = h1 + m + 2;       // m+2
+  __shared__ double s_res;
+  __shared__ int s_flag;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  CtaSolveStats out{1.0, 0, 0, ST_OK};
+
+  double fs = 0.0;
+  for (int64_t e = tid; e < N; e += nt) fs += f[e] * f[e];
+  const double fnorm = sqrt(cta_sum(fs));
+  if (!(fnorm > 0.0)) {
+    for (int64_t e = tid; e < N; e += nt) x[e] = 0.0;
+    __syncthreads();
+    out.rel = 0.0;
+    if (!(fnorm == 0.0)) out.status = ST_NONFINITE;
+    return out;
+  }
+  for (int cyc = 0; cyc < max_cycles; ++cyc) {
+    cta_contract(p1, L64, (const double*)x, T1_64);
+    cta_contract(p2, (const double*)T1_64, A64, T2_64);
+    double rs = 0.0;
+    for (int64_t e = tid; e < N; e += nt) {
+      int64_t ao, bo, co;
+      contract_offsets(p3, e, ao, bo, co);
+      const double re = f[e] - contract_sum(p3, (const double*)T2_64, R64, ao, bo);
+      r[e] = re;
+      rs += re * re;
+    }
+    const double rho = sqrt(cta_sum(rs));
+    out.rel = rho / fnorm;
+    out.cycles = cyc + 1;
+    if (!isfinite(out.rel)) {
+      out.status = ST_NONFINITE;
+      return out;
+    }
+    if (out.rel <= tol) break;
+    const double target = fmax(tol / out.rel, inner_floor);
+    for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(r[e] / rho);
+    if (tid == 0) {
+      gv[0] = 1.0;
+      for (int i = 1; i <= m; ++i) gv[i] = 0.0;
+    }
+    __syncthreads();
+    int jj = 0;
+    for (int j = 0; j < m; ++j) {
+      cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w);
+      cta_dots<TI>(V, N, j + 1, w, h1);
+      for (int64_t e = tid; e < N; e += nt) {
+        double acc = (double)w[e];
+        for (int q = 0; q <= j; ++q) acc -= h1[q] * (double)V[(int64_t)q * N + e];
+        w[e] = (TI)acc;
+      }
+      __syncthreads();
+      cta_dots<TI>(V, N, j + 1, w, h2);
+      double hn2 = h2[j + 1];
+      for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
+      const double hn = sqrt(fmax(hn2, 0.0));
+      if (hn > 0.0) {
+        const double inv = 1.0 / hn;
+        TI* vn = V + (int64_t)(j + 1) * N;
+        for (int64_t e = tid; e < N; e += nt) {
+          double acc = (double)w[e];
+          for (int q = 0; q <= j; ++q) acc -= h2[q] * (double)V[(int64_t)q * N + e];
+          vn[e] = (TI)(acc * inv);
+        }
+      }
+      if (tid == 0) {
+        double* col = H + (int64_t)j * (m + 1);
+        for (int i = 0; i <= j; ++i) col[i] = h1[i] + h2[i];
+        col[j + 1] = hn;
+        for (int i = 0; i < j; ++i) {
+          const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+          col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+          col[i] = t;
+        }
+        const double a = col[j], b = col[j + 1];
+        double c = 1.0, sg = 0.0, rr = a;
+        if (b != 0.0) {
+          rr = hypot(a, b);
+          c = a / rr;
+          sg = b / rr;
+        }
+        cs[j] = c;
+        sn[j] = sg;
+        col[j] = rr;
+        col[j + 1] = 0.0;
+        gv[j + 1] = -sg * gv[j];
+        gv[j] = c * gv[j];
+        s_res = fabs(gv[j + 1]);
+        s_flag = (hn <= 1e-300) ? 1 : 0;
+      }
+      __syncthreads();
+      jj = j + 1;
+      ++out.inner;
+      if (s_res <= target || s_flag) break;
+    }
+    if (tid == 0) {
+      int bad = 0;
+      for (int i = jj - 1; i >= 0; --i) {
+        double acc = gv[i];
+        for (int l = i + 1; l < jj; ++l) acc -= H[(int64_t)l * (m + 1) + i] * yv[l];
+        const double dg = H[(int64_t)i * (m + 1) + i];
+        if (dg == 0.0) {
+          bad = 1;
+          yv[i] = 0.0;
+        } else {
+          yv[i] = acc / dg;
+        }
+      }
+      s_flag = bad;
+    }
+    __syncthreads();
+    if (s_flag) {
+      out.status = ST_SINGULAR;
+      return out;
+    }
+    for (int64_t e = tid; e < N; e += nt) {
+      double acc = 0.0;
+      for (int q = 0; q < jj; ++q) acc += yv[q] * (double)V[(int64_t)q * N + e];
+      x[e] += rho * acc;
+    }
+    __syncthreads();
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// one instance
+// ---------------------------------------------------------------------------
+
+struct Scratch {
+  double *T1, *T2, *U, *f, *r, *w, *V, *rbuf, *qwork, *tmp0, *tmp1;
+  float *Vf, *wf, *T1f, *T2f, *Lf, *Rf, *Af;
+};
+
+__device__ Scratch scratch_of(const BatchArgs& a, int slot) {
+  char* base = a.scratch + (int64_t)slot * a.scratch_stride;
+  const BatchSizes& z = a.sizes;
+  Scratch s;
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) {
+    char* p = base + off;
+    off += (bytes + 255) / 256 * 256;
+    return p;
+  };
+  s.T1 = (double*)take(8 * z.T);
+  s.T2 = (double*)take(8 * z.T);
+  s.U = (double*)take(8 * z.U);
+  s.f = (double*)take(8 * z.N);
+  s.r = (double*)take(8 * z.N);
+  s.w = (double*)take(8 * z.N);
+  s.V = (double*)take(8 * (int64_t)(a.m + 1) * z.N);
+  s.rbuf = (double*)take(8 * z.R);
+  s.qwork = (double*)take(8 * z.Q);
+  s.tmp0 = (double*)take(8 * z.core);
+  s.tmp1 = (double*)take(8 * z.core);
+  s.Vf = (float*)take(4 * (int64_t)(a.m + 1) * z.N);
+  s.wf = (float*)take(4 * z.N);
+  s.T1f = (float*)take(4 * z.T);
+  s.T2f = (float*)take(4 * z.T);
+  s.Lf = (float*)take(4 * z.stack);
+  s.Rf = (float*)take(4 * z.stack);
+  s.Af = (float*)take(4 * z.opcore);
+  return s;
+}
+
+__device__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double* sm) {
+  const BatchInst& I = a.inst[j];
+  const int d = I.d;
+  const int64_t* M = a.meta + I.meta_off;
+  const int64_t* n = M;
+  const int64_t* R = n + d;
+  const int64_t* rb = R + d + 1;
+  const int64_t* rx0 = rb + d + 1;
+  const int64_t* cap = rx0 + d + 1;
+  const int64_t* op_off = cap + d + 1;
+  const int64_t* rhs_off = op_off + d;
+  const int64_t* x0_off = rhs_off + d;
+  const int64_t* X_off = x0_off + d;
+  const int64_t* L_off = X_off + d;
+  const int64_t* Rt_off = L_off + d;
+  const int64_t* Lb_off = Rt_off + d;
+  const int64_t* Rb_off = Lb_off + d;
+  __shared__ int64_t r[kMaxOrderB + 1];
+  for (int i = threadIdx.x; i <= d; i += blockDim.x) r[i] = cap[i];
+  __syncthreads();
+  const int tid = threadIdx.x;
+  auto X = [&](int i) { return I.X + X_off[i]; };
+  auto L = [&](int i) { return I.L + L_off[i]; };
+  auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
+  auto Lb = [&](int i) { return I.Lb + Lb_off[i]; };
+  auto Rb = [&](int i) { return I.Rb + Rb_off[i]; };
+  auto A = [&](int i) { return I.op + op_off[i]; };
+  auto B = [&](int i) { return I.rhs + rhs_off[i]; };
+
+  double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
+  int64_t nsolve = 0, nits = 0, ncyc = 0;
+  int status = ST_OK;
+  // algorithmic flops of one local-operator application / stack update
+  auto apply_fl = [&](double aa, double nn, double ss, double r0, double r1) {
+    return 2 * aa * aa * r0 * nn * ss + 2 * aa * ss * nn * nn * r0 * r1 + 2 * aa * nn * ss * ss * r1;
+  };
+  auto qr_fl = [&](double rows, double cols) {
+    const double k = rows < cols ? rows : cols;
+    return 2 * rows * cols * cols + 2 * rows * k * k;
+  };
+
+  // right-orthonormalise the guess (Householder RQ, R normalised and pushed left)
+  {
+    const double* cur = I.x0 + x0_off[d - 1];
+    int64_t cur_left = rx0[d - 1], cur_right = 1;
+    for (int i = d - 1; i >= 1; --i) {
+      const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
+      QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
+      cta_householder_qr(q);
+      const int64_t p = rx0[i - 1] * n[i - 1];
+      double* outb = (i & 1) ? S.tmp1 : S.tmp0;
+      cta_contract(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
+      cur = outb;
+      cur_left = rx0[i - 1];
+      cur_right = k;
+    }
+    cta_copy(X(0), cur, n[0] * cur_right);
+  }
+
+  auto right = [&](int i) {
+    if (i == d - 1) {
+      if (tid == 0) {
+        Rt(i)[0] = 1.0;
+        Rb(i)[0] = 1.0;
+      }
+      __syncthreads();
+      return;
+    }
+    const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
+    Contraction q1, q2, q3;
+    desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
+    cta_contract(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1);
+    cta_contract(q2, (const double*)S.T1, A(i + 1), S.T2);
+    cta_contract(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i));
+    fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
+    cta_contract(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
+    cta_contract(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
+  };
+  auto left = [&](int i) {
+    if (i == 0) {
+      if (tid == 0) {
+        L(i)[0] = 1.0;
+        Lb(i)[0] = 1.0;
+      }
+      __syncthreads();
+      return;
+    }
+    const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
+    Contraction p1, p2, p3;
+    desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
+    cta_contract(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1);
+    cta_contract(p2, (const double*)S.T1, A(i - 1), S.T2);
+    cta_contract(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i));
+    fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
+    cta_contract(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
+    cta_contract(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
+  };
+  auto solve = [&](int i) {
+    const int64_t aa = r[i], nn = n[i], ss = r[i + 1], N = aa * nn * ss;
+    cta_contract(desc_vec_u_left(aa, nn, rb[i], rb[i + 1]), (const double*)Lb(i), B(i), S.U);
+    cta_contract(desc_micro_f(aa, nn, ss, rb[i + 1]), (const double*)S.U, (const double*)Rb(i), S.f);
+    Contraction p1, p2, p3;
+    desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
+    const int m = (int)(N < a.m ? N : a.m);
+    CtaSolveStats st;
+    if (a.prec == 1) {
+      cta_to_float(S.Lf, L(i), aa * R[i] * aa);
+      cta_to_float(S.Rf, Rt(i), ss * R[i + 1] * ss);
+      cta_to_float(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
+      st = cta_gmres_ir<float>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
+                               S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm);
+    } else {
+      st = cta_gmres_ir<double>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
+                                S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm);
+    }
+    ++nsolve;
+    nits += st.inner;
+    ncyc += st.cycles;
+    {
+      const double fa = apply_fl((double)aa, (double)nn, (double)ss, (double)R[i], (double)R[i + 1]) + 2.0 * N;
+      const double per = st.cycles > 0 ? (double)st.inner / st.cycles : (double)st.inner;
+      const double inner = st.inner * fa + st.cycles * 8.0 * (double)N * per * (per + 1) / 2.0;
+      fl64 += st.cycles * fa;
+      if (a.prec == 1)
+        fl32 += inner;
+      else
+        fl64 += inner;
+    }
+    maxres = fmax(maxres, st.rel);
+    if (st.status != ST_OK && status == ST_OK) status = st.status;
+  };
+
+  for (int i = d - 1; i >= 0; --i) right(i);
+  for (int sweep = 0; sweep < I.repeats && status == ST_OK; ++sweep) {
+    for (int i = 0; i < d; ++i) {
+      left(i);
+      if (i < d - 1) {
+        solve(i);
+        const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
+        QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
+        cta_householder_qr(q);
+        fl64 += qr_fl((double)(aa * nn), (double)ss);
+        const int64_t qq = n[i + 1] * r[i + 2];
+        cta_contract(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
+        cta_copy(X(i + 1), S.tmp0, k * qq);
+        if (tid == 0) r[i + 1] = k;
+        __syncthreads();
+      }
+    }
+    for (int i = d - 1; i >= 0; --i) {
+      right(i);
+      solve(i);
+      if (i > 0) {
+        const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
+        QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
+        cta_householder_qr(q);
+        fl64 += qr_fl((double)ns, (double)aa);
+        const int64_t p = r[i - 1] * n[i - 1];
+        cta_contract(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
+        cta_copy(X(i - 1), S.tmp0, p * k);
+        if (tid == 0) r[i] = k;
+        __syncthreads();
+      }
+    }
+  }
+  // pack the final cores contiguously
+  int64_t off = 0;
+  for (int i = 0; i < d; ++i) {
+    const int64_t cnt = r[i] * n[i] * r[i + 1];
+    for (int64_t e = tid; e < cnt; e += blockDim.x) I.out[off + e] = X(i)[e];
+    off += cnt;
+  }
+  if (tid == 0) {
+    I.report[0] = maxres;
+    I.report[1] = (double)nsolve;
+    I.report[2] = (double)nits;
+    I.report[3] = (double)ncyc;
+    I.report[4] = (double)status;
+    I.report[5] = fl64;
+    I.report[6] = fl32;
+    for (int i = 0; i <= d; ++i) I.report[8 + i] = (double)r[i];
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_sle_kernel(BatchArgs a) {
+  extern __shared__ double sm[];
+  __shared__ int s_j;
+  const Scratch S = scratch_of(a, blockIdx.x);
+  for (;;) {
+    if (threadIdx.x == 0) s_j = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int j = s_j;
+    __syncthreads();
+    if (j >= a.count) return;
+    batch_solve(a, j, S, sm);
+  }
+}
+
+size_t batch_smem_bytes(int m) {
+  return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + (m + 1) + m + 2 * (m + 2));
+}
+
+int64_t batch_scratch_stride(const BatchSizes& z, int m) {
+  auto r = [](int64_t b) { return (b + 255) / 256 * 256; };
+  return r(8 * z.T) * 2 + r(8 * z.U) + r(8 * z.N) * 3 + r(8 * (int64_t)(m + 1) * z.N) + r(8 * z.R) + r(8 * z.Q) +
+         r(8 * z.core) * 2 + r(4 * (int64_t)(m + 1) * z.N) + r(4 * z.N) + r(4 * z.T) * 2 + r(4 * z.stack) * 2 +
+         r(4 * z.opcore);
+}
+
+int batch_blocks_per_sm(int m) {
+  const size_t smem = batch_smem_bytes(m);
+  cudaFuncSetAttribute(batch_sle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_sle_kernel, kBatchThreads, smem) != cudaSuccess ||
+      occ < 1)
+    occ = 1;
+  return occ;
+}
+
+cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st) {
+  const size_t smem = batch_smem_bytes(a.m);
+  cudaError_t e = cudaFuncSetAttribute(batch_sle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  batch_sle_kernel<<<grid, kBatchThreads, smem, st>>>(a);
+  ++launch_counter();
+  return cudaGetLastError();
+}
+
+}  // namespace ttals

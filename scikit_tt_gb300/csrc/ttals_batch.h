@@ -1,0 +1,44 @@
+// Shared host/device structures of the batched ALS kernel (kernels_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ttals {
+
+// One instance.  meta (int64, at meta + meta_off) holds, in order:
+// n[d], R[d+1], rb[d+1], rx0[d+1], cap[d+1], op_off[d], rhs_off[d], x0_off[d],
+// X_off[d], L_off[d], Rt_off[d], Lb_off[d], Rb_off[d].
+struct BatchInst {
+  int32_t d, repeats;
+  int64_t meta_off;
+  const double *op, *rhs, *x0;
+  double *X, *L, *Rt, *Lb, *Rb;
+  double* out;     // final cores, packed
+  double* report;  // [max rel residual, local solves, Krylov its, refinement cycles, status, -, -, -, ranks[d+1]]
+};
+
+// Largest per-CTA scratch needs over the batch (elements).
+struct BatchSizes {
+  int64_t T, U, N, R, Q, core, stack, opcore;
+};
+
+struct BatchArgs {
+  const BatchInst* inst;
+  int count;
+  const int64_t* meta;
+  int* next;  // work counter (zeroed before launch)
+  char* scratch;
+  int64_t scratch_stride;
+  BatchSizes sizes;
+  int m;
+  int prec;
+  double tol;
+};
+
+size_t batch_smem_bytes(int m);
+int batch_blocks_per_sm(int m);
+int64_t batch_scratch_stride(const BatchSizes& z, int m);
+cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st);
+
+}  // namespace ttals

@@ -35,63 +35,90 @@ enum : int {
 };
 
 // C[out] = alpha * sum_k A[a_off(out) + a_k(k)] * B[b_off(out) + b_k(k)] + beta * C[out]
-// out is the row-major multi-index over out_dim[0..nout-1]; C is dense in
-// that order unless c_stride is given.
+// out is the row-major multi-index over out_dim[0..nout-1].  Offsets and
+// element counts are 32-bit (every buffer of the path holds < 2^31 elements;
+// launchers reject larger contractions).  Output indices are decoded with
+// precomputed multiply-shift division (Granlund-Montgomery round-up method):
+// for n < 2^31, n / d == (umulhi(n, mag) + n) >> shf.
 struct Contraction {
   int nout, nk;
   int out_dim[kMaxOut];
+  uint32_t out_mag[kMaxOut];
+  int out_shf[kMaxOut];
   int k_dim[kMaxK];
-  int64_t a_os[kMaxOut], a_ks[kMaxK];
-  int64_t b_os[kMaxOut], b_ks[kMaxK];
-  int64_t c_os[kMaxOut];
+  int a_os[kMaxOut], a_ks[kMaxK];
+  int b_os[kMaxOut], b_ks[kMaxK];
+  int c_os[kMaxOut];
   int64_t total;   // product of out_dim
   int64_t ktotal;  // product of k_dim
 };
 
+__host__ __device__ __forceinline__ void fast_div_params(uint32_t d, uint32_t* mag, int* shf) {
+  int l = 0;
+  while (l < 31 && (1u << l) < d) ++l;
+  *shf = l;
+  *mag = (uint32_t)(((uint64_t)1 << 32) * ((uint64_t(1) << l) - d) / d + 1);
+}
+
+__host__ __device__ __forceinline__ uint32_t fast_div(uint32_t n, uint32_t mag, int shf) {
+#ifdef __CUDA_ARCH__
+  const uint32_t t = __umulhi(n, mag);
+#else
+  const uint32_t t = (uint32_t)(((uint64_t)n * mag) >> 32);
+#endif
+  return (t + n) >> shf;
+}
+
 // Offsets of output element e (row-major over out_dim) in A, B and C.
-__device__ __forceinline__ void contract_offsets(const Contraction& c, int64_t e, int64_t& ao,
-                                                 int64_t& bo, int64_t& co) {
-  int64_t rem = e;
-  ao = 0; bo = 0; co = 0;
+__host__ __device__ __forceinline__ void contract_offsets(const Contraction& c, int64_t e, int64_t& ao,
+                                                          int64_t& bo, int64_t& co) {
+  uint32_t rem = (uint32_t)e;
+  int a = 0, b = 0, o = 0;
 #pragma unroll
   for (int q = kMaxOut - 1; q >= 0; --q) {
     if (q < c.nout) {
-      int64_t iq = rem % c.out_dim[q];
-      rem /= c.out_dim[q];
-      ao += iq * c.a_os[q];
-      bo += iq * c.b_os[q];
-      co += iq * c.c_os[q];
+      const uint32_t qq = fast_div(rem, c.out_mag[q], c.out_shf[q]);
+      const int iq = (int)(rem - qq * (uint32_t)c.out_dim[q]);
+      rem = qq;
+      a += iq * c.a_os[q];
+      b += iq * c.b_os[q];
+      o += iq * c.c_os[q];
     }
   }
+  ao = a;
+  bo = b;
+  co = o;
 }
 
 // The contraction sum of one output element.
 template <typename T>
-__device__ __forceinline__ T contract_sum(const Contraction& c, const T* __restrict__ A,
-                                          const T* __restrict__ B, int64_t ao, int64_t bo) {
+__host__ __device__ __forceinline__ T contract_sum(const Contraction& c, const T* __restrict__ A,
+                                                   const T* __restrict__ B, int64_t ao, int64_t bo) {
   T acc = T(0);
+  const T* pa = A + ao;
+  const T* pb = B + bo;
   if (c.nk == 1) {
-    const int64_t sa = c.a_ks[0], sb = c.b_ks[0];
-    const T* pa = A + ao;
-    const T* pb = B + bo;
-    for (int k = 0; k < c.k_dim[0]; ++k) acc += pa[k * sa] * pb[k * sb];
+    const int sa = c.a_ks[0], sb = c.b_ks[0], K = c.k_dim[0];
+#pragma unroll 4
+    for (int k = 0; k < K; ++k) acc += pa[k * sa] * pb[k * sb];
   } else if (c.nk == 2) {
-    const int64_t sa = c.a_ks[1], sb = c.b_ks[1];
+    const int sa = c.a_ks[1], sb = c.b_ks[1], K1 = c.k_dim[1];
     for (int k0 = 0; k0 < c.k_dim[0]; ++k0) {
-      const T* pa = A + ao + k0 * c.a_ks[0];
-      const T* pb = B + bo + k0 * c.b_ks[0];
-      for (int k1 = 0; k1 < c.k_dim[1]; ++k1) acc += pa[k1 * sa] * pb[k1 * sb];
+      const T* qa = pa + k0 * c.a_ks[0];
+      const T* qb = pb + k0 * c.b_ks[0];
+#pragma unroll 4
+      for (int k1 = 0; k1 < K1; ++k1) acc += qa[k1 * sa] * qb[k1 * sb];
     }
   } else if (c.nk == 3) {
-    const int64_t sa = c.a_ks[2], sb = c.b_ks[2];
+    const int sa = c.a_ks[2], sb = c.b_ks[2], K2 = c.k_dim[2];
     for (int k0 = 0; k0 < c.k_dim[0]; ++k0)
       for (int k1 = 0; k1 < c.k_dim[1]; ++k1) {
-        const T* pa = A + ao + k0 * c.a_ks[0] + k1 * c.a_ks[1];
-        const T* pb = B + bo + k0 * c.b_ks[0] + k1 * c.b_ks[1];
-        for (int k2 = 0; k2 < c.k_dim[2]; ++k2) acc += pa[k2 * sa] * pb[k2 * sb];
+        const T* qa = pa + k0 * c.a_ks[0] + k1 * c.a_ks[1];
+        const T* qb = pb + k0 * c.b_ks[0] + k1 * c.b_ks[1];
+        for (int k2 = 0; k2 < K2; ++k2) acc += qa[k2 * sa] * qb[k2 * sb];
       }
   } else {  // nk == 0: elementwise product
-    acc = A[ao] * B[bo];
+    acc = pa[0] * pb[0];
   }
   return acc;
 }

@@ -1,0 +1,120 @@
+// Householder QR executed by one CTA (any block size that is a multiple of 32).
+// Column-major working copy W (rows x cols) and reflectors Vh (rows x k) live in
+// global scratch (L2 resident at ALS sizes).  Reflector j: H_j = I - tau_j v_j v_j^T
+// with v_j[j] = x_j - alpha_j, alpha_j = -sign(x_j) ||x||, so R[j][j] = alpha_j
+// (the LAPACK sign choice).  The input may alias the Q output: it is read
+// completely before the first barrier.
+#pragma once
+
+#include "ttals_internal.h"
+
+namespace ttals {
+
+__device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
+  const int64_t rows = a.rows, cols = a.cols;
+  const int64_t k = rows < cols ? rows : cols;
+  double* W = a.work;
+  double* Vh = W + rows * cols;
+  double* Qw = Vh + rows * k;
+  double* tau = Qw + rows * k;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  __shared__ double red[32];
+  __shared__ double s_alpha, s_tau, s_v0;
+
+  for (int64_t e = tid; e < rows * cols; e += nt) {
+    const int64_t i = e % rows, c = e / rows;
+    W[e] = a.in[i * a.ris + c * a.rjs];
+  }
+  __syncthreads();
+
+  for (int64_t j = 0; j < k; ++j) {
+    const double* col = W + j * rows;
+    double s = 0.0;
+    for (int64_t i = j + tid; i < rows; i += nt) s += col[i] * col[i];
+    s = warp_sum(s);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (tid == 0) {
+      double tot = 0.0;
+      for (int w = 0; w < nw; ++w) tot += red[w];
+      const double x0 = col[j];
+      const double nrm = sqrt(tot);
+      if (nrm == 0.0) {
+        s_alpha = 0.0; s_tau = 0.0; s_v0 = 1.0;
+      } else {
+        const double alpha = (x0 >= 0.0) ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        const double vn2 = tot - x0 * x0 + v0 * v0;
+        s_alpha = alpha; s_v0 = v0; s_tau = (vn2 > 0.0) ? 2.0 / vn2 : 0.0;
+      }
+      tau[j] = s_tau;
+    }
+    __syncthreads();
+    double* v = Vh + j * rows;
+    for (int64_t i = j + tid; i < rows; i += nt) v[i] = (i == j) ? s_v0 : col[i];
+    __syncthreads();
+    const double tj = s_tau;
+    for (int64_t c = j + 1 + warp; c < cols; c += nw) {
+      double* wc = W + c * rows;
+      double dot = 0.0;
+      for (int64_t i = j + lane; i < rows; i += 32) dot += v[i] * wc[i];
+      dot = warp_sum(dot) * tj;
+      for (int64_t i = j + lane; i < rows; i += 32) wc[i] -= dot * v[i];
+    }
+    __syncthreads();
+    if (tid == 0) W[j * rows + j] = s_alpha;
+    __syncthreads();
+  }
+
+  // R (k x cols, upper trapezoidal) and optional normalisation
+  double rscale = 1.0;
+  if (a.normalize_r) {
+    double s = 0.0;
+    for (int64_t e = tid; e < k * cols; e += nt) {
+      const int64_t i = e / cols, c = e % cols;
+      if (i <= c) { const double v = W[c * rows + i]; s += v * v; }
+    }
+    s = warp_sum(s);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    double tot = 0.0;
+    for (int w = 0; w < nw; ++w) tot += red[w];
+    __syncthreads();
+    const double nrm = sqrt(tot);
+    if (a.rnorm && tid == 0) *a.rnorm = nrm;
+    rscale = (nrm > 0.0) ? 1.0 / nrm : 1.0;
+  }
+  if (a.r) {
+    for (int64_t e = tid; e < k * cols; e += nt) {
+      const int64_t i = e / cols, c = e % cols;
+      a.r[i * a.r_is + c * a.r_js] = (i <= c) ? W[c * rows + i] * rscale : 0.0;
+    }
+  }
+
+  // Q = H_0 ... H_{k-1} [I_k; 0], accumulated backwards (column-major Qw)
+  for (int64_t e = tid; e < rows * k; e += nt) {
+    const int64_t i = e % rows, c = e / rows;
+    Qw[e] = (i == c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  for (int64_t j = k - 1; j >= 0; --j) {
+    const double* v = Vh + j * rows;
+    const double tj = tau[j];
+    for (int64_t c = j + warp; c < k; c += nw) {
+      double* qc = Qw + c * rows;
+      double dot = 0.0;
+      for (int64_t i = j + lane; i < rows; i += 32) dot += v[i] * qc[i];
+      dot = warp_sum(dot) * tj;
+      for (int64_t i = j + lane; i < rows; i += 32) qc[i] -= dot * v[i];
+    }
+    __syncthreads();
+  }
+  for (int64_t e = tid; e < rows * k; e += nt) {
+    const int64_t i = e % rows, c = e / rows;
+    a.q[i * a.qis + c * a.qjs] = Qw[e];
+  }
+  __syncthreads();
+}
+
+}  // namespace ttals

@@ -132,3 +132,39 @@ def __construct_micro_matrix_als(i: int, stack_left_op: List[np.ndarray], stack_
 def __construct_micro_matrix_mals(i, stack_left_op, stack_right_op, operator, solution):
     """Two-site micro matrix (sle.py:350-390): MALS is not on the device path yet."""
     raise NotImplementedError('MALS micro matrices are not implemented on the device path')
+
+
+def als_batch(problems, repeats=1, precision: str = None, tol: float = 0.0):
+    """Solve many independent systems in one launch (one CTA per system).
+
+    ``problems``: sequence of ``(operator, initial_guess, right_hand_side)`` TT
+    triples (shapes may differ); ``repeats``: int or per-problem list.  Returns
+    ``(solutions, stats)``; each solution equals what ``als`` returns for that
+    problem (to the local-solve tolerance)."""
+    precision = precision or PRECISION
+    if precision not in _PREC:
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    count = len(problems)
+    if count == 0:
+        return [], {}
+    reps = list(repeats) if isinstance(repeats, (list, tuple)) else [int(repeats)] * count
+    packs = [(_lib.Packed(a.cores), _lib.Packed(x.cores), _lib.Packed(b.cores)) for a, x, b in problems]
+    lib = _lib.load()
+    outs, ranks_all = [], []
+    for (a, x, b), (pa, px, pb) in zip(problems, packs):
+        dims = np.array(a.row_dims, dtype=np.int64)
+        rk = np.zeros(a.order + 1, dtype=np.int64)
+        _lib.check(lib.ttals_als_ranks(a.order, _lib.i64ptr(dims), _lib.i64ptr(px.ranks), _lib.i64ptr(rk)))
+        total = int(sum(rk[i] * dims[i] * rk[i + 1] for i in range(a.order)))
+        outs.append(np.empty(max(total, 1), dtype=np.float64))
+        ranks_all.append(rk)
+    ops = (_lib.TTDesc * count)(*[p[0].desc for p in packs])
+    xs = (_lib.TTDesc * count)(*[p[1].desc for p in packs])
+    bs = (_lib.TTDesc * count)(*[p[2].desc for p in packs])
+    rep_arr = (_lib.C.c_int32 * count)(*reps)
+    out_ptrs = (_lib.C.POINTER(_lib.C.c_double) * count)(*[_lib.dptr(o) for o in outs])
+    st = _lib.Stats()
+    _lib.check(lib.ttals_sle_als_batch(_lib.context(), count, ops, xs, bs, rep_arr, _PREC[precision], float(tol),
+                                       out_ptrs, 0, st))
+    sols = [TT(_lib.unpack(o, a.row_dims, [1] * a.order, rk)) for o, (a, _, _), rk in zip(outs, problems, ranks_all)]
+    return sols, st.as_dict()

@@ -1,0 +1,79 @@
+"""Batched SLE ALS (one CTA per instance) against the oracle and the
+single-instance engine, on instances of uneven order, mode size and rank."""
+
+import numpy as np
+import pytest
+
+from oracle import tt_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _tt(cores):
+    from scikit_tt_gb300.tensor_train import TT
+    return TT([np.array(c) for c in cores])
+
+
+def _instances():
+    from scikit_tt_gb300 import workloads as wl
+    out = []
+    for j, (d, n, r) in enumerate([(6, 2, 4), (5, 4, 6), (8, 3, 5), (4, 8, 9), (7, 2, 3), (9, 4, 8)]):
+        rng = np.random.default_rng(100 + j)
+        c = rng.uniform(0, 0.5, d)
+        op = wl.coupled_op(d, n, c, shift=1.0 + 0.1 * j)
+        rhs = wl.gaussian_tt(rng, d, n, 3)
+        x0 = wl.gaussian_tt(rng, d, n, r)
+        out.append((op, x0, rhs))
+    return out
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-10), ('mixed', 1e-8)])
+def test_batch_matches_oracle(precision, tol):
+    from scikit_tt_gb300.solvers import sle
+    inst = _instances()
+    probs = [(_tt(a), _tt(x), _tt(b)) for a, x, b in inst]
+    sols, st = sle.als_batch(probs, repeats=2, precision=precision)
+    assert st['local_solves'] == sum(2 * (2 * len(a) - 1) for a, _, _ in inst)
+    for (a, x, b), sol in zip(inst, sols):
+        ref = O.sle_als(a, x, b, repeats=2)
+        assert O.stable_rel_diff(sol.cores, ref) < tol
+
+
+def test_batch_equals_single_engine():
+    from scikit_tt_gb300.solvers import sle
+    inst = _instances()[:3]
+    probs = [(_tt(a), _tt(x), _tt(b)) for a, x, b in inst]
+    sols, _ = sle.als_batch(probs, repeats=[1, 2, 3])
+    for (a, x, b), sol, rep in zip(probs, sols, [1, 2, 3]):
+        single = sle.als(a, x, b, repeats=rep)
+        assert O.stable_rel_diff(sol.cores, single.cores) < 1e-11
+
+
+def test_batch_golden_reference(golden):
+    from scikit_tt_gb300.solvers import sle
+    z, cores = golden('sle_coupled_d8')
+    z2, cores2 = golden('sle_laplace_d10_r8')
+    probs = [(_tt(cores('op')), _tt(cores('x0')), _tt(cores('rhs'))),
+             (_tt(cores2('op')), _tt(cores2('x0')), _tt(cores2('rhs')))]
+    sols, _ = sle.als_batch(probs, repeats=[int(z['repeats']), int(z2['repeats'])])
+    assert O.stable_rel_diff(sols[0].cores, cores('sol')) < 1e-10
+    assert O.stable_rel_diff(sols[1].cores, cores2('sol')) < 1e-10
+
+
+def test_batch_many_instances_more_than_sms():
+    # more instances than CTAs: CTAs take several instances from the work counter
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.solvers import sle
+    probs, inst = [], []
+    for j in range(400):
+        rng = np.random.default_rng(7000 + j)
+        d, n, r = 4 + j % 3, 2, 2 + j % 3
+        op = wl.laplace_op(d, n, shift=1.0 + (j % 5) * 0.1)
+        rhs = wl.gaussian_tt(rng, d, n, 2)
+        x0 = wl.gaussian_tt(rng, d, n, r)
+        inst.append((op, x0, rhs))
+        probs.append((_tt(op), _tt(x0), _tt(rhs)))
+    sols, _ = sle.als_batch(probs, repeats=1)
+    for k in (0, 151, 152, 399):
+        a, x, b = inst[k]
+        assert O.stable_rel_diff(sols[k].cores, O.sle_als(a, x, b, repeats=1)) < 1e-10
