@@ -48,6 +48,11 @@ extern "C" {
 #define TTALS_EVP_EIGH 2
 
 typedef struct ttals_ctx ttals_ctx;
+typedef struct ttals_job ttals_job;
+
+/* request kinds of the batched / served entry points */
+#define TTALS_REQ_SLE 0 /* scikit_tt/solvers/sle.py:10 als */
+#define TTALS_REQ_EVP 1 /* scikit_tt/solvers/evp.py:17 als (symmetric, number_ev == 1) */
 
 typedef struct {
   int32_t order;
@@ -57,6 +62,22 @@ typedef struct {
   const double* data;      /* concatenated cores */
   int32_t on_device;       /* 0: host pointer, 1: device pointer */
 } ttals_tt;
+
+/* One ALS problem of a batch.  out_data receives the solution cores (ranks
+ * from ttals_als_ranks; for EVP the best sweep's eigentensor, evp.py:151-155);
+ * out_value the eigenvalue and out_iterations the sweeps run (EVP, may be
+ * NULL).  rhs is ignored for EVP. */
+typedef struct {
+  int32_t kind;
+  ttals_tt op, x0, rhs;
+  int32_t repeats;
+  int32_t solver;
+  double sigma;
+  double conv_eps;
+  double* out_data;
+  double* out_value;
+  int32_t* out_iterations;
+} ttals_request;
 
 typedef struct {
   int64_t local_solves;       /* micro systems solved                          */
@@ -111,6 +132,26 @@ int ttals_sle_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const 
 int ttals_sle_als_batch(ttals_ctx* ctx, int32_t count, const ttals_tt* ops, const ttals_tt* x0s,
                         const ttals_tt* rhss, const int32_t* repeats, int32_t precision, double tol,
                         double* const* out_data, int32_t out_on_device, ttals_stats* stats);
+
+/* Mixed batch of SLE and EVP requests (each `als` of sle.py:10 / evp.py:17),
+ * one CTA per request, synchronous.  Outputs follow out_on_device. */
+int ttals_solve_batch(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int32_t precision, double tol,
+                      int32_t out_on_device, ttals_stats* stats);
+
+/* Serving: the same as ttals_solve_batch but asynchronous.  The call copies
+ * the inputs, reserves the batch's device memory (TTALS_ERR_NOMEM, with
+ * nothing allocated, when the context's budget would be exceeded -- retry
+ * after finishing a job), launches on a stream of its own and returns; jobs
+ * submitted while others run share the GPU.  ttals_job_poll reports
+ * completion without blocking; ttals_job_finish waits, writes the outputs to
+ * the requests' host pointers, releases the memory and frees the job.
+ * No reference counterpart (the reference has no serving layer). */
+int ttals_submit(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int32_t precision, double tol,
+                 ttals_job** job);
+int ttals_job_poll(ttals_job* job, int32_t* done);
+int ttals_job_finish(ttals_job* job, ttals_stats* stats);
+/* Device bytes a batch would reserve (admission control). */
+int ttals_batch_bytes(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int64_t* bytes);
 
 /* scikit_tt/solvers/evp.py:17 `als(operator, initial_guess, previous, shift,
  * operator_gevp=None, number_ev, repeats, conv_eps, solver, sigma, real)` for

@@ -37,13 +37,24 @@ EXPORTS = (
     'ttals_create', 'ttals_destroy', 'ttals_last_error', 'ttals_set_stream', 'ttals_als_ranks',
     'ttals_sle_als', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_norm',
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
-    'ttals_stack_op_noalloc', 'ttals_sle_als_batch',
+    'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
+    'ttals_job_finish', 'ttals_batch_bytes',
 )
+
+REQ_SLE = 0
+REQ_EVP = 1
 
 
 class TTDesc(C.Structure):
     _fields_ = [('order', C.c_int32), ('row_dims', C.POINTER(C.c_int64)), ('col_dims', C.POINTER(C.c_int64)),
                 ('ranks', C.POINTER(C.c_int64)), ('data', C.POINTER(C.c_double)), ('on_device', C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [('kind', C.c_int32), ('op', TTDesc), ('x0', TTDesc), ('rhs', TTDesc), ('repeats', C.c_int32),
+                ('solver', C.c_int32), ('sigma', C.c_double), ('conv_eps', C.c_double),
+                ('out_data', C.POINTER(C.c_double)), ('out_value', C.POINTER(C.c_double)),
+                ('out_iterations', C.POINTER(C.c_int32))]
 
 
 class Stats(C.Structure):
@@ -95,6 +106,11 @@ def load():
         lib.ttals_measure_peaks.argtypes = [vp, pd, pd]
         lib.ttals_sle_als_batch.argtypes = [vp, i32, P(TTDesc), P(TTDesc), P(TTDesc), P(i32), i32, dbl,
                                             P(pd), i32, P(Stats)]
+        lib.ttals_solve_batch.argtypes = [vp, i32, P(Request), i32, dbl, i32, P(Stats)]
+        lib.ttals_submit.argtypes = [vp, i32, P(Request), i32, dbl, P(vp)]
+        lib.ttals_job_poll.argtypes = [vp, P(i32)]
+        lib.ttals_job_finish.argtypes = [vp, P(Stats)]
+        lib.ttals_batch_bytes.argtypes = [vp, i32, P(Request), P(C.c_int64)]
         lib.ttals_stack_op_noalloc.argtypes = [vp, i32, pd, pd, pd, i64, i64, i64, i64, i64, pd]
         for name in EXPORTS:
             if name not in ('ttals_last_error',):

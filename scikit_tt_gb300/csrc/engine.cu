@@ -46,6 +46,7 @@ struct ttals_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool profiling = false;
   std::vector<cudaEvent_t> evpool;  // event pairs around local-solve launches
+  size_t inflight = 0;               // device bytes held by submitted jobs
 };
 
 namespace {
@@ -622,38 +623,78 @@ void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttal
 }
 
 // ---------------------------------------------------------------------------
-// batched SLE driver: one CTA per instance (kernels_batch.cu)
+// batched driver: one CTA per request (kernels_batch.cu)
 // ---------------------------------------------------------------------------
 
-void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt* x0s, const ttals_tt* rhss,
-                   const int32_t* repeats, int prec, double tol, double* const* outs, int out_dev, ttals_stats* st) {
-  require(count >= 1, TTALS_ERR_ARG, "count must be >= 1");
-  require(ops && x0s && rhss && repeats && outs, TTALS_ERR_ARG, "null array argument");
-  require(prec == TTALS_PREC_FP64 || prec == TTALS_PREC_MIXED, TTALS_ERR_ARG, "unknown precision mode");
-  if (tol <= 0) tol = (prec == TTALS_PREC_FP64) ? 1e-13 : 1e-10;
-  launch_counter() = 0;
-  const int m = 40;
-  struct Inst {
-    TTView op, x0, b;
-    std::vector<int64_t> cap, fin;
-    int64_t region = 0, meta_off = 0;
-    std::vector<int64_t> off;  // op, rhs, x0, X, L, Rt, Lb, Rb, out, report (relative to region)
-  };
-  std::vector<Inst> in(count);
+constexpr int kBatchM = 40;     // GMRES restart length
+constexpr int kBatchMEvp = 64;  // Lanczos basis size
+
+struct BatchReqHost {
+  TTView op, x0, b;
+  int kind = 0, repeats = 1, mode = 1;
+  double sigma = 1.0, conv_eps = 1e-10;
+  std::vector<int64_t> cap, fin;
+  int64_t region = 0, meta_off = 0, out_count = 0;
+  std::vector<int64_t> off;  // op, rhs, x0, X, L, Rt, Lb, Rb, out, report, Xopt
+  double* out = nullptr;
+  double* out_val = nullptr;
+  int32_t* out_its = nullptr;
+};
+
+struct BatchPlan {
+  std::vector<BatchReqHost> in;
   BatchSizes z{1, 1, 1, 1, 1, 1, 1, 1};
   std::vector<int64_t> meta;
-  int64_t region_total = 0;
+  int64_t region_total = 0;  // doubles
+  int grid = 1;
+  int64_t stride = 0;
+  int prec = 0;
+  double tol = 0.0;
+  // byte layout of the device block: [regions | meta | inst | scratch | counter]
+  size_t off_meta = 0, off_inst = 0, off_scratch = 0, off_next = 0, bytes = 0;
+};
+
+BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol) {
+  require(count >= 1, TTALS_ERR_ARG, "count must be >= 1");
+  require(reqs != nullptr, TTALS_ERR_ARG, "null request array");
+  require(prec == TTALS_PREC_FP64 || prec == TTALS_PREC_MIXED, TTALS_ERR_ARG, "unknown precision mode");
+  BatchPlan P;
+  P.prec = prec;
+  P.tol = tol > 0 ? tol : (prec == TTALS_PREC_FP64 ? 1e-13 : 1e-10);
+  P.in.resize(count);
   for (int j = 0; j < count; ++j) {
-    Inst& I = in[j];
-    I.op = view(ops + j, "operator");
-    I.x0 = view(x0s + j, "initial_guess");
-    I.b = view(rhss + j, "right_hand_side");
+    const ttals_request& q = reqs[j];
+    BatchReqHost& I = P.in[j];
+    require(q.kind == TTALS_REQ_SLE || q.kind == TTALS_REQ_EVP, TTALS_ERR_ARG, "unknown request kind");
+    I.kind = q.kind == TTALS_REQ_EVP ? 1 : 0;
+    I.op = view(&q.op, "operator");
+    I.x0 = view(&q.x0, "initial_guess");
     validate_square_op(I.op);
     validate_vec(I.x0, I.op, "initial_guess");
-    validate_vec(I.b, I.op, "right_hand_side");
-    require(repeats[j] >= 1, TTALS_ERR_ARG, "repeats must be >= 1 in a batch");
+    if (I.kind == 0) {
+      I.b = view(&q.rhs, "right_hand_side");
+      validate_vec(I.b, I.op, "right_hand_side");
+      require(q.solver == TTALS_SLE_SOLVE || q.solver == TTALS_SLE_LU, TTALS_ERR_ARG, "solver must be 'solve' or 'lu'");
+    } else {
+      require(q.solver == TTALS_EVP_EIG || q.solver == TTALS_EVP_EIGS || q.solver == TTALS_EVP_EIGH, TTALS_ERR_ARG,
+              "solver must be 'eig', 'eigs' or 'eigh'");
+      I.mode = q.solver == TTALS_EVP_EIGH ? 0 : 1;
+      I.sigma = q.sigma;
+      I.conv_eps = q.conv_eps;
+      I.b = TTView();
+      I.b.d = I.op.d;
+      I.b.r.assign(I.op.d + 1, 1);
+      I.b.off.assign(I.op.d + 1, 0);
+      I.b.total = 0;
+    }
+    require(q.repeats >= 1, TTALS_ERR_ARG, "repeats must be >= 1 in a batch");
+    require(q.out_data != nullptr, TTALS_ERR_ARG, "request without an output buffer");
+    I.repeats = q.repeats;
+    I.out = q.out_data;
+    I.out_val = q.out_value;
+    I.out_its = q.out_iterations;
     const int d = I.op.d;
-    require(d <= 256, TTALS_ERR_UNSUPPORTED, "batched instances support order <= 256");
+    require(d <= 256, TTALS_ERR_UNSUPPORTED, "batched requests support order <= 256");
     const std::vector<int64_t>& n = I.op.m;
     const std::vector<int64_t>& R = I.op.r;
     const std::vector<int64_t>& rb = I.b.r;
@@ -661,7 +702,7 @@ void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt*
     I.cap = ro_ranks(n, rx0);
     I.fin = final_ranks(n, rx0);
     std::vector<int64_t> Xo(d), Lo(d), Rto(d), Lbo(d), Rbo(d);
-    int64_t xs = 0, ls = 0, rts = 0, lbs = 0, rbs = 0, outs_n = 0;
+    int64_t xs = 0, ls = 0, rts = 0, lbs = 0, rbs = 0;
     for (int i = 0; i < d; ++i) {
       const int64_t a = I.cap[i], nn = n[i], s = I.cap[i + 1];
       Xo[i] = xs;
@@ -674,38 +715,40 @@ void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt*
       lbs += rb[i] * a;
       Rbo[i] = rbs;
       rbs += rb[i + 1] * s;
-      outs_n += I.fin[i] * nn * I.fin[i + 1];
-      z.N = std::max(z.N, a * nn * s);
-      z.T = std::max(z.T, std::max(R[i], R[i + 1]) * std::max(a, s) * std::max(a, s) * nn);
-      z.U = std::max(z.U, std::max(a, s) * nn * std::max(rb[i], rb[i + 1]));
-      z.R = std::max(z.R, std::max(std::max(a, s) * std::max(a, s), rx0[i] * rx0[i]));
-      z.Q = std::max(z.Q, std::max(std::max(qr_work(a * nn, s), qr_work(nn * s, a)), qr_work(nn * I.cap[i + 1], rx0[i])));
-      z.core = std::max(z.core, std::max(a * nn * s, rx0[i] * nn * std::max(I.cap[i + 1], rx0[i + 1])));
-      z.stack = std::max(z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
-      z.opcore = std::max(z.opcore, R[i] * nn * nn * R[i + 1]);
+      I.out_count += I.fin[i] * nn * I.fin[i + 1];
+      P.z.N = std::max(P.z.N, a * nn * s);
+      P.z.T = std::max(P.z.T, std::max(R[i], R[i + 1]) * std::max(a, s) * std::max(a, s) * nn);
+      P.z.U = std::max(P.z.U, std::max(a, s) * nn * std::max(rb[i], rb[i + 1]));
+      P.z.R = std::max(P.z.R, std::max(std::max(a, s) * std::max(a, s), rx0[i] * rx0[i]));
+      P.z.Q = std::max(P.z.Q,
+                       std::max(std::max(qr_work(a * nn, s), qr_work(nn * s, a)), qr_work(nn * I.cap[i + 1], rx0[i])));
+      P.z.core = std::max(P.z.core, std::max(a * nn * s, rx0[i] * nn * std::max(I.cap[i + 1], rx0[i + 1])));
+      P.z.stack = std::max(P.z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
+      P.z.opcore = std::max(P.z.opcore, R[i] * nn * nn * R[i + 1]);
     }
-    // instance region layout (doubles)
-    I.off.resize(10);
+    require(P.z.T < (int64_t(1) << 31) && P.z.N * (kBatchMEvp + 1) < (int64_t(1) << 31), TTALS_ERR_UNSUPPORTED,
+            "a request exceeds the 32-bit index range of the batch kernel");
+    I.off.resize(11);
     int64_t o = 0;
     auto put = [&](int k, int64_t cnt) {
       I.off[k] = o;
       o += (cnt + 31) / 32 * 32;
     };
     put(0, I.op.total);
-    put(1, I.b.total);
+    put(1, std::max<int64_t>(I.b.total, 1));
     put(2, I.x0.total);
     put(3, xs);
     put(4, ls);
     put(5, rts);
     put(6, lbs);
     put(7, rbs);
-    put(8, outs_n);
-    put(9, 8 + d + 1);
-    I.region = region_total;
-    region_total += o;
-    // meta
-    I.meta_off = (int64_t)meta.size();
-    auto app = [&](const std::vector<int64_t>& v, int cnt) { meta.insert(meta.end(), v.begin(), v.begin() + cnt); };
+    put(8, I.out_count);
+    put(9, 10 + d);
+    put(10, I.kind == 1 ? xs : 1);
+    I.region = P.region_total;
+    P.region_total += o;
+    I.meta_off = (int64_t)P.meta.size();
+    auto app = [&](const std::vector<int64_t>& v, int cnt) { P.meta.insert(P.meta.end(), v.begin(), v.begin() + cnt); };
     app(n, d);
     app(R, d + 1);
     app(rb, d + 1);
@@ -722,27 +765,40 @@ void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt*
     app(Lbo, d);
     app(Rbo, d);
   }
-  const int grid = std::min(count, c->num_sms * batch_blocks_per_sm(m));
-  const int64_t stride = batch_scratch_stride(z, m);
-  double* data = nullptr;
-  int64_t* dmeta = nullptr;
-  BatchInst* dinst = nullptr;
-  char* scratch = nullptr;
-  int* next = nullptr;
-  Bump B{c};
-  B.want(&data, region_total);
-  B.want(&dmeta, (int64_t)meta.size());
-  B.want((char**)&dinst, (int64_t)sizeof(BatchInst) * count);
-  B.want(&scratch, stride * grid);
-  B.want(&next, 4);
-  B.commit();
+  P.grid = std::min(count, c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp));
+  P.stride = batch_scratch_stride(P.z, kBatchM, kBatchMEvp);
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  size_t o = al(sizeof(double) * P.region_total);
+  P.off_meta = o;
+  o += al(sizeof(int64_t) * P.meta.size());
+  P.off_inst = o;
+  o += al(sizeof(BatchInst) * count);
+  P.off_scratch = o;
+  o += (size_t)P.stride * P.grid;
+  P.off_next = o;
+  o += 256;
+  P.bytes = o;
+  return P;
+}
+
+// Enqueue uploads and the batch kernel on `st` into the device block `mem`
+// (P.bytes).  k0/k1 bracket the kernel.
+void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1) {
+  const int count = (int)P.in.size();
+  double* data = (double*)mem;
+  int64_t* dmeta = (int64_t*)(mem + P.off_meta);
+  BatchInst* dinst = (BatchInst*)(mem + P.off_inst);
   std::vector<BatchInst> hinst(count);
   for (int j = 0; j < count; ++j) {
-    Inst& I = in[j];
+    BatchReqHost& I = P.in[j];
     double* base = data + I.region;
     BatchInst& H = hinst[j];
     H.d = I.op.d;
-    H.repeats = repeats[j];
+    H.repeats = I.repeats;
+    H.kind = I.kind;
+    H.mode = I.mode;
+    H.sigma = I.sigma;
+    H.conv_eps = I.conv_eps;
     H.meta_off = I.meta_off;
     H.op = base + I.off[0];
     H.rhs = base + I.off[1];
@@ -754,68 +810,117 @@ void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt*
     H.Rb = base + I.off[7];
     H.out = base + I.off[8];
     H.report = base + I.off[9];
+    H.Xopt = base + I.off[10];
   }
-  CK(cudaEventRecord(c->ev0, c->stream));
-  CK(cudaMemcpyAsync(dmeta, meta.data(), sizeof(int64_t) * meta.size(), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(dmeta, P.meta.data(), sizeof(int64_t) * P.meta.size(), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, st));
   for (int j = 0; j < count; ++j) {
-    upload(c, (double*)hinst[j].op, in[j].op);
-    upload(c, (double*)hinst[j].rhs, in[j].b);
-    upload(c, (double*)hinst[j].x0, in[j].x0);
+    BatchReqHost& I = P.in[j];
+    auto up = [&](double* dst, const TTView& v) {
+      if (v.total > 0)
+        CK(cudaMemcpyAsync(dst, v.data, sizeof(double) * v.total,
+                           v.dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    };
+    up((double*)hinst[j].op, I.op);
+    if (I.kind == 0) up((double*)hinst[j].rhs, I.b);
+    up((double*)hinst[j].x0, I.x0);
   }
-  CK(cudaMemsetAsync(next, 0, sizeof(int), c->stream));
-  BatchArgs args{dinst, count, dmeta, next, scratch, stride, z, m, prec == TTALS_PREC_MIXED ? 1 : 0, tol};
-  cudaEvent_t k0 = pool_event(c, 0), k1 = pool_event(c, 1);
-  CK(cudaEventRecord(k0, c->stream));
-  CK(launch_batch_sle(args, grid, c->stream));
-  CK(cudaEventRecord(k1, c->stream));
-  CK(cudaEventRecord(c->ev1, c->stream));
-  // reports, then outputs
-  std::vector<std::vector<double>> rep(count);
-  for (int j = 0; j < count; ++j) {
-    const int d = in[j].op.d;
-    rep[j].resize(8 + d + 1);
-    CK(cudaMemcpyAsync(rep[j].data(), hinst[j].report, sizeof(double) * (8 + d + 1), cudaMemcpyDeviceToHost,
-                       c->stream));
-    int64_t cnt = 0;
-    for (int i = 0; i < d; ++i) cnt += in[j].fin[i] * in[j].op.m[i] * in[j].fin[i + 1];
-    CK(cudaMemcpyAsync(outs[j], hinst[j].out, sizeof(double) * cnt,
-                       out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
-  }
-  CK(cudaStreamSynchronize(c->stream));
+  int* next = (int*)(mem + P.off_next);
+  CK(cudaMemsetAsync(next, 0, sizeof(int), st));
+  BatchArgs args{dinst, count, dmeta, next, mem + P.off_scratch, P.stride, P.z, kBatchM, kBatchMEvp,
+                 P.prec == TTALS_PREC_MIXED ? 1 : 0, P.tol, 1e-12};
+  if (k0) CK(cudaEventRecord(k0, st));
+  CK(launch_batch_sle(args, P.grid, st));
+  if (k1) CK(cudaEventRecord(k1, st));
+}
+
+// After the stream finished: copy outputs (to host or device pointers),
+// check every request's status and fill the statistics.
+void collect_plan(BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_stats* stats, float kernel_ms,
+                  float total_ms, int64_t launches) {
+  const int count = (int)P.in.size();
+  double* data = (double*)mem;
   double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
   int64_t nsolve = 0, nits = 0, ncyc = 0;
+  std::vector<double> rep;
   for (int j = 0; j < count; ++j) {
-    fl64 += rep[j][5];
-    fl32 += rep[j][6];
-    const int st_j = (int)rep[j][4];
-    if (st_j == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in a local solve of instance " + std::to_string(j)};
-    if (st_j == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in instance " + std::to_string(j)};
-    if (st_j != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(st_j)};
-    for (int i = 0; i <= in[j].op.d; ++i)
-      require((int64_t)rep[j][8 + i] == in[j].fin[i], TTALS_ERR_CUDA, "rank schedule mismatch in batch instance");
-    maxres = std::max(maxres, rep[j][0]);
-    nsolve += (int64_t)rep[j][1];
-    nits += (int64_t)rep[j][2];
-    ncyc += (int64_t)rep[j][3];
+    BatchReqHost& I = P.in[j];
+    const int d = I.op.d;
+    rep.assign(10 + d, 0.0);
+    CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (10 + d), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const int stj = (int)rep[4];
+    if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
+    if (stj == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in request " + std::to_string(j)};
+    if (stj != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(stj)};
+    int64_t cnt = 0;
+    for (int i = 0; i < d; ++i) {
+      const int64_t ri = (int64_t)rep[8 + i], rn = (int64_t)rep[9 + i];
+      require(ri == I.fin[i] && rn == I.fin[i + 1], TTALS_ERR_CUDA, "rank schedule mismatch in a batched request");
+      cnt += ri * I.op.m[i] * rn;
+    }
+    CK(cudaMemcpyAsync(I.out, data + I.region + I.off[8], sizeof(double) * cnt,
+                       out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (I.out_val) *I.out_val = rep[7];
+    if (I.out_its) *I.out_its = (int32_t)rep[9 + d];
+    maxres = std::max(maxres, rep[0]);
+    nsolve += (int64_t)rep[1];
+    nits += (int64_t)rep[2];
+    ncyc += (int64_t)rep[3];
+    fl64 += rep[5];
+    fl32 += rep[6];
   }
-  if (st) {
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-    st->local_solves = nsolve;
-    st->krylov_iterations = nits;
-    st->refinement_steps = ncyc;
-    st->max_local_residual = maxres;
-    st->device_ms = ms;
-    st->kernel_launches = launch_counter();
-    // the batch kernel is the only local-solve launch; always timed
-    float kms = 0.f;
-    CK(cudaEventElapsedTime(&kms, k0, k1));
-    st->solver_launches = 1;
-    st->solver_ms = kms;
-    st->solver_flops64 = fl64;
-    st->solver_flops32 = fl32;
+  CK(cudaStreamSynchronize(st));
+  if (stats) {
+    stats->local_solves = nsolve;
+    stats->krylov_iterations = nits;
+    stats->refinement_steps = ncyc;
+    stats->max_local_residual = maxres;
+    stats->device_ms = total_ms;
+    stats->kernel_launches = launches;
+    stats->solver_launches = 1;
+    stats->solver_ms = kernel_ms;
+    stats->solver_flops64 = fl64;
+    stats->solver_flops32 = fl32;
   }
+}
+
+void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, int out_dev,
+                    ttals_stats* st) {
+  launch_counter() = 0;
+  BatchPlan P = plan_batch(c, count, reqs, prec, tol);
+  char* mem = nullptr;
+  Bump B{c};
+  B.want(&mem, (int64_t)P.bytes);
+  B.commit();
+  cudaEvent_t k0 = pool_event(c, 0), k1 = pool_event(c, 1);
+  CK(cudaEventRecord(c->ev0, c->stream));
+  launch_plan(c, P, mem, c->stream, k0, k1);
+  CK(cudaEventRecord(c->ev1, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float kms = 0.f, tms = 0.f;
+  CK(cudaEventElapsedTime(&kms, k0, k1));
+  CK(cudaEventElapsedTime(&tms, c->ev0, c->ev1));
+  collect_plan(P, mem, c->stream, out_dev, st, kms, tms, launch_counter());
+}
+
+void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt* x0s, const ttals_tt* rhss,
+                   const int32_t* repeats, int prec, double tol, double* const* outs, int out_dev, ttals_stats* st) {
+  require(count >= 1, TTALS_ERR_ARG, "count must be >= 1");
+  require(ops && x0s && rhss && repeats && outs, TTALS_ERR_ARG, "null array argument");
+  std::vector<ttals_request> reqs(count);
+  for (int j = 0; j < count; ++j) {
+    ttals_request& q = reqs[j];
+    std::memset(&q, 0, sizeof(q));
+    q.kind = TTALS_REQ_SLE;
+    q.op = ops[j];
+    q.x0 = x0s[j];
+    q.rhs = rhss[j];
+    q.repeats = repeats[j];
+    q.solver = TTALS_SLE_SOLVE;
+    q.out_data = outs[j];
+  }
+  run_batch_sync(c, count, reqs.data(), prec, tol, out_dev, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1035,6 +1140,33 @@ int guarded(ttals_ctx* c, F&& f) {
 
 }  // namespace
 
+struct ttals_job {
+  ttals_ctx* c = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t k0 = nullptr, k1 = nullptr, e0 = nullptr, e1 = nullptr;
+  char* mem = nullptr;
+  size_t bytes = 0;
+  BatchPlan plan;
+  int64_t launches = 0;
+};
+
+namespace {
+
+void job_release(ttals_job* j) {
+  if (!j) return;
+  if (j->mem) {
+    cudaFreeAsync(j->mem, j->st);
+    cudaStreamSynchronize(j->st);
+    j->c->inflight -= j->bytes;
+  }
+  for (cudaEvent_t e : {j->k0, j->k1, j->e0, j->e1})
+    if (e) cudaEventDestroy(e);
+  if (j->st) cudaStreamDestroy(j->st);
+  delete j;
+}
+
+}  // namespace
+
 namespace ttals {
 
 // Helpers for entry points defined in other translation units.
@@ -1148,6 +1280,72 @@ int ttals_sle_als(ttals_ctx* c, const ttals_tt* op, const ttals_tt* x0, const tt
   return guarded(c, [&] {
     run_sle(c, op, x0, rhs, repeats, solver, precision, tol, out_data, out_on_device, out_ranks, stats);
   });
+}
+
+int ttals_solve_batch(ttals_ctx* c, int32_t count, const ttals_request* reqs, int32_t precision, double tol,
+                      int32_t out_on_device, ttals_stats* stats) {
+  return guarded(c, [&] { run_batch_sync(c, count, reqs, precision, tol, out_on_device, stats); });
+}
+
+int ttals_batch_bytes(ttals_ctx* c, int32_t count, const ttals_request* reqs, int64_t* bytes) {
+  return guarded(c, [&] {
+    require(bytes != nullptr, TTALS_ERR_ARG, "null pointer");
+    *bytes = (int64_t)plan_batch(c, count, reqs, TTALS_PREC_MIXED, 0.0).bytes;
+  });
+}
+
+int ttals_submit(ttals_ctx* c, int32_t count, const ttals_request* reqs, int32_t precision, double tol,
+                 ttals_job** job) {
+  if (job) *job = nullptr;
+  ttals_job* j = nullptr;
+  const int st = guarded(c, [&] {
+    require(job != nullptr, TTALS_ERR_ARG, "null job pointer");
+    j = new ttals_job();
+    j->c = c;
+    j->plan = plan_batch(c, count, reqs, precision, tol);
+    j->bytes = j->plan.bytes;
+    require(c->inflight + j->bytes <= c->budget, TTALS_ERR_NOMEM,
+            "device memory budget of the context is held by running jobs");
+    CK(cudaStreamCreateWithFlags(&j->st, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&j->k0, &j->k1, &j->e0, &j->e1}) CK(cudaEventCreate(e));
+    launch_counter() = 0;
+    CK(cudaEventRecord(j->e0, j->st));
+    CK(cudaMallocAsync((void**)&j->mem, j->bytes, j->st));
+    c->inflight += j->bytes;
+    launch_plan(c, j->plan, j->mem, j->st, j->k0, j->k1);
+    CK(cudaEventRecord(j->e1, j->st));
+    j->launches = launch_counter();
+    *job = j;
+  });
+  if (st != TTALS_OK && j) job_release(j);
+  return st;
+}
+
+int ttals_job_poll(ttals_job* j, int32_t* done) {
+  if (!j || !done) return TTALS_ERR_ARG;
+  return guarded(j->c, [&] {
+    const cudaError_t e = cudaEventQuery(j->e1);
+    if (e == cudaErrorNotReady) {
+      *done = 0;
+      return;
+    }
+    CK(e);
+    *done = 1;
+  });
+}
+
+int ttals_job_finish(ttals_job* j, ttals_stats* stats) {
+  if (!j) return TTALS_ERR_ARG;
+  ttals_ctx* c = j->c;
+  const int st = guarded(c, [&] {
+    CK(cudaStreamSynchronize(j->st));
+    float kms = 0.f, tms = 0.f;
+    CK(cudaEventElapsedTime(&kms, j->k0, j->k1));
+    CK(cudaEventElapsedTime(&tms, j->e0, j->e1));
+    collect_plan(j->plan, j->mem, j->st, 0, stats, kms, tms, j->launches);
+  });
+  job_release(j);
+  return st;
 }
 
 int ttals_sle_als_batch(ttals_ctx* c, int32_t count, const ttals_tt* ops, const ttals_tt* x0s,

@@ -17,24 +17,43 @@
 #include "ttals_desc.cuh"
 #include "ttals_internal.h"
 #include "ttals_qr.cuh"
+#include "ttals_tri.cuh"
 
 namespace ttals {
 
 constexpr int kMaxOrderB = 256;
-constexpr int kBatchThreads = 256;  // two CTAs per SM: FP32 and FP64 phases of different instances overlap
+constexpr int kBatchThreads = 128;  // four CTAs per SM: FP32 and FP64 phases of different instances overlap
 
 // ---------------------------------------------------------------------------
 // CTA primitives
 // ---------------------------------------------------------------------------
 
+// Inlined body (used inside the Krylov loops); `c` must not alias C.
 template <typename T>
-__device__ __forceinline__ void cta_contract(const Contraction& c, const T* A, const T* B, T* C) {
-  for (int64_t e = threadIdx.x; e < c.total; e += blockDim.x) {
-    int64_t ao, bo, co;
-    contract_offsets(c, e, ao, bo, co);
-    C[co] = contract_sum(c, A, B, ao, bo);
+__device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C) {
+  constexpr int VW = DefaultVW<T>::value;
+  if (contract_vec_ok<T, VW>(c, B, C)) {
+    for (int64_t e = (int64_t)threadIdx.x * VW; e < c.total; e += (int64_t)blockDim.x * VW)
+      contract_vec_elem<T, VW>(c, A, B, C, e);
+  } else {
+    for (int64_t e = threadIdx.x; e < c.total; e += blockDim.x) {
+      int64_t ao, bo, co;
+      contract_offsets(c, e, ao, bo, co);
+      C[co] = contract_sum(c, A, B, ao, bo);
+    }
   }
   __syncthreads();
+}
+
+// Out-of-line version for the per-site bookkeeping (stacks, pushes): keeps the
+// register pressure of the instance driver low.  The descriptor is copied to
+// shared memory so that stores to C cannot alias it.
+template <typename T>
+__device__ __noinline__ void cta_contract(const Contraction& cref, const T* A, const T* B, T* C) {
+  __shared__ Contraction sc;
+  if (threadIdx.x == 0) sc = cref;
+  __syncthreads();
+  cta_contract_body<T>(sc, A, B, C);
 }
 
 __device__ __forceinline__ void cta_fill(double* p, int64_t n, double v) {
@@ -81,9 +100,9 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
 template <typename T>
 __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                           const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out) {
-  cta_contract(p1, L, y, T1);
-  cta_contract(p2, T1, A, T2);
-  cta_contract(p3, T2, R, out);
+  cta_contract_body(p1, L, y, T1);
+  cta_contract_body(p2, T1, A, T2);
+  cta_contract_body(p3, T2, R, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -96,7 +115,7 @@ struct CtaSolveStats {
 };
 
 template <typename TI>
-__device__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& p2, const Contraction& p3,
+__device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                       const double* L64, const double* A64, const double* R64, double* T1_64,
                                       double* T2_64, const TI* Li, const TI* Ai, const TI* Ri, TI* T1i, TI* T2i,
                                       const double* f, double* x, double* r, TI* V, TI* w, int64_t N, int m,
@@ -124,8 +143,8 @@ __device__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& 
     return out;
   }
   for (int cyc = 0; cyc < max_cycles; ++cyc) {
-    cta_contract(p1, L64, (const double*)x, T1_64);
-    cta_contract(p2, (const double*)T1_64, A64, T2_64);
+    cta_contract_body(p1, L64, (const double*)x, T1_64);
+    cta_contract_body(p2, (const double*)T1_64, A64, T2_64);
     double rs = 0.0;
     for (int64_t e = tid; e < N; e += nt) {
       int64_t ao, bo, co;
@@ -233,6 +252,137 @@ __device__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& 
 }
 
 // ---------------------------------------------------------------------------
+// CTA Lanczos (FP64, one eigenpair) for the symmetric local eigenproblem
+// (see lanczos_kernel for the grid version and the selection rules)
+// ---------------------------------------------------------------------------
+
+struct CtaEigStats {
+  double theta, res;
+  int its, restarts, status;
+};
+
+__device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
+                                               const double* L, const double* A, const double* R, double* T1,
+                                               double* T2, double* x, double* V, double* w, int64_t N, int m,
+                                               int mode, double sigma, int max_restarts, double tol, double* sm) {
+  double* al = sm;
+  double* be = al + m;
+  double* h1 = be + m;
+  double* h2 = h1 + m + 2;
+  double* z = h2 + m + 2;
+  double* twk = z + m;
+  int* piv = (int*)(twk + 5 * m + 8);
+  __shared__ double s_theta, s_res;
+  __shared__ int s_conv;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  CtaEigStats out{0.0, 0.0, 0, 0, ST_OK};
+  if (tid == 0) {
+    s_conv = 0;
+    s_theta = 0.0;
+    s_res = 0.0;
+  }
+  double xs = 0.0;
+  for (int64_t e = tid; e < N; e += nt) xs += x[e] * x[e];
+  const double xn = sqrt(cta_sum(xs));
+  const bool ok = xn > 0.0 && isfinite(xn);
+  for (int64_t e = tid; e < N; e += nt) V[e] = ok ? x[e] / xn : 1.0 / sqrt((double)N);
+  __syncthreads();
+  const int mm = (int)(N < m ? N : m);
+  for (;;) {
+    int nT = 0;
+    for (int j = 0; j < mm; ++j) {
+      cta_apply<double>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
+      cta_dots<double>(V, N, j + 1, w, h1);
+      for (int64_t e = tid; e < N; e += nt) {
+        double acc = w[e];
+        for (int q = 0; q <= j; ++q) acc -= h1[q] * V[(int64_t)q * N + e];
+        w[e] = acc;
+      }
+      __syncthreads();
+      cta_dots<double>(V, N, j + 1, w, h2);
+      double b2 = h2[j + 1];
+      for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
+      const double bj = sqrt(fmax(b2, 0.0));
+      if (tid == 0) {
+        al[j] = h1[j] + h2[j];
+        be[j] = bj;
+      }
+      if (bj > 0.0 && j + 1 < mm) {
+        double* vn = V + (int64_t)(j + 1) * N;
+        const double inv = 1.0 / bj;
+        for (int64_t e = tid; e < N; e += nt) {
+          double acc = w[e];
+          for (int q = 0; q <= j; ++q) acc -= h2[q] * V[(int64_t)q * N + e];
+          vn[e] = acc * inv;
+        }
+      }
+      __syncthreads();
+      ++out.its;
+      nT = j + 1;
+      double tnorm = 0.0;
+      for (int i = 0; i < nT; ++i)
+        tnorm = fmax(tnorm, fabs(al[i]) + fabs(be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      const bool breakdown = !(bj > 1e-14 * fmax(tnorm, 1e-300));
+      if ((nT % 4) == 0 || nT == mm || breakdown) {
+        if (warp == 0) {
+          double lo = 1e300, hi = -1e300;
+          for (int i = 0; i < nT; ++i) {
+            const double rad = (i > 0 ? fabs(be[i - 1]) : 0.0) + (i < nT - 1 ? fabs(be[i]) : 0.0);
+            lo = fmin(lo, al[i] - rad);
+            hi = fmax(hi, al[i] + rad);
+          }
+          const double pivmin = 1e-300 + DBL_MIN * fmax(1.0, tnorm * tnorm);
+          lo -= 1e-12 * fmax(1.0, tnorm);
+          hi += 1e-12 * fmax(1.0, tnorm);
+          int sel;
+          if (mode == 0) {
+            sel = nT - 1;
+          } else if (mode == 2) {
+            sel = 0;
+          } else {
+            const int below = sturm_count(al, be, nT, sigma, pivmin);
+            const double vdn = below > 0 ? tri_eigval(al, be, nT, below - 1, lo, hi, pivmin) : 0.0;
+            const double vup = below < nT ? tri_eigval(al, be, nT, below, lo, hi, pivmin) : 0.0;
+            sel = (below > 0 && (below >= nT || fabs(vdn - sigma) <= fabs(vup - sigma))) ? below - 1 : below;
+          }
+          const double th = tri_eigval(al, be, nT, sel, lo, hi, pivmin);
+          if (lane == 0) {
+            tri_eigvec(al, be, nT, th, fmax(tnorm, 1e-300), z, twk, piv);
+            s_theta = th;
+            s_res = bj * fabs(z[nT - 1]) / fmax(tnorm, 1e-300);
+            s_conv = (s_res <= tol) || breakdown;
+          }
+        }
+        __syncthreads();
+        if (s_conv || nT == mm) break;
+      } else if (breakdown) {
+        break;
+      }
+    }
+    // Ritz vector
+    for (int64_t e = tid; e < N; e += nt) {
+      double acc = 0.0;
+      for (int l = 0; l < nT; ++l) acc += z[l] * V[(int64_t)l * N + e];
+      x[e] = acc;
+    }
+    __syncthreads();
+    if (s_conv || out.restarts >= max_restarts) break;
+    ++out.restarts;
+    double s2 = 0.0;
+    for (int64_t e = tid; e < N; e += nt) s2 += x[e] * x[e];
+    const double nrm = sqrt(cta_sum(s2));
+    for (int64_t e = tid; e < N; e += nt) V[e] = nrm > 0.0 ? x[e] / nrm : 1.0 / sqrt((double)N);
+    __syncthreads();
+  }
+  out.theta = s_theta;
+  out.res = s_res;
+  if (!s_conv) out.status = ST_OK;  // not converged within the restart budget: reported through res
+  return out;
+}
+
+__device__ __noinline__ void cta_qr(const QrArgs& q) { cta_householder_qr(q); }
+
+// ---------------------------------------------------------------------------
 // one instance
 // ---------------------------------------------------------------------------
 
@@ -257,12 +407,13 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   s.f = (double*)take(8 * z.N);
   s.r = (double*)take(8 * z.N);
   s.w = (double*)take(8 * z.N);
-  s.V = (double*)take(8 * (int64_t)(a.m + 1) * z.N);
+  const int mv = a.m > a.m_evp ? a.m : a.m_evp;
+  s.V = (double*)take(8 * (int64_t)(mv + 1) * z.N);
   s.rbuf = (double*)take(8 * z.R);
   s.qwork = (double*)take(8 * z.Q);
   s.tmp0 = (double*)take(8 * z.core);
   s.tmp1 = (double*)take(8 * z.core);
-  s.Vf = (float*)take(4 * (int64_t)(a.m + 1) * z.N);
+  s.Vf = (float*)take(4 * (int64_t)(mv + 1) * z.N);
   s.wf = (float*)take(4 * z.N);
   s.T1f = (float*)take(4 * z.T);
   s.T2f = (float*)take(4 * z.T);
@@ -272,7 +423,7 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   return s;
 }
 
-__device__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double* sm) {
+__device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double* sm) {
   const BatchInst& I = a.inst[j];
   const int d = I.d;
   const int64_t* M = a.meta + I.meta_off;
@@ -320,7 +471,7 @@ __device__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double*
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_householder_qr(q);
+      cta_qr(q);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
       cta_contract(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
@@ -412,7 +563,7 @@ __device__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double*
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_householder_qr(q);
+        cta_qr(q);
         fl64 += qr_fl((double)(aa * nn), (double)ss);
         const int64_t qq = n[i + 1] * r[i + 2];
         cta_contract(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
@@ -427,7 +578,7 @@ __device__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double*
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_householder_qr(q);
+        cta_qr(q);
         fl64 += qr_fl((double)ns, (double)aa);
         const int64_t p = r[i - 1] * n[i - 1];
         cta_contract(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
@@ -452,12 +603,179 @@ __device__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double*
     I.report[4] = (double)status;
     I.report[5] = fl64;
     I.report[6] = fl32;
+    I.report[7] = 0.0;
     for (int i = 0; i <= d; ++i) I.report[8 + i] = (double)r[i];
+    I.report[9 + d] = (double)I.repeats;
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kBatchThreads, 2) batch_sle_kernel(BatchArgs a) {
+// ---------------------------------------------------------------------------
+// one eigenproblem instance (evp.py:17-179, symmetric, number_ev == 1)
+// ---------------------------------------------------------------------------
+
+__device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch& S, double* sm) {
+  const BatchInst& I = a.inst[j];
+  const int d = I.d;
+  const int64_t* M = a.meta + I.meta_off;
+  const int64_t* n = M;
+  const int64_t* R = n + d;
+  const int64_t* rb = R + d + 1;
+  const int64_t* rx0 = rb + d + 1;
+  const int64_t* cap = rx0 + d + 1;
+  const int64_t* op_off = cap + d + 1;
+  const int64_t* x0_off = op_off + 2 * d;
+  const int64_t* X_off = x0_off + d;
+  const int64_t* L_off = X_off + d;
+  const int64_t* Rt_off = L_off + d;
+  __shared__ int64_t r[kMaxOrderB + 1];
+  __shared__ int64_t ropt[kMaxOrderB + 1];
+  for (int i = threadIdx.x; i <= d; i += blockDim.x) r[i] = cap[i];
+  __syncthreads();
+  const int tid = threadIdx.x;
+  auto X = [&](int i) { return I.X + X_off[i]; };
+  auto Xo = [&](int i) { return I.Xopt + X_off[i]; };
+  auto L = [&](int i) { return I.L + L_off[i]; };
+  auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
+  auto A = [&](int i) { return I.op + op_off[i]; };
+  double fl64 = 0.0, maxres = 0.0, theta = 0.0;
+  int64_t nsolve = 0, nits = 0, nrst = 0;
+  auto apply_fl = [&](double aa, double nn, double ss, double r0, double r1) {
+    return 2 * aa * aa * r0 * nn * ss + 2 * aa * ss * nn * nn * r0 * r1 + 2 * aa * nn * ss * ss * r1;
+  };
+  {
+    const double* cur = I.x0 + x0_off[d - 1];
+    int64_t cur_left = rx0[d - 1], cur_right = 1;
+    for (int i = d - 1; i >= 1; --i) {
+      const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
+      QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
+      cta_qr(q);
+      const int64_t p = rx0[i - 1] * n[i - 1];
+      double* outb = (i & 1) ? S.tmp1 : S.tmp0;
+      cta_contract(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
+      cur = outb;
+      cur_left = rx0[i - 1];
+      cur_right = k;
+    }
+    cta_copy(X(0), cur, n[0] * cur_right);
+  }
+  auto right = [&](int i) {
+    if (i == d - 1) {
+      if (tid == 0) Rt(i)[0] = 1.0;
+      __syncthreads();
+      return;
+    }
+    const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
+    Contraction q1, q2, q3;
+    desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
+    cta_contract(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1);
+    cta_contract(q2, (const double*)S.T1, A(i + 1), S.T2);
+    cta_contract(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i));
+    fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
+  };
+  auto left = [&](int i) {
+    if (i == 0) {
+      if (tid == 0) L(i)[0] = 1.0;
+      __syncthreads();
+      return;
+    }
+    const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
+    Contraction p1, p2, p3;
+    desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
+    cta_contract(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1);
+    cta_contract(p2, (const double*)S.T1, A(i - 1), S.T2);
+    cta_contract(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i));
+    fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
+  };
+  auto solve = [&](int i) {
+    const int64_t aa = r[i], nn = n[i], ss = r[i + 1], N = aa * nn * ss;
+    Contraction p1, p2, p3;
+    desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
+    const int m = (int)(N < a.m_evp ? N : a.m_evp);
+    const CtaEigStats st = cta_lanczos(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m, I.mode,
+                                       I.sigma, 40, a.tol_evp, sm);
+    theta = st.theta;
+    ++nsolve;
+    nits += st.its;
+    nrst += st.restarts;
+    maxres = fmax(maxres, st.res);
+    const double fa = apply_fl((double)aa, (double)nn, (double)ss, (double)R[i], (double)R[i + 1]);
+    fl64 += st.its * (fa + 8.0 * (double)N * (m + 1) / 2.0);
+  };
+  for (int i = d - 1; i >= 0; --i) right(i);
+  double hist[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
+  int nh = 1;  // the reference starts its history with one row of inf (evp.py:110)
+  double val_opt = INFINITY;
+  int it = 1;
+  bool conv = false, have_opt = false;
+  while (it <= I.repeats && !conv) {
+    for (int i = 0; i < d; ++i) {
+      left(i);
+      if (i < d - 1) {
+        solve(i);
+        const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
+        QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
+        cta_qr(q);
+        const int64_t qq = n[i + 1] * r[i + 2];
+        cta_contract(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
+        cta_copy(X(i + 1), S.tmp0, k * qq);
+        if (tid == 0) r[i + 1] = k;
+        __syncthreads();
+      }
+    }
+    for (int i = d - 1; i >= 0; --i) {
+      right(i);
+      solve(i);
+      if (i > 0) {
+        const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
+        QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
+        cta_qr(q);
+        const int64_t p = r[i - 1] * n[i - 1];
+        cta_contract(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
+        cta_copy(X(i - 1), S.tmp0, p * k);
+        if (tid == 0) r[i] = k;
+        __syncthreads();
+      }
+    }
+    ++it;
+    const double lam = theta;
+    if (fabs(lam - I.sigma) < fabs(val_opt - I.sigma)) {
+      val_opt = lam;
+      have_opt = true;
+      for (int i = 0; i < d; ++i) cta_copy(Xo(i), X(i), r[i] * n[i] * r[i + 1]);
+      for (int i = tid; i <= d; i += blockDim.x) ropt[i] = r[i];
+      __syncthreads();
+    }
+    double diff = 0.0;
+    const int nl = nh < 3 ? nh : 3;
+    for (int q = nh - nl; q < nh; ++q) diff = fmax(diff, fabs(hist[q % 4] - lam));
+    if (diff < I.conv_eps) conv = true;
+    hist[nh % 4] = lam;
+    ++nh;
+  }
+  // pack the best sweep's cores
+  int64_t off = 0;
+  for (int i = 0; i < d; ++i) {
+    const int64_t cnt = have_opt ? ropt[i] * n[i] * ropt[i + 1] : 0;
+    for (int64_t e = tid; e < cnt; e += blockDim.x) I.out[off + e] = Xo(i)[e];
+    off += cnt;
+  }
+  if (tid == 0) {
+    I.report[0] = maxres;
+    I.report[1] = (double)nsolve;
+    I.report[2] = (double)nits;
+    I.report[3] = (double)nrst;
+    I.report[4] = (double)ST_OK;
+    I.report[5] = fl64;
+    I.report[6] = 0.0;
+    I.report[7] = val_opt;
+    for (int i = 0; i <= d; ++i) I.report[8 + i] = have_opt ? (double)ropt[i] : 0.0;
+    I.report[9 + d] = (double)(it - 1);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 4) batch_sle_kernel(BatchArgs a) {
   extern __shared__ double sm[];
   __shared__ int s_j;
   const Scratch S = scratch_of(a, blockIdx.x);
@@ -467,23 +785,29 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_sle_kernel(BatchArgs a
     const int j = s_j;
     __syncthreads();
     if (j >= a.count) return;
-    batch_solve(a, j, S, sm);
+    if (a.inst[j].kind == 1)
+      batch_evp(a, j, S, sm);
+    else
+      batch_solve(a, j, S, sm);
   }
 }
 
-size_t batch_smem_bytes(int m) {
-  return sizeof(double) * ((size_t)(m + 1) * m + 2 * m + (m + 1) + m + 2 * (m + 2));
+size_t batch_smem_bytes(int m, int m_evp) {
+  const size_t g = (size_t)(m + 1) * m + 2 * m + (m + 1) + m + 2 * (m + 2);
+  const size_t e = (size_t)10 * m_evp + 12 + m_evp / 2 + 1;  // Lanczos arrays + pivots
+  return sizeof(double) * (g > e ? g : e);
 }
 
-int64_t batch_scratch_stride(const BatchSizes& z, int m) {
+int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
+  const int m = mg > m_evp ? mg : m_evp;
   auto r = [](int64_t b) { return (b + 255) / 256 * 256; };
   return r(8 * z.T) * 2 + r(8 * z.U) + r(8 * z.N) * 3 + r(8 * (int64_t)(m + 1) * z.N) + r(8 * z.R) + r(8 * z.Q) +
          r(8 * z.core) * 2 + r(4 * (int64_t)(m + 1) * z.N) + r(4 * z.N) + r(4 * z.T) * 2 + r(4 * z.stack) * 2 +
          r(4 * z.opcore);
 }
 
-int batch_blocks_per_sm(int m) {
-  const size_t smem = batch_smem_bytes(m);
+int batch_blocks_per_sm(int m, int m_evp) {
+  const size_t smem = batch_smem_bytes(m, m_evp);
   cudaFuncSetAttribute(batch_sle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_sle_kernel, kBatchThreads, smem) != cudaSuccess ||
@@ -493,7 +817,7 @@ int batch_blocks_per_sm(int m) {
 }
 
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st) {
-  const size_t smem = batch_smem_bytes(a.m);
+  const size_t smem = batch_smem_bytes(a.m, a.m_evp);
   cudaError_t e = cudaFuncSetAttribute(batch_sle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   batch_sle_kernel<<<grid, kBatchThreads, smem, st>>>(a);

@@ -11,11 +11,16 @@ namespace ttals {
 // X_off[d], L_off[d], Rt_off[d], Lb_off[d], Rb_off[d].
 struct BatchInst {
   int32_t d, repeats;
+  int32_t kind;  // 0: linear system (sle.als), 1: eigenproblem (evp.als)
+  int32_t mode;  // EVP selection: 0 largest (eigh), 1 closest to sigma (eig/eigs), 2 smallest
+  double sigma, conv_eps;
   int64_t meta_off;
   const double *op, *rhs, *x0;
   double *X, *L, *Rt, *Lb, *Rb;
+  double* Xopt;    // EVP: cores of the best sweep (evp.py:151-155)
   double* out;     // final cores, packed
-  double* report;  // [max rel residual, local solves, Krylov its, refinement cycles, status, -, -, -, ranks[d+1]]
+  double* report;  // [max rel residual, local solves, Krylov its, refinement cycles, status, flops64, flops32,
+                   //  eigenvalue, ranks[d+1], sweeps run]
 };
 
 // Largest per-CTA scratch needs over the batch (elements).
@@ -31,14 +36,16 @@ struct BatchArgs {
   char* scratch;
   int64_t scratch_stride;
   BatchSizes sizes;
-  int m;
+  int m;      // GMRES restart length
+  int m_evp;  // Lanczos basis size
   int prec;
-  double tol;
+  double tol;      // local linear solves
+  double tol_evp;  // local eigen solves (Ritz residual relative to |T|)
 };
 
-size_t batch_smem_bytes(int m);
-int batch_blocks_per_sm(int m);
-int64_t batch_scratch_stride(const BatchSizes& z, int m);
+size_t batch_smem_bytes(int m, int m_evp);
+int batch_blocks_per_sm(int m, int m_evp);
+int64_t batch_scratch_stride(const BatchSizes& z, int m, int m_evp);
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st);
 
 }  // namespace ttals

@@ -90,43 +90,184 @@ __host__ __device__ __forceinline__ void contract_offsets(const Contraction& c, 
   co = o;
 }
 
-// The contraction sum of one output element.
+// The contraction sum of one output element.  Split into independent
+// accumulator chains so consecutive FMAs do not wait on each other.
 template <typename T>
 __host__ __device__ __forceinline__ T contract_sum(const Contraction& c, const T* __restrict__ A,
                                                    const T* __restrict__ B, int64_t ao, int64_t bo) {
-  T acc = T(0);
   const T* pa = A + ao;
   const T* pb = B + bo;
   if (c.nk == 1) {
     const int sa = c.a_ks[0], sb = c.b_ks[0], K = c.k_dim[0];
-#pragma unroll 4
-    for (int k = 0; k < K; ++k) acc += pa[k * sa] * pb[k * sb];
-  } else if (c.nk == 2) {
-    const int sa = c.a_ks[1], sb = c.b_ks[1], K1 = c.k_dim[1];
-    for (int k0 = 0; k0 < c.k_dim[0]; ++k0) {
-      const T* qa = pa + k0 * c.a_ks[0];
-      const T* qb = pb + k0 * c.b_ks[0];
-#pragma unroll 4
-      for (int k1 = 0; k1 < K1; ++k1) acc += qa[k1 * sa] * qb[k1 * sb];
+    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+    int k = 0;
+    for (; k + 3 < K; k += 4) {
+      a0 += pa[k * sa] * pb[k * sb];
+      a1 += pa[(k + 1) * sa] * pb[(k + 1) * sb];
+      a2 += pa[(k + 2) * sa] * pb[(k + 2) * sb];
+      a3 += pa[(k + 3) * sa] * pb[(k + 3) * sb];
     }
-  } else if (c.nk == 3) {
+    for (; k < K; ++k) a0 += pa[k * sa] * pb[k * sb];
+    return (a0 + a1) + (a2 + a3);
+  }
+  if (c.nk == 2) {
+    const int sa0 = c.a_ks[0], sb0 = c.b_ks[0], sa = c.a_ks[1], sb = c.b_ks[1];
+    const int K0 = c.k_dim[0], K1 = c.k_dim[1];
+    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+    int k0 = 0;
+    for (; k0 + 1 < K0; k0 += 2) {
+      const T* qa = pa + k0 * sa0;
+      const T* qb = pb + k0 * sb0;
+      const T* ra = qa + sa0;
+      const T* rb = qb + sb0;
+      int k1 = 0;
+      for (; k1 + 1 < K1; k1 += 2) {
+        a0 += qa[k1 * sa] * qb[k1 * sb];
+        a1 += ra[k1 * sa] * rb[k1 * sb];
+        a2 += qa[(k1 + 1) * sa] * qb[(k1 + 1) * sb];
+        a3 += ra[(k1 + 1) * sa] * rb[(k1 + 1) * sb];
+      }
+      if (k1 < K1) {
+        a0 += qa[k1 * sa] * qb[k1 * sb];
+        a1 += ra[k1 * sa] * rb[k1 * sb];
+      }
+    }
+    if (k0 < K0) {
+      const T* qa = pa + k0 * sa0;
+      const T* qb = pb + k0 * sb0;
+      for (int k1 = 0; k1 < K1; ++k1) a2 += qa[k1 * sa] * qb[k1 * sb];
+    }
+    return (a0 + a1) + (a2 + a3);
+  }
+  if (c.nk == 3) {
     const int sa = c.a_ks[2], sb = c.b_ks[2], K2 = c.k_dim[2];
+    T a0 = T(0), a1 = T(0);
     for (int k0 = 0; k0 < c.k_dim[0]; ++k0)
       for (int k1 = 0; k1 < c.k_dim[1]; ++k1) {
         const T* qa = pa + k0 * c.a_ks[0] + k1 * c.a_ks[1];
         const T* qb = pb + k0 * c.b_ks[0] + k1 * c.b_ks[1];
-        for (int k2 = 0; k2 < K2; ++k2) acc += qa[k2 * sa] * qb[k2 * sb];
+        int k2 = 0;
+        for (; k2 + 1 < K2; k2 += 2) {
+          a0 += qa[k2 * sa] * qb[k2 * sb];
+          a1 += qa[(k2 + 1) * sa] * qb[(k2 + 1) * sb];
+        }
+        if (k2 < K2) a0 += qa[k2 * sa] * qb[k2 * sb];
       }
-  } else {  // nk == 0: elementwise product
-    acc = pa[0] * pb[0];
+    return a0 + a1;
   }
-  return acc;
+  return pa[0] * pb[0];  // nk == 0: elementwise product
 }
+
+// ---------------------------------------------------------------------------
+// register-tiled variant: VW consecutive outputs along the innermost output axis
+// when that axis has stride 0 in A and stride 1 in B and C (true for every
+// apply / stack / rhs phase of the path).  One A load and one VW-wide vector B
+// load feed VW FMAs.
+// ---------------------------------------------------------------------------
+
+template <typename T, int VW>
+struct VecOf;
+template <>
+struct VecOf<float, 4> {
+  using type = float4;
+};
+template <>
+struct VecOf<double, 2> {
+  using type = double2;
+};
+template <>
+struct VecOf<double, 1> {
+  using type = double;
+};
+
+template <typename T, int VW>
+__host__ __device__ __forceinline__ bool contract_vec_ok(const Contraction& c, const T* B, const T* C) {
+  if (VW < 2) return false;
+  const int last = c.nout - 1;
+  if (c.nout < 1 || c.out_dim[last] % VW != 0) return false;
+  if (c.a_os[last] != 0 || c.b_os[last] != 1 || c.c_os[last] != 1) return false;
+  for (int q = 0; q < last; ++q)
+    if (c.b_os[q] % VW != 0 || c.c_os[q] % VW != 0) return false;
+  for (int q = 0; q < c.nk; ++q)
+    if (c.b_ks[q] % VW != 0) return false;
+  const uintptr_t align = sizeof(T) * VW;
+  return ((uintptr_t)B % align == 0) && ((uintptr_t)C % align == 0);
+}
+
+// Computes outputs e0 .. e0+VW-1 (e0 a multiple of VW) into C.  The
+// contraction axis with the largest extent runs innermost, unrolled by two
+// with separate accumulators (2*VW independent FMA chains).
+template <typename T, int VW>
+__device__ __forceinline__ void contract_vec_elem(const Contraction& c, const T* __restrict__ A,
+                                                  const T* __restrict__ B, T* __restrict__ C, int64_t e0) {
+  using V = typename VecOf<T, VW>::type;
+  int64_t ao, bo, co;
+  contract_offsets(c, e0, ao, bo, co);
+  int K[3] = {1, 1, 1}, sa[3] = {0, 0, 0}, sb[3] = {0, 0, 0};
+  int inner = 0;
+  for (int q = 0; q < c.nk; ++q) {
+    K[q] = c.k_dim[q];
+    sa[q] = c.a_ks[q];
+    sb[q] = c.b_ks[q];
+    if (K[q] > K[inner]) inner = q;
+  }
+  const int o0 = inner == 0 ? 1 : 0, o1 = inner == 2 ? 1 : 2;
+  const int Ki = K[inner], sai = sa[inner], sbi = sb[inner];
+  T acc0[VW], acc1[VW];
+#pragma unroll
+  for (int v = 0; v < VW; ++v) acc0[v] = acc1[v] = T(0);
+  for (int k0 = 0; k0 < K[o0]; ++k0)
+    for (int k1 = 0; k1 < K[o1]; ++k1) {
+      const T* pa = A + ao + k0 * sa[o0] + k1 * sa[o1];
+      const T* pb = B + bo + k0 * sb[o0] + k1 * sb[o1];
+      int k = 0;
+      for (; k + 1 < Ki; k += 2) {
+        const T a0 = pa[k * sai], a1 = pa[(k + 1) * sai];
+        const V b0 = *reinterpret_cast<const V*>(pb + k * sbi);
+        const V b1 = *reinterpret_cast<const V*>(pb + (k + 1) * sbi);
+        const T* x0 = reinterpret_cast<const T*>(&b0);
+        const T* x1 = reinterpret_cast<const T*>(&b1);
+#pragma unroll
+        for (int v = 0; v < VW; ++v) {
+          acc0[v] += a0 * x0[v];
+          acc1[v] += a1 * x1[v];
+        }
+      }
+      if (k < Ki) {
+        const T a0 = pa[k * sai];
+        const V b0 = *reinterpret_cast<const V*>(pb + k * sbi);
+        const T* x0 = reinterpret_cast<const T*>(&b0);
+#pragma unroll
+        for (int v = 0; v < VW; ++v) acc0[v] += a0 * x0[v];
+      }
+    }
+  V out;
+  T* ov = reinterpret_cast<T*>(&out);
+#pragma unroll
+  for (int v = 0; v < VW; ++v) ov[v] = acc0[v] + acc1[v];
+  *reinterpret_cast<V*>(C + co) = out;
+}
+
+template <typename T>
+struct DefaultVW;
+template <>
+struct DefaultVW<float> {
+  static constexpr int value = 4;
+};
+template <>
+struct DefaultVW<double> {
+  static constexpr int value = 1;  // FP64 is DFMA-bound: keep the scalar 4-chain path
+};
 
 template <typename T>
 __device__ __forceinline__ void contract_range(const Contraction& c, const T* __restrict__ A,
                                                const T* __restrict__ B, T* __restrict__ C,
                                                T alpha, T beta, int64_t first, int64_t step) {
+  constexpr int VW = DefaultVW<T>::value;
+  if (alpha == T(1) && beta == T(0) && contract_vec_ok<T, VW>(c, B, C)) {
+    for (int64_t e = first * VW; e < c.total; e += step * VW) contract_vec_elem<T, VW>(c, A, B, C, e);
+    return;
+  }
   for (int64_t e = first; e < c.total; e += step) {
     int64_t ao, bo, co;
     contract_offsets(c, e, ao, bo, co);

@@ -25,6 +25,7 @@ def main():
     ap.add_argument('--rank', type=int, default=None)
     ap.add_argument('--count', type=int, default=1)
     ap.add_argument('--tol', type=float, default=0.0)
+    ap.add_argument('--batch', type=int, default=0, help='solve this many seeded instances in one batch launch')
     a = ap.parse_args()
     kw = {}
     if a.d:
@@ -41,6 +42,17 @@ def main():
         return
     w = wl.laplace_sle(**kw) if a.workload == 'laplace' else wl.coupled_sle(**kw)
     rep = a.repeats or w.repeats
+    if a.batch:
+        build = wl.laplace_sle if a.workload == 'laplace' else wl.coupled_sle
+        probs = []
+        for j in range(a.batch):
+            wj = build(seed=j, **kw)
+            probs.append((TT([c.copy() for c in wj.op]), TT([c.copy() for c in wj.x0]),
+                          TT([c.copy() for c in wj.rhs])))
+        for k in range(a.count + 1):
+            _, st = sle.als_batch(probs, repeats=rep, precision=a.precision, tol=a.tol)
+        print(json.dumps(st))
+        return
     for k in range(a.count + 1):
         _, st = sle.als_ex(TT([c.copy() for c in w.op]), TT([c.copy() for c in w.x0]),
                            TT([c.copy() for c in w.rhs]), repeats=rep, precision=a.precision, tol=a.tol)

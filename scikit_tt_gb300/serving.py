@@ -1,0 +1,178 @@
+"""Batched and served ALS requests (linear systems and eigenproblems).
+
+``solve_batch`` runs a list of requests in one launch (one CTA per request).
+``Server`` is the continuous-batching loop: requests are admitted as they
+arrive, grouped into jobs launched on their own streams while earlier jobs
+still run (so their work overlaps on the device), and admitted only while
+the device-memory budget holds; each request's latency is measured from its
+arrival to its completion.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from .tensor_train import TT
+
+_PREC = {'fp64': _lib.PREC_FP64, 'mixed': _lib.PREC_MIXED}
+
+
+@dataclass
+class Request:
+    """One ALS problem.  kind 'sle': ``op @ x = rhs`` (sle.py:10); kind 'evp':
+    eigenpair of the symmetric ``op`` (evp.py:17)."""
+    kind: str
+    op: List[np.ndarray]
+    x0: List[np.ndarray]
+    rhs: Optional[List[np.ndarray]] = None
+    repeats: int = 1
+    solver: str = None
+    sigma: float = 1.0
+    conv_eps: float = 1e-10
+    arrival: float = 0.0
+    # filled on completion
+    solution: Optional[TT] = None
+    value: Optional[float] = None
+    iterations: Optional[int] = None
+    done: float = 0.0
+    _keep: list = field(default_factory=list, repr=False)
+
+    def _descriptor(self):
+        lib = _lib.load()
+        op, x0 = _lib.Packed(self.op), _lib.Packed(self.x0)
+        rhs = _lib.Packed(self.rhs) if self.kind == 'sle' else x0
+        dims = np.array([c.shape[1] for c in self.op], dtype=np.int64)
+        ranks = np.zeros(len(dims) + 1, dtype=np.int64)
+        _lib.check(lib.ttals_als_ranks(len(dims), _lib.i64ptr(dims), _lib.i64ptr(x0.ranks), _lib.i64ptr(ranks)))
+        out = np.empty(max(1, int(sum(ranks[i] * dims[i] * ranks[i + 1] for i in range(len(dims))))))
+        val = np.zeros(1)
+        its = np.zeros(1, dtype=np.int32)
+        r = _lib.Request()
+        r.kind = _lib.REQ_SLE if self.kind == 'sle' else _lib.REQ_EVP
+        r.op, r.x0, r.rhs = op.desc, x0.desc, rhs.desc
+        r.repeats = int(self.repeats)
+        solver = self.solver or ('solve' if self.kind == 'sle' else 'eig')
+        r.solver = (_lib.SLE_SOLVERS if self.kind == 'sle' else _lib.EVP_SOLVERS)[solver]
+        r.sigma = float(self.sigma)
+        r.conv_eps = float(self.conv_eps)
+        r.out_data = _lib.dptr(out)
+        r.out_value = _lib.dptr(val)
+        r.out_iterations = its.ctypes.data_as(C.POINTER(C.c_int32))
+        self._keep = [op, x0, rhs, out, val, its, ranks, dims]
+        return r
+
+    def _complete(self):
+        _, _, _, out, val, its, ranks, dims = self._keep
+        self.solution = TT(_lib.unpack(out, dims, [1] * len(dims), ranks))
+        if self.kind == 'evp':
+            self.value = float(val[0])
+            self.iterations = int(its[0])
+        self._keep = []
+
+
+def solve_batch(requests: List[Request], precision: str = 'mixed', tol: float = 0.0):
+    """Solve all requests in one launch; returns the engine statistics."""
+    arr = (_lib.Request * len(requests))(*[r._descriptor() for r in requests])
+    st = _lib.Stats()
+    _lib.check(_lib.load().ttals_solve_batch(_lib.context(), len(requests), arr, _PREC[precision], float(tol), 0, st))
+    for r in requests:
+        r._complete()
+    return st.as_dict()
+
+
+class Server:
+    """Continuous batching over the asynchronous job API (ttals_submit)."""
+
+    def __init__(self, precision: str = 'mixed', tol: float = 0.0, max_batch: int = 304, max_jobs: int = 4):
+        self.prec = _PREC[precision]
+        self.tol = float(tol)
+        self.max_batch = max_batch
+        self.max_jobs = max_jobs
+        self.queue: List[Request] = []
+        self.jobs = []       # (handle, requests, descriptor array)
+        self.finished: List[Request] = []
+        self.stats = []
+
+    def submit(self, req: Request):
+        self.queue.append(req)
+
+    def _launch(self, clock):
+        lib, ctx = _lib.load(), _lib.context()
+        take = self.queue[:self.max_batch]
+        arr = (_lib.Request * len(take))(*[r._descriptor() for r in take])
+        h = C.c_void_p()
+        st = lib.ttals_submit(ctx, len(take), arr, self.prec, self.tol, C.byref(h))
+        if st == _lib.ERR_NOMEM:
+            return False         # budget held by running jobs: admit later
+        _lib.check(st)
+        self.queue = self.queue[len(take):]
+        self.jobs.append((h, take, arr))
+        return True
+
+    def pump(self, clock, launch: bool = True) -> int:
+        """Complete finished jobs and (if ``launch``) launch queued requests;
+        returns the number of requests completed by this call."""
+        lib = _lib.load()
+        completed = 0
+        still = []
+        for h, reqs, arr in self.jobs:
+            done = C.c_int32(0)
+            _lib.check(lib.ttals_job_poll(h, C.byref(done)))
+            if done.value:
+                st = _lib.Stats()
+                _lib.check(lib.ttals_job_finish(h, C.byref(st)))
+                t = clock()
+                for r in reqs:
+                    r._complete()
+                    r.done = t
+                self.finished.extend(reqs)
+                self.stats.append(st.as_dict())
+                completed += len(reqs)
+            else:
+                still.append((h, reqs, arr))
+        self.jobs = still
+        while launch and self.queue and len(self.jobs) < self.max_jobs:
+            if not self._launch(clock):
+                break
+        return completed
+
+    def drain(self, clock, timeout: float = 600.0):
+        t0 = time.perf_counter()
+        while (self.queue or self.jobs) and time.perf_counter() - t0 < timeout:
+            if self.pump(clock) == 0:
+                time.sleep(0.0005)
+
+
+def run_stream(stream, duration_cap: float, precision='mixed', max_batch=304, max_jobs=4, batch_window=0.005):
+    """Replay ``(arrival_s, kind, instance)`` items against a Server in real
+    time.  Requests are admitted when they arrive; a job is launched when the
+    queue holds ``max_batch`` requests or the oldest has waited
+    ``batch_window`` seconds.  Returns the finished requests and wall time."""
+    srv = Server(precision=precision, max_batch=max_batch, max_jobs=max_jobs)
+    items = list(stream)
+    t0 = time.perf_counter()
+    clock = lambda: time.perf_counter() - t0  # noqa: E731
+    k = 0
+    while k < len(items) or srv.queue or srv.jobs:
+        now = clock()
+        while k < len(items) and items[k][0] <= now:
+            t, kind, inst = items[k]
+            if kind == 'sle':
+                r = Request('sle', inst.op, inst.x0, inst.rhs, repeats=inst.repeats, arrival=t)
+            else:
+                r = Request('evp', inst.op, inst.x0, repeats=inst.repeats, sigma=inst.sigma, arrival=t)
+            srv.queue.append(r)
+            k += 1
+        ready = bool(srv.queue) and (len(srv.queue) >= max_batch or now - srv.queue[0].arrival >= batch_window
+                                     or k >= len(items))
+        if srv.pump(clock, launch=ready) == 0 and not ready:
+            time.sleep(0.0005)
+        if now > duration_cap + 600:
+            break
+    return srv.finished, clock(), srv.stats

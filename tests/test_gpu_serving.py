@@ -1,0 +1,94 @@
+"""Batched eigenproblems, mixed SLE/EVP batches and the continuous-batching
+server: every result equals the same request solved alone."""
+
+import numpy as np
+import pytest
+
+from oracle import tt_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _tt(cores):
+    from scikit_tt_gb300.tensor_train import TT
+    return TT([np.array(c) for c in cores])
+
+
+@pytest.mark.parametrize('name', ['evp_ising_d12_eig', 'evp_ising_d12_eigh', 'evp_ising_d16_eig', 'evp_ising_d16_eigh'])
+def test_batched_evp_matches_reference(golden, name):
+    from scikit_tt_gb300.serving import Request, solve_batch
+    z, cores = golden(name)
+    reqs = [Request('evp', cores('op'), cores('x0'), repeats=int(z['repeats']), solver=str(z['solver']),
+                    sigma=float(z['sigma']), conv_eps=float(z['conv_eps'])) for _ in range(3)]
+    solve_batch(reqs, precision='fp64')
+    d = len(cores('op'))
+    for r in reqs:
+        assert abs(r.value - float(z['val'])) < 1e-10
+        assert abs(abs(r.value) - abs(O.ising_exact_e0(d, 1.0, 1.0))) < 1e-10
+        v, ref = O.full_vector(r.solution.cores), O.full_vector(cores('vec'))
+        assert min(np.linalg.norm(v - ref), np.linalg.norm(v + ref)) / np.linalg.norm(ref) < 1e-7
+
+
+def _mixed_requests():
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.serving import Request
+    reqs = []
+    for j in range(6):
+        rng = np.random.default_rng(300 + j)
+        d, n, r = 5 + j % 4, [2, 4, 3][j % 3], 3 + j % 4
+        op = wl.coupled_op(d, n, rng.uniform(0, 0.5, d), shift=0.5 + 0.2 * j)
+        reqs.append(Request('sle', op, wl.gaussian_tt(rng, d, n, r), wl.gaussian_tt(rng, d, n, 2), repeats=2))
+    for j in range(3):
+        e = wl.ising_evp(d=8 + 2 * j, g=0.7 + 0.2 * j, x_rank=8, repeats=4, seed=50 + j)
+        reqs.append(Request('evp', e.op, e.x0, repeats=e.repeats, sigma=e.sigma))
+    return reqs
+
+
+def _alone(req, precision):
+    from scikit_tt_gb300.solvers import evp, sle
+    if req.kind == 'sle':
+        sol, _ = sle.als_ex(_tt(req.op), _tt(req.x0), _tt(req.rhs), repeats=req.repeats, precision=precision)
+        return sol, None
+    val, vec, _ = evp.als(_tt(req.op), _tt(req.x0), repeats=req.repeats, sigma=req.sigma)
+    return vec, val
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-10), ('mixed', 1e-8)])
+def test_mixed_batch_equals_alone(precision, tol):
+    from scikit_tt_gb300.serving import solve_batch
+    reqs = _mixed_requests()
+    solve_batch(reqs, precision=precision)
+    for r in reqs:
+        sol, val = _alone(r, precision)
+        if r.kind == 'sle':
+            assert O.stable_rel_diff(r.solution.cores, sol.cores) < tol
+            assert O.stable_rel_diff(r.solution.cores, O.sle_als(r.op, r.x0, r.rhs, repeats=r.repeats)) < tol
+        else:
+            assert abs(r.value - val) < 1e-10
+            ref_val, _, _ = O.evp_als(r.op, O.ortho_right(r.x0), repeats=r.repeats, sigma=r.sigma)
+            assert abs(r.value - ref_val) < 1e-9
+
+
+def test_server_overlapping_jobs_equal_alone():
+    # requests arrive in waves; later waves are launched while earlier jobs run
+    import time
+    from scikit_tt_gb300.serving import Server
+    reqs = _mixed_requests() + _mixed_requests()
+    srv = Server(precision='mixed', max_batch=3, max_jobs=4)
+    t0 = time.perf_counter()
+    clock = lambda: time.perf_counter() - t0  # noqa: E731
+    overlapped = 0
+    for k in range(0, len(reqs), 3):
+        for r in reqs[k:k + 3]:
+            srv.submit(r)
+        srv.pump(clock)
+        overlapped = max(overlapped, len(srv.jobs))
+    srv.drain(clock)
+    assert len(srv.finished) == len(reqs)
+    assert overlapped >= 2          # several jobs were in flight at once
+    for r in reqs:
+        sol, val = _alone(r, 'mixed')
+        if r.kind == 'sle':
+            assert O.stable_rel_diff(r.solution.cores, sol.cores) < 1e-8
+        else:
+            assert abs(r.value - val) < 1e-10
