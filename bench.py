@@ -3,7 +3,7 @@
 
 Workload: SLE ALS on the coupled Laplacian (d=32 sites, mode size n=8,
 operator rank 4, right-hand side rank 8, solution rank 32, 4 sweeps, seeded
-inputs).  A *step* is one batch of independent solves of that workload (2 per
+inputs).  A *step* is one batch of independent solves of that workload (4 per
 SM by default) in one launch, one CTA per solve.
 
 * ``value``: solves/s of the mixed-precision engine (FP32 Krylov inner solves,
@@ -205,6 +205,66 @@ class ClockSampler:
                 'samples': len(sm)}
 
 
+def other_workloads(lib, ctx, args):
+    """The remaining seeded workloads, each measured once (device time from the
+    engine's CUDA events; serving by wall clock)."""
+    import torch
+    from oracle import tt_oracle as O
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.serving import Request, run_stream, solve_batch
+    from scikit_tt_gb300.solvers import evp, sle
+    from scikit_tt_gb300.tensor_train import TT
+
+    def T(c):
+        return TT([x.copy() for x in c])
+    out = {}
+    # shifted Laplacian d=10 n=4, ranks 5/3, 2 sweeps: single-solve latency, parity with the oracle
+    w1 = wl.laplace_sle()
+    sle.als_ex(T(w1.op), T(w1.x0), T(w1.rhs), repeats=w1.repeats)
+    ms = []
+    for _ in range(5):
+        sol, st = sle.als_ex(T(w1.op), T(w1.x0), T(w1.rhs), repeats=w1.repeats)
+        ms.append(st['device_ms'])
+    ref = O.sle_als(w1.op, w1.x0, w1.rhs, repeats=w1.repeats)
+    out['laplace_d10_n4_r5'] = {'fp64_ms_per_solve': float(np.median(ms)),
+                                'rel_diff_vs_oracle': O.stable_rel_diff(sol.cores, ref),
+                                'global_rel_residual': O.stable_residual(w1.op, sol.cores, w1.rhs)}
+    # Ising d=48 g=1 rank 64, 6 sweeps, lowest eigenpair: single-solve drop-in and a 2-per-SM batch
+    w3 = wl.ising_evp()
+    val, _, its = evp.als(T(w3.op), T(w3.x0), repeats=w3.repeats, sigma=w3.sigma)
+    e0 = O.ising_exact_e0(48, 1.0, 1.0)
+    out['ising_d48_r64'] = {'dropin_fp64_ms': evp.last_stats['device_ms'], 'eigenvalue': val,
+                            'abs_err_vs_exact': abs(val - e0), 'sweeps': its,
+                            'lanczos_iterations': evp.last_stats['krylov_iterations']}
+    # 256 uneven instances (d 8..32, n in {2,4,8}, rank 4..48), 4 sweeps, one launch
+    b4 = wl.batch_sle(256)
+    probs = [(T(w.op), T(w.x0), T(w.rhs)) for w in b4]
+    res4 = {}
+    for prec in ('mixed', 'fp64'):
+        sle.als_batch(probs, repeats=4, precision=prec, tol=1e-10 if prec == 'mixed' else 0.0)
+        sols, st = sle.als_batch(probs, repeats=4, precision=prec, tol=1e-10 if prec == 'mixed' else 0.0)
+        res4[prec] = {'solves_per_s': 256 / (st['device_ms'] / 1e3), 'device_ms': st['device_ms'],
+                      'max_local_residual': st['max_local_residual']}
+    res4['mixed_over_plain'] = res4['mixed']['solves_per_s'] / res4['fp64']['solves_per_s']
+    out['batch256_uneven'] = res4
+    # serving: Poisson arrivals at 2000/s (80 % SLE from the uneven distribution, 20 % Ising EVP
+    # d 16..48, rank 16..64), replayed in real time for a bounded window
+    window = args.serve_window
+    items = list(wl.serving_stream(rate=2000.0, duration=window))
+    fin, wall, stats = run_stream(items, window, precision='mixed', max_batch=608, max_jobs=64)
+    lat = np.array([r.done - r.arrival for r in fin])
+    kinds = np.array([r.kind for r in fin])
+    out['serving_poisson_2000'] = {
+        'arrival_window_s': window, 'requests': len(fin), 'wall_s': wall, 'solves_per_s': len(fin) / wall,
+        'p50_latency_s': float(np.percentile(lat, 50)), 'p99_latency_s': float(np.percentile(lat, 99)),
+        'sle_p50_s': float(np.percentile(lat[kinds == 'sle'], 50)) if (kinds == 'sle').any() else None,
+        'evp_p50_s': float(np.percentile(lat[kinds == 'evp'], 50)) if (kinds == 'evp').any() else None,
+        'jobs': len(stats), 'max_local_residual': max(s['max_local_residual'] for s in stats),
+        'note': 'offered load exceeds one GPU: latency includes queueing'}
+    torch.cuda.synchronize()
+    return out
+
+
 def _desc_array(lib_mod, packs, bufs=None):
     C = lib_mod.C
     arr = (lib_mod.TTDesc * len(packs))()
@@ -234,7 +294,7 @@ def main_gpu(args):
     stream = torch.cuda.current_stream(dev)
     _lib.check(lib.ttals_set_stream(ctx, _lib.C.c_void_p(stream.cuda_stream)))
     C = _lib.C
-    B = args.batch or 2 * torch.cuda.get_device_properties(dev).multi_processor_count
+    B = args.batch or 4 * torch.cuda.get_device_properties(dev).multi_processor_count
 
     # B independent seeded instances per rank (weak scaling: each rank its own batch)
     inst = [wl.coupled_sle(seed=rank * B + j, **WORKLOAD) for j in range(B)]
@@ -347,6 +407,7 @@ def main_gpu(args):
     if os.path.exists(tf):
         traffic = json.load(open(tf)).get('batch_sle_kernel')
 
+    extra = {} if args.quick else other_workloads(lib, ctx, args)
     if rank != 0:
         return
     cpu_est, nsamp, nmax = cpu_sample(inst[0], nsites=2)
@@ -385,6 +446,7 @@ def main_gpu(args):
                          'sample': f'{nsamp} oracle local steps at N={nmax} (stack, dense matrix, LU, QR), '
                                    f'extrapolated by N^3 to all local solves of one solve'},
         'clocks': clk.summary(),
+        'other_workloads': extra,
     }
     print(json.dumps(line), flush=True)
 
@@ -395,7 +457,9 @@ def main():
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--batch', type=int, default=0, help='solves per step and GPU (default 2 x SM count)')
+    ap.add_argument('--batch', type=int, default=0, help='solves per step and GPU (default 4 x SM count)')
+    ap.add_argument('--quick', action='store_true', help='headline only (skip the other workloads)')
+    ap.add_argument('--serve-window', type=float, default=0.1, help='seconds of Poisson arrivals to replay')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)

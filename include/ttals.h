@@ -149,6 +149,11 @@ int ttals_solve_batch(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, 
 int ttals_submit(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int32_t precision, double tol,
                  ttals_job** job);
 int ttals_job_poll(ttals_job* job, int32_t* done);
+/* Per-request completion: done[i] = 1 once request i's CTA has finished
+ * (host-mapped flags, no device call).  ttals_job_fetch copies request i's
+ * outputs while the rest of the job keeps running. */
+int ttals_job_poll_each(ttals_job* job, int32_t* done);
+int ttals_job_fetch(ttals_job* job, int32_t index);
 int ttals_job_finish(ttals_job* job, ttals_stats* stats);
 /* Device bytes a batch would reserve (admission control). */
 int ttals_batch_bytes(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int64_t* bytes);

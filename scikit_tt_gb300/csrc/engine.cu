@@ -783,7 +783,8 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
 
 // Enqueue uploads and the batch kernel on `st` into the device block `mem`
 // (P.bytes).  k0/k1 bracket the kernel.
-void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1) {
+void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1,
+                 int* done_dev = nullptr) {
   const int count = (int)P.in.size();
   double* data = (double*)mem;
   int64_t* dmeta = (int64_t*)(mem + P.off_meta);
@@ -811,6 +812,7 @@ void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEve
     H.out = base + I.off[8];
     H.report = base + I.off[9];
     H.Xopt = base + I.off[10];
+    H.done = done_dev ? done_dev + j : nullptr;
   }
   CK(cudaMemcpyAsync(dmeta, P.meta.data(), sizeof(int64_t) * P.meta.size(), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(dinst, hinst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, st));
@@ -834,35 +836,40 @@ void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEve
   if (k1) CK(cudaEventRecord(k1, st));
 }
 
-// After the stream finished: copy outputs (to host or device pointers),
-// check every request's status and fill the statistics.
-void collect_plan(BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_stats* stats, float kernel_ms,
-                  float total_ms, int64_t launches) {
-  const int count = (int)P.in.size();
+// Copy request j's outputs (to host or device pointers) on `st`, check its
+// status and return its report.  The request's CTA must have finished.
+std::vector<double> collect_one(BatchPlan& P, int j, char* mem, cudaStream_t st, int out_dev) {
   double* data = (double*)mem;
+  BatchReqHost& I = P.in[j];
+  const int d = I.op.d;
+  std::vector<double> rep(10 + d, 0.0);
+  CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (10 + d), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const int stj = (int)rep[4];
+  if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
+  if (stj == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in request " + std::to_string(j)};
+  if (stj != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(stj)};
+  int64_t cnt = 0;
+  for (int i = 0; i < d; ++i) {
+    const int64_t ri = (int64_t)rep[8 + i], rn = (int64_t)rep[9 + i];
+    require(ri == I.fin[i] && rn == I.fin[i + 1], TTALS_ERR_CUDA, "rank schedule mismatch in a batched request");
+    cnt += ri * I.op.m[i] * rn;
+  }
+  CK(cudaMemcpyAsync(I.out, data + I.region + I.off[8], sizeof(double) * cnt,
+                     out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (I.out_val) *I.out_val = rep[7];
+  if (I.out_its) *I.out_its = (int32_t)rep[9 + d];
+  return rep;
+}
+
+void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats* stats, float kernel_ms,
+                      float total_ms, int64_t launches) {
+  if (!stats) return;
   double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
   int64_t nsolve = 0, nits = 0, ncyc = 0;
-  std::vector<double> rep;
-  for (int j = 0; j < count; ++j) {
-    BatchReqHost& I = P.in[j];
-    const int d = I.op.d;
-    rep.assign(10 + d, 0.0);
-    CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (10 + d), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    const int stj = (int)rep[4];
-    if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
-    if (stj == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in request " + std::to_string(j)};
-    if (stj != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(stj)};
-    int64_t cnt = 0;
-    for (int i = 0; i < d; ++i) {
-      const int64_t ri = (int64_t)rep[8 + i], rn = (int64_t)rep[9 + i];
-      require(ri == I.fin[i] && rn == I.fin[i + 1], TTALS_ERR_CUDA, "rank schedule mismatch in a batched request");
-      cnt += ri * I.op.m[i] * rn;
-    }
-    CK(cudaMemcpyAsync(I.out, data + I.region + I.off[8], sizeof(double) * cnt,
-                       out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
-    if (I.out_val) *I.out_val = rep[7];
-    if (I.out_its) *I.out_its = (int32_t)rep[9 + d];
+  for (const auto& rep : reps) {
+    if (rep.empty()) continue;
     maxres = std::max(maxres, rep[0]);
     nsolve += (int64_t)rep[1];
     nits += (int64_t)rep[2];
@@ -870,19 +877,24 @@ void collect_plan(BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_s
     fl64 += rep[5];
     fl32 += rep[6];
   }
-  CK(cudaStreamSynchronize(st));
-  if (stats) {
-    stats->local_solves = nsolve;
-    stats->krylov_iterations = nits;
-    stats->refinement_steps = ncyc;
-    stats->max_local_residual = maxres;
-    stats->device_ms = total_ms;
-    stats->kernel_launches = launches;
-    stats->solver_launches = 1;
-    stats->solver_ms = kernel_ms;
-    stats->solver_flops64 = fl64;
-    stats->solver_flops32 = fl32;
-  }
+  stats->local_solves = nsolve;
+  stats->krylov_iterations = nits;
+  stats->refinement_steps = ncyc;
+  stats->max_local_residual = maxres;
+  stats->device_ms = total_ms;
+  stats->kernel_launches = launches;
+  stats->solver_launches = 1;
+  stats->solver_ms = kernel_ms;
+  stats->solver_flops64 = fl64;
+  stats->solver_flops32 = fl32;
+}
+
+// After the stream finished: copy every request's outputs and fill the statistics.
+void collect_plan(BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_stats* stats, float kernel_ms,
+                  float total_ms, int64_t launches) {
+  std::vector<std::vector<double>> reps(P.in.size());
+  for (size_t j = 0; j < P.in.size(); ++j) reps[j] = collect_one(P, (int)j, mem, st, out_dev);
+  fill_batch_stats(reps, stats, kernel_ms, total_ms, launches);
 }
 
 void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, int out_dev,
@@ -1142,12 +1154,15 @@ int guarded(ttals_ctx* c, F&& f) {
 
 struct ttals_job {
   ttals_ctx* c = nullptr;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;     // the batch kernel
+  cudaStream_t fetch = nullptr;  // copies of finished requests while the kernel runs
   cudaEvent_t k0 = nullptr, k1 = nullptr, e0 = nullptr, e1 = nullptr;
   char* mem = nullptr;
   size_t bytes = 0;
   BatchPlan plan;
   int64_t launches = 0;
+  int* flags = nullptr;  // host-mapped completion flags, one per request
+  std::vector<std::vector<double>> reps;  // reports of fetched requests
 };
 
 namespace {
@@ -1162,6 +1177,8 @@ void job_release(ttals_job* j) {
   for (cudaEvent_t e : {j->k0, j->k1, j->e0, j->e1})
     if (e) cudaEventDestroy(e);
   if (j->st) cudaStreamDestroy(j->st);
+  if (j->fetch) cudaStreamDestroy(j->fetch);
+  if (j->flags) cudaFreeHost(j->flags);
   delete j;
 }
 
@@ -1307,12 +1324,18 @@ int ttals_submit(ttals_ctx* c, int32_t count, const ttals_request* reqs, int32_t
     require(c->inflight + j->bytes <= c->budget, TTALS_ERR_NOMEM,
             "device memory budget of the context is held by running jobs");
     CK(cudaStreamCreateWithFlags(&j->st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&j->fetch, cudaStreamNonBlocking));
     for (cudaEvent_t* e : {&j->k0, &j->k1, &j->e0, &j->e1}) CK(cudaEventCreate(e));
+    CK(cudaHostAlloc((void**)&j->flags, sizeof(int) * count, cudaHostAllocMapped));
+    std::memset(j->flags, 0, sizeof(int) * count);
+    int* flags_dev = nullptr;
+    CK(cudaHostGetDevicePointer((void**)&flags_dev, j->flags, 0));
+    j->reps.assign(count, std::vector<double>());
     launch_counter() = 0;
     CK(cudaEventRecord(j->e0, j->st));
     CK(cudaMallocAsync((void**)&j->mem, j->bytes, j->st));
     c->inflight += j->bytes;
-    launch_plan(c, j->plan, j->mem, j->st, j->k0, j->k1);
+    launch_plan(c, j->plan, j->mem, j->st, j->k0, j->k1, flags_dev);
     CK(cudaEventRecord(j->e1, j->st));
     j->launches = launch_counter();
     *job = j;
@@ -1334,6 +1357,22 @@ int ttals_job_poll(ttals_job* j, int32_t* done) {
   });
 }
 
+int ttals_job_poll_each(ttals_job* j, int32_t* done) {
+  if (!j || !done) return TTALS_ERR_ARG;
+  const int n = (int)j->plan.in.size();
+  for (int q = 0; q < n; ++q) done[q] = ((volatile int*)j->flags)[q] != 0 ? 1 : 0;
+  return TTALS_OK;
+}
+
+int ttals_job_fetch(ttals_job* j, int32_t index) {
+  if (!j) return TTALS_ERR_ARG;
+  return guarded(j->c, [&] {
+    require(index >= 0 && index < (int)j->plan.in.size(), TTALS_ERR_ARG, "request index out of range");
+    require(((volatile int*)j->flags)[index] != 0, TTALS_ERR_ARG, "request has not finished");
+    if (j->reps[index].empty()) j->reps[index] = collect_one(j->plan, index, j->mem, j->fetch, 0);
+  });
+}
+
 int ttals_job_finish(ttals_job* j, ttals_stats* stats) {
   if (!j) return TTALS_ERR_ARG;
   ttals_ctx* c = j->c;
@@ -1342,7 +1381,9 @@ int ttals_job_finish(ttals_job* j, ttals_stats* stats) {
     float kms = 0.f, tms = 0.f;
     CK(cudaEventElapsedTime(&kms, j->k0, j->k1));
     CK(cudaEventElapsedTime(&tms, j->e0, j->e1));
-    collect_plan(j->plan, j->mem, j->st, 0, stats, kms, tms, j->launches);
+    for (size_t q = 0; q < j->plan.in.size(); ++q)
+      if (j->reps[q].empty()) j->reps[q] = collect_one(j->plan, (int)q, j->mem, j->st, 0);
+    fill_batch_stats(j->reps, stats, kms, tms, j->launches);
   });
   job_release(j);
   return st;

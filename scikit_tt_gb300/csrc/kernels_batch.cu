@@ -261,10 +261,14 @@ struct CtaEigStats {
   int its, restarts, status;
 };
 
+// TI: arithmetic of the operator, basis and products (double, or float for
+// the first stage of the mixed-precision eigensolve).  x (in: start vector,
+// out: Ritz vector) and all scalars stay FP64.
+template <typename TI>
 __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
-                                               const double* L, const double* A, const double* R, double* T1,
-                                               double* T2, double* x, double* V, double* w, int64_t N, int m,
-                                               int mode, double sigma, int max_restarts, double tol, double* sm) {
+                                               const TI* L, const TI* A, const TI* R, TI* T1, TI* T2, double* x,
+                                               TI* V, TI* w, int64_t N, int m, int mode, double sigma,
+                                               int max_restarts, double tol, double* sm) {
   double* al = sm;
   double* be = al + m;
   double* h1 = be + m;
@@ -285,21 +289,21 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   for (int64_t e = tid; e < N; e += nt) xs += x[e] * x[e];
   const double xn = sqrt(cta_sum(xs));
   const bool ok = xn > 0.0 && isfinite(xn);
-  for (int64_t e = tid; e < N; e += nt) V[e] = ok ? x[e] / xn : 1.0 / sqrt((double)N);
+  for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(ok ? x[e] / xn : 1.0 / sqrt((double)N));
   __syncthreads();
   const int mm = (int)(N < m ? N : m);
   for (;;) {
     int nT = 0;
     for (int j = 0; j < mm; ++j) {
-      cta_apply<double>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
-      cta_dots<double>(V, N, j + 1, w, h1);
+      cta_apply<TI>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
+      cta_dots<TI>(V, N, j + 1, w, h1);
       for (int64_t e = tid; e < N; e += nt) {
-        double acc = w[e];
-        for (int q = 0; q <= j; ++q) acc -= h1[q] * V[(int64_t)q * N + e];
-        w[e] = acc;
+        double acc = (double)w[e];
+        for (int q = 0; q <= j; ++q) acc -= h1[q] * (double)V[(int64_t)q * N + e];
+        w[e] = (TI)acc;
       }
       __syncthreads();
-      cta_dots<double>(V, N, j + 1, w, h2);
+      cta_dots<TI>(V, N, j + 1, w, h2);
       double b2 = h2[j + 1];
       for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
       const double bj = sqrt(fmax(b2, 0.0));
@@ -308,12 +312,12 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
         be[j] = bj;
       }
       if (bj > 0.0 && j + 1 < mm) {
-        double* vn = V + (int64_t)(j + 1) * N;
+        TI* vn = V + (int64_t)(j + 1) * N;
         const double inv = 1.0 / bj;
         for (int64_t e = tid; e < N; e += nt) {
-          double acc = w[e];
-          for (int q = 0; q <= j; ++q) acc -= h2[q] * V[(int64_t)q * N + e];
-          vn[e] = acc * inv;
+          double acc = (double)w[e];
+          for (int q = 0; q <= j; ++q) acc -= h2[q] * (double)V[(int64_t)q * N + e];
+          vn[e] = (TI)(acc * inv);
         }
       }
       __syncthreads();
@@ -362,7 +366,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
     // Ritz vector
     for (int64_t e = tid; e < N; e += nt) {
       double acc = 0.0;
-      for (int l = 0; l < nT; ++l) acc += z[l] * V[(int64_t)l * N + e];
+      for (int l = 0; l < nT; ++l) acc += z[l] * (double)V[(int64_t)l * N + e];
       x[e] = acc;
     }
     __syncthreads();
@@ -371,7 +375,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
     double s2 = 0.0;
     for (int64_t e = tid; e < N; e += nt) s2 += x[e] * x[e];
     const double nrm = sqrt(cta_sum(s2));
-    for (int64_t e = tid; e < N; e += nt) V[e] = nrm > 0.0 ? x[e] / nrm : 1.0 / sqrt((double)N);
+    for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(nrm > 0.0 ? x[e] / nrm : 1.0 / sqrt((double)N));
     __syncthreads();
   }
   out.theta = s_theta;
@@ -381,6 +385,17 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
 }
 
 __device__ __noinline__ void cta_qr(const QrArgs& q) { cta_householder_qr(q); }
+
+// Make this request's outputs visible to the host and to copy engines, then
+// raise its completion flag (host-mapped memory).
+__device__ __forceinline__ void signal_done(int* flag) {
+  __syncthreads();
+  if (threadIdx.x == 0 && flag) {
+    __threadfence_system();
+    asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
+  }
+  __syncthreads();
+}
 
 // ---------------------------------------------------------------------------
 // one instance
@@ -607,7 +622,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     for (int i = 0; i <= d; ++i) I.report[8 + i] = (double)r[i];
     I.report[9 + d] = (double)I.repeats;
   }
-  __syncthreads();
+  signal_done(I.done);
 }
 
 // ---------------------------------------------------------------------------
@@ -638,7 +653,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   auto L = [&](int i) { return I.L + L_off[i]; };
   auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
   auto A = [&](int i) { return I.op + op_off[i]; };
-  double fl64 = 0.0, maxres = 0.0, theta = 0.0;
+  double fl64 = 0.0, fl32 = 0.0, maxres = 0.0, theta = 0.0;
   int64_t nsolve = 0, nits = 0, nrst = 0;
   auto apply_fl = [&](double aa, double nn, double ss, double r0, double r1) {
     return 2 * aa * aa * r0 * nn * ss + 2 * aa * ss * nn * nn * r0 * r1 + 2 * aa * nn * ss * ss * r1;
@@ -692,15 +707,18 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
     const int m = (int)(N < a.m_evp ? N : a.m_evp);
-    const CtaEigStats st = cta_lanczos(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m, I.mode,
-                                       I.sigma, 40, a.tol_evp, sm);
+    const double fa = apply_fl((double)aa, (double)nn, (double)ss, (double)R[i], (double)R[i + 1]);
+    // Eigen solves stay FP64 in both precision modes: warm-started from the
+    // previous sweep's core, FP64 Lanczos converges in ~12 steps per site, and
+    // an FP32 Lanczos pre-stage (then FP64 polish) measured 2.8x slower.
+    const CtaEigStats st = cta_lanczos<double>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m,
+                                               I.mode, I.sigma, 40, a.tol_evp, sm);
     theta = st.theta;
-    ++nsolve;
     nits += st.its;
     nrst += st.restarts;
     maxres = fmax(maxres, st.res);
-    const double fa = apply_fl((double)aa, (double)nn, (double)ss, (double)R[i], (double)R[i + 1]);
     fl64 += st.its * (fa + 8.0 * (double)N * (m + 1) / 2.0);
+    ++nsolve;
   };
   for (int i = d - 1; i >= 0; --i) right(i);
   double hist[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
@@ -767,12 +785,12 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     I.report[3] = (double)nrst;
     I.report[4] = (double)ST_OK;
     I.report[5] = fl64;
-    I.report[6] = 0.0;
+    I.report[6] = fl32;
     I.report[7] = val_opt;
     for (int i = 0; i <= d; ++i) I.report[8 + i] = have_opt ? (double)ropt[i] : 0.0;
     I.report[9 + d] = (double)(it - 1);
   }
-  __syncthreads();
+  signal_done(I.done);
 }
 
 __global__ void __launch_bounds__(kBatchThreads, 4) batch_sle_kernel(BatchArgs a) {

@@ -19,6 +19,7 @@ struct BatchInst {
   double *X, *L, *Rt, *Lb, *Rb;
   double* Xopt;    // EVP: cores of the best sweep (evp.py:151-155)
   double* out;     // final cores, packed
+  int* done;       // per-request completion flag in host-mapped memory (may be null)
   double* report;  // [max rel residual, local solves, Krylov its, refinement cycles, status, flops64, flops32,
                    //  eigenvalue, ranks[d+1], sweeps run]
 };

@@ -89,7 +89,7 @@ def solve_batch(requests: List[Request], precision: str = 'mixed', tol: float = 
 class Server:
     """Continuous batching over the asynchronous job API (ttals_submit)."""
 
-    def __init__(self, precision: str = 'mixed', tol: float = 0.0, max_batch: int = 304, max_jobs: int = 4):
+    def __init__(self, precision: str = 'mixed', tol: float = 0.0, max_batch: int = 608, max_jobs: int = 64):
         self.prec = _PREC[precision]
         self.tol = float(tol)
         self.max_batch = max_batch
@@ -112,7 +112,8 @@ class Server:
             return False         # budget held by running jobs: admit later
         _lib.check(st)
         self.queue = self.queue[len(take):]
-        self.jobs.append((h, take, arr))
+        self.jobs.append({'h': h, 'reqs': take, 'arr': arr, 'fetched': set(),
+                          'flags': (C.c_int32 * len(take))()})
         return True
 
     def pump(self, clock, launch: bool = True) -> int:
@@ -121,21 +122,24 @@ class Server:
         lib = _lib.load()
         completed = 0
         still = []
-        for h, reqs, arr in self.jobs:
-            done = C.c_int32(0)
-            _lib.check(lib.ttals_job_poll(h, C.byref(done)))
-            if done.value:
+        for job in self.jobs:
+            h, reqs, fetched, flags = job['h'], job['reqs'], job['fetched'], job['flags']
+            # requests complete one by one: a slow request does not hold the others back
+            _lib.check(lib.ttals_job_poll_each(h, flags))
+            for i in range(len(reqs)):
+                if flags[i] and i not in fetched:
+                    _lib.check(lib.ttals_job_fetch(h, i))
+                    reqs[i]._complete()
+                    reqs[i].done = clock()
+                    fetched.add(i)
+                    self.finished.append(reqs[i])
+                    completed += 1
+            if len(fetched) == len(reqs):
                 st = _lib.Stats()
                 _lib.check(lib.ttals_job_finish(h, C.byref(st)))
-                t = clock()
-                for r in reqs:
-                    r._complete()
-                    r.done = t
-                self.finished.extend(reqs)
                 self.stats.append(st.as_dict())
-                completed += len(reqs)
             else:
-                still.append((h, reqs, arr))
+                still.append(job)
         self.jobs = still
         while launch and self.queue and len(self.jobs) < self.max_jobs:
             if not self._launch(clock):
@@ -149,7 +153,7 @@ class Server:
                 time.sleep(0.0005)
 
 
-def run_stream(stream, duration_cap: float, precision='mixed', max_batch=304, max_jobs=4, batch_window=0.005):
+def run_stream(stream, duration_cap: float, precision='mixed', max_batch=608, max_jobs=64, batch_window=0.005):
     """Replay ``(arrival_s, kind, instance)`` items against a Server in real
     time.  Requests are admitted when they arrive; a job is launched when the
     queue holds ``max_batch`` requests or the oldest has waited

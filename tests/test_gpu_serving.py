@@ -14,13 +14,15 @@ def _tt(cores):
     return TT([np.array(c) for c in cores])
 
 
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
 @pytest.mark.parametrize('name', ['evp_ising_d12_eig', 'evp_ising_d12_eigh', 'evp_ising_d16_eig', 'evp_ising_d16_eigh'])
-def test_batched_evp_matches_reference(golden, name):
+def test_batched_evp_matches_reference(golden, name, precision):
+    # mixed: FP32 Lanczos, then FP64 Lanczos from its Ritz vector (eigenvalue tolerance unchanged)
     from scikit_tt_gb300.serving import Request, solve_batch
     z, cores = golden(name)
     reqs = [Request('evp', cores('op'), cores('x0'), repeats=int(z['repeats']), solver=str(z['solver']),
                     sigma=float(z['sigma']), conv_eps=float(z['conv_eps'])) for _ in range(3)]
-    solve_batch(reqs, precision='fp64')
+    solve_batch(reqs, precision=precision)
     d = len(cores('op'))
     for r in reqs:
         assert abs(r.value - float(z['val'])) < 1e-10
