@@ -207,6 +207,12 @@ int ttals_stack_op_noalloc(ttals_ctx* ctx, int32_t left, const double* stack, co
                            const double* op, int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1,
                            double* out);
 
+/* Diagnostic: y -> M y for the local operator in FP32 as the mixed-precision
+ * inner solver computes it (tensor cores, 3xTF32), host pointers, one CTA.
+ * No reference counterpart; used to test the tensor-core path directly. */
+int ttals_apply_f32(ttals_ctx* ctx, const float* L, const float* A, const float* Rt, const float* y, int64_t r0,
+                    int64_t n, int64_t r1, int64_t R0, int64_t R1, float* out);
+
 /* scikit_tt/solvers/sle.py:308-347 `__construct_micro_matrix_als`: dense
  * local operator (r0*n*r1)^2 from stacks L (r0, R0, r0), Rt (r1, R1, r1) and
  * operator core op (R0, n, n, R1). */

@@ -38,7 +38,7 @@ EXPORTS = (
     'ttals_sle_als', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_norm',
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
-    'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch',
+    'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_apply_f32',
 )
 
 REQ_SLE = 0
@@ -111,6 +111,8 @@ def load():
         lib.ttals_job_poll.argtypes = [vp, P(i32)]
         lib.ttals_job_finish.argtypes = [vp, P(Stats)]
         lib.ttals_job_poll_each.argtypes = [vp, P(i32)]
+        pf = P(C.c_float)
+        lib.ttals_apply_f32.argtypes = [vp, pf, pf, pf, pf, i64, i64, i64, i64, i64, pf]
         lib.ttals_job_fetch.argtypes = [vp, i32]
         lib.ttals_batch_bytes.argtypes = [vp, i32, P(Request), P(C.c_int64)]
         lib.ttals_stack_op_noalloc.argtypes = [vp, i32, pd, pd, pd, i64, i64, i64, i64, i64, pd]

@@ -1603,6 +1603,33 @@ int ttals_stack_op(ttals_ctx* c, int32_t left, const double* stack, const double
   });
 }
 
+int ttals_apply_f32(ttals_ctx* c, const float* L, const float* A, const float* Rt, const float* y, int64_t a,
+                    int64_t n, int64_t s, int64_t R0, int64_t R1, float* out) {
+  return guarded(c, [&] {
+    require(L && A && Rt && y && out, TTALS_ERR_ARG, "null pointer");
+    require(a > 0 && n > 0 && s > 0 && R0 > 0 && R1 > 0, TTALS_ERR_ARG, "dimensions must be positive");
+    const int64_t nl = a * R0 * a, na = R0 * n * n * R1, nr = s * R1 * s, N = a * n * s;
+    const int64_t nt = std::max(R0, R1) * N;
+    float *dl, *da, *dr, *dy, *t1, *t2, *dout;
+    Bump B{c};
+    B.want(&dl, nl);
+    B.want(&da, na);
+    B.want(&dr, nr);
+    B.want(&dy, N);
+    B.want(&t1, nt);
+    B.want(&t2, nt);
+    B.want(&dout, N);
+    B.commit();
+    CK(cudaMemcpyAsync(dl, L, 4 * nl, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(da, A, 4 * na, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dr, Rt, 4 * nr, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dy, y, 4 * N, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_apply_f32(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, c->stream));
+    CK(cudaMemcpyAsync(out, dout, 4 * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
 int ttals_micro_matrix(ttals_ctx* c, const double* L, const double* op, const double* Rt, int64_t r0, int64_t n,
                        int64_t r1, int64_t R0, int64_t R1, double* out, int32_t on_device) {
   return guarded(c, [&] {

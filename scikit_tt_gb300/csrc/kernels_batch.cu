@@ -13,10 +13,13 @@
 // reorthogonalisation.  Contractions use the descriptors of ttals_desc.cuh.
 #include <float.h>
 
+#include <type_traits>
+
 #include "ttals_batch.h"
 #include "ttals_desc.cuh"
 #include "ttals_internal.h"
 #include "ttals_qr.cuh"
+#include "ttals_tc.cuh"
 #include "ttals_tri.cuh"
 
 namespace ttals {
@@ -31,6 +34,11 @@ constexpr int kBatchThreads = 128;  // four CTAs per SM: FP32 and FP64 phases of
 // Inlined body (used inside the Krylov loops); `c` must not alias C.
 template <typename T>
 __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C) {
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 (inner Krylov) contractions go to the tensor cores when GEMM-shaped
+    __shared__ int ktab[2 * kTcMaxK];
+    if (cta_gemm_tf32x3(c, A, B, C, ktab)) return;
+  }
   constexpr int VW = DefaultVW<T>::value;
   if (contract_vec_ok<T, VW>(c, B, C)) {
     for (int64_t e = (int64_t)threadIdx.x * VW; e < c.total; e += (int64_t)blockDim.x * VW)
@@ -83,13 +91,22 @@ __device__ __forceinline__ double cta_sum(double v) {
 }
 
 // out[kk] = <X_kk, w> for kk < nvec (X_kk = V + kk*N), out[nvec] = <w, w>
+// Dots accumulate in the vectors' own precision (FP32 for the inner solver:
+// its Gram-Schmidt only needs inner-solver accuracy, and FP64 arithmetic is
+// 57x slower on this part); lane partial sums keep the rounding error ~sqrt(N).
 template <typename T>
 __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const T* w, double* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int kk = warp; kk <= nvec; kk += nw) {
     const T* xv = (kk < nvec) ? V + (int64_t)kk * N : w;
-    double s = 0.0;
-    for (int64_t e = lane; e < N; e += 32) s += (double)xv[e] * (double)w[e];
+    T s0 = T(0), s1 = T(0);
+    int64_t e = lane;
+    for (; e + 32 < N; e += 64) {
+      s0 += xv[e] * w[e];
+      s1 += xv[e + 32] * w[e + 32];
+    }
+    if (e < N) s0 += xv[e] * w[e];
+    double s = (double)s0 + (double)s1;
     s = warp_sum(s);
     if (lane == 0) out[kk] = s;
   }
@@ -173,9 +190,9 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w);
       cta_dots<TI>(V, N, j + 1, w, h1);
       for (int64_t e = tid; e < N; e += nt) {
-        double acc = (double)w[e];
-        for (int q = 0; q <= j; ++q) acc -= h1[q] * (double)V[(int64_t)q * N + e];
-        w[e] = (TI)acc;
+        TI acc = w[e];
+        for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
+        w[e] = acc;
       }
       __syncthreads();
       cta_dots<TI>(V, N, j + 1, w, h2);
@@ -183,12 +200,12 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
       const double hn = sqrt(fmax(hn2, 0.0));
       if (hn > 0.0) {
-        const double inv = 1.0 / hn;
+        const TI inv = (TI)(1.0 / hn);
         TI* vn = V + (int64_t)(j + 1) * N;
         for (int64_t e = tid; e < N; e += nt) {
-          double acc = (double)w[e];
-          for (int q = 0; q <= j; ++q) acc -= h2[q] * (double)V[(int64_t)q * N + e];
-          vn[e] = (TI)(acc * inv);
+          TI acc = w[e];
+          for (int q = 0; q <= j; ++q) acc -= (TI)h2[q] * V[(int64_t)q * N + e];
+          vn[e] = acc * inv;
         }
       }
       if (tid == 0) {
@@ -808,6 +825,22 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_sle_kernel(BatchArgs a
     else
       batch_solve(a, j, S, sm);
   }
+}
+
+// Diagnostic: one CTA applies the FP32 local operator (tensor-core path).
+__global__ void __launch_bounds__(kBatchThreads) apply_f32_kernel(Contraction p1, Contraction p2, Contraction p3,
+                                                                  const float* L, const float* A, const float* R,
+                                                                  const float* y, float* T1, float* T2, float* out) {
+  cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out);
+}
+
+cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
+                             const float* R, const float* y, float* T1, float* T2, float* out, cudaStream_t st) {
+  Contraction p1, p2, p3;
+  desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
+  apply_f32_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out);
+  ++launch_counter();
+  return cudaGetLastError();
 }
 
 size_t batch_smem_bytes(int m, int m_evp) {

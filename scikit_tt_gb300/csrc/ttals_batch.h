@@ -48,5 +48,7 @@ size_t batch_smem_bytes(int m, int m_evp);
 int batch_blocks_per_sm(int m, int m_evp);
 int64_t batch_scratch_stride(const BatchSizes& z, int m, int m_evp);
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st);
+cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
+                             const float* R, const float* y, float* T1, float* T2, float* out, cudaStream_t st);
 
 }  // namespace ttals
