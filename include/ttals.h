@@ -91,6 +91,10 @@ typedef struct {
   double solver_ms;           /* their summed duration (CUDA events)            */
   double solver_flops64;      /* algorithmic FP64 flops of the local solves     */
   double solver_flops32;      /* algorithmic FP32 flops of the local solves     */
+  /* batched calls: SM cycles summed over requests, per phase: guess
+   * orthonormalisation, operator/RHS stacks, local right-hand sides, FP64
+   * residuals, inner Krylov iterations, QR/RQ + gauge push, eigensolves, total */
+  double phase_cycles[8];
 } ttals_stats;
 
 /* Context: one device, one stream, one device-memory arena capped at
@@ -212,6 +216,13 @@ int ttals_stack_op_noalloc(ttals_ctx* ctx, int32_t left, const double* stack, co
  * No reference counterpart; used to test the tensor-core path directly. */
 int ttals_apply_f32(ttals_ctx* ctx, const float* L, const float* A, const float* Rt, const float* y, int64_t r0,
                     int64_t n, int64_t r1, int64_t R0, int64_t R1, float* out);
+
+/* Diagnostic: y -> M y in FP64 accuracy with the products on the BF16 tensor
+ * cores (6-slice Ozaki splitting, FP32 accumulation, FP64 recombination), as
+ * the mixed-precision path computes its stacks and refinement residuals.
+ * Host pointers, one CTA.  No reference counterpart. */
+int ttals_apply_f64emu(ttals_ctx* ctx, const double* L, const double* A, const double* Rt, const double* y,
+                       int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1, double* out);
 
 /* scikit_tt/solvers/sle.py:308-347 `__construct_micro_matrix_als`: dense
  * local operator (r0*n*r1)^2 from stacks L (r0, R0, r0), Rt (r1, R1, r1) and

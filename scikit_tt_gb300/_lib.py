@@ -39,6 +39,7 @@ EXPORTS = (
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
     'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_apply_f32',
+    'ttals_apply_f64emu',
 )
 
 REQ_SLE = 0
@@ -61,10 +62,12 @@ class Stats(C.Structure):
     _fields_ = [('local_solves', C.c_int64), ('krylov_iterations', C.c_int64), ('refinement_steps', C.c_int64),
                 ('max_local_residual', C.c_double), ('device_ms', C.c_double), ('kernel_launches', C.c_int64),
                 ('solver_launches', C.c_int64), ('solver_ms', C.c_double), ('solver_flops64', C.c_double),
-                ('solver_flops32', C.c_double)]
+                ('solver_flops32', C.c_double), ('phase_cycles', C.c_double * 8)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d['phase_cycles'] = list(self.phase_cycles)
+        return d
 
 
 _lib = None
@@ -113,6 +116,7 @@ def load():
         lib.ttals_job_poll_each.argtypes = [vp, P(i32)]
         pf = P(C.c_float)
         lib.ttals_apply_f32.argtypes = [vp, pf, pf, pf, pf, i64, i64, i64, i64, i64, pf]
+        lib.ttals_apply_f64emu.argtypes = [vp, pd, pd, pd, pd, i64, i64, i64, i64, i64, pd]
         lib.ttals_job_fetch.argtypes = [vp, i32]
         lib.ttals_batch_bytes.argtypes = [vp, i32, P(Request), P(C.c_int64)]
         lib.ttals_stack_op_noalloc.argtypes = [vp, i32, pd, pd, pd, i64, i64, i64, i64, i64, pd]

@@ -643,7 +643,7 @@ struct BatchReqHost {
 
 struct BatchPlan {
   std::vector<BatchReqHost> in;
-  BatchSizes z{1, 1, 1, 1, 1, 1, 1, 1};
+  BatchSizes z{1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
   std::vector<int64_t> meta;
   int64_t region_total = 0;  // doubles
   int grid = 1;
@@ -725,6 +725,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
       P.z.core = std::max(P.z.core, std::max(a * nn * s, rx0[i] * nn * std::max(I.cap[i + 1], rx0[i + 1])));
       P.z.stack = std::max(P.z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
       P.z.opcore = std::max(P.z.opcore, R[i] * nn * nn * R[i + 1]);
+      if (prec == TTALS_PREC_MIXED && I.kind == 0) oz_need_site(P.z, a, nn, s, R[i], R[i + 1]);
     }
     require(P.z.T < (int64_t(1) << 31) && P.z.N * (kBatchMEvp + 1) < (int64_t(1) << 31), TTALS_ERR_UNSUPPORTED,
             "a request exceeds the 32-bit index range of the batch kernel");
@@ -743,7 +744,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     put(6, lbs);
     put(7, rbs);
     put(8, I.out_count);
-    put(9, 10 + d);
+    put(9, 18 + d);
     put(10, I.kind == 1 ? xs : 1);
     I.region = P.region_total;
     P.region_total += o;
@@ -842,8 +843,8 @@ std::vector<double> collect_one(BatchPlan& P, int j, char* mem, cudaStream_t st,
   double* data = (double*)mem;
   BatchReqHost& I = P.in[j];
   const int d = I.op.d;
-  std::vector<double> rep(10 + d, 0.0);
-  CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (10 + d), cudaMemcpyDeviceToHost, st));
+  std::vector<double> rep(18 + d, 0.0);
+  CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (18 + d), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const int stj = (int)rep[4];
   if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
@@ -866,10 +867,12 @@ std::vector<double> collect_one(BatchPlan& P, int j, char* mem, cudaStream_t st,
 void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats* stats, float kernel_ms,
                       float total_ms, int64_t launches) {
   if (!stats) return;
-  double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
+  double maxres = 0.0, fl64 = 0.0, fl32 = 0.0, ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t nsolve = 0, nits = 0, ncyc = 0;
   for (const auto& rep : reps) {
     if (rep.empty()) continue;
+    const size_t d = rep.size() - 18;
+    for (int k = 0; k < 8; ++k) ph[k] += rep[10 + d + k];
     maxres = std::max(maxres, rep[0]);
     nsolve += (int64_t)rep[1];
     nits += (int64_t)rep[2];
@@ -887,6 +890,7 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
   stats->solver_ms = kernel_ms;
   stats->solver_flops64 = fl64;
   stats->solver_flops32 = fl32;
+  for (int k = 0; k < 8; ++k) stats->phase_cycles[k] = ph[k];
 }
 
 // After the stream finished: copy every request's outputs and fill the statistics.
@@ -1626,6 +1630,36 @@ int ttals_apply_f32(ttals_ctx* c, const float* L, const float* A, const float* R
     CK(cudaMemcpyAsync(dy, y, 4 * N, cudaMemcpyHostToDevice, c->stream));
     CK(launch_apply_f32(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, c->stream));
     CK(cudaMemcpyAsync(out, dout, 4 * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int ttals_apply_f64emu(ttals_ctx* c, const double* L, const double* A, const double* Rt, const double* y,
+                       int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, double* out) {
+  return guarded(c, [&] {
+    require(L && A && Rt && y && out, TTALS_ERR_ARG, "null pointer");
+    require(a > 0 && n > 0 && s > 0 && R0 > 0 && R1 > 0, TTALS_ERR_ARG, "dimensions must be positive");
+    const int64_t nl = a * R0 * a, na = R0 * n * n * R1, nr = s * R1 * s, N = a * n * s;
+    const int64_t nt = std::max(R0, R1) * N;
+    const size_t ozb = apply_f64emu_scratch_bytes(a, n, s, R0, R1);
+    double *dl, *da, *dr, *dy, *t1, *t2, *dout;
+    char* oz;
+    Bump B{c};
+    B.want(&dl, nl);
+    B.want(&da, na);
+    B.want(&dr, nr);
+    B.want(&dy, N);
+    B.want(&t1, nt);
+    B.want(&t2, nt);
+    B.want(&dout, N);
+    B.want(&oz, (int64_t)ozb);
+    B.commit();
+    CK(cudaMemcpyAsync(dl, L, 8 * nl, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(da, A, 8 * na, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dr, Rt, 8 * nr, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dy, y, 8 * N, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_apply_f64emu(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, oz, ozb, c->stream));
+    CK(cudaMemcpyAsync(out, dout, 8 * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   });
 }

@@ -20,6 +20,7 @@
 #include "ttals_internal.h"
 #include "ttals_qr.cuh"
 #include "ttals_tc.cuh"
+#include "ttals_ozaki.cuh"
 #include "ttals_tri.cuh"
 
 namespace ttals {
@@ -51,6 +52,18 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
     }
   }
   __syncthreads();
+}
+
+// FP64 contraction; with `oz` set, GEMM-shaped ones run as emulated FP64 on the
+// BF16 tensor cores (ttals_ozaki.cuh), the rest natively.
+__device__ __noinline__ void cta_contract_f64(const Contraction& cref, const double* A, const double* B, double* C,
+                                              const OzScratch* oz) {
+  __shared__ Contraction sc;
+  __shared__ int oktab[2 * kTcMaxK];
+  if (threadIdx.x == 0) sc = cref;
+  __syncthreads();
+  if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oktab)) return;
+  cta_contract_body<double>(sc, A, B, C);
 }
 
 // Out-of-line version for the per-site bookkeeping (stacks, pushes): keeps the
@@ -136,7 +149,8 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
                                       const double* L64, const double* A64, const double* R64, double* T1_64,
                                       double* T2_64, const TI* Li, const TI* Ai, const TI* Ri, TI* T1i, TI* T2i,
                                       const double* f, double* x, double* r, TI* V, TI* w, int64_t N, int m,
-                                      int max_cycles, double tol, double inner_floor, double* sm) {
+                                      int max_cycles, double tol, double inner_floor, double* sm,
+                                      const OzScratch* oz, long long* cyc_res, long long* cyc_inner) {
   double* H = sm;                // (m+1) x m
   double* cs = H + (m + 1) * m;  // m
   double* sn = cs + m;           // m
@@ -160,17 +174,32 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     return out;
   }
   for (int cyc = 0; cyc < max_cycles; ++cyc) {
-    cta_contract_body(p1, L64, (const double*)x, T1_64);
-    cta_contract_body(p2, (const double*)T1_64, A64, T2_64);
+    const long long c0 = clock64();
     double rs = 0.0;
-    for (int64_t e = tid; e < N; e += nt) {
-      int64_t ao, bo, co;
-      contract_offsets(p3, e, ao, bo, co);
-      const double re = f[e] - contract_sum(p3, (const double*)T2_64, R64, ao, bo);
-      r[e] = re;
-      rs += re * re;
+    if (oz) {
+      // FP64-accurate residual with the products on the BF16 tensor cores
+      cta_contract_f64(p1, L64, (const double*)x, T1_64, oz);
+      cta_contract_f64(p2, (const double*)T1_64, A64, T2_64, oz);
+      cta_contract_f64(p3, (const double*)T2_64, R64, r, oz);
+      for (int64_t e = tid; e < N; e += nt) {
+        const double re = f[e] - r[e];
+        r[e] = re;
+        rs += re * re;
+      }
+    } else {
+      cta_contract_body(p1, L64, (const double*)x, T1_64);
+      cta_contract_body(p2, (const double*)T1_64, A64, T2_64);
+      for (int64_t e = tid; e < N; e += nt) {
+        int64_t ao, bo, co;
+        contract_offsets(p3, e, ao, bo, co);
+        const double re = f[e] - contract_sum(p3, (const double*)T2_64, R64, ao, bo);
+        r[e] = re;
+        rs += re * re;
+      }
     }
     const double rho = sqrt(cta_sum(rs));
+    *cyc_res += clock64() - c0;
+    const long long c1 = clock64();
     out.rel = rho / fnorm;
     out.cycles = cyc + 1;
     if (!isfinite(out.rel)) {
@@ -264,6 +293,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       x[e] += rho * acc;
     }
     __syncthreads();
+    *cyc_inner += clock64() - c1;
   }
   return out;
 }
@@ -421,6 +451,7 @@ __device__ __forceinline__ void signal_done(int* flag) {
 struct Scratch {
   double *T1, *T2, *U, *f, *r, *w, *V, *rbuf, *qwork, *tmp0, *tmp1;
   float *Vf, *wf, *T1f, *T2f, *Lf, *Rf, *Af;
+  OzScratch oz;
 };
 
 __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
@@ -452,6 +483,14 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   s.Lf = (float*)take(4 * z.stack);
   s.Rf = (float*)take(4 * z.stack);
   s.Af = (float*)take(4 * z.opcore);
+  s.oz.as = (uint16_t*)take(2 * z.oz_a);
+  s.oz.bs = (uint16_t*)take(2 * z.oz_b);
+  s.oz.rexp = (int*)take(4 * z.oz_r);
+  s.oz.cexp = (int*)take(4 * z.oz_c);
+  s.oz.cap_a = z.oz_a;
+  s.oz.cap_b = z.oz_b;
+  s.oz.cap_r = z.oz_r;
+  s.oz.cap_c = z.oz_c;
   return s;
 }
 
@@ -487,6 +526,14 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
   int64_t nsolve = 0, nits = 0, ncyc = 0;
   int status = ST_OK;
+  long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const long long t_start = clock64();
+  long long tp = t_start;
+  auto lap = [&](int k) {
+    const long long now = clock64();
+    ph[k] += now - tp;
+    tp = now;
+  };
   // algorithmic flops of one local-operator application / stack update
   auto apply_fl = [&](double aa, double nn, double ss, double r0, double r1) {
     return 2 * aa * aa * r0 * nn * ss + 2 * aa * ss * nn * nn * r0 * r1 + 2 * aa * nn * ss * ss * r1;
@@ -513,6 +560,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     }
     cta_copy(X(0), cur, n[0] * cur_right);
   }
+  lap(0);
 
   auto right = [&](int i) {
     if (i == d - 1) {
@@ -526,12 +574,14 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
     Contraction q1, q2, q3;
     desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
-    cta_contract(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1);
-    cta_contract(q2, (const double*)S.T1, A(i + 1), S.T2);
-    cta_contract(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i));
+    const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
+    cta_contract_f64(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
+    cta_contract_f64(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
+    cta_contract_f64(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
     cta_contract(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
     cta_contract(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
+    lap(1);
   };
   auto left = [&](int i) {
     if (i == 0) {
@@ -545,12 +595,14 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
-    cta_contract(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1);
-    cta_contract(p2, (const double*)S.T1, A(i - 1), S.T2);
-    cta_contract(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i));
+    const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
+    cta_contract_f64(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
+    cta_contract_f64(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
+    cta_contract_f64(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
     cta_contract(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
     cta_contract(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
+    lap(1);
   };
   auto solve = [&](int i) {
     const int64_t aa = r[i], nn = n[i], ss = r[i + 1], N = aa * nn * ss;
@@ -560,16 +612,21 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
     const int m = (int)(N < a.m ? N : a.m);
     CtaSolveStats st;
+    lap(2);
+    long long cr = 0, ci = 0;
     if (a.prec == 1) {
       cta_to_float(S.Lf, L(i), aa * R[i] * aa);
       cta_to_float(S.Rf, Rt(i), ss * R[i + 1] * ss);
       cta_to_float(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
       st = cta_gmres_ir<float>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
-                               S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm);
+                               S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm, &S.oz, &cr, &ci);
     } else {
       st = cta_gmres_ir<double>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
-                                S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm);
+                                S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm, nullptr, &cr, &ci);
     }
+    ph[3] += cr;
+    ph[4] += ci;
+    tp = clock64();
     ++nsolve;
     nits += st.inner;
     ncyc += st.cycles;
@@ -602,6 +659,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         cta_copy(X(i + 1), S.tmp0, k * qq);
         if (tid == 0) r[i + 1] = k;
         __syncthreads();
+        lap(5);
       }
     }
     for (int i = d - 1; i >= 0; --i) {
@@ -617,6 +675,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         cta_copy(X(i - 1), S.tmp0, p * k);
         if (tid == 0) r[i] = k;
         __syncthreads();
+        lap(5);
       }
     }
   }
@@ -638,6 +697,8 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     I.report[7] = 0.0;
     for (int i = 0; i <= d; ++i) I.report[8 + i] = (double)r[i];
     I.report[9 + d] = (double)I.repeats;
+    ph[7] = clock64() - t_start;
+    for (int k = 0; k < 8; ++k) I.report[10 + d + k] = (double)ph[k];
   }
   signal_done(I.done);
 }
@@ -806,6 +867,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     I.report[7] = val_opt;
     for (int i = 0; i <= d; ++i) I.report[8 + i] = have_opt ? (double)ropt[i] : 0.0;
     I.report[9 + d] = (double)(it - 1);
+    for (int k = 0; k < 8; ++k) I.report[10 + d + k] = 0.0;
   }
   signal_done(I.done);
 }
@@ -825,6 +887,66 @@ __global__ void __launch_bounds__(kBatchThreads, 4) batch_sle_kernel(BatchArgs a
     else
       batch_solve(a, j, S, sm);
   }
+}
+
+void oz_need_site(BatchSizes& z, int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
+  Contraction cs[7];
+  desc_apply(a, n, s, R0, R1, &cs[0], &cs[1], &cs[2]);
+  cs[3] = desc_left_p3(a, n, s, R1);
+  desc_right(a, n, s, R0, R1, &cs[4], &cs[5], &cs[6]);
+  for (const Contraction& c : cs) {
+    GemmAxes rows, cols;
+    if (!gemm_split(c, rows, cols)) continue;
+    const int64_t Kp = (c.ktotal + 15) / 16 * 16;
+    z.oz_a = std::max<int64_t>(z.oz_a, (int64_t)kOzSlices * rows.total * Kp);
+    z.oz_b = std::max<int64_t>(z.oz_b, (int64_t)kOzSlices * cols.total * Kp);
+    z.oz_r = std::max<int64_t>(z.oz_r, rows.total);
+    z.oz_c = std::max<int64_t>(z.oz_c, cols.total);
+  }
+}
+
+// Diagnostic: one CTA applies the local operator with emulated FP64 (Ozaki) products.
+__global__ void __launch_bounds__(kBatchThreads) apply_f64emu_kernel(Contraction p1, Contraction p2, Contraction p3,
+                                                                     const double* L, const double* A,
+                                                                     const double* R, const double* y, double* T1,
+                                                                     double* T2, double* out, OzScratch oz) {
+  cta_contract_f64(p1, L, y, T1, &oz);
+  cta_contract_f64(p2, T1, A, T2, &oz);
+  cta_contract_f64(p3, T2, R, out, &oz);
+}
+
+size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
+  BatchSizes z{};
+  oz_need_site(z, a, n, s, R0, R1);
+  return (size_t)(2 * z.oz_a + 2 * z.oz_b + 4 * z.oz_r + 4 * z.oz_c + 4 * 256);
+}
+
+cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const double* L,
+                                const double* A, const double* R, const double* y, double* T1, double* T2,
+                                double* out, char* ozmem, size_t ozbytes, cudaStream_t st) {
+  BatchSizes z{};
+  oz_need_site(z, a, n, s, R0, R1);
+  auto rnd = [](int64_t b) { return (b + 255) / 256 * 256; };
+  OzScratch oz;
+  char* p = ozmem;
+  oz.as = (uint16_t*)p;
+  p += rnd(2 * z.oz_a);
+  oz.bs = (uint16_t*)p;
+  p += rnd(2 * z.oz_b);
+  oz.rexp = (int*)p;
+  p += rnd(4 * z.oz_r);
+  oz.cexp = (int*)p;
+  p += rnd(4 * z.oz_c);
+  if ((size_t)(p - ozmem) > ozbytes) return cudaErrorInvalidValue;
+  oz.cap_a = z.oz_a;
+  oz.cap_b = z.oz_b;
+  oz.cap_r = z.oz_r;
+  oz.cap_c = z.oz_c;
+  Contraction p1, p2, p3;
+  desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
+  apply_f64emu_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
+  ++launch_counter();
+  return cudaGetLastError();
 }
 
 // Diagnostic: one CTA applies the FP32 local operator (tensor-core path).
@@ -854,7 +976,7 @@ int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
   auto r = [](int64_t b) { return (b + 255) / 256 * 256; };
   return r(8 * z.T) * 2 + r(8 * z.U) + r(8 * z.N) * 3 + r(8 * (int64_t)(m + 1) * z.N) + r(8 * z.R) + r(8 * z.Q) +
          r(8 * z.core) * 2 + r(4 * (int64_t)(m + 1) * z.N) + r(4 * z.N) + r(4 * z.T) * 2 + r(4 * z.stack) * 2 +
-         r(4 * z.opcore);
+         r(4 * z.opcore) + r(2 * z.oz_a) + r(2 * z.oz_b) + r(4 * z.oz_r) + r(4 * z.oz_c);
 }
 
 int batch_blocks_per_sm(int m, int m_evp) {

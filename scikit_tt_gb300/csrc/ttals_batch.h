@@ -27,7 +27,12 @@ struct BatchInst {
 // Largest per-CTA scratch needs over the batch (elements).
 struct BatchSizes {
   int64_t T, U, N, R, Q, core, stack, opcore;
+  int64_t oz_a, oz_b, oz_r, oz_c;  // emulated-FP64 GEMM scratch: slice arrays and exponent vectors
 };
+
+// Adds the emulated-FP64 (Ozaki) scratch needs of one site's contractions
+// (apply, left and right stack updates) to z.
+void oz_need_site(BatchSizes& z, int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1);
 
 struct BatchArgs {
   const BatchInst* inst;
@@ -48,6 +53,10 @@ size_t batch_smem_bytes(int m, int m_evp);
 int batch_blocks_per_sm(int m, int m_evp);
 int64_t batch_scratch_stride(const BatchSizes& z, int m, int m_evp);
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st);
+cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const double* L,
+                                const double* A, const double* R, const double* y, double* T1, double* T2,
+                                double* out, char* ozmem, size_t ozbytes, cudaStream_t st);
+size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1);
 cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
                              const float* R, const float* y, float* T1, float* T2, float* out, cudaStream_t st);
 

@@ -46,7 +46,7 @@ struct GemmAxes {
   int total;
 };
 
-__device__ __forceinline__ void gemm_axes_offsets(const GemmAxes& g, int idx, int& op, int& co) {
+__host__ __device__ __forceinline__ void gemm_axes_offsets(const GemmAxes& g, int idx, int& op, int& co) {
   uint32_t rem = (uint32_t)idx;
   int o = 0, c = 0;
 #pragma unroll
@@ -65,7 +65,7 @@ __device__ __forceinline__ void gemm_axes_offsets(const GemmAxes& g, int idx, in
 
 // Splits `c` into row (A) and column (B) axes; false if some output axis is
 // indexed by both operands or the contraction is too long for the tables.
-__device__ __forceinline__ bool gemm_split(const Contraction& c, GemmAxes& rows, GemmAxes& cols) {
+__host__ __device__ __forceinline__ bool gemm_split(const Contraction& c, GemmAxes& rows, GemmAxes& cols) {
   rows.n = cols.n = 0;
   rows.total = cols.total = 1;
   if (c.ktotal > kTcMaxK || c.ktotal < 1) return false;
