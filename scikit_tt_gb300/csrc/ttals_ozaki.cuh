@@ -16,8 +16,11 @@
 //   C[i,j] = 2^{E_i+F_j} sum_{L=0}^{S-1} 2^{-8(L+2)} sum_{p+q=L} (a_p b_q)[i,j]
 //
 // is evaluated with warp-level mma.sync m16n8k16 BF16 products (FP32
-// accumulate), one FP32 accumulator per level L, flushed to FP64 every 64
-// contraction steps.  Products with p + q >= S are dropped.  The result is
+// accumulate), one FP32 accumulator per level L, flushed every 64 contraction
+// steps into a double-float (hi, lo) FP32 pair with error-free TwoSum.  FP64
+// arithmetic is rationed on this part, so the only FP64 operation per output is
+// the final hi + lo; slicing, exponents and scaling are integer bit work.
+// Products with p + q >= S are dropped.  The result is
 // accurate to ~2^-47 relative to |A||B| (truncation of the 48-bit slicing),
 // which keeps the refinement residual and the stacks of the mixed path far
 // below its 1e-10 local tolerance; the plain FP64 path never uses this.
@@ -43,17 +46,16 @@ __device__ __forceinline__ void mma_bf16_16x8x16(float (&d)[4], const uint32_t (
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// exponent E with |v| < 2^E for every v of magnitude <= amax (amax finite, >= 0)
-__device__ __forceinline__ int oz_exponent(double amax) {
-  if (!(amax > 0.0)) return 0;
-  int e;
-  frexp(amax, &e);  // amax = f * 2^e, f in [0.5, 1)  ->  amax < 2^e
-  return e;
+// exponent E with |v| < 2^E for every v whose magnitude bits are <= abits
+// (abits = FP64 bits with the sign cleared; integer order = magnitude order)
+__device__ __forceinline__ int oz_exponent_bits(uint64_t abits) {
+  if (abits == 0) return 0;
+  const int ev = (int)(abits >> 52);
+  return ev == 0 ? -1022 : ev - 1022;  // |v| = 1.f * 2^(ev-1023) < 2^(ev-1022)
 }
 
 // 48-bit fixed-point magnitude of v relative to 2^E (truncated), sign apart
-__device__ __forceinline__ uint64_t oz_fixed48(double v, int E) {
-  const uint64_t bits = (uint64_t)__double_as_longlong(v);
+__device__ __forceinline__ uint64_t oz_fixed48(uint64_t bits, int E) {
   const int ev = (int)((bits >> 52) & 0x7ff);
   if (ev == 0) return 0;  // zero or subnormal: below the slicing's resolution
   const uint64_t m = (bits & 0xfffffffffffffull) | (1ull << 52);
@@ -64,17 +66,44 @@ __device__ __forceinline__ uint64_t oz_fixed48(double v, int E) {
   return m >> (-sh);
 }
 
-// Packs slice p of two values into a bf16x2 word (low half = first value).
-__device__ __forceinline__ uint32_t oz_pack(int64_t lo, int64_t hi) {
-  const __nv_bfloat16 a = __float2bfloat16_rn((float)lo);
-  const __nv_bfloat16 b = __float2bfloat16_rn((float)hi);
-  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+// BF16 bits of the signed integer slice p (0 = most significant) of a 48-bit
+// magnitude.  |slice| <= 255 has at most 8 significant bits, so it is exact in
+// BF16: the FP32 value is formed with the 2^23 magic-number trick and its upper
+// half taken (no rounding happens).
+__device__ __forceinline__ uint32_t oz_slice_bf16(uint64_t mag, uint32_t sign, int p) {
+  const uint32_t s = (uint32_t)(mag >> (8 * (kOzSlices - 1 - p))) & 0xffu;
+  const float f = __uint_as_float(0x4B000000u | s) - 8388608.0f;
+  return (__float_as_uint(f) >> 16) | sign;
 }
 
-// Signed slice p (0 = most significant) of a 48-bit magnitude.
-__device__ __forceinline__ int oz_slice(uint64_t mag, int neg, int p) {
-  const int s = (int)((mag >> (8 * (kOzSlices - 1 - p))) & 0xff);
-  return neg ? -s : s;
+// FP32 -> FP64 by bit manipulation for zero and normal values (the only ones
+// the level sums produce: multiples of 2^-56 below 2^40).
+__device__ __forceinline__ double oz_f2d(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0) return 0.0;
+  const uint64_t r = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                     ((uint64_t)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)r);
+}
+
+// v * 2^sh: exponent-field add while the result stays normal, ldexp otherwise.
+__device__ __forceinline__ double oz_scale(double v, int sh) {
+  const uint64_t b = (uint64_t)__double_as_longlong(v);
+  const int ev = (int)((b >> 52) & 0x7ff);
+  if (ev == 0) return v;
+  const int en = ev + sh;
+  if (en >= 1 && en <= 2046) return __longlong_as_double((long long)(b + ((uint64_t)(int64_t)sh << 52)));
+  return ldexp(v, sh);
+}
+
+// Error-free FP32 accumulation: (hi, lo) += x with hi + lo exact up to lo's rounding.
+__device__ __forceinline__ void oz_two_sum(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
 }
 
 struct OzScratch {
@@ -119,59 +148,64 @@ __device__ __forceinline__ bool cta_gemm_ozaki(const Contraction& c, const doubl
     const bool isrow = i < M;
     int op, dummy;
     gemm_axes_offsets(isrow ? rows : cols, isrow ? i : i - M, op, dummy);
-    double amax = 0.0;
-    bool bad = false;
+    unsigned long long amax = 0;
     for (int kk = lane; kk < K; kk += 32) {
       const double v = isrow ? A[op + koffA[kk]] : B[op + koffB[kk]];
-      if (!isfinite(v)) bad = true;
-      amax = fmax(amax, fabs(v));
+      const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+      amax = ab > amax ? ab : amax;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    if (__any_sync(0xffffffffu, bad) && lane == 0) s_bad = 1;
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(0xffffffffu, amax, o);
+      amax = other > amax ? other : amax;
+    }
+    // NaN / Inf have the all-ones exponent: larger than every finite magnitude
+    if (lane == 0 && amax >= 0x7ff0000000000000ull) s_bad = 1;
     if (lane == 0) {
       if (isrow)
-        z.rexp[i] = oz_exponent(amax);
+        z.rexp[i] = oz_exponent_bits(amax);
       else
-        z.cexp[i - M] = oz_exponent(amax);
+        z.cexp[i - M] = oz_exponent_bits(amax);
     }
   }
   __syncthreads();
   if (s_bad) return false;
   // slice A (row-major, k contiguous) and B (column-major, k contiguous), zero-padded to Kp
-  for (int64_t e = threadIdx.x; e < (int64_t)M * Kp; e += blockDim.x) {
-    const int i = (int)(e / Kp), kk = (int)(e - (int64_t)i * Kp);
-    int op, dummy;
-    gemm_axes_offsets(rows, i, op, dummy);
-    const double v = kk < K ? A[op + koffA[kk]] : 0.0;
-    const uint64_t mag = oz_fixed48(v, z.rexp[i]);
-    const int neg = v < 0.0;
+  const int Kw = Kp >> 1;  // 32-bit words (bf16 pairs) per slice row
+  uint32_t* as32w = reinterpret_cast<uint32_t*>(z.as);
+  uint32_t* bs32w = reinterpret_cast<uint32_t*>(z.bs);
+  for (int side = 0; side < 2; ++side) {
+    const GemmAxes& ax = side == 0 ? rows : cols;
+    const double* src = side == 0 ? A : B;
+    const int* koff = side == 0 ? koffA : koffB;
+    const int* ex = side == 0 ? z.rexp : z.cexp;
+    uint32_t* dst = side == 0 ? as32w : bs32w;
+    const int MN = side == 0 ? M : N;
+    for (int64_t e = threadIdx.x; e < (int64_t)MN * Kw; e += blockDim.x) {
+      const int i = (int)(e / Kw), kk = 2 * (int)(e - (int64_t)i * Kw);
+      int op, dummy;
+      gemm_axes_offsets(ax, i, op, dummy);
+      const uint64_t b0 = kk < K ? (uint64_t)__double_as_longlong(src[op + koff[kk]]) : 0ull;
+      const uint64_t b1 = kk + 1 < K ? (uint64_t)__double_as_longlong(src[op + koff[kk + 1]]) : 0ull;
+      const int E = ex[i];
+      const uint64_t m0 = oz_fixed48(b0, E), m1 = oz_fixed48(b1, E);
+      const uint32_t s0 = (uint32_t)(b0 >> 48) & 0x8000u, s1 = (uint32_t)(b1 >> 48) & 0x8000u;
 #pragma unroll
-    for (int p = 0; p < kOzSlices; ++p)
-      z.as[(int64_t)p * M * Kp + e] = __bfloat16_as_ushort(__float2bfloat16_rn((float)oz_slice(mag, neg, p)));
-  }
-  for (int64_t e = threadIdx.x; e < (int64_t)N * Kp; e += blockDim.x) {
-    const int j = (int)(e / Kp), kk = (int)(e - (int64_t)j * Kp);
-    int op, dummy;
-    gemm_axes_offsets(cols, j, op, dummy);
-    const double v = kk < K ? B[op + koffB[kk]] : 0.0;
-    const uint64_t mag = oz_fixed48(v, z.cexp[j]);
-    const int neg = v < 0.0;
-#pragma unroll
-    for (int p = 0; p < kOzSlices; ++p)
-      z.bs[(int64_t)p * N * Kp + e] = __bfloat16_as_ushort(__float2bfloat16_rn((float)oz_slice(mag, neg, p)));
+      for (int p = 0; p < kOzSlices; ++p)
+        dst[(int64_t)p * MN * Kw + e] = oz_slice_bf16(m0, s0, p) | (oz_slice_bf16(m1, s1, p) << 16);
+    }
   }
   __syncthreads();
   const int g = lane >> 2, t = lane & 3;
   const int tilesM = (M + 15) >> 4, tilesN = (N + 7) >> 3;
-  const uint32_t* as32 = reinterpret_cast<const uint32_t*>(z.as);
-  const uint32_t* bs32 = reinterpret_cast<const uint32_t*>(z.bs);
-  const int Kw = Kp >> 1;  // 32-bit words per slice row
+  const uint32_t* as32 = as32w;
+  const uint32_t* bs32 = bs32w;
   for (int tile = warp; tile < tilesM * tilesN; tile += nw) {
     const int tm = tile / tilesN, tn = tile - tm * tilesN;
     const int r0 = tm * 16 + g, r1 = r0 + 8, cb = tn * 8 + g;
     const int rr0 = r0 < M ? r0 : M - 1, rr1 = r1 < M ? r1 : M - 1, ccb = cb < N ? cb : N - 1;
-    double out[4] = {0.0, 0.0, 0.0, 0.0};
+    // running double-float sum of all levels and chunks (FP32 only)
+    float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
     for (int k0 = 0; k0 < Kp; k0 += kOzChunk) {
       float acc[kOzSlices][4];
 #pragma unroll
@@ -196,23 +230,27 @@ __device__ __forceinline__ bool cta_gemm_ozaki(const Contraction& c, const doubl
 #pragma unroll
           for (int q = 0; q < kOzSlices - p; ++q) mma_bf16_16x8x16(acc[p + q], af[p], bf[q]);
       }
+      // level sums are integers below 2^25; scaling by 2^-8(L+2) is exact in FP32
 #pragma unroll
       for (int L = 0; L < kOzSlices; ++L) {
-        const double sc = ldexp(1.0, -8 * (L + 2));
+        const float sc = __uint_as_float((uint32_t)(127 - 8 * (L + 2)) << 23);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) out[u] += (double)acc[L][u] * sc;
+        for (int u = 0; u < 4; ++u) oz_two_sum(hi[u], lo[u], __fmul_rn(acc[L][u], sc));
       }
     }
+    double out[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) out[u] = oz_f2d(hi[u]) + oz_f2d(lo[u]);
     const int cc0 = tn * 8 + 2 * t, cc1 = cc0 + 1;
     int ccol0 = 0, ccol1 = 0, cr0 = 0, cr1 = 0, dummy;
     if (r0 < M) gemm_axes_offsets(rows, r0, dummy, cr0);
     if (r1 < M) gemm_axes_offsets(rows, r1, dummy, cr1);
     if (cc0 < N) gemm_axes_offsets(cols, cc0, dummy, ccol0);
     if (cc1 < N) gemm_axes_offsets(cols, cc1, dummy, ccol1);
-    if (r0 < M && cc0 < N) C[cr0 + ccol0] = ldexp(out[0], z.rexp[r0] + z.cexp[cc0]);
-    if (r0 < M && cc1 < N) C[cr0 + ccol1] = ldexp(out[1], z.rexp[r0] + z.cexp[cc1]);
-    if (r1 < M && cc0 < N) C[cr1 + ccol0] = ldexp(out[2], z.rexp[r1] + z.cexp[cc0]);
-    if (r1 < M && cc1 < N) C[cr1 + ccol1] = ldexp(out[3], z.rexp[r1] + z.cexp[cc1]);
+    if (r0 < M && cc0 < N) C[cr0 + ccol0] = oz_scale(out[0], z.rexp[r0] + z.cexp[cc0]);
+    if (r0 < M && cc1 < N) C[cr0 + ccol1] = oz_scale(out[1], z.rexp[r0] + z.cexp[cc1]);
+    if (r1 < M && cc0 < N) C[cr1 + ccol0] = oz_scale(out[2], z.rexp[r1] + z.cexp[cc0]);
+    if (r1 < M && cc1 < N) C[cr1 + ccol1] = oz_scale(out[3], z.rexp[r1] + z.cexp[cc1]);
   }
   __syncthreads();
   return true;
