@@ -258,6 +258,8 @@ void check_status(Engine& E) {
   if (st == ST_TIMEOUT) throw Fail{TTALS_ERR_TIMEOUT, "device-side barrier wait timed out in a local solve"};
   if (st == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in a local solve"};
   if (st == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system (Krylov breakdown)"};
+  if (st == ST_UNSUPPORTED)
+    throw Fail{TTALS_ERR_UNSUPPORTED, "a wanted local eigenvalue is complex; the device path holds real cores only"};
   if (st != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(st)};
 }
 
@@ -951,7 +953,7 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
   validate_vec(x0, op, "initial_guess");
   require(solver == TTALS_EVP_EIG || solver == TTALS_EVP_EIGS || solver == TTALS_EVP_EIGH, TTALS_ERR_ARG,
           "solver must be 'eig', 'eigs' or 'eigh'");
-  require(k == 1, TTALS_ERR_UNSUPPORTED, "number_ev > 1 is not implemented on the device path");
+  require(k >= 1 && k <= 8, TTALS_ERR_UNSUPPORTED, "number_ev must be between 1 and 8 on the device path");
   require(nprev >= 0 && nprev <= 8, TTALS_ERR_UNSUPPORTED, "at most 8 previous eigentensors are supported");
   require(prec == TTALS_PREC_FP64, TTALS_ERR_UNSUPPORTED, "the eigenvalue path runs in FP64 only");
   require(out != nullptr && out_vals != nullptr, TTALS_ERR_ARG, "output buffer is null");
@@ -960,6 +962,30 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
   for (int p = 0; p < nprev; ++p) {
     prev.push_back(view(prev_t + p, "previous"));
     validate_vec(prev.back(), op, "previous");
+  }
+
+  // 'eig' / 'eigs' on an operator whose cores are not all symmetric run Arnoldi;
+  // 'eigh' assumes a symmetric operator, as the dense reference solver does
+  bool nonsym = false;
+  if (solver != TTALS_EVP_EIGH) {
+    std::vector<double> hop((size_t)op.total);
+    CK(cudaMemcpy(hop.data(), op.data, sizeof(double) * op.total,
+                  op.dev ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    for (int i = 0; i < op.d && !nonsym; ++i) {
+      const int64_t R0 = op.r[i], n = op.m[i], R1 = op.r[i + 1];
+      const double* a = hop.data() + op.off[i];
+      double amax = 0.0;
+      for (int64_t e = 0; e < R0 * n * n * R1; ++e) amax = std::max(amax, std::fabs(a[e]));
+      for (int64_t r0 = 0; r0 < R0 && !nonsym; ++r0)
+        for (int64_t u = 0; u < n && !nonsym; ++u)
+          for (int64_t v = 0; v < n && !nonsym; ++v)
+            for (int64_t r1 = 0; r1 < R1; ++r1)
+              if (std::fabs(a[((r0 * n + u) * n + v) * R1 + r1] - a[((r0 * n + v) * n + u) * R1 + r1]) >
+                  1e-14 * std::max(1.0, amax)) {
+                nonsym = true;
+                break;
+              }
+    }
   }
 
   launch_counter() = 0;
@@ -978,6 +1004,25 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
 
   Bump B{c};
   alloc_common(E, B, op.total, 0, x0.total, 0);
+  // number_ev > 1: eigenvector block, first core with the k variants, truncation work
+  double *evec = nullptr, *core0k = nullptr, *trwork = nullptr;
+  if (k > 1) {
+    int64_t tw = 1;
+    for (int i = 0; i < d; ++i) {
+      const int64_t a = P.cap[i], n = P.n[i], s = P.cap[i + 1];
+      if (i < d - 1) {
+        require(std::min(a * n, s * k) <= 1024, TTALS_ERR_UNSUPPORTED, "number_ev > 1: local block too large");
+        tw = std::max<int64_t>(tw, (int64_t)trunc_work_doubles(a * n, s * k, std::min(s, a * n)));
+      }
+      if (i > 0) {
+        require(std::min(k * a, n * s) <= 1024, TTALS_ERR_UNSUPPORTED, "number_ev > 1: local block too large");
+        tw = std::max<int64_t>(tw, (int64_t)trunc_work_doubles(k * a, n * s, std::min(a, n * s)));
+      }
+    }
+    B.want(&evec, E.maxN * k);
+    B.want(&core0k, P.cap[0] * P.n[0] * P.cap[1] * k);
+    B.want(&trwork, tw);
+  }
   // previous-vector stacks and projected vectors
   std::vector<double*> pdat(nprev), pt(nprev);
   std::vector<std::vector<double*>> PL(nprev, std::vector<double*>(d)), PR(nprev, std::vector<double*>(d));
@@ -1030,7 +1075,7 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
       stack_left_vec(c, PL[p][i - 1], pdat[p] + prev[p].off[i - 1], E.X[i - 1], a, n, s, prev[p].r[i - 1],
                      prev[p].r[i], E.U, PL[p][i]);
   };
-  const int mode = (solver == TTALS_EVP_EIGH) ? 0 : 1;
+  const int mode = (solver == TTALS_EVP_EIGH) ? 0 : (solver == TTALS_EVP_EIG ? 1 : 3);
   auto solve = [&](int i) {
     const int64_t a = P.r[i], n = P.n[i], s = P.r[i + 1];
     LocalShape sh{a, n, s, P.R[i], P.R[i + 1]};
@@ -1048,6 +1093,11 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
     l.prevt = prevt;
     l.shift = shift;
     l.x = E.X[i];
+    if (k > 1) {
+      // start vector = current core; the k Ritz vectors come back as an N x k block
+      CK(cudaMemcpyAsync(evec, E.X[i], sizeof(double) * sh.N(), cudaMemcpyDeviceToDevice, c->stream));
+      l.x = evec;
+    }
     l.vals = E.vals;
     l.V = E.V;
     l.w = E.w;
@@ -1055,6 +1105,7 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
     l.m = (int)std::min<int64_t>(E.m, sh.N());
     l.k = k;
     l.mode = mode;
+    l.nonsym = nonsym ? 1 : 0;
     l.sigma = sigma;
     l.max_restarts = 40;
     l.tol = tol;
@@ -1073,7 +1124,55 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
   double val_opt = INFINITY;
   std::vector<int64_t> r_opt;
   double lam = 0.0;
+  // number_ev > 1: keep the r leading singular directions of the eigenvector block
+  // (evp.py:455-486); the neighbouring core is only the next start vector
+  auto trunc_forward = [&](int i) {
+    const int64_t a = P.r[i], n = P.n[i], s = P.r[i + 1], r = std::min(s, a * n);
+    CK(launch_trunc_basis(evec, a * n, s * k, 0, (int)r, 0, trwork, E.X[i], E.status, c->stream));
+    P.r[i + 1] = r;  // the next core keeps its leading r rows as start vector
+  };
+  auto trunc_backward = [&](int i) {
+    const int64_t a = P.r[i], n = P.n[i], s = P.r[i + 1], r = std::min(a, n * s);
+    CK(launch_trunc_basis(evec, k * a, n * s, k, (int)r, 1, trwork, E.X[i], E.status, c->stream));
+    if (r < a) {
+      // previous core (p, n', a) -> its leading r columns
+      const int64_t rows = P.r[i - 1] * P.n[i - 1];
+      CK(cudaMemcpy2DAsync(E.tmp, sizeof(double) * r, E.X[i - 1], sizeof(double) * a, sizeof(double) * r, rows,
+                           cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemcpyAsync(E.X[i - 1], E.tmp, sizeof(double) * rows * r, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    P.r[i] = r;
+  };
+  std::vector<double> lams(k, 0.0);
   while (it <= repeats && !conv) {
+    if (k > 1) {
+      for (int i = 0; i < d; ++i) {
+        left(i);
+        if (i < d - 1) {
+          solve(i);
+          trunc_forward(i);
+        }
+      }
+      for (int i = d - 1; i >= 0; --i) {
+        right(i);
+        solve(i);
+        if (i > 0)
+          trunc_backward(i);
+        else
+          CK(cudaMemcpyAsync(core0k, evec, sizeof(double) * P.r[0] * P.n[0] * P.r[1] * k, cudaMemcpyDeviceToDevice,
+                             c->stream));
+      }
+      ++it;
+      CK(cudaMemcpyAsync(lams.data(), E.vals, sizeof(double) * k, cudaMemcpyDeviceToHost, c->stream));
+      check_status(E);
+      double diff = 0.0;
+      const int nlast = std::min<int>(3, (int)hist.size());
+      for (int q = (int)hist.size() - nlast; q < (int)hist.size(); ++q)
+        for (int e = 0; e < k; ++e) diff = std::max(diff, std::fabs(hist[q][e] - lams[e]));
+      if (diff < conv_eps) conv = true;
+      hist.push_back(lams);
+      continue;
+    }
     for (int i = 0; i < d; ++i) {
       left(i);
       if (i < d - 1) {
@@ -1118,6 +1217,22 @@ void run_evp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int nprev,
     hist.push_back(std::vector<double>(1, lam));
   }
   CK(cudaEventRecord(c->ev1, c->stream));
+  if (k > 1) {
+    // last sweep's block (evp.py:174-177): the first core carries the k variants
+    for (int e = 0; e < k; ++e) out_vals[e] = repeats >= 1 ? lams[e] : INFINITY;
+    if (repeats >= 1) {
+      E.X[0] = core0k;
+      download_x(E, out, out_dev, out_ranks, k);
+    } else {
+      download_x(E, out, out_dev, out_ranks);
+    }
+    check_status(E);
+    if (iterations) *iterations = it - 1;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    fill_stats(E, st, ms);
+    return;
+  }
   if (!r_opt.empty()) {
     for (int i = 0; i < d; ++i) E.X[i] = Xopt[i];
     P.r = r_opt;

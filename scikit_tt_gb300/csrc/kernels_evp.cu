@@ -1,0 +1,227 @@
+// Rank-r orthonormal bases of the local eigenvector blocks (number_ev > 1).
+//
+// The reference re-gauges a block of k local eigenvectors by an SVD and keeps
+// the r leading singular vectors (scikit_tt/solvers/evp.py:455-468 forward:
+// left singular vectors of the (a n) x (s k) reshape, r = min(s, u.shape[1]);
+// evp.py:470-486 backward: right singular vectors of the (k a) x (n s)
+// reshape of the transposed block, r = min(a, v.shape[0])).  Only the spanned
+// subspace matters to the sweep (the next micro problem is a Galerkin
+// projection onto it), so this kernel computes an orthonormal basis of the
+// same r-dimensional dominant singular subspace without a full SVD:
+//
+//   * the Gram matrix of the smaller side (at most a few hundred rows) is
+//     diagonalised by the cyclic Jacobi method, parallel over disjoint
+//     rotation pairs (round-robin ordering), one CTA;
+//   * if the Gram matrix lives on the wanted side its r leading eigenvectors
+//     are the basis; otherwise they are mapped through M and re-orthonormalised
+//     by Householder QR (span(M w_1..w_r) = span(u_1..u_r)).
+#include <float.h>
+
+#include "ttals_internal.h"
+#include "ttals_qr.cuh"
+
+namespace ttals {
+
+constexpr int kTrThreads = 1024;
+constexpr int kTrMaxGram = 1024;
+
+struct TruncK {
+  const double* M;  // row-major p x q, or (transposed) the N x k eigenvector block, see tr
+  int64_t p, q;
+  int tr_k;         // > 0: M(x, y) = E[(ai * q + y) * tr_k + e], x = e * (p / tr_k) + ai
+  int r, side;      // side 0: left basis (p x r) out; 1: right basis (r x q) out
+  double* G;        // n x n
+  double* V;        // n x n
+  double* B;        // max(p, q) x r
+  double* qrwork;
+  double* out;
+  int* status;
+};
+
+__device__ __forceinline__ double tr_get(const TruncK& a, int64_t x, int64_t y) {
+  if (a.tr_k > 0) {
+    const int64_t pa = a.p / a.tr_k;
+    const int64_t e = x / pa, ai = x - e * pa;
+    return a.M[(ai * a.q + y) * a.tr_k + e];
+  }
+  return a.M[x * a.q + y];
+}
+
+__global__ void __launch_bounds__(kTrThreads) trunc_basis_kernel(TruncK a) {
+  __shared__ double s_c[kTrMaxGram / 2], s_s[kTrMaxGram / 2];
+  __shared__ int s_a[kTrMaxGram / 2], s_b[kTrMaxGram / 2];
+  __shared__ double red[64];
+  __shared__ int s_sel[kTrMaxGram];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t p = a.p, q = a.q;
+  // Gram side: gram_rows = true -> G = M M^T (p x p), else G = M^T M (q x q)
+  const bool gram_rows = p <= q;
+  const int n = (int)(gram_rows ? p : q);
+  const int64_t other = gram_rows ? q : p;
+  double* G = a.G;
+  double* V = a.V;
+  for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
+    const int i = (int)(e / n), j = (int)(e - (int64_t)i * n);
+    if (j < i) continue;
+    double acc = 0.0;
+    for (int64_t z = 0; z < other; ++z)
+      acc += gram_rows ? tr_get(a, i, z) * tr_get(a, j, z) : tr_get(a, z, i) * tr_get(a, z, j);
+    G[(int64_t)i * n + j] = acc;
+    G[(int64_t)j * n + i] = acc;
+  }
+  for (int64_t e = tid; e < (int64_t)n * n; e += nt) V[e] = (e / n == e % n) ? 1.0 : 0.0;
+  __syncthreads();
+  // cyclic Jacobi, round-robin pairs over nn (even) positions; position n is a dummy
+  const int nn = (n + 1) & ~1;
+  const int npairs = nn / 2;
+  for (int sweep = 0; sweep < 40 && n > 1; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int64_t e = tid; e < (int64_t)n * n; e += nt) {
+      const double g = G[e];
+      if (e / n == e % n) dia += g * g;
+      else off += g * g;
+    }
+    off = warp_sum(off);
+    dia = warp_sum(dia);
+    if (lane == 0) {
+      red[warp] = off;
+      red[32 + warp] = dia;
+    }
+    __syncthreads();
+    double to = 0.0, td = 0.0;
+    for (int w = 0; w < (nt >> 5); ++w) {
+      to += red[w];
+      td += red[32 + w];
+    }
+    __syncthreads();
+    if (!(to > 1e-30 * td) || !(td > 0.0)) break;
+    for (int step = 0; step < nn - 1; ++step) {
+      for (int pi = tid; pi < npairs; pi += nt) {
+        auto pos = [&](int j) { return j == 0 ? 0 : ((j - 1 + step) % (nn - 1)) + 1; };
+        int ia = pos(pi), ib = pos(nn - 1 - pi);
+        if (ia > ib) {
+          const int t = ia;
+          ia = ib;
+          ib = t;
+        }
+        double c = 1.0, s = 0.0;
+        if (ib < n) {
+          const double apq = G[(int64_t)ia * n + ib];
+          if (apq != 0.0) {
+            const double tau = (G[(int64_t)ib * n + ib] - G[(int64_t)ia * n + ia]) / (2.0 * apq);
+            const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        }
+        s_a[pi] = ia;
+        s_b[pi] = ib;
+        s_c[pi] = c;
+        s_s[pi] = s;
+      }
+      __syncthreads();
+      // rows: G <- J^T G
+      for (int64_t e = tid; e < (int64_t)npairs * n; e += nt) {
+        const int pi = (int)(e / n), j = (int)(e - (int64_t)pi * n);
+        const int ia = s_a[pi], ib = s_b[pi];
+        if (ib >= n || s_s[pi] == 0.0) continue;
+        const double c = s_c[pi], s = s_s[pi];
+        const double ga = G[(int64_t)ia * n + j], gb = G[(int64_t)ib * n + j];
+        G[(int64_t)ia * n + j] = c * ga - s * gb;
+        G[(int64_t)ib * n + j] = s * ga + c * gb;
+      }
+      __syncthreads();
+      // columns: G <- G J, V <- V J
+      for (int64_t e = tid; e < (int64_t)npairs * n; e += nt) {
+        const int pi = (int)(e / n), i = (int)(e - (int64_t)pi * n);
+        const int ia = s_a[pi], ib = s_b[pi];
+        if (ib >= n || s_s[pi] == 0.0) continue;
+        const double c = s_c[pi], s = s_s[pi];
+        const double ga = G[(int64_t)i * n + ia], gb = G[(int64_t)i * n + ib];
+        G[(int64_t)i * n + ia] = c * ga - s * gb;
+        G[(int64_t)i * n + ib] = s * ga + c * gb;
+        const double va = V[(int64_t)i * n + ia], vb = V[(int64_t)i * n + ib];
+        V[(int64_t)i * n + ia] = c * va - s * vb;
+        V[(int64_t)i * n + ib] = s * va + c * vb;
+      }
+      __syncthreads();
+    }
+  }
+  // the r largest eigenvalues, descending
+  const int r = a.r;
+  if (tid == 0) {
+    for (int i = 0; i < n; ++i) s_sel[i] = i;
+    for (int c = 0; c < r; ++c) {
+      int best = c;
+      for (int i = c + 1; i < n; ++i)
+        if (G[(int64_t)s_sel[i] * n + s_sel[i]] > G[(int64_t)s_sel[best] * n + s_sel[best]]) best = i;
+      const int t = s_sel[c];
+      s_sel[c] = s_sel[best];
+      s_sel[best] = t;
+    }
+  }
+  __syncthreads();
+  const bool direct = (a.side == 0) == gram_rows;  // eigenvectors already on the wanted side
+  if (direct) {
+    if (a.side == 0) {
+      for (int64_t e = tid; e < p * r; e += nt) {
+        const int64_t x = e / r;
+        const int c = (int)(e - x * r);
+        a.out[e] = V[x * n + s_sel[c]];
+      }
+    } else {
+      for (int64_t e = tid; e < (int64_t)r * q; e += nt) {
+        const int c = (int)(e / q);
+        const int64_t y = e - (int64_t)c * q;
+        a.out[e] = V[y * n + s_sel[c]];
+      }
+    }
+    return;
+  }
+  // map through M: B = M W (left side wanted, Gram of columns) or M^T Y (right side wanted)
+  const int64_t rows = a.side == 0 ? p : q;
+  for (int64_t e = tid; e < rows * r; e += nt) {
+    const int64_t x = e / r;
+    const int c = (int)(e - x * r);
+    const int col = s_sel[c];
+    double acc = 0.0;
+    if (a.side == 0)
+      for (int64_t y = 0; y < q; ++y) acc += tr_get(a, x, y) * V[y * n + col];
+    else
+      for (int64_t y = 0; y < p; ++y) acc += tr_get(a, y, x) * V[y * n + col];
+    a.B[e] = acc;
+  }
+  __syncthreads();
+  // Householder QR of B (rows x r); Q -> out (p x r) or out^T (r x q)
+  QrArgs qa{a.B, r, 1, a.out, a.side == 0 ? r : 1, a.side == 0 ? 1 : q, a.G, r, 1, rows, r, 0, nullptr, a.qrwork};
+  cta_householder_qr(qa);
+}
+
+size_t trunc_work_doubles(int64_t p, int64_t q, int64_t r) {
+  const int64_t n = p < q ? p : q, rows = p > q ? p : q;
+  return (size_t)(2 * n * n + rows * r + (rows * r + 2 * rows * r + r) + 64);
+}
+
+cudaError_t launch_trunc_basis(const double* M, int64_t p, int64_t q, int tr_k, int r, int side, double* work,
+                               double* out, int* status, cudaStream_t st) {
+  const int64_t n = p < q ? p : q, rows = p > q ? p : q;
+  if (n > kTrMaxGram || r < 1 || r > n) return cudaErrorInvalidValue;
+  TruncK a{};
+  a.M = M;
+  a.p = p;
+  a.q = q;
+  a.tr_k = tr_k;
+  a.r = r;
+  a.side = side;
+  a.G = work;
+  a.V = a.G + n * n;
+  a.B = a.V + n * n;
+  a.qrwork = a.B + rows * r;
+  a.out = out;
+  a.status = status;
+  trunc_basis_kernel<<<1, kTrThreads, 0, st>>>(a);
+  ++launch_counter();
+  return cudaGetLastError();
+}
+
+}  // namespace ttals

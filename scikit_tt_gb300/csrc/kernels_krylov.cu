@@ -18,6 +18,12 @@
 //   vectors by inverse iteration; selection "largest k" (eigh),
 //   "closest to sigma" (eig/eigs) or "smallest".  Deflation by previous
 //   eigentensors (evp.py:376-381) is applied matrix-free: M += shift t t^T.
+//   With nonsym set the same kernel runs Arnoldi: the full Hessenberg
+//   projection is kept, Ritz values come from the Francis QR iteration
+//   (ttals_hess.cuh) and are ranked by their complex distance to sigma, Ritz
+//   vectors by inverse iteration on H - theta I.  A wanted Ritz value with a
+//   nonzero imaginary part ends the solve with ST_UNSUPPORTED (the real-valued
+//   cores cannot hold a complex eigenvector).
 //
 // One CTA per SM, co-resident (cooperative launch).  Vector work uses a fixed
 // chunk of elements per CTA; every scalar (dot, norm, Givens rotation, Ritz
@@ -26,6 +32,7 @@
 
 #include <algorithm>
 
+#include "ttals_hess.cuh"
 #include "ttals_internal.h"
 #include "ttals_tri.cuh"
 
@@ -319,7 +326,7 @@ struct LanczosK {
   double* V;
   double* w;
   double* partials;
-  int m, k, mode;
+  int m, k, mode, nonsym;
   double sigma;
   int max_restarts;
   double tol;
@@ -330,10 +337,13 @@ struct LanczosK {
 
 constexpr int kMaxEv = 8;
 
-// smem: al m, be m, h1 (m+2), h2 (m+2), svec m*kMaxEv, tri work 6m, piv m (ints)
-size_t lanczos_smem_bytes(int m) {
-  return sizeof(double) * ((size_t)2 * m + 2 * (m + 2) + (size_t)m * kMaxEv + 6 * (size_t)m + 8) +
-         sizeof(int) * (size_t)m;
+// smem: al m, be m, h1 (m+2), h2 (m+2), svec m*kMaxEv, tri work 6m, piv m (ints);
+// Arnoldi adds H (m+1) x m, its work copy m x m, wr m, wi m
+size_t lanczos_smem_bytes(int m, int nonsym) {
+  size_t b = sizeof(double) * ((size_t)2 * m + 2 * (m + 2) + (size_t)m * kMaxEv + 6 * (size_t)m + 8) +
+             sizeof(int) * (size_t)((m + 3) & ~1);
+  if (nonsym) b += sizeof(double) * ((size_t)(m + 1) * m + (size_t)m * m + 2 * (size_t)m);
+  return b;
 }
 size_t lanczos_partials_doubles(int m, int num_sms) { return (size_t)2 * num_sms * (m + 2 + 8); }
 
@@ -347,10 +357,14 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
   double* svec = h2 + m + 2;       // m x kMaxEv, column c at svec + c*m
   double* twk = svec + m * kMaxEv; // 5m tri work + m z
   int* piv = (int*)(twk + 6 * m + 8);
+  // Arnoldi: H row-major (m+1) x m (leading dimension m), work copy, Ritz values
+  double* Hs = (double*)(piv + ((m + 3) & ~1));  // even int count keeps 8-byte alignment
+  double* Hw = Hs + (m + 1) * m;
+  double* wr = Hw + m * m;
+  double* wi = wr + m;
   __shared__ double s_theta[kMaxEv];
   __shared__ double s_res;
-  __shared__ int s_sel[kMaxEv];
-  __shared__ int s_conv, s_nt;
+  __shared__ int s_conv, s_cplx;
 
   const GridBarrier bar{k.bar, k.bar + 1};
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -363,19 +377,42 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
   auto prow = [&](int buf) { return k.partials + ((int64_t)buf * gridDim.x + blockIdx.x) * ps; };
   auto pbuf = [&](int buf) { return k.partials + (int64_t)buf * gridDim.x * ps; };
   const int kev = k.k;
+  if (tid == 0) {
+    s_cplx = 0;
+    s_conv = 0;
+    s_res = 0.0;
+  }
 
-  // V_0 = x / |x|
+  // V_0 = x / |x| + 0.01 z / |z| (normalised), z a fixed pseudo-random vector: a
+  // start vector inside one symmetry sector of the local operator would keep
+  // the whole Krylov space there and miss the wanted eigenvalues of the others
   {
-    double s = 0.0;
-    for (int e = e0 + tid; e < e1; e += nt) s += k.x[e] * k.x[e];
-    block_partial(s, prow(rb));
+    auto noise = [](int e) {
+      uint32_t hsh = (uint32_t)e * 2654435761u ^ 0x9e3779b9u;
+      hsh ^= hsh >> 15;
+      hsh *= 2246822519u;
+      hsh ^= hsh >> 13;
+      return (double)(hsh & 0xffffff) / 8388608.0 - 1.0;
+    };
+    double sxx = 0.0, szz = 0.0, sxz = 0.0;
+    for (int e = e0 + tid; e < e1; e += nt) {
+      const double z = noise(e);
+      sxx += k.x[e] * k.x[e];
+      szz += z * z;
+      sxz += k.x[e] * z;
+    }
+    block_partial(sxx, prow(rb));
+    block_partial(szz, prow(rb) + 1);
+    block_partial(sxz, prow(rb) + 2);
     if (!grid_sync(bar, k.status)) return;
-    reduce_partials(pbuf(rb), ps, 1, h1);
+    reduce_partials(pbuf(rb), ps, 3, h1);
     rb ^= 1;
-    const double nrm = sqrt(h1[0]);
-    const bool ok = nrm > 0.0 && isfinite(nrm);
-    for (int e = e0 + tid; e < e1; e += nt)
-      k.V[e] = ok ? k.x[e] / nrm : 1.0 / sqrt((double)N);
+    const double nx = sqrt(h1[0]), nz = sqrt(h1[1]);
+    const bool ok = nx > 0.0 && isfinite(nx);
+    const double eps = 0.01;
+    const double ax = ok ? 1.0 / nx : 0.0, az = eps / nz;
+    const double nv = sqrt(fmax((ok ? 1.0 : 0.0) + eps * eps + 2.0 * ax * az * h1[2], 1e-300));
+    for (int e = e0 + tid; e < e1; e += nt) k.V[e] = (ax * k.x[e] + az * noise(e)) / nv;
     if (!grid_sync(bar, k.status)) return;
   }
 
@@ -424,11 +461,26 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
       double b2 = h2[j + 1];
       for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
       const double bj = sqrt(fmax(b2, 0.0));
+      const double alj = h1[j] + h2[j];
+      double tnorm = 0.0;
+      for (int i = 0; i <= j; ++i)
+        tnorm = fmax(tnorm, fabs(i == j ? alj : al[i]) + fabs(i == j ? bj : be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      // Breakdown: the basis spans an invariant subspace.  Unless the basis is
+      // full, continue from a fresh direction orthogonal to it (zero coupling in
+      // T / H), so that eigenvalues outside the subspace -- other symmetry
+      // sectors, further copies of a multiple eigenvalue -- stay reachable.
+      const bool breakdown = !(bj > 1e-14 * fmax(tnorm, 1e-300));
+      const bool fresh = breakdown && j + 1 < mm;
+      __syncthreads();
       if (tid == 0) {
-        al[j] = h1[j] + h2[j];
-        be[j] = bj;
+        al[j] = alj;
+        be[j] = fresh ? 0.0 : bj;
+        if (k.nonsym) {
+          for (int q = 0; q <= j; ++q) Hs[q * m + j] = h1[q] + h2[q];
+          Hs[(j + 1) * m + j] = fresh ? 0.0 : bj;
+        }
       }
-      if (bj > 0.0 && j + 1 < mm) {
+      if (!breakdown && j + 1 < mm) {
         double* vn = k.V + (int64_t)(j + 1) * N;
         const double inv = 1.0 / bj;
         for (int e = e0 + tid; e < e1; e += nt) {
@@ -438,15 +490,105 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
         }
       }
       __syncthreads();
+      if (fresh) {
+        // deterministic pseudo-random direction, two classical Gram-Schmidt passes
+        for (int e = e0 + tid; e < e1; e += nt) {
+          uint32_t hsh = (uint32_t)e * 2654435761u ^ (uint32_t)(j + 1) * 40503u ^ (uint32_t)restarts * 97u;
+          hsh ^= hsh >> 15;
+          hsh *= 2246822519u;
+          hsh ^= hsh >> 13;
+          k.w[e] = (double)(hsh & 0xffffff) / 8388608.0 - 1.0;
+        }
+        __syncthreads();
+        double nb2 = 0.0;
+        for (int pass = 0; pass < 2; ++pass) {
+          chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+          if (!grid_sync(bar, k.status)) return;
+          reduce_partials(pbuf(rb), ps, j + 2, h2);
+          rb ^= 1;
+          nb2 = h2[j + 1];
+          for (int q = 0; q <= j; ++q) nb2 -= h2[q] * h2[q];
+          for (int e = e0 + tid; e < e1; e += nt) {
+            double acc = k.w[e];
+            for (int q = 0; q <= j; ++q) acc -= h2[q] * k.V[(int64_t)q * N + e];
+            k.w[e] = acc;
+          }
+          __syncthreads();
+        }
+        const double nb = sqrt(fmax(nb2, 0.0));
+        double* vn = k.V + (int64_t)(j + 1) * N;
+        for (int e = e0 + tid; e < e1; e += nt) vn[e] = nb > 0.0 ? k.w[e] / nb : 0.0;
+        __syncthreads();
+      }
       ++total_it;
       nT = j + 1;
-      // Rayleigh-Ritz on T_nT every 4 steps, at the end of the basis, or on breakdown
-      double tnorm = 0.0;
-      for (int i = 0; i < nT; ++i)
-        tnorm = fmax(tnorm, fabs(al[i]) + fabs(be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
-      const bool breakdown = !(bj > 1e-14 * fmax(tnorm, 1e-300));
-      const bool check = nT >= kev && ((nT % 4) == 0 || nT == mm || breakdown);
-      if (check) {
+      const double bres = fresh ? 0.0 : bj;  // norm of the residual direction of the Ritz pairs
+      // Rayleigh-Ritz on T_nT every 4 steps or at the end of the basis
+      const bool check = !fresh && nT >= kev && ((nT % 4) == 0 || nT == mm);
+      if (check && k.nonsym) {
+        if (warp == 0) {
+          // Ritz values of the nT x nT Hessenberg projection
+          for (int i = lane; i < nT; i += 32)
+            for (int q = 0; q < nT; ++q) Hw[i * m + q] = (q >= i - 1) ? Hs[i * m + q] : 0.0;
+          double hn = 0.0;
+          for (int q = lane; q < nT; q += 32) {
+            double cs = 0.0;
+            for (int i = 0; i <= (q + 1 < nT ? q + 1 : nT - 1); ++i) cs += fabs(Hs[i * m + q]);
+            hn = fmax(hn, cs);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) hn = fmax(hn, __shfl_xor_sync(0xffffffffu, hn, o));
+          hn = fmax(hn, 1e-300);
+          __syncwarp();
+          const bool qr_ok = hess_eigvals_warp(Hw, m, nT, wr, wi);
+          double resmax = 0.0;
+          if (lane == 0) {
+            // wanted indices: closest to sigma (complex distance), ascending; mode 3 reversed
+            int sel[kMaxEv];
+            bool used[64];
+            for (int i = 0; i < nT; ++i) used[i] = false;
+            for (int c = 0; c < kev; ++c) {
+              int best = -1;
+              double bd = 0.0;
+              for (int i = 0; i < nT; ++i) {
+                if (used[i]) continue;
+                double dist;
+                if (k.mode == 0) dist = -wr[i];
+                else if (k.mode == 2) dist = wr[i];
+                else dist = hypot(wr[i] - k.sigma, wi[i]);
+                if (best < 0 || dist < bd) {
+                  best = i;
+                  bd = dist;
+                }
+              }
+              sel[c] = best < 0 ? 0 : best;
+              if (best >= 0) used[best] = true;
+            }
+            if (k.mode == 3)
+              for (int c = 0; c < kev / 2; ++c) {
+                const int t = sel[c];
+                sel[c] = sel[kev - 1 - c];
+                sel[kev - 1 - c] = t;
+              }
+            int cplx = 0;
+            for (int c = 0; c < kev; ++c) {
+              const double th = wr[sel[c]];
+              if (fabs(wi[sel[c]]) > 1e-10 * hn) cplx = 1;
+              double* z = svec + c * m;
+              hess_eigvec(Hs, m, nT, th, hn, z, Hw, piv);
+              s_theta[c] = th;
+              resmax = fmax(resmax, bres * fabs(z[nT - 1]) / hn);
+            }
+            s_cplx = cplx;
+            s_res = resmax;
+            s_conv = qr_ok && !cplx && (resmax <= k.tol);
+          }
+          __syncwarp();
+        }
+        __syncthreads();
+        last_res = s_res;
+        if (s_conv || nT == mm) break;
+      } else if (check) {
         if (warp == 0) {
           double lo = 1e300, hi = -1e300;
           for (int i = 0; i < nT; ++i) {
@@ -479,6 +621,12 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
                 if (up < nT) vup = tri_eigval(al, be, nT, up, lo, hi, pivmin);
               }
             }
+            if (k.mode == 3)
+              for (int c = 0; c < kev / 2; ++c) {
+                const int t = sel[c];
+                sel[c] = sel[kev - 1 - c];
+                sel[kev - 1 - c] = t;
+              }
           }
           double resmax = 0.0;
           for (int c = 0; c < kev; ++c) {
@@ -499,21 +647,18 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
                   for (int i = 0; i < nT; ++i) z[i] /= nr;
               }
               s_theta[c] = th;
-              s_sel[c] = sel[c];
             }
             __syncwarp();
-            resmax = fmax(resmax, bj * fabs(z[nT - 1]) / fmax(tnorm, 1e-300));
+            resmax = fmax(resmax, bres * fabs(z[nT - 1]) / fmax(tnorm, 1e-300));
           }
           if (lane == 0) {
             s_res = resmax;
-            s_conv = (resmax <= k.tol) || breakdown;
+            s_conv = resmax <= k.tol;
           }
         }
         __syncthreads();
         last_res = s_res;
         if (s_conv || nT == mm) break;
-      } else if (breakdown) {
-        break;
       }
       if (!grid_sync(bar, k.status)) return;  // V_{j+1} complete
     }
@@ -546,6 +691,7 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
     for (int e = e0 + tid; e < e1; e += nt) k.V[e] = (nrm > 0.0) ? k.w[e] / nrm : 1.0 / sqrt((double)N);
     if (!grid_sync(bar, k.status)) return;
   }
+  if (k.nonsym && s_cplx && blockIdx.x == 0 && tid == 0) atomicExch(k.status, ST_UNSUPPORTED);
   if (blockIdx.x == 0 && tid == 0) {
     for (int c = 0; c < kev; ++c) k.vals[c] = s_theta[c];
     k.report[0] = last_res;
@@ -560,10 +706,11 @@ cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st)
   if (l.k < 1 || l.k > kMaxEv) return cudaErrorInvalidValue;
   Contraction p1, p2, p3;
   local_apply_descs(l.sh, &p1, &p2, &p3);
+  if (l.nonsym && l.m > 64) return cudaErrorInvalidValue;
   LanczosK k{p1, p2, p3, (int)l.sh.N(), l.L, l.A, l.R, l.T1, l.T2, l.nprev, l.prevt, l.shift, l.x, l.vals,
-             l.V, l.w, l.partials, l.m, l.k, l.mode, l.sigma, l.max_restarts, l.tol, l.bar, l.status,
+             l.V, l.w, l.partials, l.m, l.k, l.mode, l.nonsym, l.sigma, l.max_restarts, l.tol, l.bar, l.status,
              l.report};
-  const size_t smem = lanczos_smem_bytes(l.m);
+  const size_t smem = lanczos_smem_bytes(l.m, l.nonsym);
   cudaError_t e = cudaFuncSetAttribute(lanczos_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {&k};

@@ -106,7 +106,9 @@ struct LanczosLaunch {
   double* V;               // (m+1) x N
   double* w;               // N
   double* partials;
-  int m, k, mode;          // mode 0: largest, 1: closest to sigma, 2: smallest
+  int m, k, mode;          // mode 0: largest, 1: closest to sigma, 2: smallest,
+                           // 3: closest to sigma, farthest of the k first (eigs order)
+  int nonsym;              // Arnoldi (nonsymmetric operator), m <= 64
   double sigma;
   int max_restarts;
   double tol;
@@ -116,7 +118,14 @@ struct LanczosLaunch {
 };
 cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st);
 size_t lanczos_partials_doubles(int m, int num_sms);
-size_t lanczos_smem_bytes(int m);
+size_t lanczos_smem_bytes(int m, int nonsym);
+
+// rank-r orthonormal basis of an eigenvector block (kernels_evp.cu): side 0 ->
+// left basis (p x r) of M (p x q), side 1 -> right basis (r x q); tr_k > 0 reads
+// M as the transposed-and-reshaped N x tr_k block (backward sweep)
+size_t trunc_work_doubles(int64_t p, int64_t q, int64_t r);
+cudaError_t launch_trunc_basis(const double* M, int64_t p, int64_t q, int tr_k, int r, int side, double* work,
+                               double* out, int* status, cudaStream_t st);
 
 // engine.cu helpers used by the allocation-free entry point (noalloc.cu)
 }  // namespace ttals

@@ -1,17 +1,23 @@
-"""Alternating linear scheme for (symmetric) eigenproblems in the TT format, on
-the GPU.
+"""Alternating linear scheme for eigenproblems in the TT format, on the GPU.
 
 Drop-in for ``scikit_tt/solvers/evp.py``: ``als`` keeps its signature
 (evp.py:17-27) and return convention ``(eigenvalue(s), eigentensor(s),
 iterations)``.  The sweep runs in ``libttals.so`` (``ttals_evp_als``): the
 local eigenproblem is solved matrix-free by Lanczos with full
-reorthogonalisation, and the eigenvalue is selected by the reference's rule
-for ``solver`` -- largest for ``'eigh'`` (evp.py:434-439), closest to
-``sigma`` for ``'eig'`` / ``'eigs'`` (evp.py:417-432).
+reorthogonalisation (symmetric operators) or Arnoldi with Francis-QR Ritz
+values (operators with nonsymmetric cores, ``'eig'`` / ``'eigs'``), and the
+eigenvalues are selected by the reference's rule for ``solver`` -- the
+``number_ev`` largest, descending, for ``'eigh'`` (evp.py:434-439); the
+``number_ev`` closest to ``sigma`` for ``'eig'`` (ascending distance,
+evp.py:423-432) and ``'eigs'`` (descending distance, evp.py:414-421).  With
+``number_ev > 1`` the eigenvector block is re-gauged to its ``r`` leading
+singular directions as in evp.py:455-486, and the last sweep's eigenvalues and
+eigentensors are returned (evp.py:170-177).
 
-Implemented: symmetric operators, ``number_ev == 1``, ``previous`` / ``shift``
-deflation, ``operator_gevp`` equal to the identity train.  Other cases raise
-``NotImplementedError`` (general generalised problems, ``number_ev > 1``).
+Implemented: ``number_ev`` 1..8, ``previous`` / ``shift`` deflation,
+``operator_gevp`` equal to the identity train.  Generalised problems with
+another ``operator_gevp``, ``'eigh'`` on a nonsymmetric operator and wanted
+eigenvalues with a nonzero imaginary part raise ``NotImplementedError``.
 """
 
 from __future__ import annotations
@@ -48,10 +54,10 @@ def als(operator: 'TT', initial_guess: 'TT', previous: List['TT'] = [], shift: f
     if not _is_identity(operator_gevp):
         raise NotImplementedError('generalised eigenproblems (operator_gevp other than the identity) are not '
                                   'implemented on the device path')
-    if not _is_symmetric(operator):
-        raise NotImplementedError('the device eigen path needs a symmetric operator (core-wise symmetric cores)')
-    if number_ev != 1:
-        raise NotImplementedError('number_ev > 1 is not implemented on the device path')
+    if solver == 'eigh' and not _is_symmetric(operator):
+        raise NotImplementedError("solver='eigh' needs a symmetric operator (core-wise symmetric cores)")
+    if not 1 <= number_ev <= 8:
+        raise NotImplementedError('number_ev must be between 1 and 8 on the device path')
     op, x0 = _lib.Packed(operator.cores), _lib.Packed(initial_guess.cores)
     prev = [_lib.Packed(p.cores) for p in previous]
     prev_arr = (_lib.TTDesc * max(1, len(prev)))(*[p.desc for p in prev]) if prev else None
@@ -59,22 +65,32 @@ def als(operator: 'TT', initial_guess: 'TT', previous: List['TT'] = [], shift: f
     dims = np.array(operator.row_dims, dtype=np.int64)
     ranks = np.zeros(operator.order + 1, dtype=np.int64)
     _lib.check(lib.ttals_als_ranks(operator.order, _lib.i64ptr(dims), _lib.i64ptr(x0.ranks), _lib.i64ptr(ranks)))
-    total = int(sum(max(ranks[i], x0.ranks[i]) * dims[i] * max(ranks[i + 1], x0.ranks[i + 1])
-                    for i in range(operator.order)))
+    sizes = [int(max(ranks[i], x0.ranks[i]) * dims[i] * max(ranks[i + 1], x0.ranks[i + 1]))
+             for i in range(operator.order)]
+    total = sum(sizes) + (number_ev - 1) * sizes[0]
     out = np.empty(max(total, 1), dtype=np.float64)
     out_ranks = np.zeros(operator.order + 1, dtype=np.int64)
     vals = np.zeros(max(1, number_ev), dtype=np.float64)
     its = _lib.C.c_int32(0)
     st = _lib.Stats()
-    _lib.check(lib.ttals_evp_als(_lib.context(), op.desc, x0.desc, len(prev), prev_arr, float(shift),
-                                 int(number_ev), int(repeats), float(conv_eps), _lib.EVP_SOLVERS[solver],
-                                 float(sigma), _lib.PREC_FP64, 0.0, _lib.dptr(vals), _lib.dptr(out), 0,
-                                 _lib.i64ptr(out_ranks), _lib.C.byref(its), st))
+    code = lib.ttals_evp_als(_lib.context(), op.desc, x0.desc, len(prev), prev_arr, float(shift),
+                             int(number_ev), int(repeats), float(conv_eps), _lib.EVP_SOLVERS[solver],
+                             float(sigma), _lib.PREC_FP64, 0.0, _lib.dptr(vals), _lib.dptr(out), 0,
+                             _lib.i64ptr(out_ranks), _lib.C.byref(its), st)
+    _lib.check(code)
     last_stats = st.as_dict()
     if repeats < 1:
         return np.inf, None, 0
-    cores = _lib.unpack(out, operator.row_dims, [1] * operator.order, out_ranks)
-    return np.float64(vals[0]), TT(cores), int(its.value)
+    if number_ev == 1:
+        cores = _lib.unpack(out, operator.row_dims, [1] * operator.order, out_ranks)
+        return np.float64(vals[0]), TT(cores), int(its.value)
+    # first core holds the number_ev variants as (r0, n0, 1, r1, number_ev)
+    r0, n0, r1 = int(out_ranks[0]), operator.row_dims[0], int(out_ranks[1])
+    c0 = out[:r0 * n0 * r1 * number_ev].reshape(r0, n0, 1, r1, number_ev)
+    rest = _lib.unpack(out[r0 * n0 * r1 * number_ev:], operator.row_dims[1:], [1] * (operator.order - 1),
+                       out_ranks[1:])
+    tts = [TT([c0[:, :, :, :, e].copy()] + [c.copy() for c in rest]) for e in range(number_ev)]
+    return vals[:number_ev].copy(), tts, int(its.value)
 
 
 def power_method(operator, initial_guess, operator_gevp=None, repeats=10, sigma=0.999):

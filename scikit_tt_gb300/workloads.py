@@ -116,6 +116,48 @@ def ising_evp(d=48, g=1.0, x_rank=64, repeats=6, seed=1) -> EVPInstance:
     return EVPInstance(ising_op(d, 1.0, g), x0, repeats, sigma, dict(d=d, g=g, x_rank=x_rank))
 
 
+def reversible_markov(rng, n: int) -> np.ndarray:
+    """Column-stochastic n x n transition matrix S D^-1 of a reversible chain
+    (S symmetric positive, D its column sums): similar to the symmetric
+    D^-1/2 S D^-1/2, so its spectrum is real, with the Perron root 1."""
+    s = rng.uniform(0.05, 1.0, (n, n))
+    s = s + s.T
+    return s / s.sum(axis=0, keepdims=True)
+
+
+def markov_op(d: int, n: int, eps: float, rng) -> List[np.ndarray]:
+    """Nonsymmetric rank-2 TT operator (P_1 x ... x P_d + eps Q_1 x ... x Q_d) / (1 + eps)
+    of reversible transition matrices: column-stochastic, dominant eigenvalue 1,
+    the leading eigenvalues real (a small perturbation of a real spectrum); the
+    shape of the Ulam transfer operators that evp.als is applied to."""
+    ps = [reversible_markov(rng, n) for _ in range(d)]
+    qs = [reversible_markov(rng, n) for _ in range(d)]
+    cores = []
+    for i in range(d):
+        if i == 0:
+            c = np.zeros((1, n, n, 2))
+            c[0, :, :, 0] = ps[i] / (1.0 + eps)
+            c[0, :, :, 1] = qs[i] * eps / (1.0 + eps)
+        elif i == d - 1:
+            c = np.zeros((2, n, n, 1))
+            c[0, :, :, 0] = ps[i]
+            c[1, :, :, 0] = qs[i]
+        else:
+            c = np.zeros((2, n, n, 2))
+            c[0, :, :, 0] = ps[i]
+            c[1, :, :, 1] = qs[i]
+        cores.append(c)
+    return cores
+
+
+def markov_evp(d=4, n=4, eps=0.2, x_rank=6, repeats=4, seed=3) -> EVPInstance:
+    """Leading eigenvalues of a nonsymmetric transfer operator ('eig' near sigma=1)."""
+    rng = np.random.default_rng(seed)
+    op = markov_op(d, n, eps, rng)
+    x0 = [np.abs(c) + 0.1 for c in gaussian_tt(rng, d, n, x_rank)]
+    return EVPInstance(op, x0, repeats, 1.0, dict(d=d, n=n, eps=eps, x_rank=x_rank))
+
+
 def batch_instance(j: int, repeats: int = 4) -> SLEInstance:
     rng = np.random.default_rng(1000 + j)
     d = int(rng.integers(8, 33))

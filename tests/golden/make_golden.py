@@ -107,6 +107,45 @@ def ttops_case():
     print('ttops norm', out['norm'])
 
 
+def evp_block_case(name, op, x0, repeats, solver, sigma, number_ev, conv_eps=1e-10):
+    """number_ev >= 1 on any operator: the eigenvalue list and one TT per eigenvector.
+
+    The reference keeps the complex dtype of scipy's eig vectors; the wanted
+    eigenpairs of these cases are real, so each eigentensor is stored as its
+    full real vector (global phase removed)."""
+    val, vec, its = revp.als(RTT([c.copy() for c in op]), RTT([c.copy() for c in x0]), repeats=repeats,
+                             solver=solver, sigma=sigma, number_ev=number_ev, conv_eps=conv_eps)
+    vecs = [vec] if number_ev == 1 else vec
+    vals = np.atleast_1d(np.real(np.asarray(val)))
+    out = {'repeats': np.array(repeats), 'solver': np.array(solver), 'sigma': np.array(sigma),
+           'number_ev': np.array(number_ev), 'conv_eps': np.array(conv_eps), 'vals': vals, 'its': np.array(its)}
+    pack('op', op, out)
+    pack('x0', x0, out)
+    for e, t in enumerate(vecs):
+        # cores carry arbitrary complex phases (SVD of a complex-typed block);
+        # the tensor itself is real up to one global phase: store it as a vector
+        v = np.asarray(t.full()).reshape(-1)
+        v = v * np.exp(-1j * np.angle(v[np.argmax(np.abs(v))]))
+        assert np.abs(np.imag(v)).max() < 1e-10 * np.abs(v).max(), np.abs(np.imag(v)).max()
+        out[f'vec{e}'] = np.real(v)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'vals', vals, 'its', its)
+
+
+def evp_blocks():
+    # nonsymmetric transfer operator (Arnoldi path): one and three eigenpairs near sigma = 1
+    w = wl.markov_evp()
+    x0 = [c.copy() for c in RTT([c.copy() for c in w.x0]).ortho_right().cores]
+    evp_block_case('evp_markov_eig_k1', w.op, x0, 4, 'eig', 1.0, 1)
+    evp_block_case('evp_markov_eig_k3', w.op, x0, 4, 'eig', 1.0, 3)
+    evp_block_case('evp_markov_eigs_k3', w.op, x0, 4, 'eigs', 1.0, 3)
+    # symmetric block of three (Lanczos with three Ritz pairs)
+    w3 = wl.ising_evp(d=8, x_rank=8, repeats=4)
+    x0 = [c.copy() for c in RTT([c.copy() for c in w3.x0]).ortho_right().cores]
+    evp_block_case('evp_ising_d8_eigh_k3', w3.op, x0, 4, 'eigh', 1.0, 3)
+    evp_block_case('evp_ising_d8_eig_k3', w3.op, x0, 4, 'eig', w3.sigma, 3)
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -134,7 +173,11 @@ def main():
         evp_case(f'evp_ising_d{d}_eigh', w3.op, [c.copy() for c in x0o.cores], 6, 'eigh', 1.0, negate=True)
     helpers_case()
     ttops_case()
+    evp_blocks()
 
 
 if __name__ == '__main__':
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == 'evp_blocks':
+        evp_blocks()
+    else:
+        main()

@@ -51,3 +51,72 @@ def test_evp_deflation_second_eigenvalue():
     oracle = O.evp_als(w.op, x0, previous=[t0n], shift=100.0, repeats=8, sigma=w.sigma)
     assert abs(v1 - oracle[0]) < 1e-9
     assert abs(v1 - ref_vals[1]) < 1e-8
+
+
+def _same_up_to_sign(v, r):
+    return min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r)
+
+
+@pytest.mark.parametrize('solver,k', [('eig', 1), ('eigs', 1), ('eig', 3), ('eigs', 3)])
+def test_evp_nonsymmetric_matches_oracle(solver, k):
+    # column-stochastic transfer operator with nonsymmetric cores: Arnoldi path
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.solvers import evp
+    w = wl.markov_evp()
+    x0 = O.ortho_right(w.x0)
+    ref_vals, ref_vecs, ref_its = O.evp_als(w.op, x0, number_ev=k, repeats=4, solver=solver, sigma=1.0,
+                                            conv_eps=0.0)
+    vals, vecs, its = evp.als(_tt(w.op), _tt(x0), number_ev=k, repeats=4, solver=solver, sigma=1.0, conv_eps=0.0)
+    assert its == ref_its
+    if k == 1:
+        assert abs(vals - np.real(ref_vals)) < 1e-9
+        assert _same_up_to_sign(O.full_vector(vecs.cores), np.real(O.full_vector(ref_vecs))) < 1e-6
+    else:
+        assert np.max(np.abs(np.asarray(vals) - np.real(ref_vals))) < 1e-9
+        for e in range(k):
+            assert _same_up_to_sign(O.full_vector(vecs[e].cores), np.real(O.full_vector(ref_vecs[e]))) < 1e-6
+
+
+@pytest.mark.parametrize('solver', ['eigh', 'eig'])
+def test_evp_symmetric_block_of_three(solver):
+    # number_ev = 3 on the Ising chain: Lanczos with three Ritz pairs and the
+    # rank-r re-gauging of the eigenvector block
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.solvers import evp
+    w = wl.ising_evp(d=8, x_rank=8, repeats=4)
+    x0 = O.ortho_right(w.x0)
+    sigma = w.sigma if solver == 'eig' else 1.0
+    ref_vals, ref_vecs, ref_its = O.evp_als(w.op, x0, number_ev=3, repeats=4, solver=solver, sigma=sigma,
+                                            conv_eps=0.0)
+    vals, vecs, its = evp.als(_tt(w.op), _tt(x0), number_ev=3, repeats=4, solver=solver, sigma=sigma, conv_eps=0.0)
+    assert np.max(np.abs(np.asarray(vals) - np.real(ref_vals))) < 1e-9
+    for e in range(3):
+        assert _same_up_to_sign(O.full_vector(vecs[e].cores), np.real(O.full_vector(ref_vecs[e]))) < 1e-6
+
+
+def test_evp_complex_wanted_eigenvalue_is_refused():
+    # a plane rotation has eigenvalues exp(+-i t): the pair closest to sigma = 1
+    # is complex, which real cores cannot hold
+    from scikit_tt_gb300.solvers import evp
+    t = 0.3
+    rot = np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]])
+    op = [rot.reshape(1, 2, 2, 1), np.eye(2).reshape(1, 2, 2, 1)]
+    x0 = [np.ones((1, 2, 1, 2)), np.ones((2, 2, 1, 1))]
+    with pytest.raises(NotImplementedError):
+        evp.als(_tt(op), _tt(x0), repeats=1, solver='eig', sigma=1.0)
+
+
+@pytest.mark.parametrize('name', ['evp_markov_eig_k1', 'evp_markov_eig_k3', 'evp_markov_eigs_k3',
+                                  'evp_ising_d8_eigh_k3', 'evp_ising_d8_eig_k3'])
+def test_evp_blocks_match_reference(golden, name):
+    # device Arnoldi / block path against the reference's own outputs
+    from scikit_tt_gb300.solvers import evp
+    z, cores = golden(name)
+    k = int(z['number_ev'])
+    vals, vecs, its = evp.als(_tt(cores('op')), _tt(cores('x0')), number_ev=k, repeats=int(z['repeats']),
+                              solver=str(z['solver']), sigma=float(z['sigma']), conv_eps=float(z['conv_eps']))
+    assert its == int(z['its'])
+    assert np.max(np.abs(np.atleast_1d(vals) - z['vals'])) < 1e-9
+    vecs = [vecs] if k == 1 else vecs
+    for e in range(k):
+        assert _same_up_to_sign(O.full_vector(vecs[e].cores), z[f'vec{e}']) < 1e-6

@@ -70,3 +70,28 @@ def test_oracle_tt_ops_match_reference(golden):
     np.testing.assert_allclose(O.full_vector(O.ortho_left(t)), z['left_full'], rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(O.full_vector(O.ortho_right(t)), z['right_full'], rtol=1e-12, atol=1e-12)
     assert abs(O.stable_norm(t) - float(z['norm'])) < 1e-12 * float(z['norm'])
+
+
+BLOCK_CASES = ['evp_markov_eig_k1', 'evp_markov_eig_k3', 'evp_markov_eigs_k3', 'evp_ising_d8_eigh_k3',
+               'evp_ising_d8_eig_k3']
+
+
+def _up_to_sign(v, r):
+    return min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r)
+
+
+@pytest.mark.parametrize('name', BLOCK_CASES)
+def test_oracle_evp_blocks_match_reference(golden, name):
+    # nonsymmetric operators and number_ev > 1 (evp.py:386-495 with eig / eigs / eigh)
+    z, cores = golden(name)
+    k = int(z['number_ev'])
+    vals, vecs, its = O.evp_als(cores('op'), cores('x0'), number_ev=k, repeats=int(z['repeats']),
+                                solver=str(z['solver']), sigma=float(z['sigma']), conv_eps=float(z['conv_eps']))
+    assert its == int(z['its'])
+    vals = np.atleast_1d(np.real(vals))
+    assert np.max(np.abs(vals - z['vals'])) < 1e-10
+    vecs = [vecs] if k == 1 else vecs
+    for e in range(k):
+        v = O.full_vector(vecs[e])
+        v = v * np.exp(-1j * np.angle(v[np.argmax(np.abs(v))]))
+        assert _up_to_sign(np.real(v), z[f'vec{e}']) < 1e-8
