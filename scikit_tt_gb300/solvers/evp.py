@@ -93,6 +93,29 @@ def als(operator: 'TT', initial_guess: 'TT', previous: List['TT'] = [], shift: f
     return vals[:number_ev].copy(), tts, int(its.value)
 
 
-def power_method(operator, initial_guess, operator_gevp=None, repeats=10, sigma=0.999):
-    """Inverse power iteration (evp.py:182-250) is not on the device path yet."""
-    raise NotImplementedError('evp.power_method is not implemented on the device path')
+def power_method(operator: 'TT', initial_guess: 'TT', operator_gevp: 'TT' = None, repeats: int = 10,
+                 sigma: float = 0.999):
+    """Inverse power iteration (evp.py:182-250) on the device engine.
+
+    Each step solves ``(operator - sigma * operator_gevp) x_new = operator_gevp x``
+    with the device ``sle.als`` (one sweep, the current iterate as initial
+    guess), normalises with the device ``TT.norm`` and returns the Rayleigh
+    quotient ``x^T A x (/ x^T M x)`` of the last iterate, as the reference does."""
+    from .. import tensor_train as tt
+    from . import sle
+    if operator_gevp is None:
+        operator_shift = operator - sigma * tt.eye(operator.row_dims)
+    else:
+        operator_shift = operator - sigma * operator_gevp
+    eigenvalue = 0
+    eigentensor = initial_guess
+    for _ in range(repeats):
+        if operator_gevp is None:
+            eigentensor = sle.als(operator_shift, eigentensor, eigentensor)
+        else:
+            eigentensor = sle.als(operator_shift, eigentensor, operator_gevp.dot(eigentensor))
+        eigentensor = eigentensor * (1 / eigentensor.norm())
+        eigenvalue = eigentensor.transpose().dot(operator).dot(eigentensor)
+        if operator_gevp is not None:
+            eigenvalue *= 1 / (eigentensor.transpose().dot(operator_gevp).dot(eigentensor))
+    return eigenvalue, eigentensor

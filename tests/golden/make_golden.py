@@ -146,6 +146,26 @@ def evp_blocks():
     evp_block_case('evp_ising_d8_eig_k3', w3.op, x0, 4, 'eig', w3.sigma, 3)
 
 
+def power_case(name, op, x0, gevp, repeats=10, sigma=0.999):
+    """evp.power_method (inverse power iteration through sle.als) on a nonsymmetric operator."""
+    A = RTT([c.copy() for c in op])
+    M = rtt.eye(A.row_dims) if gevp else None
+    val, vec = revp.power_method(A, RTT([c.copy() for c in x0]), operator_gevp=M, repeats=repeats, sigma=sigma)
+    out = {'repeats': np.array(repeats), 'sigma': np.array(sigma), 'gevp': np.array(gevp), 'val': np.array(val),
+           'vec0': np.asarray(vec.full()).reshape(-1)}
+    pack('op', op, out)
+    pack('x0', x0, out)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'val', val)
+
+
+def power_cases():
+    w = wl.markov_evp()
+    x0 = [c.copy() for c in RTT([c.copy() for c in w.x0]).ortho_right().cores]
+    power_case('evp_power_markov', w.op, x0, False)
+    power_case('evp_power_markov_gevp', w.op, x0, True)
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -174,10 +194,13 @@ def main():
     helpers_case()
     ttops_case()
     evp_blocks()
+    power_cases()
 
 
 if __name__ == '__main__':
     if len(sys.argv) > 1 and sys.argv[1] == 'evp_blocks':
         evp_blocks()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'power':
+        power_cases()
     else:
         main()

@@ -120,3 +120,17 @@ def test_evp_blocks_match_reference(golden, name):
     vecs = [vecs] if k == 1 else vecs
     for e in range(k):
         assert _same_up_to_sign(O.full_vector(vecs[e].cores), z[f'vec{e}']) < 1e-6
+
+
+@pytest.mark.parametrize('name', ['evp_power_markov', 'evp_power_markov_gevp'])
+def test_power_method_matches_reference(golden, name):
+    # inverse power iteration through the device sle.als, TT.norm and TT.dot
+    from scikit_tt_gb300 import tensor_train as tt
+    from scikit_tt_gb300.solvers import evp
+    z, cores = golden(name)
+    op = _tt(cores('op'))
+    gevp = tt.eye(op.row_dims) if bool(z['gevp']) else None
+    val, vec = evp.power_method(op, _tt(cores('x0')), operator_gevp=gevp, repeats=int(z['repeats']),
+                                sigma=float(z['sigma']))
+    assert abs(val - float(z['val'])) < 1e-10
+    assert _same_up_to_sign(O.full_vector(vec.cores), z['vec0']) < 1e-7
