@@ -184,6 +184,16 @@ int ttals_tt_matmul(ttals_ctx* ctx, const ttals_tt* a, const ttals_tt* b, double
 int ttals_tt_ortho(ttals_ctx* ctx, const ttals_tt* t, int32_t direction, int32_t first, int32_t last,
                    double* out_data, int32_t out_on_device, int64_t* out_ranks);
 
+/* scikit_tt/tensor_train.py:1150-1181 and 1262-1296 (`ortho_left` /
+ * `ortho_right` with `threshold` / `max_rank`): per core a one-sided Jacobi
+ * SVD; singular values with sigma_i / sigma_0 <= threshold are dropped (none
+ * when threshold == 0), then at most max_ranks[i + 1] (left) or max_ranks[i]
+ * (right) are kept (max_ranks may be NULL; entries <= 0 mean no cap); S V^T
+ * (left) or U S (right) moves into the neighbouring core. */
+int ttals_tt_ortho_trunc(ttals_ctx* ctx, const ttals_tt* t, int32_t direction, int32_t first, int32_t last,
+                         double threshold, const int64_t* max_ranks, double* out_data, int32_t out_on_device,
+                         int64_t* out_ranks);
+
 /* scikit_tt/tensor_train.py:1334-1430 (`norm(p=2)`): Euclidean/Frobenius
  * norm, computed by a QR sweep with the scale carried as a logarithm. */
 int ttals_tt_norm(ttals_ctx* ctx, const ttals_tt* t, double* out_norm);

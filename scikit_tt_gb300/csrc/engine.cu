@@ -1627,6 +1627,83 @@ int ttals_tt_ortho(ttals_ctx* c, const ttals_tt* t_t, int32_t direction, int32_t
   });
 }
 
+int ttals_tt_ortho_trunc(ttals_ctx* c, const ttals_tt* t_t, int32_t direction, int32_t first, int32_t last,
+                         double threshold, const int64_t* max_ranks, double* out, int32_t out_dev,
+                         int64_t* out_ranks) {
+  return guarded(c, [&] {
+    TTView t = view(t_t, "tensor train");
+    require(out != nullptr && out_ranks != nullptr, TTALS_ERR_ARG, "output buffer is null");
+    require(threshold >= 0.0, TTALS_ERR_ARG, "threshold must be >= 0");
+    const int d = t.d;
+    std::vector<int64_t> r = t.r, mn(d);
+    for (int i = 0; i < d; ++i) mn[i] = t.m[i] * t.n[i];
+    std::vector<double*> core(d);
+    double *rbuf = nullptr, *work = nullptr, *tmp = nullptr, *cbuf = nullptr, *kept = nullptr;
+    int64_t maxc = 1, maxw = 1;
+    for (int i = 0; i < d; ++i) {
+      const int64_t cs = r[i] * mn[i] * r[i + 1];
+      maxc = std::max(maxc, cs);
+      maxw = std::max(maxw, (int64_t)std::max(svd_trunc_work_doubles(r[i] * mn[i], r[i + 1]),
+                                              svd_trunc_work_doubles(r[i], mn[i] * r[i + 1])));
+      require(std::min(r[i] * mn[i], r[i + 1]) <= 1024 && std::min(r[i], mn[i] * r[i + 1]) <= 1024,
+              TTALS_ERR_UNSUPPORTED, "truncated orthonormalisation: core too large");
+    }
+    Bump B{c};
+    for (int i = 0; i < d; ++i) B.want(&core[i], r[i] * mn[i] * r[i + 1]);
+    B.want(&rbuf, maxc);
+    B.want(&cbuf, maxc);
+    B.want(&work, maxw);
+    B.want(&tmp, maxc);
+    B.want(&kept, 1);
+    B.commit();
+    int* kdev = reinterpret_cast<int*>(kept);
+    int* status = kdev + 1;
+    CK(cudaMemsetAsync(kept, 0, sizeof(double), c->stream));
+    for (int i = 0; i < d; ++i)
+      CK(cudaMemcpyAsync(core[i], t.data + t.off[i], sizeof(double) * (t.off[i + 1] - t.off[i]),
+                         t.dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+    auto read_k = [&]() {
+      int k = 0;
+      CK(cudaMemcpyAsync(&k, kdev, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      return (int64_t)k;
+    };
+    auto cap = [&](int idx) -> int64_t { return max_ranks ? max_ranks[idx] : 0; };
+    if (direction == 0) {
+      for (int i = std::max(0, first); i <= std::min(last, d - 2); ++i) {
+        const int64_t p = r[i] * mn[i], q = r[i + 1];
+        CK(launch_svd_trunc(core[i], p, q, 0, threshold, cap(i + 1), work, cbuf, rbuf, kdev, status, c->stream));
+        const int64_t k = read_k();
+        CK(cudaMemcpyAsync(core[i], cbuf, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+        const int64_t qq = mn[i + 1] * r[i + 2];
+        push_left(c, rbuf, core[i + 1], k, q, qq, tmp);
+        CK(cudaMemcpyAsync(core[i + 1], tmp, sizeof(double) * k * qq, cudaMemcpyDeviceToDevice, c->stream));
+        r[i + 1] = k;
+      }
+    } else {
+      for (int i = std::min(first, d - 1); i >= std::max(1, last); --i) {
+        const int64_t a = r[i], q = mn[i] * r[i + 1];
+        CK(launch_svd_trunc(core[i], a, q, 1, threshold, cap(i), work, cbuf, rbuf, kdev, status, c->stream));
+        const int64_t k = read_k();
+        CK(cudaMemcpyAsync(core[i], cbuf, sizeof(double) * k * q, cudaMemcpyDeviceToDevice, c->stream));
+        const int64_t p = r[i - 1] * mn[i - 1];
+        push_right(c, core[i - 1], rbuf, p, a, k, tmp);
+        CK(cudaMemcpyAsync(core[i - 1], tmp, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+        r[i] = k;
+      }
+    }
+    int64_t off = 0;
+    for (int i = 0; i < d; ++i) {
+      const int64_t cnt = r[i] * mn[i] * r[i + 1];
+      CK(cudaMemcpyAsync(out + off, core[i], sizeof(double) * cnt,
+                         out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+      off += cnt;
+    }
+    for (int i = 0; i <= d; ++i) out_ranks[i] = r[i];
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
 int ttals_tt_norm(ttals_ctx* c, const ttals_tt* t_t, double* out_norm) {
   return guarded(c, [&] {
     TTView t = view(t_t, "tensor train");

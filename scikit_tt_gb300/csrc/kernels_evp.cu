@@ -225,3 +225,188 @@ cudaError_t launch_trunc_basis(const double* M, int64_t p, int64_t q, int tr_k, 
 }
 
 }  // namespace ttals
+
+namespace ttals {
+
+// ---------------------------------------------------------------------------
+// Truncated SVD of one TT core (TT.ortho_left / ortho_right with threshold or
+// max_rank, scikit_tt/tensor_train.py:1150-1181 and 1262-1296).
+//
+// One-sided (Hestenes) Jacobi on the columns of X = M (q <= p) or X = M^T:
+// column pairs are rotated until mutually orthogonal to machine precision;
+// then the column norms are the singular values (computed to high relative
+// accuracy, which the relative cut sigma_i / sigma_0 > threshold needs), the
+// normalised columns the left singular vectors of X and the accumulated
+// rotations its right singular vectors.  Rotation pairs follow the round-robin
+// ordering, one warp per pair, one CTA.  Kept rank k = #{sigma_i / sigma_0 >
+// threshold} (all when threshold == 0), capped at max_rank, at least 1.
+// Outputs for M = U S V^T:
+//   side 0 (left):  core = U (p x k),    r = S V^T (k x q)
+//   side 1 (right): core = V^T (k x q),  r = U S (p x k)
+// ---------------------------------------------------------------------------
+
+struct SvdK {
+  const double* M;   // p x q row-major
+  int64_t p, q;
+  int side;
+  double threshold;
+  int64_t max_rank;  // <= 0: no cap
+  double* W;         // working columns, n_rows x ncols column-major
+  double* Vr;        // ncols x ncols rotations (column-major)
+  double* core;
+  double* r;
+  int* kept;         // out: k
+  int* status;
+};
+
+__global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
+  __shared__ int s_a[kTrMaxGram / 2], s_b[kTrMaxGram / 2];
+  __shared__ double s_sig[kTrMaxGram];
+  __shared__ int s_ord[kTrMaxGram];
+  __shared__ int s_rot;
+  __shared__ int s_k;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const bool tr = a.q > a.p;                 // work on M^T when M is wide
+  const int64_t rows = tr ? a.q : a.p;       // length of a working column
+  const int ncols = (int)(tr ? a.p : a.q);   // number of working columns
+  double* W = a.W;
+  double* V = a.Vr;
+  for (int64_t e = tid; e < rows * ncols; e += nt) {
+    const int64_t c = e / rows, i = e - c * rows;
+    W[e] = tr ? a.M[c * a.q + i] : a.M[i * a.q + c];
+  }
+  for (int64_t e = tid; e < (int64_t)ncols * ncols; e += nt) V[e] = (e / ncols == e % ncols) ? 1.0 : 0.0;
+  __syncthreads();
+  const int nn = (ncols + 1) & ~1, npairs = nn / 2;
+  for (int sweep = 0; sweep < 60 && ncols > 1; ++sweep) {
+    if (tid == 0) s_rot = 0;
+    __syncthreads();
+    for (int step = 0; step < nn - 1; ++step) {
+      if (tid < npairs) {
+        auto pos = [&](int j) { return j == 0 ? 0 : ((j - 1 + step) % (nn - 1)) + 1; };
+        int ia = pos(tid), ib = pos(nn - 1 - tid);
+        if (ia > ib) {
+          const int t = ia;
+          ia = ib;
+          ib = t;
+        }
+        s_a[tid] = ia;
+        s_b[tid] = ib;
+      }
+      __syncthreads();
+      for (int pi = warp; pi < npairs; pi += nw) {
+        const int ia = s_a[pi], ib = s_b[pi];
+        if (ib >= ncols) continue;
+        double* ca = W + (int64_t)ia * rows;
+        double* cb = W + (int64_t)ib * rows;
+        double alpha = 0.0, beta = 0.0, gamma = 0.0;
+        for (int64_t i = lane; i < rows; i += 32) {
+          alpha += ca[i] * ca[i];
+          beta += cb[i] * cb[i];
+          gamma += ca[i] * cb[i];
+        }
+        alpha = warp_sum(alpha);
+        beta = warp_sum(beta);
+        gamma = warp_sum(gamma);
+        if (fabs(gamma) > 1e-15 * sqrt(alpha * beta) && gamma != 0.0) {
+          const double zeta = (beta - alpha) / (2.0 * gamma);
+          const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+          for (int64_t i = lane; i < rows; i += 32) {
+            const double x = ca[i], y = cb[i];
+            ca[i] = c * x - s * y;
+            cb[i] = s * x + c * y;
+          }
+          double* va = V + (int64_t)ia * ncols;
+          double* vb = V + (int64_t)ib * ncols;
+          for (int i = lane; i < ncols; i += 32) {
+            const double x = va[i], y = vb[i];
+            va[i] = c * x - s * y;
+            vb[i] = s * x + c * y;
+          }
+          if (lane == 0) s_rot = 1;
+        }
+      }
+      __syncthreads();
+    }
+    if (!s_rot) break;
+    __syncthreads();
+  }
+  // singular values, descending order, kept rank
+  for (int c = warp; c < ncols; c += nw) {
+    const double* cc = W + (int64_t)c * rows;
+    double s = 0.0;
+    for (int64_t i = lane; i < rows; i += 32) s += cc[i] * cc[i];
+    s = warp_sum(s);
+    if (lane == 0) s_sig[c] = sqrt(s);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int i = 0; i < ncols; ++i) s_ord[i] = i;
+    for (int i = 1; i < ncols; ++i) {  // insertion sort, descending, stable
+      const int v = s_ord[i];
+      int j = i - 1;
+      while (j >= 0 && s_sig[s_ord[j]] < s_sig[v]) {
+        s_ord[j + 1] = s_ord[j];
+        --j;
+      }
+      s_ord[j + 1] = v;
+    }
+    const double s0 = s_sig[s_ord[0]];
+    int k = ncols;
+    if (a.threshold != 0.0) {
+      k = 0;
+      while (k < ncols && s0 > 0.0 && s_sig[s_ord[k]] / s0 > a.threshold) ++k;
+    }
+    if (a.max_rank > 0 && k > a.max_rank) k = (int)a.max_rank;
+    if (k < 1) k = 1;
+    s_k = k;
+    *a.kept = k;
+  }
+  __syncthreads();
+  const int k = s_k;
+  // M = U S V^T.  Working X (= M or M^T) = Ux S Vx^T with Ux = W[:, c] / sigma_c, Vx = V[:, c].
+  // not transposed: U = Ux, V = Vx.  transposed: U = Vx, V = Ux.
+  const int64_t p = a.p, q = a.q;
+  auto Uel = [&](int64_t i, int j) -> double {  // U[i][j] * sigma_j   (unnormalised left vector)
+    const int c = s_ord[j];
+    return tr ? V[(int64_t)c * ncols + i] * s_sig[c] : W[(int64_t)c * rows + i];
+  };
+  auto Vel = [&](int64_t i, int j) -> double {  // V[i][j] * sigma_j
+    const int c = s_ord[j];
+    return tr ? W[(int64_t)c * rows + i] : V[(int64_t)c * ncols + i] * s_sig[c];
+  };
+  for (int64_t e = tid; e < p * k; e += nt) {
+    const int64_t i = e / k;
+    const int j = (int)(e - i * k);
+    const double sg = s_sig[s_ord[j]];
+    const double u = Uel(i, j);
+    if (a.side == 0) a.core[e] = sg > 0.0 ? u / sg : (i == j ? 1.0 : 0.0);
+    else a.r[e] = u;
+  }
+  for (int64_t e = tid; e < (int64_t)k * q; e += nt) {
+    const int j = (int)(e / q);
+    const int64_t i = e - (int64_t)j * q;
+    const double sg = s_sig[s_ord[j]];
+    const double v = Vel(i, j);
+    if (a.side == 0) a.r[e] = v;
+    else a.core[e] = sg > 0.0 ? v / sg : (i == j ? 1.0 : 0.0);
+  }
+}
+
+size_t svd_trunc_work_doubles(int64_t p, int64_t q) {
+  const int64_t n = p < q ? p : q, rows = p > q ? p : q;
+  return (size_t)(rows * n + n * n + 64);
+}
+
+cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
+                             double* work, double* core, double* r, int* kept, int* status, cudaStream_t st) {
+  const int64_t n = p < q ? p : q, rows = p > q ? p : q;
+  if (n > kTrMaxGram || n < 1) return cudaErrorInvalidValue;
+  SvdK a{M, p, q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status};
+  svd_trunc_kernel<<<1, kTrThreads, 0, st>>>(a);
+  ++launch_counter();
+  return cudaGetLastError();
+}
+
+}  // namespace ttals

@@ -127,6 +127,12 @@ size_t trunc_work_doubles(int64_t p, int64_t q, int64_t r);
 cudaError_t launch_trunc_basis(const double* M, int64_t p, int64_t q, int tr_k, int r, int side, double* work,
                                double* out, int* status, cudaStream_t st);
 
+// truncated SVD of one core (kernels_evp.cu): M (p x q) = U S V^T, kept rank k
+// -> side 0: core = U (p x k), r = S V^T (k x q); side 1: core = V^T, r = U S
+size_t svd_trunc_work_doubles(int64_t p, int64_t q);
+cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
+                             double* work, double* core, double* r, int* kept, int* status, cudaStream_t st);
+
 // engine.cu helpers used by the allocation-free entry point (noalloc.cu)
 }  // namespace ttals
 struct ttals_ctx;

@@ -1,0 +1,156 @@
+"""Linear-ODE integrators in the TT format on the device engine.
+
+Drop-ins for the step methods of ``scikit_tt/solvers/ode.py`` that are built on
+the ALS hot path: every implicit step is one device ``sle.als`` call on the
+shifted operator ``I - h A`` (or ``I - h/2 A``), warm-started from the previous
+step's solution; products and norms run through the device ``TT.dot`` and
+``TT.norm``.  Signatures, defaults and return values follow the reference:
+
+* ``explicit_euler``      ode.py:16-83   (x_{k+1} = (I + h A) x_k, re-truncated)
+* ``errors_expl_euler``   ode.py:85-115
+* ``implicit_euler``      ode.py:249-331 ((I - h A) x_{k+1} = x_k)
+* ``errors_impl_euler``   ode.py:333-364
+* ``trapezoidal_rule``    ode.py:366-451 ((I - h/2 A) x_{k+1} = (I + h/2 A) x_k)
+* ``errors_trapezoidal``  ode.py:453-485
+* ``adaptive_step_size``  ode.py:487-636 (implicit Euler against two half steps
+  or the trapezoidal rule, step control by local error and closeness to the
+  stationary state)
+
+``tt_solver='mals'`` raises ``NotImplementedError`` (two-site MALS is not on
+the device path); ``progress`` is accepted and ignored.
+"""
+
+from __future__ import annotations
+
+from typing import List
+
+import numpy as np
+
+from .. import tensor_train as tt
+from . import sle
+
+
+def _shifted(operator, alpha):
+    """I + alpha * operator as a TT operator (rank sum, tensor_train.py:282-344)."""
+    return tt.eye(operator.row_dims) + alpha * operator
+
+
+def _solve(op, guess, rhs, tt_solver, micro_solver, repeats, threshold, max_rank):
+    if tt_solver == 'als':
+        return sle.als(op, guess, rhs, solver=micro_solver, repeats=repeats)
+    if tt_solver == 'mals':
+        return sle.mals(op, guess, rhs, solver=micro_solver, threshold=threshold, repeats=repeats, max_rank=max_rank)
+    raise ValueError("tt_solver must be 'als' or 'mals'")
+
+
+def explicit_euler(operator, initial_value, step_sizes: List[float], threshold: float = 1e-12,
+                   max_rank=np.inf, normalize: int = 1, progress: bool = True) -> List:
+    """x_{k+1} = (I + h_k A) x_k, re-truncated by ``ortho(threshold, max_rank)``."""
+    solution = [initial_value]
+    for h in step_sizes:
+        nxt = _shifted(operator, h).dot(solution[-1])
+        nxt = nxt.ortho(threshold=threshold, max_rank=max_rank)
+        if normalize > 0:
+            nxt = (1 / nxt.norm(p=normalize)) * nxt
+        solution.append(nxt.copy())
+    return solution
+
+
+def errors_expl_euler(operator, solution: List, step_sizes: List[float]) -> List[float]:
+    """Relative residuals |x_{k+1} - (I + h A) x_k| / |x_k|."""
+    return [(solution[k + 1] - _shifted(operator, step_sizes[k]).dot(solution[k])).norm() / solution[k].norm()
+            for k in range(len(solution) - 1)]
+
+
+def implicit_euler(operator, initial_value, initial_guess, step_sizes: List[float], repeats: int = 1,
+                   tt_solver: str = 'als', threshold: float = 1e-12, max_rank=np.inf, micro_solver='solve',
+                   normalize=1, progress=True) -> List:
+    """(I - h_k A) x_{k+1} = x_k, each step one device ALS solve warm-started from the last."""
+    solution = [initial_value]
+    current = initial_guess
+    for h in step_sizes:
+        current = _solve(_shifted(operator, -h), current, solution[-1], tt_solver, micro_solver, repeats, threshold,
+                         max_rank)
+        if normalize > 0:
+            current = (1 / current.norm(p=normalize)) * current
+        solution.append(current.copy())
+    return solution
+
+
+def errors_impl_euler(operator, solution: List, step_sizes: List[float]) -> List[float]:
+    """Relative residuals |(I - h A) x_{k+1} - x_k| / |x_k|."""
+    return [(_shifted(operator, -step_sizes[k]).dot(solution[k + 1]) - solution[k]).norm() / solution[k].norm()
+            for k in range(len(solution) - 1)]
+
+
+def trapezoidal_rule(operator, initial_value, initial_guess, step_sizes: List[float], repeats: int = 1,
+                     tt_solver: str = 'als', threshold=1e-12, max_rank: int = np.inf, micro_solver: str = 'solve',
+                     normalize: int = 1, progress: bool = True) -> List:
+    """(I - h/2 A) x_{k+1} = (I + h/2 A) x_k."""
+    solution = [initial_value]
+    current = initial_guess
+    for h in step_sizes:
+        rhs = _shifted(operator, 0.5 * h).dot(solution[-1])
+        current = _solve(_shifted(operator, -0.5 * h), current, rhs, tt_solver, micro_solver, repeats, threshold,
+                         max_rank)
+        if normalize > 0:
+            current = (1 / current.norm(p=normalize)) * current
+        solution.append(current.copy())
+    return solution
+
+
+def errors_trapezoidal(operator, solution: List, step_sizes: List[float]) -> List[float]:
+    """Relative residuals of the trapezoidal steps."""
+    errs = []
+    for k in range(len(solution) - 1):
+        rhs = _shifted(operator, 0.5 * step_sizes[k]).dot(solution[k])
+        errs.append((_shifted(operator, -0.5 * step_sizes[k]).dot(solution[k + 1]) - rhs).norm() / rhs.norm())
+    return errs
+
+
+def adaptive_step_size(operator, initial_value, initial_guess, time_end: float, step_size_first: float = 1e-10,
+                       repeats: int = 1, solver: str = 'solve', error_tol: float = 1e-1, closeness_tol: float = 0.5,
+                       step_size_min: float = 1e-14, step_size_max: float = 10, closeness_min: float = 1e-3,
+                       factor_max: float = 2, factor_safe: float = 0.9, second_method: str = 'two_step_Euler',
+                       normalize: int = 1, progress: bool = True):
+    """Adaptive implicit Euler (ode.py:487-636); returns ``(solution, time_steps)``.
+
+    A step of size h is implicit Euler (normalised in the 1-norm); its
+    companion is two implicit Euler half steps or one trapezoidal step.  The
+    step is accepted when both the relative local error and the relative
+    change of |A x| (closeness to the stationary state) are within tolerance;
+    the next step size is the safety-scaled minimum of the three factors."""
+    solution = [initial_value]
+    closeness_pre = operator.dot(initial_value).norm()
+    guess = initial_guess
+    time = 0
+    time_steps = [0]
+    h = step_size_first
+    while time < time_end and closeness_pre > closeness_min and h > step_size_min:
+        t_1 = sle.als(_shifted(operator, -h), guess.copy(), solution[-1], solver=solver, repeats=repeats)
+        t_1 = (1 / t_1.norm(p=1)) * t_1
+        t_2 = []
+        if second_method == 'two_step_Euler':
+            t_2 = sle.als(_shifted(operator, -0.5 * h), guess.copy(), solution[-1], solver=solver, repeats=repeats)
+            t_2 = sle.als(_shifted(operator, -0.5 * h), t_2.copy(), solution[-1], solver=solver, repeats=repeats)
+        if second_method == 'trapezoidal_rule':
+            t_2 = sle.als(_shifted(operator, -0.5 * h), guess.copy(), _shifted(operator, 0.5 * h).dot(solution[-1]),
+                          solver=solver, repeats=repeats)
+        if normalize > 0:
+            t_2 = (1 / t_2.norm(p=normalize)) * t_2
+        closeness = operator.dot(t_1).norm()
+        local_error = (t_1 - t_2).norm() / t_1.norm()
+        closeness_difference = (closeness - closeness_pre) / closeness_pre
+        factor_local = error_tol / local_error
+        factor_closeness = closeness_tol / np.abs(closeness_difference)
+        h_new = np.amin([factor_max, factor_safe * factor_local, factor_safe * factor_closeness]) * h
+        if factor_local > 1 and factor_closeness > 1:
+            time = np.min([time + h, time_end])
+            h = np.amin([h_new, time_end - time, step_size_max])
+            solution.append(t_2.copy())
+            time_steps.append(time)
+            guess = t_1
+            closeness_pre = closeness
+        else:
+            h = h_new
+    return solution, time_steps

@@ -188,37 +188,59 @@ class TT(object):
         self.ranks = [int(r) for r in ranks]
         return self
 
-    @staticmethod
-    def _check_trunc(threshold, max_rank):
+    def _ortho_trunc(self, direction, first, last, threshold, max_ranks):
+        p = _lib.Packed(self.cores)
+        out = np.empty(p.data.size, dtype=np.float64)
+        ranks = np.zeros(self.order + 1, dtype=np.int64)
+        caps = np.array([0 if m == np.inf else int(m) for m in max_ranks], dtype=np.int64)
+        _lib.check(_lib.load().ttals_tt_ortho_trunc(_lib.context(), p.desc, direction, first, last, float(threshold),
+                                                    _lib.i64ptr(caps), _lib.dptr(out), 0, _lib.i64ptr(ranks)))
+        self.cores = _lib.unpack(out, self.row_dims, self.col_dims, ranks)
+        self.ranks = [int(r) for r in ranks]
+        return self
+
+    def _check_trunc(self, threshold, max_rank):
+        """Validates the truncation arguments as tensor_train.py:1124-1145 does and
+        returns the per-bond rank caps, or None when nothing is truncated."""
         if not (isinstance(threshold, (int, float, np.floating, np.integer)) and threshold >= 0):
             raise ValueError('Threshold must be greater or equal 0.')
-        if not ((isinstance(max_rank, (int, np.integer)) and max_rank > 0) or max_rank == np.inf
-                or isinstance(max_rank, list)):
+        if (isinstance(max_rank, (int, np.integer)) and max_rank > 0) or max_rank == np.inf:
+            caps = [1] + [max_rank] * (self.order - 1) + [1]
+        elif isinstance(max_rank, list) and len(max_rank) == self.order + 1 and \
+                all((isinstance(m, (int, np.integer)) and m > 0) or m == np.inf for m in max_rank):
+            caps = list(max_rank)
+        else:
             raise ValueError('Maximum rank(s) must be positive integers.')
-        if threshold != 0 or (not isinstance(max_rank, list) and max_rank != np.inf) or \
-                (isinstance(max_rank, list) and any(m != np.inf for m in max_rank[1:-1])):
-            raise NotImplementedError('truncated orthonormalisation is not implemented on the device path')
+        if threshold == 0 and all(m == np.inf for m in caps[1:-1]):
+            return None
+        return caps
 
     def ortho_left(self, start_index: int = 0, end_index: Optional[int] = None, threshold: float = 0.0,
                    max_rank=np.inf, progress: bool = False, string: str = 'Left-orthonormalization') -> 'TT':
         """Left-orthonormalise cores ``start_index..end_index`` (default
-        ``0..d-2``) by device Householder QR (tensor_train.py:1092-1205)."""
+        ``0..d-2``, tensor_train.py:1092-1205): device Householder QR, or a
+        device SVD per core when ``threshold`` / ``max_rank`` truncate."""
         if end_index is None:
             end_index = self.order - 2
         if not (isinstance(start_index, (int, np.integer)) and isinstance(end_index, (int, np.integer))):
             raise TypeError('Start and end indices must be integers.')
-        self._check_trunc(threshold, max_rank)
+        caps = self._check_trunc(threshold, max_rank)
+        if caps is not None:
+            return self._ortho_trunc(0, int(start_index), int(end_index), threshold, caps)
         return self._ortho(0, int(start_index), int(end_index))
 
     def ortho_right(self, start_index: Optional[int] = None, end_index: int = 1, threshold: float = 0,
                     max_rank=np.inf) -> 'TT':
         """Right-orthonormalise cores ``start_index..end_index`` (default
-        ``d-1..1``) by device Householder RQ (tensor_train.py:1207-1310)."""
+        ``d-1..1``, tensor_train.py:1207-1310): device Householder RQ, or a
+        device SVD per core when ``threshold`` / ``max_rank`` truncate."""
         if start_index is None:
             start_index = self.order - 1
         if not (isinstance(start_index, (int, np.integer)) and isinstance(end_index, (int, np.integer))):
             raise TypeError('Start and end indices must be integers.')
-        self._check_trunc(threshold, max_rank)
+        caps = self._check_trunc(threshold, max_rank)
+        if caps is not None:
+            return self._ortho_trunc(1, int(start_index), int(end_index), threshold, caps)
         return self._ortho(1, int(start_index), int(end_index))
 
     def ortho(self, threshold: float = 0, max_rank=np.inf) -> 'TT':

@@ -25,6 +25,7 @@ import scikit_tt.tensor_train as rtt  # noqa: E402
 import scikit_tt.models as rmodels  # noqa: E402
 import scikit_tt.solvers.sle as rsle  # noqa: E402
 import scikit_tt.solvers.evp as revp  # noqa: E402
+import scikit_tt.solvers.ode as rode  # noqa: E402
 from scikit_tt.tensor_train import TT as RTT  # noqa: E402
 
 from scikit_tt_gb300 import workloads as wl  # noqa: E402
@@ -166,6 +167,62 @@ def power_cases():
     power_case('evp_power_markov_gevp', w.op, x0, True)
 
 
+def ode_cases():
+    """Implicit / explicit / trapezoidal / adaptive integrators on a Markov generator."""
+    rng = np.random.default_rng(11)
+    d, n = 4, 4
+    gen = RTT(wl.markov_op(d, n, 0.2, rng)) - rtt.eye([n] * d)
+    x0 = (1.0 / n ** d) * rtt.ones([n] * d, [1] * d)
+    guess = RTT([np.abs(c) + 0.1 for c in wl.gaussian_tt(rng, d, n, 4)])
+    out = {}
+    pack('op', [c.copy() for c in gen.cores], out)
+    pack('x0', [c.copy() for c in x0.cores], out)
+    pack('guess', [c.copy() for c in guess.cores], out)
+    steps = [0.1, 0.2, 0.4, 0.8]
+    out['steps'] = np.array(steps)
+
+    def store(prefix, sol):
+        out[prefix + '_n'] = np.array(len(sol))
+        for k, t in enumerate(sol):
+            out[f'{prefix}_{k}'] = np.asarray(t.full()).reshape(-1)
+
+    sol = rode.implicit_euler(gen, x0, guess, steps, progress=False)
+    store('impl', sol)
+    out['impl_err'] = np.array(rode.errors_impl_euler(gen, sol, steps))
+    sol = rode.trapezoidal_rule(gen, x0, guess, steps, progress=False)
+    store('trap', sol)
+    out['trap_err'] = np.array(rode.errors_trapezoidal(gen, sol, steps))
+    sol = rode.explicit_euler(gen, x0, [0.05, 0.05, 0.05], progress=False)
+    store('expl', sol)
+    out['expl_err'] = np.array(rode.errors_expl_euler(gen, sol, [0.05, 0.05, 0.05]))
+    sol, times = rode.adaptive_step_size(gen, x0, guess, 2.0, step_size_first=0.05, progress=False)
+    store('adapt', sol)
+    out['adapt_times'] = np.array(times)
+    np.savez_compressed(os.path.join(HERE, 'ode_markov.npz'), **out)
+    print('ode_markov', 'adaptive steps', len(times), times[-1], 'impl err', out['impl_err'])
+
+
+def trunc_cases():
+    """ortho_left / ortho_right / ortho with threshold and max_rank (SVD truncation)."""
+    rng = np.random.default_rng(21)
+    d, n = 6, 3
+    a = RTT(wl.gaussian_tt(rng, d, n, 2))
+    b = RTT(wl.gaussian_tt(rng, d, n, 2))
+    c = RTT(wl.gaussian_tt(rng, d, n, 4))
+    t = a + b + 1e-9 * c          # rank 8 with a 1e-9 tail: truncates to rank <= 4
+    out = {}
+    pack('t', [x.copy() for x in t.cores], out)
+    cases = {'left_thr': lambda x: x.ortho_left(threshold=1e-6),
+             'right_max': lambda x: x.ortho_right(max_rank=3),
+             'ortho_both': lambda x: x.ortho(threshold=1e-12, max_rank=4)}
+    for key, fn in cases.items():
+        r = fn(t.copy())
+        out[key + '_ranks'] = np.array(r.ranks)
+        out[key + '_full'] = np.asarray(r.full()).reshape(-1)
+        print(key, r.ranks)
+    np.savez_compressed(os.path.join(HERE, 'ttops_trunc.npz'), **out)
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -195,6 +252,8 @@ def main():
     ttops_case()
     evp_blocks()
     power_cases()
+    ode_cases()
+    trunc_cases()
 
 
 if __name__ == '__main__':
@@ -202,5 +261,9 @@ if __name__ == '__main__':
         evp_blocks()
     elif len(sys.argv) > 1 and sys.argv[1] == 'power':
         power_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'ode':
+        ode_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'trunc':
+        trunc_cases()
     else:
         main()

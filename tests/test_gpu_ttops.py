@@ -50,3 +50,23 @@ def test_ode_helpers(golden):
     np.testing.assert_allclose(sl[1], z['left'], rtol=1e-12, atol=1e-12 * np.abs(z['left']).max())
     np.testing.assert_allclose(sr[0], z['right'], rtol=1e-12, atol=1e-12 * np.abs(z['right']).max())
     np.testing.assert_allclose(M, z['micro'], rtol=1e-12, atol=1e-12 * np.abs(z['micro']).max())
+
+
+@pytest.mark.parametrize('key', ['left_thr', 'right_max', 'ortho_both'])
+def test_truncated_ortho_matches_reference(golden, key):
+    # device one-sided Jacobi SVD per core with the reference's rank rule
+    from scikit_tt_gb300.tensor_train import TT
+    z, cores = golden('ttops_trunc')
+    t = TT([np.array(c) for c in cores('t')])
+    fn = {'left_thr': lambda x: x.ortho_left(threshold=1e-6),
+          'right_max': lambda x: x.ortho_right(max_rank=3),
+          'ortho_both': lambda x: x.ortho(threshold=1e-12, max_rank=4)}[key]
+    r = fn(t)
+    assert list(r.ranks) == list(z[key + '_ranks'])
+    v, ref = O.full_vector(r.cores), z[key + '_full']
+    assert np.linalg.norm(v - ref) / np.linalg.norm(ref) < 1e-12
+    # the swept cores are orthonormal
+    if key == 'left_thr':
+        for c in r.cores[:-1]:
+            m = c.reshape(-1, c.shape[3])
+            assert np.allclose(m.T @ m, np.eye(m.shape[1]), atol=1e-12)
