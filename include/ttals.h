@@ -129,6 +129,16 @@ int ttals_sle_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const 
                   int32_t repeats, int32_t solver, int32_t precision, double tol,
                   double* out_data, int32_t out_on_device, int64_t* out_ranks, ttals_stats* stats);
 
+/* scikit_tt/solvers/sle.py:98-191 (`mals`): two-site ALS with a truncated SVD
+ * split (sle.py:550-650): singular values with sigma_k / sigma_0 <= threshold
+ * are dropped (none when threshold == 0) and at most max_rank (<= 0: no cap)
+ * are kept.  The two-site micro system is solved matrix-free in FP64 (tol <= 0
+ * picks 1e-13).  With out_data == NULL and out_capacity != NULL the call only
+ * stores in *out_capacity the number of doubles the output may need. */
+int ttals_sle_mals(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const ttals_tt* rhs, int32_t repeats,
+                   int32_t solver, double threshold, int64_t max_rank, double tol, double* out_data,
+                   int32_t out_on_device, int64_t* out_ranks, int64_t* out_capacity, ttals_stats* stats);
+
 /* Batched scikit_tt/solvers/sle.py:10 `als`: `count` independent systems
  * (each with its own order, mode sizes and ranks) solved in one launch, one
  * CTA per system.  out_data[j] receives system j's cores with the ranks

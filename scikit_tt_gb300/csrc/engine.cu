@@ -625,6 +625,230 @@ void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttal
 }
 
 // ---------------------------------------------------------------------------
+// two-site MALS (scikit_tt/solvers/sle.py:98-191, 350-472, 550-650)
+// ---------------------------------------------------------------------------
+//
+// The two-site micro problem of sites (i, i+1) is the one-site problem of a
+// merged site: mode n_i n_{i+1}, operator core A_i x A_{i+1} contracted over
+// their shared rank, right-hand-side core b_i x b_{i+1}.  It is solved by the
+// same matrix-free GMRES as ALS (FP64), then split by a truncated SVD of the
+// (r_i n_i) x (n_{i+1} r_{i+2}) solution: forward keeps U as core i, backward
+// keeps V^T as core i+1 (and U S as core 0 at the end), with the reference's
+// rank rule (sigma_k / sigma_0 > threshold, at most max_rank).
+
+// out[R, m1, m2, n1, n2, Q] = sum_R' A1[R, m1, n1, R'] A2[R', m2, n2, Q]
+Contraction desc_merge_op(int64_t R0, int64_t n1, int64_t R1, int64_t n2, int64_t R2) {
+  const Ax o[6] = {{R0, n1 * n1 * R1, 0, n1 * n2 * n1 * n2 * R2}, {n1, n1 * R1, 0, n2 * n1 * n2 * R2},
+                   {n2, 0, n2 * R2, n1 * n2 * R2},                {n1, R1, 0, n2 * R2},
+                   {n2, 0, R2, R2},                               {R2, 0, 1, 1}};
+  const Ax k[1] = {{R1, 1, n2 * n2 * R2, 0}};
+  return desc_make(6, o, 1, k);
+}
+// out[b, n1, n2, g'] = sum_g B1[b, n1, g] B2[g, n2, g']
+Contraction desc_merge_vec(int64_t h0, int64_t n1, int64_t h1, int64_t n2, int64_t h2) {
+  const Ax o[4] = {{h0, n1 * h1, 0, n1 * n2 * h2}, {n1, h1, 0, n2 * h2}, {n2, 0, h2, h2}, {h2, 0, 1, 1}};
+  const Ax k[1] = {{h1, 1, n2 * h2, 0}};
+  return desc_make(4, o, 1, k);
+}
+
+void run_mals(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttals_tt* b_t, int repeats, int solver,
+              double threshold, int64_t max_rank, double tol, double* out, int out_dev, int64_t* out_ranks,
+              ttals_stats* st) {
+  TTView op = view(op_t, "operator"), x0 = view(x_t, "initial_guess"), b = view(b_t, "right_hand_side");
+  validate_square_op(op);
+  validate_vec(x0, op, "initial_guess");
+  validate_vec(b, op, "right_hand_side");
+  require(solver == TTALS_SLE_SOLVE || solver == TTALS_SLE_LU, TTALS_ERR_ARG, "solver must be 'solve' or 'lu'");
+  require(repeats >= 0, TTALS_ERR_ARG, "repeats must be >= 0");
+  require(threshold >= 0.0, TTALS_ERR_ARG, "threshold must be >= 0");
+  require(out != nullptr, TTALS_ERR_ARG, "output buffer is null");
+  require(op.d >= 2, TTALS_ERR_UNSUPPORTED, "MALS needs at least two cores");
+  if (tol <= 0) tol = 1e-13;
+
+  launch_counter() = 0;
+  Engine E;
+  E.c = c;
+  E.prec = TTALS_PREC_FP64;
+  auto& P = E.P;
+  const int d = op.d;
+  P.d = d;
+  P.n = op.m;
+  P.R = op.r;
+  P.rx0 = x0.r;
+  // the first sweep works in the frames of the raw initial guess, as the
+  // reference does: a truncated split depends on that (non-orthonormal) gauge
+  const std::vector<int64_t> r_init = P.rx0;
+  // bond capacities: ranks never exceed the smaller side's dimension nor max_rank
+  std::vector<int64_t> cap(d + 1, 1);
+  {
+    const int64_t big = int64_t(1) << 40;
+    std::vector<int64_t> left(d + 1, 1), right(d + 1, 1);
+    for (int i = 1; i <= d; ++i) left[i] = std::min(big, left[i - 1] * P.n[i - 1]);
+    for (int i = d - 1; i >= 0; --i) right[i] = std::min(big, right[i + 1] * P.n[i]);
+    for (int i = 1; i < d; ++i) {
+      int64_t cpi = std::min(left[i], right[i]);
+      if (max_rank > 0) cpi = std::min(cpi, max_rank);
+      cap[i] = std::max(cpi, r_init[i]);
+    }
+  }
+  P.cap = cap;
+  P.r = r_init;
+  E.op_off = op.off;
+  E.rhs_off = b.off;
+  E.rb = b.r;
+  // two-site sizes
+  int64_t n2max = 1, svdw = 1, mop_total = 0, mb_total = 0;
+  std::vector<int64_t> mop_off(d, 0), mb_off(d, 0);
+  for (int i = 0; i + 1 < d; ++i) {
+    const int64_t a = cap[i], nn = P.n[i] * P.n[i + 1], s = cap[i + 2];
+    n2max = std::max(n2max, a * nn * s);
+    E.maxT = std::max(E.maxT, std::max(P.R[i], P.R[i + 2]) * a * nn * s);
+    E.maxU = std::max(E.maxU, a * nn * std::max(E.rb[i], E.rb[i + 2]));
+    require(std::min(a * P.n[i], P.n[i + 1] * s) <= 1024, TTALS_ERR_UNSUPPORTED,
+            "MALS: bond dimension above 1024 (set max_rank)");
+    svdw = std::max(svdw, (int64_t)svd_trunc_work_doubles(a * P.n[i], P.n[i + 1] * s));
+    mop_off[i] = mop_total;
+    mop_total += P.R[i] * nn * nn * P.R[i + 2];
+    mb_off[i] = mb_total;
+    mb_total += E.rb[i] * nn * E.rb[i + 2];
+  }
+  E.maxN = std::max(E.maxN, n2max);
+  E.maxCore = std::max(E.maxCore, n2max);
+  Bump B{c};
+  alloc_common(E, B, op.total, b.total, x0.total, 1);
+  E.Lb.resize(d);
+  E.Rb.resize(d);
+  for (int i = 0; i < d; ++i) {
+    B.want(&E.Lb[i], E.rb[i] * cap[i]);
+    B.want(&E.Rb[i], E.rb[i + 1] * cap[i + 1]);
+    E.maxU = std::max(E.maxU, cap[i] * P.n[i] * std::max(E.rb[i], E.rb[i + 1]));
+    E.maxU = std::max(E.maxU, cap[i + 1] * P.n[i] * E.rb[i + 1]);
+  }
+  B.want(&E.U, E.maxU);
+  double *mop = nullptr, *mb = nullptr, *x2 = nullptr, *cbuf = nullptr, *sbuf = nullptr, *swork = nullptr,
+         *kept = nullptr;
+  B.want(&mop, std::max<int64_t>(mop_total, 1));
+  B.want(&mb, std::max<int64_t>(mb_total, 1));
+  B.want(&x2, n2max);
+  B.want(&cbuf, n2max);
+  B.want(&sbuf, n2max);
+  B.want(&swork, svdw);
+  B.want(&kept, 1);
+  B.commit();
+  int* kdev = reinterpret_cast<int*>(kept);
+
+  CK(cudaEventRecord(c->ev0, c->stream));
+  upload(c, E.op, op);
+  upload(c, E.rhs, b);
+  upload(c, E.x0, x0);
+  init_barrier(E);
+  for (int i = 0; i < d; ++i)
+    CK(cudaMemcpyAsync(E.X[i], E.x0 + x0.off[i], sizeof(double) * (x0.off[i + 1] - x0.off[i]),
+                       cudaMemcpyDeviceToDevice, c->stream));
+  for (int i = 0; i + 1 < d; ++i) {
+    CK(launch_contract<double>(desc_merge_op(P.R[i], P.n[i], P.R[i + 1], P.n[i + 1], P.R[i + 2]),
+                               E.op + op.off[i], E.op + op.off[i + 1], mop + mop_off[i], 1.0, 0.0, c->stream));
+    CK(launch_contract<double>(desc_merge_vec(E.rb[i], P.n[i], E.rb[i + 1], P.n[i + 1], E.rb[i + 2]),
+                               E.rhs + b.off[i], E.rhs + b.off[i + 1], mb + mb_off[i], 1.0, 0.0, c->stream));
+  }
+
+  auto Aop = [&](int i) { return E.op + E.op_off[i]; };
+  auto Bc = [&](int i) { return E.rhs + E.rhs_off[i]; };
+  auto right = [&](int i) {
+    if (i == d - 1) {
+      set_ones(E, E.Rt[i]);
+      set_ones(E, E.Rb[i]);
+      return;
+    }
+    const int64_t a = P.r[i + 1], n = P.n[i + 1], s = P.r[i + 2];
+    stack_right_op(c, E.Rt[i + 1], E.X[i + 1], Aop(i + 1), a, n, s, P.R[i + 1], P.R[i + 2], E.T1, E.T2, E.Rt[i]);
+    stack_right_vec(c, E.Rb[i + 1], Bc(i + 1), E.X[i + 1], a, n, s, E.rb[i + 1], E.rb[i + 2], E.U, E.Rb[i]);
+  };
+  auto left = [&](int i) {
+    if (i == 0) {
+      set_ones(E, E.L[i]);
+      set_ones(E, E.Lb[i]);
+      return;
+    }
+    const int64_t a = P.r[i - 1], n = P.n[i - 1], s = P.r[i];
+    stack_left_op(c, E.L[i - 1], E.X[i - 1], Aop(i - 1), a, n, s, P.R[i - 1], P.R[i], E.T1, E.T2, E.L[i]);
+    stack_left_vec(c, E.Lb[i - 1], Bc(i - 1), E.X[i - 1], a, n, s, E.rb[i - 1], E.rb[i], E.U, E.Lb[i]);
+  };
+  // two-site solve of (i, i+1) into x2 (r_i, n_i n_{i+1}, r_{i+2})
+  auto solve_pair = [&](int i) {
+    const int64_t a = P.r[i], nn = P.n[i] * P.n[i + 1], s = P.r[i + 2];
+    micro_vec(c, E.Lb[i], mb + mb_off[i], E.Rb[i + 1], a, nn, s, E.rb[i], E.rb[i + 2], E.U, E.f);
+    LocalShape sh{a, nn, s, P.R[i], P.R[i + 2]};
+    CK(cudaMemsetAsync(x2, 0, sizeof(double) * sh.N(), c->stream));
+    GmresLaunch g{};
+    g.sh = sh;
+    g.L64 = E.L[i];
+    g.A64 = mop + mop_off[i];
+    g.R64 = E.Rt[i + 1];
+    g.T1_64 = E.T1;
+    g.T2_64 = E.T2;
+    g.f = E.f;
+    g.x = x2;
+    g.r = E.rvec;
+    g.partials = E.partials;
+    g.m = (int)std::min<int64_t>(E.m, sh.N());
+    g.tol = tol;
+    g.bar = E.bar;
+    g.status = E.status;
+    g.report = E.reports + 4 * (int64_t)(E.nsolve % E.solve_cap);
+    ++E.nsolve;
+    g.Li = g.L64;
+    g.Ai = g.A64;
+    g.Ri = g.R64;
+    g.T1i = E.T1;
+    g.T2i = E.T2;
+    g.V = E.V;
+    g.w = E.w;
+    g.max_cycles = 60;
+    g.inner_floor = 0.0;
+    g.precision = 0;
+    timed_solve(E, sh, 0, [&] { CK(launch_gmres(g, E.c->num_sms, E.c->stream)); });
+  };
+  auto read_k = [&]() {
+    int k = 0;
+    CK(cudaMemcpyAsync(&k, kdev, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return (int64_t)k;
+  };
+
+  for (int i = d - 1; i >= 1; --i) right(i);
+  for (int sweep = 0; sweep < repeats; ++sweep) {
+    for (int i = 0; i + 1 < d; ++i) {
+      left(i);
+      if (i < d - 2) {
+        solve_pair(i);
+        const int64_t p = P.r[i] * P.n[i], q = P.n[i + 1] * P.r[i + 2];
+        CK(launch_svd_trunc(x2, p, q, 0, threshold, max_rank, swork, cbuf, sbuf, kdev, E.status, c->stream));
+        const int64_t k = read_k();
+        CK(cudaMemcpyAsync(E.X[i], cbuf, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+        P.r[i + 1] = k;
+      }
+    }
+    for (int i = d - 2; i >= 0; --i) {
+      right(i + 1);
+      solve_pair(i);
+      const int64_t p = P.r[i] * P.n[i], q = P.n[i + 1] * P.r[i + 2];
+      CK(launch_svd_trunc(x2, p, q, 1, threshold, max_rank, swork, cbuf, sbuf, kdev, E.status, c->stream));
+      const int64_t k = read_k();
+      CK(cudaMemcpyAsync(E.X[i + 1], cbuf, sizeof(double) * k * q, cudaMemcpyDeviceToDevice, c->stream));
+      if (i == 0) CK(cudaMemcpyAsync(E.X[0], sbuf, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+      P.r[i + 1] = k;
+    }
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
+  download_x(E, out, out_dev, out_ranks);
+  check_status(E);
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  fill_stats(E, st, ms);
+}
+
+// ---------------------------------------------------------------------------
 // batched driver: one CTA per request (kernels_batch.cu)
 // ---------------------------------------------------------------------------
 
@@ -1415,6 +1639,32 @@ int ttals_sle_als(ttals_ctx* c, const ttals_tt* op, const ttals_tt* x0, const tt
                   int64_t* out_ranks, ttals_stats* stats) {
   return guarded(c, [&] {
     run_sle(c, op, x0, rhs, repeats, solver, precision, tol, out_data, out_on_device, out_ranks, stats);
+  });
+}
+
+int ttals_sle_mals(ttals_ctx* c, const ttals_tt* op, const ttals_tt* x0, const ttals_tt* b, int32_t repeats,
+                   int32_t solver, double threshold, int64_t max_rank, double tol, double* out_data,
+                   int32_t out_on_device, int64_t* out_ranks, int64_t* out_capacity, ttals_stats* stats) {
+  return guarded(c, [&] {
+    if (out_capacity && !out_data) {
+      // capacity query: doubles the output may need
+      TTView o = view(op, "operator"), x = view(x0, "initial_guess");
+      const int d = o.d;
+      std::vector<int64_t> r0 = x.r, left(d + 1, 1), right(d + 1, 1), cp(d + 1, 1);
+      const int64_t big = int64_t(1) << 40;
+      for (int i = 1; i <= d; ++i) left[i] = std::min(big, left[i - 1] * o.m[i - 1]);
+      for (int i = d - 1; i >= 0; --i) right[i] = std::min(big, right[i + 1] * o.m[i]);
+      for (int i = 1; i < d; ++i) {
+        int64_t v = std::min(left[i], right[i]);
+        if (max_rank > 0) v = std::min(v, max_rank);
+        cp[i] = std::max(v, r0[i]);
+      }
+      int64_t tot = 0;
+      for (int i = 0; i < d; ++i) tot += cp[i] * o.m[i] * cp[i + 1];
+      *out_capacity = tot;
+      return;
+    }
+    run_mals(c, op, x0, b, repeats, solver, threshold, max_rank, tol, out_data, out_on_device, out_ranks, stats);
   });
 }
 

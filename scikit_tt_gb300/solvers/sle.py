@@ -75,8 +75,33 @@ def als(operator: 'TT', initial_guess: 'TT', right_hand_side: 'TT', repeats: int
 
 def mals(operator: 'TT', initial_guess: 'TT', right_hand_side: 'TT', repeats: int = 1, solver: str = 'solve',
          threshold: float = 1e-12, max_rank: int = np.inf) -> 'TT':
-    """Two-site MALS (sle.py:98) is not on the device path yet."""
-    raise NotImplementedError('sle.mals is not implemented on the device path')
+    """Modified ALS (two-site, rank-adaptive), signature of sle.py:98.
+
+    Each pair of neighbouring cores is solved as one merged site by the device
+    matrix-free GMRES, then split by a truncated SVD (singular values with
+    sigma_k / sigma_0 <= ``threshold`` dropped, at most ``max_rank`` kept), in
+    the reference's sweep order (sle.py:128-189).  Ranks above 1024 on a bond
+    need a ``max_rank``."""
+    global last_stats
+    if solver not in _lib.SLE_SOLVERS:
+        raise ValueError("solver must be 'solve' or 'lu'")
+    if operator.order < 2:
+        raise NotImplementedError('mals needs at least two cores')
+    op, x0, b = _lib.Packed(operator.cores), _lib.Packed(initial_guess.cores), _lib.Packed(right_hand_side.cores)
+    lib = _lib.load()
+    mr = 0 if max_rank == np.inf else int(max_rank)
+    cap = np.zeros(1, dtype=np.int64)
+    _lib.check(lib.ttals_sle_mals(_lib.context(), op.desc, x0.desc, b.desc, int(repeats), _lib.SLE_SOLVERS[solver],
+                                  float(threshold), mr, 0.0, None, 0, None, _lib.i64ptr(cap), None))
+    out = np.empty(max(int(cap[0]), 1), dtype=np.float64)
+    out_ranks = np.zeros(operator.order + 1, dtype=np.int64)
+    st = _lib.Stats()
+    _lib.check(lib.ttals_sle_mals(_lib.context(), op.desc, x0.desc, b.desc, int(repeats), _lib.SLE_SOLVERS[solver],
+                                  float(threshold), mr, 0.0, _lib.dptr(out), 0, _lib.i64ptr(out_ranks), None, st))
+    last_stats = st.as_dict()
+    if repeats == 0:
+        return initial_guess.copy()
+    return TT(_lib.unpack(out, operator.row_dims, [1] * operator.order, out_ranks))
 
 
 # ---------------------------------------------------------------------------
@@ -130,8 +155,20 @@ def __construct_micro_matrix_als(i: int, stack_left_op: List[np.ndarray], stack_
 
 
 def __construct_micro_matrix_mals(i, stack_left_op, stack_right_op, operator, solution):
-    """Two-site micro matrix (sle.py:350-390): MALS is not on the device path yet."""
-    raise NotImplementedError('MALS micro matrices are not implemented on the device path')
+    """Dense two-site micro matrix (sle.py:350-390): the one-site assembly of the
+    merged site (mode n_i n_{i+1}, operator core A_i x A_{i+1}) on the device."""
+    A1, A2 = operator.cores[i], operator.cores[i + 1]
+    n1, n2 = A1.shape[1], A2.shape[1]
+    merged = np.einsum('abcd,defg->abecfg', A1, A2).reshape(A1.shape[0], n1 * n2, n1 * n2, A2.shape[3])
+    r0, r1 = solution.ranks[i], solution.ranks[i + 2]
+    L = np.ascontiguousarray(stack_left_op[i], dtype=np.float64)
+    Rt = np.ascontiguousarray(stack_right_op[i + 1], dtype=np.float64)
+    A = np.ascontiguousarray(merged, dtype=np.float64)
+    N = r0 * n1 * n2 * r1
+    out = np.empty((N, N), dtype=np.float64)
+    _lib.check(_lib.load().ttals_micro_matrix(_lib.context(), _lib.dptr(L), _lib.dptr(A), _lib.dptr(Rt), r0, n1 * n2,
+                                              r1, A.shape[0], A.shape[3], _lib.dptr(out), 0))
+    return out
 
 
 def als_batch(problems, repeats=1, precision: str = None, tol: float = 0.0):

@@ -223,6 +223,27 @@ def trunc_cases():
     np.savez_compressed(os.path.join(HERE, 'ttops_trunc.npz'), **out)
 
 
+def mals_case(name, op, rhs, x0, repeats, threshold, max_rank, solver='solve'):
+    sol = rsle.mals(RTT([c.copy() for c in op]), RTT([c.copy() for c in x0]), RTT([c.copy() for c in rhs]),
+                    repeats=repeats, solver=solver, threshold=threshold, max_rank=max_rank)
+    out = {'repeats': np.array(repeats), 'threshold': np.array(threshold),
+           'max_rank': np.array(-1 if max_rank == np.inf else max_rank), 'solver': np.array(solver),
+           'ranks': np.array(sol.ranks), 'full': np.asarray(sol.full()).reshape(-1)}
+    pack('op', op, out)
+    pack('rhs', rhs, out)
+    pack('x0', x0, out)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'ranks', sol.ranks)
+
+
+def mals_cases():
+    w = wl.laplace_sle(d=6, n=4, rhs_rank=2, x_rank=2, repeats=2)
+    mals_case('sle_mals_laplace_d6', w.op, w.rhs, w.x0, 2, 1e-12, np.inf)
+    mals_case('sle_mals_laplace_d6_r4', w.op, w.rhs, w.x0, 2, 1e-12, 4)
+    w2 = wl.coupled_sle(d=5, n=4, rhs_rank=3, x_rank=3, repeats=1)
+    mals_case('sle_mals_coupled_d5_lu', w2.op, w2.rhs, w2.x0, 1, 1e-10, 8, 'lu')
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -254,6 +275,7 @@ def main():
     power_cases()
     ode_cases()
     trunc_cases()
+    mals_cases()
 
 
 if __name__ == '__main__':
@@ -265,5 +287,7 @@ if __name__ == '__main__':
         ode_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'trunc':
         trunc_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'mals':
+        mals_cases()
     else:
         main()

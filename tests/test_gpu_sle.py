@@ -125,3 +125,20 @@ def test_sle_singular_operator_raises():
     x0 = [rng.standard_normal((1, 3, 1, 1)) for _ in range(3)]
     with pytest.raises(np.linalg.LinAlgError):
         sle.als(_tt(op), _tt(x0), _tt(rhs), repeats=1)
+
+
+@pytest.mark.parametrize('name', ['sle_mals_laplace_d6', 'sle_mals_laplace_d6_r4', 'sle_mals_coupled_d5_lu'])
+def test_mals_matches_reference(golden, name):
+    # two-site MALS: merged-site matrix-free solve + one-sided Jacobi SVD split
+    from scikit_tt_gb300.solvers import sle
+    z, cores = golden(name)
+    mr = int(z['max_rank'])
+    sol = sle.mals(_tt(cores('op')), _tt(cores('x0')), _tt(cores('rhs')), repeats=int(z['repeats']),
+                   solver=str(z['solver']), threshold=float(z['threshold']), max_rank=np.inf if mr < 0 else mr)
+    ref = z['full']
+    v = O.full_vector(sol.cores)
+    assert np.linalg.norm(v - ref) / np.linalg.norm(ref) < 1e-9
+    if mr > 0:
+        assert list(sol.ranks) == list(z['ranks'])
+    else:
+        assert max(abs(a - b) for a, b in zip(sol.ranks, z['ranks'])) <= 2
