@@ -383,9 +383,11 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
     s_res = 0.0;
   }
 
-  // V_0 = x / |x| + 0.01 z / |z| (normalised), z a fixed pseudo-random vector: a
-  // start vector inside one symmetry sector of the local operator would keep
-  // the whole Krylov space there and miss the wanted eigenvalues of the others
+  // V_0 = x / |x| + eps z / |z| (normalised), z a fixed pseudo-random vector.
+  // With several wanted eigenpairs, a start vector inside one symmetry sector
+  // of the local operator would keep the whole Krylov space there and miss the
+  // wanted eigenvalues of the other sectors: eps = 0.01.  A single eigenpair
+  // keeps the pure warm start (eps = 0), whose residual is already small.
   {
     auto noise = [](int e) {
       uint32_t hsh = (uint32_t)e * 2654435761u ^ 0x9e3779b9u;
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(kKThreads, 1) lanczos_kernel(LanczosK k) {
     rb ^= 1;
     const double nx = sqrt(h1[0]), nz = sqrt(h1[1]);
     const bool ok = nx > 0.0 && isfinite(nx);
-    const double eps = 0.01;
+    const double eps = kev > 1 ? 0.01 : 0.0;
     const double ax = ok ? 1.0 / nx : 0.0, az = eps / nz;
     const double nv = sqrt(fmax((ok ? 1.0 : 0.0) + eps * eps + 2.0 * ax * az * h1[2], 1e-300));
     for (int e = e0 + tid; e < e1; e += nt) k.V[e] = (ax * k.x[e] + az * noise(e)) / nv;
