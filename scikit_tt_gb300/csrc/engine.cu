@@ -2056,8 +2056,9 @@ int ttals_apply_f32(ttals_ctx* c, const float* L, const float* A, const float* R
     require(a > 0 && n > 0 && s > 0 && R0 > 0 && R1 > 0, TTALS_ERR_ARG, "dimensions must be positive");
     const int64_t nl = a * R0 * a, na = R0 * n * n * R1, nr = s * R1 * s, N = a * n * s;
     const int64_t nt = std::max(R0, R1) * N;
-    float *dl, *da, *dr, *dy, *t1, *t2, *dout;
+    float *dl, *da, *dr, *dy, *t1, *t2, *dout, *kt;
     Bump B{c};
+    B.want(&kt, 2048);  // contraction-offset table: 2 x 1024 ints
     B.want(&dl, nl);
     B.want(&da, na);
     B.want(&dr, nr);
@@ -2070,7 +2071,7 @@ int ttals_apply_f32(ttals_ctx* c, const float* L, const float* A, const float* R
     CK(cudaMemcpyAsync(da, A, 4 * na, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dr, Rt, 4 * nr, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dy, y, 4 * N, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_apply_f32(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, c->stream));
+    CK(launch_apply_f32(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, reinterpret_cast<int*>(kt), c->stream));
     CK(cudaMemcpyAsync(out, dout, 4 * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   });

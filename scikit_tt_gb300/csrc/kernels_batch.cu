@@ -34,11 +34,14 @@ constexpr int kBatchThreads = 128;  // four CTAs per SM: FP32 and FP64 phases of
 
 // Inlined body (used inside the Krylov loops); `c` must not alias C.
 template <typename T>
-__device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C) {
+__device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C,
+                                                  int* ktab = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
-    // FP32 (inner Krylov) contractions go to the tensor cores when GEMM-shaped
-    __shared__ int ktab[2 * kTcMaxK];
-    if (cta_gemm_tf32x3(c, A, B, C, ktab)) return;
+    // FP32 (inner Krylov) contractions go to the tensor cores when GEMM-shaped;
+    // the contraction-offset table lives in per-CTA global scratch (L1
+    // resident): this kernel is memory-latency bound and every KB of shared
+    // memory is taken from L1
+    if (ktab && cta_gemm_tf32x3(c, A, B, C, ktab)) return;
   }
   constexpr int VW = DefaultVW<T>::value;
   if (contract_vec_ok<T, VW>(c, B, C)) {
@@ -59,10 +62,9 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
 __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const double* A, const double* B, double* C,
                                               const OzScratch* oz) {
   __shared__ Contraction sc;
-  __shared__ int oktab[2 * kTcMaxK];
   if (threadIdx.x == 0) sc = cref;
   __syncthreads();
-  if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oktab)) return;
+  if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
   cta_contract_body<double>(sc, A, B, C);
 }
 
@@ -129,10 +131,11 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
 // y -> out = M y (three contraction phases through T1, T2)
 template <typename T>
 __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
-                                          const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out) {
-  cta_contract_body(p1, L, y, T1);
-  cta_contract_body(p2, T1, A, T2);
-  cta_contract_body(p3, T2, R, out);
+                                          const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out,
+                                          int* ktab = nullptr) {
+  cta_contract_body(p1, L, y, T1, ktab);
+  cta_contract_body(p2, T1, A, T2, ktab);
+  cta_contract_body(p3, T2, R, out, ktab);
 }
 
 // ---------------------------------------------------------------------------
@@ -216,25 +219,49 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     __syncthreads();
     int jj = 0;
     for (int j = 0; j < m; ++j) {
-      cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w);
+      cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr);
       cta_dots<TI>(V, N, j + 1, w, h1);
-      for (int64_t e = tid; e < N; e += nt) {
-        TI acc = w[e];
-        for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
-        w[e] = acc;
-      }
-      __syncthreads();
-      cta_dots<TI>(V, N, j + 1, w, h2);
-      double hn2 = h2[j + 1];
-      for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
-      const double hn = sqrt(fmax(hn2, 0.0));
-      if (hn > 0.0) {
-        const TI inv = (TI)(1.0 / hn);
-        TI* vn = V + (int64_t)(j + 1) * N;
+      // Classical Gram-Schmidt with selective reorthogonalisation (FP32 inner
+      // solves): one projection suffices when it keeps at least 1/sqrt(2) of the
+      // norm ("twice is enough" criterion); then the projection and the
+      // normalisation are one pass over the basis.  The FP64 solver always
+      // projects twice.
+      double wn2 = h1[j + 1], hn2 = wn2;
+      for (int q = 0; q <= j; ++q) hn2 -= h1[q] * h1[q];
+      const bool single = sizeof(TI) == 4 && hn2 >= 0.5 * wn2;
+      double hn;
+      if (single) {
+        if (tid == 0)
+          for (int q = 0; q <= j + 1; ++q) h2[q] = 0.0;
+        hn = sqrt(fmax(hn2, 0.0));
+        if (hn > 0.0) {
+          const TI inv = (TI)(1.0 / hn);
+          TI* vn = V + (int64_t)(j + 1) * N;
+          for (int64_t e = tid; e < N; e += nt) {
+            TI acc = w[e];
+            for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
+            vn[e] = acc * inv;
+          }
+        }
+      } else {
         for (int64_t e = tid; e < N; e += nt) {
           TI acc = w[e];
-          for (int q = 0; q <= j; ++q) acc -= (TI)h2[q] * V[(int64_t)q * N + e];
-          vn[e] = acc * inv;
+          for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
+          w[e] = acc;
+        }
+        __syncthreads();
+        cta_dots<TI>(V, N, j + 1, w, h2);
+        hn2 = h2[j + 1];
+        for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
+        hn = sqrt(fmax(hn2, 0.0));
+        if (hn > 0.0) {
+          const TI inv = (TI)(1.0 / hn);
+          TI* vn = V + (int64_t)(j + 1) * N;
+          for (int64_t e = tid; e < N; e += nt) {
+            TI acc = w[e];
+            for (int q = 0; q <= j; ++q) acc -= (TI)h2[q] * V[(int64_t)q * N + e];
+            vn[e] = acc * inv;
+          }
         }
       }
       if (tid == 0) {
@@ -448,6 +475,8 @@ __device__ __forceinline__ void signal_done(int* flag) {
 // one instance
 // ---------------------------------------------------------------------------
 
+__host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp);
+
 struct Scratch {
   double *T1, *T2, *U, *f, *r, *w, *V, *rbuf, *qwork, *tmp0, *tmp1;
   float *Vf, *wf, *T1f, *T2f, *Lf, *Rf, *Af;
@@ -487,6 +516,7 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   s.oz.bs = (uint16_t*)take(2 * z.oz_b);
   s.oz.rexp = (int*)take(4 * z.oz_r);
   s.oz.cexp = (int*)take(4 * z.oz_c);
+  s.oz.ktab = nullptr;  // set by the kernel: a shared-memory table
   s.oz.cap_a = z.oz_a;
   s.oz.cap_b = z.oz_b;
   s.oz.cap_r = z.oz_r;
@@ -875,7 +905,8 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
 __global__ void __launch_bounds__(kBatchThreads, 4) batch_sle_kernel(BatchArgs a) {
   extern __shared__ double sm[];
   __shared__ int s_j;
-  const Scratch S = scratch_of(a, blockIdx.x);
+  Scratch S = scratch_of(a, blockIdx.x);
+  S.oz.ktab = reinterpret_cast<int*>(reinterpret_cast<char*>(sm) + batch_smem_scalar_bytes(a.m, a.m_evp));
   for (;;) {
     if (threadIdx.x == 0) s_j = atomicAdd(a.next, 1);
     __syncthreads();
@@ -918,7 +949,7 @@ __global__ void __launch_bounds__(kBatchThreads) apply_f64emu_kernel(Contraction
 size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
   BatchSizes z{};
   oz_need_site(z, a, n, s, R0, R1);
-  return (size_t)(2 * z.oz_a + 2 * z.oz_b + 4 * z.oz_r + 4 * z.oz_c + 4 * 256);
+  return (size_t)(2 * z.oz_a + 2 * z.oz_b + 4 * z.oz_r + 4 * z.oz_c + 4 * 2 * kTcMaxK + 5 * 256);
 }
 
 cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const double* L,
@@ -937,6 +968,8 @@ cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int
   p += rnd(4 * z.oz_r);
   oz.cexp = (int*)p;
   p += rnd(4 * z.oz_c);
+  oz.ktab = (int*)p;
+  p += rnd(4 * 2 * kTcMaxK);
   if ((size_t)(p - ozmem) > ozbytes) return cudaErrorInvalidValue;
   oz.cap_a = z.oz_a;
   oz.cap_b = z.oz_b;
@@ -952,23 +985,32 @@ cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int
 // Diagnostic: one CTA applies the FP32 local operator (tensor-core path).
 __global__ void __launch_bounds__(kBatchThreads) apply_f32_kernel(Contraction p1, Contraction p2, Contraction p3,
                                                                   const float* L, const float* A, const float* R,
-                                                                  const float* y, float* T1, float* T2, float* out) {
-  cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out);
+                                                                  const float* y, float* T1, float* T2, float* out,
+                                                                  int* ktab) {
+  cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
 }
 
 cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
-                             const float* R, const float* y, float* T1, float* T2, float* out, cudaStream_t st) {
+                             const float* R, const float* y, float* T1, float* T2, float* out, int* ktab,
+                             cudaStream_t st) {
   Contraction p1, p2, p3;
   desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
-  apply_f32_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out);
+  apply_f32_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
   ++launch_counter();
   return cudaGetLastError();
 }
 
-size_t batch_smem_bytes(int m, int m_evp) {
+// dynamic shared memory: the GMRES / Lanczos scalars, then one contraction-offset
+// table shared by the FP32 tensor-core apply and the emulated-FP64 contractions
+// (never used at the same time); the rest of the SM's 256 KB stays L1
+__host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp) {
   const size_t g = (size_t)(m + 1) * m + 2 * m + (m + 1) + m + 2 * (m + 2);
   const size_t e = (size_t)10 * m_evp + 12 + m_evp / 2 + 1;  // Lanczos arrays + pivots
   return sizeof(double) * (g > e ? g : e);
+}
+
+size_t batch_smem_bytes(int m, int m_evp) {
+  return batch_smem_scalar_bytes(m, m_evp) + sizeof(int) * 2 * kTcMaxK;
 }
 
 int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {

@@ -58,6 +58,7 @@ cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int
                                 double* out, char* ozmem, size_t ozbytes, cudaStream_t st);
 size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1);
 cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
-                             const float* R, const float* y, float* T1, float* T2, float* out, cudaStream_t st);
+                             const float* R, const float* y, float* T1, float* T2, float* out, int* ktab,
+                             cudaStream_t st);
 
 }  // namespace ttals

@@ -111,6 +111,7 @@ struct OzScratch {
   uint16_t* bs;  // S slices of B, column-major [j][k_pad] (bf16 bits)
   int* rexp;     // E_i
   int* cexp;     // F_j
+  int* ktab;     // 2 * kTcMaxK contraction offsets (global: shared memory is left to L1)
   int64_t cap_a, cap_b, cap_r, cap_c;  // capacities (elements)
 };
 
