@@ -25,6 +25,11 @@
 // which keeps the refinement residual and the stacks of the mixed path far
 // below its 1e-10 local tolerance; the plain FP64 path never uses this.
 //
+// Slices are stored in mma-fragment order (oz_word_pos), so that one lane
+// fetches all six slices of a fragment with three 16-byte loads, and are cut
+// with coalesced reads: one thread per row when the operand's rows are
+// unit-stride, one warp per row (lanes along the contraction) otherwise.
+//
 // Operands containing NaN/Inf (or contractions that are not GEMM-shaped or
 // too long) return false and the caller falls back to native FP64.
 #pragma once
@@ -111,12 +116,22 @@ struct OzScratch {
   uint16_t* bs;  // S slices of B, column-major [j][k_pad] (bf16 bits)
   int* rexp;     // E_i
   int* cexp;     // F_j
-  int* ktab;     // 2 * kTcMaxK contraction offsets (global: shared memory is left to L1)
+  int* ktab;     // 2 * kTcMaxK contraction offsets
   int64_t cap_a, cap_b, cap_r, cap_c;  // capacities (elements)
 };
 
 // C = contraction(A, B) with FP64-level accuracy on the BF16 tensor cores,
 // executed by the whole CTA.  ktab: 2 * kTcMaxK ints of shared memory.
+//
+// Slice layout (both operands): for row i (A) / column j (B), 16-step block kb
+// of the contraction and quad lane t, the 12 words [p][h] (slice p, h = 0 for
+// k = 16kb + 2t..2t+1, h = 1 for k = 16kb + 2t+8..2t+9) are contiguous, so one
+// lane fetches all six slices of its mma fragment with three 128-bit loads.
+__device__ __forceinline__ int oz_word_pos(int i, int w, int nkb) {
+  const int kb = w >> 3, wl = w & 7;
+  return (((i * nkb + kb) << 2) + (wl & 3)) * 12 + (wl >> 2);
+}
+
 __device__ __forceinline__ bool cta_gemm_ozaki(const Contraction& c, const double* __restrict__ A,
                                                const double* __restrict__ B, double* __restrict__ C,
                                                const OzScratch& z, int* ktab) {
@@ -143,88 +158,152 @@ __device__ __forceinline__ bool cta_gemm_ozaki(const Contraction& c, const doubl
     koffB[kk] = ob;
   }
   __syncthreads();
-  // row exponents of A and column exponents of B (one warp per row / column)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = warp; i < M + N; i += nw) {
-    const bool isrow = i < M;
-    int op, dummy;
-    gemm_axes_offsets(isrow ? rows : cols, isrow ? i : i - M, op, dummy);
-    unsigned long long amax = 0;
-    for (int kk = lane; kk < K; kk += 32) {
-      const double v = isrow ? A[op + koffA[kk]] : B[op + koffB[kk]];
-      const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
-      amax = ab > amax ? ab : amax;
-    }
+  const int Kw = Kp >> 1, nkb = Kp >> 4;
+  // exponents and slices, one warp per row (A) / column (B), four in flight
+  constexpr int kRows = 4;
+  for (int side = 0; side < 2; ++side) {
+    const GemmAxes& ax = side == 0 ? rows : cols;
+    const double* __restrict__ src = side == 0 ? A : B;
+    const int* koff = side == 0 ? koffA : koffB;
+    int* ex = side == 0 ? z.rexp : z.cexp;
+    uint32_t* dst = reinterpret_cast<uint32_t*>(side == 0 ? z.as : z.bs);
+    const int MN = side == 0 ? M : N;
+    if (ax.n > 0 && ax.sop[ax.n - 1] == 1 && MN >= (int)blockDim.x) {
+      // rows (columns) are unit-stride in the operand and at least one per
+      // thread: one thread per row, so that consecutive lanes read consecutive
+      // addresses; each thread writes its fragment chunks (12 words) with three
+      // 16-byte stores.  Otherwise one warp per row, lanes along the contraction.
+      for (int i = threadIdx.x; i < MN; i += blockDim.x) {
+        int op, dummy;
+        gemm_axes_offsets(ax, i, op, dummy);
+        unsigned long long amax = 0;
+#pragma unroll 4
+        for (int k = 0; k < K; ++k) {
+          const unsigned long long b = (unsigned long long)__double_as_longlong(src[op + koff[k]]) & 0x7fffffffffffffffull;
+          amax = b > amax ? b : amax;
+        }
+        if (amax >= 0x7ff0000000000000ull) s_bad = 1;
+        const int E = oz_exponent_bits(amax);
+        ex[i] = E;
+        uint32_t* base = dst + (int64_t)i * nkb * 48;
+        for (int kb = 0; kb < nkb; ++kb) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long other = __shfl_xor_sync(0xffffffffu, amax, o);
-      amax = other > amax ? other : amax;
+          for (int t = 0; t < 4; ++t) {
+            uint32_t wv[12];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int k0 = 2 * (kb * 8 + t + 4 * h);
+              const uint64_t b0 = k0 < K ? (uint64_t)__double_as_longlong(src[op + koff[k0]]) : 0ull;
+              const uint64_t b1 = k0 + 1 < K ? (uint64_t)__double_as_longlong(src[op + koff[k0 + 1]]) : 0ull;
+              const uint64_t m0 = oz_fixed48(b0, E), m1 = oz_fixed48(b1, E);
+              const uint32_t s0 = (uint32_t)(b0 >> 48) & 0x8000u, s1 = (uint32_t)(b1 >> 48) & 0x8000u;
+#pragma unroll
+              for (int p = 0; p < kOzSlices; ++p) wv[2 * p + h] = oz_slice_bf16(m0, s0, p) | (oz_slice_bf16(m1, s1, p) << 16);
+            }
+            uint4* q = reinterpret_cast<uint4*>(base + (kb * 4 + t) * 12);
+            q[0] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+            q[1] = make_uint4(wv[4], wv[5], wv[6], wv[7]);
+            q[2] = make_uint4(wv[8], wv[9], wv[10], wv[11]);
+          }
+        }
+      }
+      continue;
     }
-    // NaN / Inf have the all-ones exponent: larger than every finite magnitude
-    if (lane == 0 && amax >= 0x7ff0000000000000ull) s_bad = 1;
-    if (lane == 0) {
-      if (isrow)
-        z.rexp[i] = oz_exponent_bits(amax);
-      else
-        z.cexp[i - M] = oz_exponent_bits(amax);
+    for (int ib = warp * kRows; ib < MN; ib += nw * kRows) {
+      int op[kRows];
+#pragma unroll
+      for (int u = 0; u < kRows; ++u) {
+        int dummy;
+        op[u] = 0;
+        if (ib + u < MN) gemm_axes_offsets(ax, ib + u, op[u], dummy);
+      }
+      unsigned long long amax[kRows];
+#pragma unroll
+      for (int u = 0; u < kRows; ++u) amax[u] = 0;
+      for (int w = lane; w < Kw; w += 32) {
+        const int k0 = 2 * w;
+#pragma unroll
+        for (int u = 0; u < kRows; ++u) {
+          if (ib + u < MN) {
+            const unsigned long long b0 =
+                k0 < K ? (unsigned long long)__double_as_longlong(src[op[u] + koff[k0]]) & 0x7fffffffffffffffull : 0;
+            const unsigned long long b1 =
+                k0 + 1 < K ? (unsigned long long)__double_as_longlong(src[op[u] + koff[k0 + 1]]) & 0x7fffffffffffffffull
+                           : 0;
+            const unsigned long long m = b0 > b1 ? b0 : b1;
+            amax[u] = m > amax[u] ? m : amax[u];
+          }
+        }
+      }
+      int E[kRows];
+#pragma unroll
+      for (int u = 0; u < kRows; ++u) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long other = __shfl_xor_sync(0xffffffffu, amax[u], o);
+          amax[u] = other > amax[u] ? other : amax[u];
+        }
+        // NaN / Inf have the all-ones exponent: larger than every finite magnitude
+        if (amax[u] >= 0x7ff0000000000000ull) s_bad = 1;
+        E[u] = oz_exponent_bits(amax[u]);
+        if (lane == 0 && ib + u < MN) ex[ib + u] = E[u];
+      }
+      for (int w = lane; w < Kw; w += 32) {
+        const int k0 = 2 * w;
+#pragma unroll
+        for (int u = 0; u < kRows; ++u) {
+          if (ib + u < MN) {
+            const uint64_t b0 = k0 < K ? (uint64_t)__double_as_longlong(src[op[u] + koff[k0]]) : 0ull;
+            const uint64_t b1 = k0 + 1 < K ? (uint64_t)__double_as_longlong(src[op[u] + koff[k0 + 1]]) : 0ull;
+            const uint64_t m0 = oz_fixed48(b0, E[u]), m1 = oz_fixed48(b1, E[u]);
+            const uint32_t s0 = (uint32_t)(b0 >> 48) & 0x8000u, s1 = (uint32_t)(b1 >> 48) & 0x8000u;
+            uint32_t* d = dst + oz_word_pos(ib + u, w, nkb);
+#pragma unroll
+            for (int p = 0; p < kOzSlices; ++p) d[2 * p] = oz_slice_bf16(m0, s0, p) | (oz_slice_bf16(m1, s1, p) << 16);
+          }
+        }
+      }
     }
   }
   __syncthreads();
   if (s_bad) return false;
-  // slice A (row-major, k contiguous) and B (column-major, k contiguous), zero-padded to Kp
-  const int Kw = Kp >> 1;  // 32-bit words (bf16 pairs) per slice row
-  uint32_t* as32w = reinterpret_cast<uint32_t*>(z.as);
-  uint32_t* bs32w = reinterpret_cast<uint32_t*>(z.bs);
-  for (int side = 0; side < 2; ++side) {
-    const GemmAxes& ax = side == 0 ? rows : cols;
-    const double* src = side == 0 ? A : B;
-    const int* koff = side == 0 ? koffA : koffB;
-    const int* ex = side == 0 ? z.rexp : z.cexp;
-    uint32_t* dst = side == 0 ? as32w : bs32w;
-    const int MN = side == 0 ? M : N;
-    for (int64_t e = threadIdx.x; e < (int64_t)MN * Kw; e += blockDim.x) {
-      const int i = (int)(e / Kw), kk = 2 * (int)(e - (int64_t)i * Kw);
-      int op, dummy;
-      gemm_axes_offsets(ax, i, op, dummy);
-      const uint64_t b0 = kk < K ? (uint64_t)__double_as_longlong(src[op + koff[kk]]) : 0ull;
-      const uint64_t b1 = kk + 1 < K ? (uint64_t)__double_as_longlong(src[op + koff[kk + 1]]) : 0ull;
-      const int E = ex[i];
-      const uint64_t m0 = oz_fixed48(b0, E), m1 = oz_fixed48(b1, E);
-      const uint32_t s0 = (uint32_t)(b0 >> 48) & 0x8000u, s1 = (uint32_t)(b1 >> 48) & 0x8000u;
-#pragma unroll
-      for (int p = 0; p < kOzSlices; ++p)
-        dst[(int64_t)p * MN * Kw + e] = oz_slice_bf16(m0, s0, p) | (oz_slice_bf16(m1, s1, p) << 16);
-    }
-  }
-  __syncthreads();
   const int g = lane >> 2, t = lane & 3;
   const int tilesM = (M + 15) >> 4, tilesN = (N + 7) >> 3;
-  const uint32_t* as32 = as32w;
-  const uint32_t* bs32 = bs32w;
+  const uint4* as4 = reinterpret_cast<const uint4*>(z.as);
+  const uint4* bs4 = reinterpret_cast<const uint4*>(z.bs);
   for (int tile = warp; tile < tilesM * tilesN; tile += nw) {
     const int tm = tile / tilesN, tn = tile - tm * tilesN;
     const int r0 = tm * 16 + g, r1 = r0 + 8, cb = tn * 8 + g;
     const int rr0 = r0 < M ? r0 : M - 1, rr1 = r1 < M ? r1 : M - 1, ccb = cb < N ? cb : N - 1;
     // running double-float sum of all levels and chunks (FP32 only)
     float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k0 = 0; k0 < Kp; k0 += kOzChunk) {
+    for (int kb0 = 0; kb0 < nkb; kb0 += kOzChunk / 16) {
       float acc[kOzSlices][4];
 #pragma unroll
       for (int L = 0; L < kOzSlices; ++L) acc[L][0] = acc[L][1] = acc[L][2] = acc[L][3] = 0.f;
-      const int kend = k0 + kOzChunk < Kp ? k0 + kOzChunk : Kp;
-      for (int kk = k0; kk < kend; kk += 16) {
-        const int w = (kk >> 1) + t;  // word of columns (kk + 2t, kk + 2t + 1)
+      const int kbe = kb0 + kOzChunk / 16 < nkb ? kb0 + kOzChunk / 16 : nkb;
+      for (int kb = kb0; kb < kbe; ++kb) {
+        const uint4* pa0 = as4 + (((int64_t)rr0 * nkb + kb) * 4 + t) * 3;
+        const uint4* pa1 = as4 + (((int64_t)rr1 * nkb + kb) * 4 + t) * 3;
+        const uint4* pb = bs4 + (((int64_t)ccb * nkb + kb) * 4 + t) * 3;
+        uint32_t wa0[12], wa1[12], wb[12];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const uint4 x0 = pa0[q], x1 = pa1[q], y = pb[q];
+          wa0[4 * q] = x0.x; wa0[4 * q + 1] = x0.y; wa0[4 * q + 2] = x0.z; wa0[4 * q + 3] = x0.w;
+          wa1[4 * q] = x1.x; wa1[4 * q + 1] = x1.y; wa1[4 * q + 2] = x1.z; wa1[4 * q + 3] = x1.w;
+          wb[4 * q] = y.x; wb[4 * q + 1] = y.y; wb[4 * q + 2] = y.z; wb[4 * q + 3] = y.w;
+        }
         uint32_t af[kOzSlices][4], bf[kOzSlices][2];
 #pragma unroll
         for (int p = 0; p < kOzSlices; ++p) {
-          const uint32_t* ap = as32 + (int64_t)p * M * Kw;
-          const uint32_t* bp = bs32 + (int64_t)p * N * Kw;
-          af[p][0] = ap[(int64_t)rr0 * Kw + w];
-          af[p][1] = ap[(int64_t)rr1 * Kw + w];
-          af[p][2] = ap[(int64_t)rr0 * Kw + w + 4];
-          af[p][3] = ap[(int64_t)rr1 * Kw + w + 4];
-          bf[p][0] = bp[(int64_t)ccb * Kw + w];
-          bf[p][1] = bp[(int64_t)ccb * Kw + w + 4];
+          af[p][0] = wa0[2 * p];
+          af[p][1] = wa1[2 * p];
+          af[p][2] = wa0[2 * p + 1];
+          af[p][3] = wa1[2 * p + 1];
+          bf[p][0] = wb[2 * p];
+          bf[p][1] = wb[2 * p + 1];
         }
 #pragma unroll
         for (int p = 0; p < kOzSlices; ++p)
