@@ -251,7 +251,10 @@ def other_workloads(lib, ctx, args):
     # d 16..48, rank 16..64), replayed in real time for a bounded window
     window = args.serve_window
     items = list(wl.serving_stream(rate=2000.0, duration=window))
-    fin, wall, stats = run_stream(items, window, precision='mixed', max_batch=608, max_jobs=64)
+    from scikit_tt_gb300 import _lib as L_
+    slots = L_.C.c_int32(0)
+    L_.check(lib.ttals_batch_slots(ctx, L_.C.byref(slots)))
+    fin, wall, stats = run_stream(items, window, precision='mixed', max_batch=int(slots.value), max_jobs=64)
     lat = np.array([r.done - r.arrival for r in fin])
     kinds = np.array([r.kind for r in fin])
     out['serving_poisson_2000'] = {
@@ -294,7 +297,9 @@ def main_gpu(args):
     stream = torch.cuda.current_stream(dev)
     _lib.check(lib.ttals_set_stream(ctx, _lib.C.c_void_p(stream.cuda_stream)))
     C = _lib.C
-    B = args.batch or 4 * torch.cuda.get_device_properties(dev).multi_processor_count
+    slots = C.c_int32(0)
+    _lib.check(lib.ttals_batch_slots(ctx, C.byref(slots)))
+    B = args.batch or int(slots.value)
 
     # B independent seeded instances per rank (weak scaling: each rank its own batch)
     inst = [wl.coupled_sle(seed=rank * B + j, **WORKLOAD) for j in range(B)]
@@ -471,7 +476,7 @@ def main():
     ap.add_argument('--steps', type=int, default=5)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--batch', type=int, default=0, help='solves per step and GPU (default 4 x SM count)')
+    ap.add_argument('--batch', type=int, default=0, help='solves per step and GPU (default: resident CTAs x SMs)')
     ap.add_argument('--quick', action='store_true', help='headline only (skip the other workloads)')
     ap.add_argument('--serve-window', type=float, default=0.1, help='seconds of Poisson arrivals to replay')
     args = ap.parse_args()

@@ -139,6 +139,11 @@ int ttals_sle_mals(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const
                    int32_t solver, double threshold, int64_t max_rank, double tol, double* out_data,
                    int32_t out_on_device, int64_t* out_ranks, int64_t* out_capacity, ttals_stats* stats);
 
+/* Number of requests one batched launch runs at the same time on this device
+ * (SMs x resident CTAs per SM): a batch of this size keeps every SM busy.  No
+ * reference counterpart. */
+int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
+
 /* Batched scikit_tt/solvers/sle.py:10 `als`: `count` independent systems
  * (each with its own order, mode sizes and ranks) solved in one launch, one
  * CTA per system.  out_data[j] receives system j's cores with the ranks

@@ -1758,6 +1758,13 @@ int ttals_job_finish(ttals_job* j, ttals_stats* stats) {
   return st;
 }
 
+int ttals_batch_slots(ttals_ctx* c, int32_t* slots) {
+  return guarded(c, [&] {
+    require(slots != nullptr, TTALS_ERR_ARG, "null output pointer");
+    *slots = c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp);
+  });
+}
+
 int ttals_sle_als_batch(ttals_ctx* c, int32_t count, const ttals_tt* ops, const ttals_tt* x0s,
                         const ttals_tt* rhss, const int32_t* repeats, int32_t precision, double tol,
                         double* const* out_data, int32_t out_on_device, ttals_stats* stats) {
