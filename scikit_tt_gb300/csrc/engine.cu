@@ -189,23 +189,26 @@ void push_left(ttals_ctx* c, const double* R, const double* X, int64_t k, int64_
   CK(launch_contract<double>(desc_push_left(k, s, q), R, X, out, 1.0, 0.0, c->stream));
 }
 
+// work of one QR call: the Householder kernel's (W, reflectors, Q, tau) or the
+// CholeskyQR2 path's (flag, partial Gram matrices, factors), whichever is larger,
+// plus the flag slot in front of the Householder fallback's region
 int64_t qr_work(int64_t rows, int64_t cols) {
   const int64_t k = std::min(rows, cols);
-  return rows * cols + 2 * rows * k + k;
+  return 8 + std::max(rows * cols + 2 * rows * k + k, cqr_work_doubles(cols));
 }
 
 // forward QR of core (a*n x s): Q -> core (a, n, k), R (k x s) -> rbuf
 void qr_forward(ttals_ctx* c, double* core, int64_t a, int64_t n, int64_t s, double* rbuf, double* work) {
   const int64_t rows = a * n, cols = s, k = std::min(rows, cols);
   QrArgs q{core, s, 1, core, k, 1, rbuf, s, 1, rows, cols, 0, nullptr, work};
-  CK(launch_qr(q, c->stream));
+  CK(launch_qr_fast(q, c->stream));
 }
 // backward RQ of core (a x n*s): Q -> core (k, n, s), R (a x k) -> rbuf
 void rq_backward(ttals_ctx* c, double* core, int64_t a, int64_t n, int64_t s, double* rbuf, double* work,
                  int normalize, double* rnorm) {
   const int64_t ns = n * s, k = std::min(a, ns);
   QrArgs q{core, 1, ns, core, 1, ns, rbuf, 1, k, ns, a, normalize, rnorm, work};
-  CK(launch_qr(q, c->stream));
+  CK(launch_qr_fast(q, c->stream));
 }
 
 // ---------------------------------------------------------------------------
@@ -1855,7 +1858,7 @@ int ttals_tt_ortho(ttals_ctx* c, const ttals_tt* t_t, int32_t direction, int32_t
       for (int i = std::max(0, first); i <= std::min(last, d - 2); ++i) {
         const int64_t a = r[i], n = mn[i], s = r[i + 1], k = std::min(a * n, s);
         QrArgs q{core[i], s, 1, core[i], k, 1, rbuf, s, 1, a * n, s, 0, nullptr, work};
-        CK(launch_qr(q, c->stream));
+        CK(launch_qr_fast(q, c->stream));
         const int64_t qq = mn[i + 1] * r[i + 2];
         push_left(c, rbuf, core[i + 1], k, s, qq, tmp);
         CK(cudaMemcpyAsync(core[i + 1], tmp, sizeof(double) * k * qq, cudaMemcpyDeviceToDevice, c->stream));
@@ -1865,7 +1868,7 @@ int ttals_tt_ortho(ttals_ctx* c, const ttals_tt* t_t, int32_t direction, int32_t
       for (int i = std::min(first, d - 1); i >= std::max(1, last); --i) {
         const int64_t a = r[i], ns = mn[i] * r[i + 1], k = std::min(a, ns);
         QrArgs q{core[i], 1, ns, core[i], 1, ns, rbuf, 1, k, ns, a, 0, nullptr, work};
-        CK(launch_qr(q, c->stream));
+        CK(launch_qr_fast(q, c->stream));
         const int64_t p = r[i - 1] * mn[i - 1];
         push_right(c, core[i - 1], rbuf, p, a, k, tmp);
         CK(cudaMemcpyAsync(core[i - 1], tmp, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));

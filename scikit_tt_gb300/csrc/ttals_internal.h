@@ -66,6 +66,10 @@ struct QrArgs {
   double* work;
 };
 cudaError_t launch_qr(const QrArgs& a, cudaStream_t st);
+// CholeskyQR2 over many CTAs for tall cores (Householder fallback on the device
+// when the Gram matrix is not numerically SPD); a.work: qr_work_fast doubles
+cudaError_t launch_qr_fast(const QrArgs& a, cudaStream_t st);
+int64_t cqr_work_doubles(int64_t cols);
 
 // ---------------------------------------------------------------------------
 // persistent Krylov solvers (kernels_krylov.cu)
