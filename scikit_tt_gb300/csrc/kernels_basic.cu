@@ -41,9 +41,23 @@ cudaError_t launch_contract(const Contraction& c, const T* A, const T* B, T* C, 
                             cudaStream_t st) {
   if (c.total <= 0) return cudaSuccess;
   if (c.total >= (int64_t(1) << 31)) return cudaErrorInvalidValue;  // 32-bit index arithmetic
-  int64_t blocks = (c.total + 255) / 256;
+  // Spread the outputs over every SM: FP64 runs at two lanes a clock per SM, so a
+  // small contraction in 256-thread blocks would sit on a few SMs.  Blocks shrink
+  // (down to one warp) until there are about two per SM.
+  static int sms[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && sms[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = v > 0 ? v : 1;
+  }
+  const int64_t nsm = (dev >= 0 && dev < 64) ? sms[dev] : 1;
+  int64_t threads = (c.total + 2 * nsm - 1) / (2 * nsm);
+  threads = std::max<int64_t>(32, std::min<int64_t>(256, (threads + 31) / 32 * 32));
+  int64_t blocks = (c.total + threads - 1) / threads;
   blocks = std::min<int64_t>(blocks, 65535);
-  contract_kernel<T><<<(unsigned)blocks, 256, 0, st>>>(c, A, B, C, alpha, beta);
+  contract_kernel<T><<<(unsigned)blocks, (unsigned)threads, 0, st>>>(c, A, B, C, alpha, beta);
   ++launch_counter();
   return cudaGetLastError();
 }
