@@ -42,6 +42,11 @@ namespace ttals {
 
 constexpr int kOzSlices = 6;
 constexpr int kOzChunk = 64;  // contraction steps per exact FP32 accumulation chunk
+// The fragment-ordered slice layout below (oz_word_pos, the 16-byte slice stores
+// and loads) packs 2 words x 6 slices = 12 words = three 16-byte vectors per
+// (row, 16-step block, quad lane) chunk; the scratch capacity is kOzSlices
+// values per element.  Both must change together.
+static_assert(kOzSlices == 6, "the fragment-ordered slice layout is built for exactly 6 slices");
 
 __device__ __forceinline__ void mma_bf16_16x8x16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
   asm volatile(
