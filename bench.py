@@ -72,9 +72,35 @@ def site_sizes(w):
     return sizes
 
 
+LU_CAP = 8192   # dense LU timed on the leading LU_CAP x LU_CAP block, scaled by (N / LU_CAP)^3 (larger N only)
+
+
+def lu_note(n):
+    return 'LU solve at full size' if n <= LU_CAP else f'LU solve on the leading {LU_CAP} block scaled by (N/{LU_CAP})^3'
+
+
+def _stack_left(prev, x, a):
+    """L_new[s,R',s'] = sum L[a,R,a'] x[a,n,s] A[R,m,n,R'] x[a',m,s'] as three pairwise
+    contractions, the pattern of sle.py:217-219 (a single four-operand einsum runs
+    without intermediates at these shapes and is two orders of magnitude slower)."""
+    t1 = np.tensordot(prev, x, axes=([0], [0]))
+    t2 = np.tensordot(t1, a, axes=([0, 2], [0, 2]))
+    return np.tensordot(t2, x, axes=([0, 2], [0, 1]))
+
+
+def _stack_right(nxt, x, a):
+    """R_new[a,R,a'] = sum x[a,n,s] A[R,m,n,R'] x[a',m,s'] R[s,R',s'] (sle.py:274-276)."""
+    t1 = np.tensordot(x, nxt, axes=([2], [0]))
+    t2 = np.tensordot(t1, a, axes=([1, 2], [2, 3]))
+    return np.tensordot(t2, x, axes=([3, 1], [1, 2]))
+
+
 def cpu_sample(w, nsites=2):
-    """Time ``nsites`` full-size local steps (stack update, dense local matrix,
-    LU solve, QR) of the oracle and extrapolate to the whole run by N^3."""
+    """Time ``nsites`` full-size local steps of the oracle (stack update, dense
+    local matrix, LU solve, QR) and extrapolate to the whole run by N^3.  The
+    LU solve, the cubic part, is timed on the leading LU_CAP x LU_CAP block of
+    the local matrix and scaled by (N / LU_CAP)^3, so that a sample costs
+    seconds, not minutes, of CPU time."""
     from oracle import tt_oracle as O
     d = len(w.op)
     cores = O.ortho_right(w.x0)
@@ -83,7 +109,7 @@ def cpu_sample(w, nsites=2):
     sr_op[d - 1], sr_b[d - 1] = np.ones((1, 1, 1)), np.ones((1, 1))
     for i in range(d - 2, -1, -1):
         x = cores[i + 1][:, :, 0, :]
-        sr_op[i] = O.stack_right_op(sr_op[i + 1], x, w.op[i + 1])
+        sr_op[i] = _stack_right(sr_op[i + 1], x, w.op[i + 1])
         sr_b[i] = O.stack_right_vec(sr_b[i + 1], x, b[i + 1][:, :, 0, :])
     L, Lb = np.ones((1, 1, 1)), np.ones((1, 1))
     times, ns = [], []
@@ -92,17 +118,28 @@ def cpu_sample(w, nsites=2):
         t0 = time.perf_counter()
         if i > 0:
             x = cores[i - 1][:, :, 0, :]
-            L = O.stack_left_op(L, x, w.op[i - 1])
+            L = _stack_left(L, x, w.op[i - 1])
             Lb = O.stack_left_vec(Lb, x, b[i - 1][:, :, 0, :])
         M = O.micro_matrix(L, w.op[i], sr_op[i])
         f = O.micro_vec(Lb, b[i][:, :, 0, :], sr_b[i])
-        y = np.linalg.solve(M, f)
         a, n, s = ranks[i], w.op[i].shape[1], ranks[i + 1]
+        N = a * n * s
+        t_build = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        if N > LU_CAP:
+            # time the cubic part on the leading block; the sweep goes on with the
+            # current core (only the time of this step is sampled)
+            np.linalg.solve(M[:LU_CAP, :LU_CAP], f[:LU_CAP])
+            t_solve = (time.perf_counter() - t1) * (N / LU_CAP) ** 3
+            y = cores[i].reshape(-1)
+        else:
+            y = np.linalg.solve(M, f)
+            t_solve = time.perf_counter() - t1
+        t2 = time.perf_counter()
         q, _ = np.linalg.qr(y.reshape(a * n, s))
         ranks[i + 1] = q.shape[1]
         cores[i] = q.reshape(a, n, 1, q.shape[1])
-        dt = time.perf_counter() - t0
-        N = a * n * s
+        dt = t_build + t_solve + (time.perf_counter() - t2)
         if N == max(site_sizes(w)):
             times.append(dt)
             ns.append(N)
@@ -134,7 +171,7 @@ def run_reference(args):
         est, k, nmax = cpu_sample(w, nsites=1)
         vals.append(1.0 / est)
     v = float(np.median(vals))
-    sample = f'{1} local step(s) at N={nmax} per step (stack, dense N x N matrix, LU solve, QR), ' \
+    sample = f'1 local step at N={nmax} per step (stack, dense N x N matrix, {lu_note(nmax)}, QR), ' \
              f'extrapolated by N^3 to the {len(site_sizes(w))} local solves of one run'
     line = {
         'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': UNIT, 'n_gpus': args.gpus, 'steps': args.steps,
@@ -462,8 +499,8 @@ def main_gpu(args):
                                            'frac': plain_ach64 / p64.value, 'bound': 'fp64 pipe',
                                            'peak_source': 'FP64 FMA-chain microbenchmark (ttals_measure_peaks)'}},
         'cpu_baseline': {'value': 1.0 / cpu_est, 'unit': UNIT, 'cores': cpu_threads(), 'kind': 'port',
-                         'sample': f'{nsamp} oracle local steps at N={nmax} (stack, dense matrix, LU, QR), '
-                                   f'extrapolated by N^3 to all local solves of one solve'},
+                         'sample': f'{nsamp} oracle local steps at N={nmax} (stack, dense matrix, '
+                                   f'{lu_note(nmax)}, QR), extrapolated by N^3 to all local solves of one solve'},
         'clocks': clk.summary(),
         'other_workloads': extra,
     }
