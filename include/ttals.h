@@ -111,6 +111,13 @@ int ttals_set_stream(ttals_ctx* ctx, void* stream);
  * per launch) and report it in ttals_stats.  No reference counterpart. */
 int ttals_set_profiling(ttals_ctx* ctx, int32_t enable);
 
+/* Failure-detection probe: one device thread waits, through the engine's
+ * bounded spin (the one every grid barrier uses), for a flag to leave 0 --
+ * set beforehand when preset != 0, never set otherwise.  *status_out receives
+ * TTALS_OK or TTALS_ERR_TIMEOUT (limit polls of ~64 ns, at most 2^22).  The
+ * context stays usable either way.  No reference counterpart. */
+int ttals_wait_probe(ttals_ctx* ctx, int32_t preset, uint32_t limit, int32_t* status_out);
+
 /* Measured arithmetic peaks of this device (FMA-chain microbenchmarks), in
  * GFLOP/s.  Used to state roofline fractions.  No reference counterpart. */
 int ttals_measure_peaks(ttals_ctx* ctx, double* fp64_gflops, double* fp32_gflops);

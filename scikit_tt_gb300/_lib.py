@@ -35,7 +35,7 @@ EVP_SOLVERS = {'eig': 0, 'eigs': 1, 'eigh': 2}
 # every symbol include/ttals.h declares
 EXPORTS = (
     'ttals_create', 'ttals_destroy', 'ttals_last_error', 'ttals_set_stream', 'ttals_als_ranks',
-    'ttals_batch_slots', 'ttals_sle_als', 'ttals_sle_mals', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_ortho_trunc', 'ttals_tt_norm',
+    'ttals_batch_slots', 'ttals_wait_probe', 'ttals_sle_als', 'ttals_sle_mals', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_ortho_trunc', 'ttals_tt_norm',
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
     'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_apply_f32',
@@ -104,6 +104,7 @@ def load():
                                       dbl, pd, pd, i32, pi64, P(i32), P(Stats)]
         lib.ttals_tt_matmul.argtypes = [vp, P(TTDesc), P(TTDesc), pd, i32]
         lib.ttals_batch_slots.argtypes = [vp, C.POINTER(i32)]
+        lib.ttals_wait_probe.argtypes = [vp, i32, C.c_uint32, C.POINTER(i32)]
         lib.ttals_tt_ortho.argtypes = [vp, P(TTDesc), i32, i32, i32, pd, i32, pi64]
         lib.ttals_tt_ortho_trunc.argtypes = [vp, P(TTDesc), i32, i32, i32, C.c_double, pi64, pd, i32, pi64]
         lib.ttals_tt_norm.argtypes = [vp, P(TTDesc), pd]

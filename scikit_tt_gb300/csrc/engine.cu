@@ -1616,6 +1616,26 @@ int ttals_set_stream(ttals_ctx* c, void* stream) {
   return TTALS_OK;
 }
 
+int ttals_wait_probe(ttals_ctx* c, int32_t preset, uint32_t limit, int32_t* status_out) {
+  return guarded(c, [&] {
+    require(status_out != nullptr, TTALS_ERR_ARG, "null output pointer");
+    require(limit >= 1 && limit <= (1u << 22), TTALS_ERR_ARG, "limit must be in [1, 2^22] polls");
+    double* mem = nullptr;
+    Bump B{c};
+    B.want(&mem, 1);
+    B.commit();
+    unsigned* flag = reinterpret_cast<unsigned*>(mem);
+    int* status = reinterpret_cast<int*>(flag + 1);
+    const unsigned init[2] = {preset ? 1u : 0u, 0u};
+    CK(cudaMemcpyAsync(flag, init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_wait_probe(flag, limit, status, c->stream));
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *status_out = st == ST_TIMEOUT ? TTALS_ERR_TIMEOUT : (st == ST_OK ? TTALS_OK : TTALS_ERR_CUDA);
+  });
+}
+
 int ttals_set_profiling(ttals_ctx* c, int32_t enable) {
   if (!c) return TTALS_ERR_ARG;
   c->profiling = enable != 0;

@@ -348,6 +348,23 @@ cudaError_t launch_qr_fast(const QrArgs& a, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
+// failure-detection probe: the engine's bounded wait on a flag
+// ---------------------------------------------------------------------------
+
+// Waits (bounded) for *flag to leave 0; records ST_TIMEOUT in *status when the
+// limit runs out.  With a flag that nothing sets this exercises the timeout
+// path of every device-side wait without hanging or faulting anything.
+__global__ void wait_probe_kernel(const unsigned* flag, unsigned limit, int* status) {
+  if (threadIdx.x == 0 && !bounded_wait_change(flag, 0u, limit)) atomicCAS(status, ST_OK, ST_TIMEOUT);
+}
+
+cudaError_t launch_wait_probe(const unsigned* flag, unsigned limit, int* status, cudaStream_t st) {
+  wait_probe_kernel<<<1, 32, 0, st>>>(flag, limit, status);
+  ++launch_counter();
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // arithmetic peak microbenchmark: 8 independent FMA chains per thread
 // ---------------------------------------------------------------------------
 

@@ -307,6 +307,18 @@ __device__ __forceinline__ int ld_acquire_s32(const int* p) {
   return v;
 }
 
+// Polls *p (acquire) until it differs from `old`, at most `limit` times with a
+// 64 ns sleep between polls; false when the limit ran out.  Every spin-wait of
+// the engine goes through here.
+__device__ __forceinline__ bool bounded_wait_change(const unsigned* p, unsigned old, unsigned limit) {
+  unsigned spins = 0;
+  while (ld_acquire_u32(p) == old) {
+    if (++spins > limit) return false;
+    __nanosleep(64);
+  }
+  return true;
+}
+
 // Returns false (all threads of the CTA) if the barrier timed out or another
 // CTA has already flagged an error in *status.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b, int* status) {
@@ -320,16 +332,9 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, int* status) {
     if (arrived == gridDim.x - 1) {
       *b.count = 0u;
       st_release_u32(b.gen, g + 1u);
-    } else {
-      unsigned spins = 0;
-      while (ld_acquire_u32(b.gen) == g) {
-        if (++spins > kSpinLimit) {
-          atomicCAS(status, ST_OK, ST_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
+    } else if (!bounded_wait_change(b.gen, g, kSpinLimit)) {
+      atomicCAS(status, ST_OK, ST_TIMEOUT);
+      ok = 0;
     }
     if (ok && ld_acquire_s32(status) != ST_OK) ok = 0;
     s_ok = ok;

@@ -137,6 +137,9 @@ size_t svd_trunc_work_doubles(int64_t p, int64_t q);
 cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
                              double* work, double* core, double* r, int* kept, int* status, cudaStream_t st);
 
+// failure-detection probe (kernels_basic.cu): bounded wait on *flag leaving 0
+cudaError_t launch_wait_probe(const unsigned* flag, unsigned limit, int* status, cudaStream_t st);
+
 // engine.cu helpers used by the allocation-free entry point (noalloc.cu)
 }  // namespace ttals
 struct ttals_ctx;
