@@ -305,7 +305,7 @@ def other_workloads(lib, ctx, args):
     return out
 
 
-def _desc_array(lib_mod, packs, bufs=None):
+def _desc_array(lib_mod, packs, bufs=None, on_device=1):
     C = lib_mod.C
     arr = (lib_mod.TTDesc * len(packs))()
     for k, p in enumerate(packs):
@@ -313,7 +313,7 @@ def _desc_array(lib_mod, packs, bufs=None):
             arr[k] = p.desc
         else:
             arr[k] = lib_mod.TTDesc(p.order, lib_mod.i64ptr(p.row), lib_mod.i64ptr(p.col), lib_mod.i64ptr(p.ranks),
-                                    C.cast(bufs[k].data_ptr(), C.POINTER(C.c_double)), 1)
+                                    C.cast(bufs[k].data_ptr(), C.POINTER(C.c_double)), on_device)
     return arr
 
 
@@ -345,19 +345,22 @@ def main_gpu(args):
     dev_ops = _desc_array(_lib, [pk[0] for pk in packs], [b[0] for b in dbufs])
     dev_x0s = _desc_array(_lib, [pk[1] for pk in packs], [b[1] for b in dbufs])
     dev_rhs = _desc_array(_lib, [pk[2] for pk in packs], [b[2] for b in dbufs])
-    host_ops = _desc_array(_lib, [pk[0] for pk in packs])
-    host_x0s = _desc_array(_lib, [pk[1] for pk in packs])
-    host_rhs = _desc_array(_lib, [pk[2] for pk in packs])
+    # end-to-end leg: inputs and outputs in pinned host memory (filled once, outside the timed region)
+    hbufs = [[torch.from_numpy(p.data).pin_memory() for p in pk] for pk in packs]
+    host_ops = _desc_array(_lib, [pk[0] for pk in packs], [b[0] for b in hbufs], 0)
+    host_x0s = _desc_array(_lib, [pk[1] for pk in packs], [b[1] for b in hbufs], 0)
+    host_rhs = _desc_array(_lib, [pk[2] for pk in packs], [b[2] for b in hbufs], 0)
     dims = np.array([c.shape[1] for c in inst[0].op], dtype=np.int64)
     out_ranks = np.zeros(len(dims) + 1, dtype=np.int64)
     _lib.check(lib.ttals_als_ranks(len(dims), _lib.i64ptr(dims), _lib.i64ptr(packs[0][1].ranks),
                                    _lib.i64ptr(out_ranks)))
     out_n = int(sum(out_ranks[i] * dims[i] * out_ranks[i + 1] for i in range(len(dims))))
     out_dev = torch.empty((B, out_n), dtype=torch.float64, device=dev)
-    out_host = np.empty((B, out_n), dtype=np.float64)
+    out_host = torch.empty((B, out_n), dtype=torch.float64, pin_memory=True)
     dev_ptrs = (C.POINTER(C.c_double) * B)(*[C.cast(out_dev[j].data_ptr(), C.POINTER(C.c_double))
                                              for j in range(B)])
-    host_ptrs = (C.POINTER(C.c_double) * B)(*[_lib.dptr(out_host[j]) for j in range(B)])
+    host_ptrs = (C.POINTER(C.c_double) * B)(*[C.cast(out_host[j].data_ptr(), C.POINTER(C.c_double))
+                                              for j in range(B)])
     reps = (C.c_int32 * B)(*([WORKLOAD['repeats']] * B))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -435,7 +438,7 @@ def main_gpu(args):
         batch(_lib.PREC_MIXED, MIXED_TOL, on_device=False)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     h2d = sum(p.data.nbytes for pk in packs for p in pk)
-    d2h = out_host.nbytes
+    d2h = out_host.numel() * out_host.element_size()
 
     # roofline of the batch kernel (its CUDA-event duration, algorithmic flops from the kernel's own counters)
     sm_ = st_mixed[-1]
