@@ -195,6 +195,24 @@ int ttals_evp_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, int32_
                   double* out_vals, double* out_data, int32_t out_on_device, int64_t* out_ranks,
                   int32_t* iterations, ttals_stats* stats);
 
+/* Time-dependent variational principle, scikit_tt/solvers/ode.py:1188
+ * `tdvp1site` (kind 1), ode.py:1290 `tdvp2site` (kind 2) and the adaptive
+ * one-/two-site mix of ode.py:1076 `tdvp` (kind 0, exact local exponentials).
+ * Each step is x <- exp(tau H) x with REAL tau = -i * step_size (imaginary-time
+ * steps; the caller refuses complex exponents).  krylov_dim > 1: the local
+ * Krylov method of ode.py:1689 with that dimension where the reference uses it
+ * (local_solver 'krylov'); 0: converged Krylov exponentials with relative
+ * tolerance tol (<= 0: 1e-15) in place of scipy's expm_multiply.  threshold /
+ * max_rank (<= 0: unbounded) truncate the two-site SVDs; normalize 0/1/2 scales
+ * each step's state to unit 1- or 2-norm.  out receives the states after each
+ * of the `steps` steps back to back (capacity: steps * sum_i c_i n_i c_{i+1}
+ * doubles, c the initial ranks for kind 1, else min(prod left dims, prod
+ * right dims, max_rank) but at least the initial rank); out_ranks[steps*(d+1)]. */
+int ttals_tdvp(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, int32_t kind, double tau, int32_t steps,
+               int32_t krylov_dim, double threshold, int64_t max_rank, int32_t normalize, double tol,
+               double* out, int64_t out_capacity, int32_t out_on_device, int64_t* out_ranks,
+               ttals_stats* stats);
+
 /* scikit_tt/tensor_train.py:422-501 (`__matmul__` / `dot`): core-wise
  * product of two trains; out has ranks a.ranks[i] * b.ranks[i]. */
 int ttals_tt_matmul(ttals_ctx* ctx, const ttals_tt* a, const ttals_tt* b, double* out_data,

@@ -261,6 +261,7 @@ void check_status(Engine& E) {
   if (st == ST_TIMEOUT) throw Fail{TTALS_ERR_TIMEOUT, "device-side barrier wait timed out in a local solve"};
   if (st == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in a local solve"};
   if (st == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system (Krylov breakdown)"};
+  if (st == ST_NOCONV) throw Fail{TTALS_ERR_NOCONV, "a local exponential missed its tolerance within the substep limit"};
   if (st == ST_UNSUPPORTED)
     throw Fail{TTALS_ERR_UNSUPPORTED, "a wanted local eigenvalue is complex; the device path holds real cores only"};
   if (st != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(st)};
@@ -845,6 +846,349 @@ void run_mals(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const tta
   }
   CK(cudaEventRecord(c->ev1, c->stream));
   download_x(E, out, out_dev, out_ranks);
+  check_status(E);
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  fill_stats(E, st, ms);
+}
+
+// ---------------------------------------------------------------------------
+// TDVP time stepping (scikit_tt/solvers/ode.py:1076-1616)
+// ---------------------------------------------------------------------------
+//
+// x(t + h) = exp(tau H) x(t) with real tau (imaginary-time steps h = -i|h|, or
+// any step whose exponent -i h is real).  kind 1: one-site TDVP
+// (tdvp1site, ode.py:1188-1288 with __update_core_tdvp, 1398-1509); kind 2:
+// two-site TDVP (tdvp2site, ode.py:1290-1396 with __update_core_tdvp2site,
+// 1512-1614); kind 0: the adaptive mix of ode.py:1076-1186 (two-site update on
+// a bond whose rank is below max_rank and below both sides' dimensions, else
+// one-site), run with the exact local exponential.  Every local step is one
+// expm_kernel launch on the matrix-free local operator; the backward steps on
+// the bond matrices use the zero-site operator (left stack, identity operator
+// core, right stack), which equals the projected micro matrix q^H M q of the
+// reference.  kdim > 0 selects the fixed-dimension local Krylov recurrence
+// (ode.py:1689-1758) where the reference uses it; kdim == 0 the converged
+// Krylov exponential (scipy expm_multiply in the reference).  The initial
+// value's cores are used as given (no orthonormalisation), as in the
+// reference.  After each step the state is scaled to unit p-norm (normalize
+// = p > 0) and written to out.
+
+double tt_sum_host(const std::vector<std::vector<double>>& cores, const std::vector<int64_t>& n,
+                   const std::vector<int64_t>& r) {
+  // sum of all entries: v^T = v^T sum_k core[:, k, :] over the cores
+  std::vector<double> v(1, 1.0);
+  for (size_t i = 0; i < cores.size(); ++i) {
+    std::vector<double> nv((size_t)r[i + 1], 0.0);
+    for (int64_t a = 0; a < r[i]; ++a)
+      for (int64_t k = 0; k < n[i]; ++k)
+        for (int64_t s = 0; s < r[i + 1]; ++s) nv[s] += v[a] * cores[i][(a * n[i] + k) * r[i + 1] + s];
+    v.swap(nv);
+  }
+  return v[0];
+}
+
+void run_tdvp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int kind, double tau, int steps, int kdim,
+              double threshold, int64_t max_rank, int normalize, double tol, double* out, int64_t out_capacity,
+              int out_dev, int64_t* out_ranks, ttals_stats* st) {
+  TTView op = view(op_t, "operator"), x0 = view(x_t, "initial_value");
+  validate_square_op(op);
+  validate_vec(x0, op, "initial_value");
+  require(kind >= 0 && kind <= 2, TTALS_ERR_ARG, "kind must be 0 (adaptive), 1 (one-site) or 2 (two-site)");
+  require(steps >= 0, TTALS_ERR_ARG, "number_of_steps must be >= 0");
+  require(kdim >= 0 && kdim <= 64, TTALS_ERR_UNSUPPORTED, "local Krylov dimension must be between 1 and 64");
+  require(kdim != 1, TTALS_ERR_ARG, "local Krylov dimension must be larger than 1");
+  require(normalize >= 0 && normalize <= 2, TTALS_ERR_ARG, "normalize must be 0, 1 or 2");
+  require(std::isfinite(tau), TTALS_ERR_ARG, "step exponent must be finite");
+  require(threshold >= 0.0, TTALS_ERR_ARG, "threshold must be >= 0");
+  require(out != nullptr || steps == 0, TTALS_ERR_ARG, "output buffer is null");
+  require(kind == 1 || op.d >= 2, TTALS_ERR_UNSUPPORTED, "two-site TDVP needs at least two cores");
+  if (kind == 0) kdim = 0;
+  if (tol <= 0) tol = 1e-15;
+
+  launch_counter() = 0;
+  Engine E;
+  E.c = c;
+  E.m = 64;
+  auto& P = E.P;
+  const int d = op.d;
+  P.d = d;
+  P.n = op.m;
+  P.R = op.r;
+  P.rx0 = x0.r;
+  std::vector<int64_t> cap = P.rx0;
+  if (kind != 1) {
+    const int64_t big = int64_t(1) << 40;
+    std::vector<int64_t> lft(d + 1, 1), rgt(d + 1, 1);
+    for (int i = 1; i <= d; ++i) lft[i] = std::min(big, lft[i - 1] * P.n[i - 1]);
+    for (int i = d - 1; i >= 0; --i) rgt[i] = std::min(big, rgt[i + 1] * P.n[i]);
+    for (int i = 1; i < d; ++i) {
+      int64_t cpi = std::min(lft[i], rgt[i]);
+      if (max_rank > 0) cpi = std::min(cpi, max_rank);
+      cap[i] = std::max(cpi, P.rx0[i]);
+    }
+  }
+  P.cap = cap;
+  P.r = P.rx0;
+  E.op_off = op.off;
+  int64_t step_total = 0;
+  for (int i = 0; i < d; ++i) step_total += cap[i] * P.n[i] * cap[i + 1];
+  require(out_capacity >= (int64_t)steps * step_total, TTALS_ERR_ARG,
+          "output buffer too small: need number_of_steps * sum_i cap_i n_i cap_{i+1} doubles");
+
+  // two-site sizes
+  int64_t n2max = 1, svdw = 1, mop_total = 0, eye_total = 0;
+  std::vector<int64_t> mop_off(d, 0), eye_off(d + 1, 0);
+  if (kind != 1) {
+    for (int i = 0; i + 1 < d; ++i) {
+      const int64_t a = cap[i], nn = P.n[i] * P.n[i + 1], s = cap[i + 2];
+      n2max = std::max(n2max, a * nn * s);
+      E.maxT = std::max(E.maxT, std::max(P.R[i], P.R[i + 2]) * a * nn * s);
+      require(std::min(a * P.n[i], P.n[i + 1] * s) <= 1024, TTALS_ERR_UNSUPPORTED,
+              "two-site TDVP: bond dimension above 1024 (set max_rank)");
+      svdw = std::max(svdw, (int64_t)svd_trunc_work_doubles(a * P.n[i], P.n[i + 1] * s));
+      mop_off[i] = mop_total;
+      mop_total += P.R[i] * nn * nn * P.R[i + 2];
+    }
+  }
+  // zero-site operator cores: identity on each inner bond's operator rank
+  for (int b = 1; b < d; ++b) {
+    eye_off[b] = eye_total;
+    eye_total += P.R[b] * P.R[b];
+  }
+  E.maxN = std::max(E.maxN, n2max);
+  E.maxCore = std::max(E.maxCore, n2max);
+  Bump B{c};
+  alloc_common(E, B, op.total, 0, x0.total, 0);
+  double *mop = nullptr, *x2 = nullptr, *cbuf = nullptr, *sbuf = nullptr, *swork = nullptr, *kept = nullptr,
+         *eye = nullptr, *nrm = nullptr;
+  B.want(&mop, std::max<int64_t>(mop_total, 1));
+  B.want(&x2, n2max);
+  B.want(&cbuf, n2max);
+  B.want(&sbuf, n2max);
+  B.want(&swork, svdw);
+  B.want(&kept, 1);
+  B.want(&eye, std::max<int64_t>(eye_total, 1));
+  B.want(&nrm, 2);
+  B.commit();
+  int* kdev = reinterpret_cast<int*>(kept);
+
+  CK(cudaEventRecord(c->ev0, c->stream));
+  upload(c, E.op, op);
+  upload(c, E.x0, x0);
+  init_barrier(E);
+  for (int i = 0; i < d; ++i)
+    CK(cudaMemcpyAsync(E.X[i], E.x0 + x0.off[i], sizeof(double) * (x0.off[i + 1] - x0.off[i]),
+                       cudaMemcpyDeviceToDevice, c->stream));
+  if (eye_total > 0) {
+    std::vector<double> h((size_t)eye_total, 0.0);
+    for (int b = 1; b < d; ++b)
+      for (int64_t q = 0; q < P.R[b]; ++q) h[eye_off[b] + q * P.R[b] + q] = 1.0;
+    CK(cudaMemcpyAsync(eye, h.data(), sizeof(double) * eye_total, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));  // h is released on return
+  }
+  for (int i = 0; i + 1 < d && kind != 1; ++i)
+    CK(launch_contract<double>(desc_merge_op(P.R[i], P.n[i], P.R[i + 1], P.n[i + 1], P.R[i + 2]),
+                               E.op + op.off[i], E.op + op.off[i + 1], mop + mop_off[i], 1.0, 0.0, c->stream));
+
+  auto Aop = [&](int i) { return E.op + E.op_off[i]; };
+  auto right = [&](int i) {
+    if (i == d - 1) return set_ones(E, E.Rt[i]);
+    const int64_t a = P.r[i + 1], n = P.n[i + 1], s = P.r[i + 2];
+    stack_right_op(c, E.Rt[i + 1], E.X[i + 1], Aop(i + 1), a, n, s, P.R[i + 1], P.R[i + 2], E.T1, E.T2, E.Rt[i]);
+  };
+  auto left = [&](int i) {
+    if (i == 0) return set_ones(E, E.L[i]);
+    const int64_t a = P.r[i - 1], n = P.n[i - 1], s = P.r[i];
+    stack_left_op(c, E.L[i - 1], E.X[i - 1], Aop(i - 1), a, n, s, P.R[i - 1], P.R[i], E.T1, E.T2, E.L[i]);
+  };
+  // x <- exp(coef H_local) x on one local problem; literal: the reference's
+  // fixed-dimension local Krylov recurrence
+  auto expm = [&](const LocalShape& sh, const double* L, const double* A, const double* Rt, double* x, double coef,
+                  bool literal) {
+    ExpmLaunch l{};
+    l.sh = sh;
+    l.L = L;
+    l.A = A;
+    l.R = Rt;
+    l.T1 = E.T1;
+    l.T2 = E.T2;
+    l.x = x;
+    l.V = E.V;
+    l.w = E.w;
+    l.partials = E.partials;
+    l.literal = literal ? 1 : 0;
+    l.m = literal ? kdim : (int)std::min<int64_t>(E.m, sh.N());
+    l.max_substeps = 1000;
+    l.tau = coef;
+    l.tol = tol;
+    l.bar = E.bar;
+    l.status = E.status;
+    l.report = E.reports + 4 * (int64_t)(E.nsolve % E.solve_cap);
+    ++E.nsolve;
+    timed_solve(E, sh, 0, [&] { CK(launch_expm(l, c->num_sms, c->stream)); });
+  };
+  const bool local = kdim > 0;
+  auto expm1 = [&](int i, double coef, bool lit) {
+    LocalShape sh{P.r[i], P.n[i], P.r[i + 1], P.R[i], P.R[i + 1]};
+    expm(sh, E.L[i], Aop(i), E.Rt[i], E.X[i], coef, lit);
+  };
+  // bond matrix (a x s) between cores b-1 and b: left stack L[b], right stack Rt[b-1]
+  auto expm0 = [&](int b, int64_t a, int64_t s, double* buf, double coef, bool lit) {
+    LocalShape sh{a, 1, s, P.R[b], P.R[b]};
+    expm(sh, E.L[b], eye + eye_off[b], E.Rt[b - 1], buf, coef, lit);
+  };
+  auto expm2 = [&](int i, double coef, bool lit) {
+    const int64_t a = P.r[i], s = P.r[i + 2];
+    CK(launch_contract<double>(desc_merge_vec(a, P.n[i], P.r[i + 1], P.n[i + 1], s), E.X[i], E.X[i + 1], x2, 1.0,
+                               0.0, c->stream));
+    LocalShape sh{a, P.n[i] * P.n[i + 1], s, P.R[i], P.R[i + 2]};
+    expm(sh, E.L[i], mop + mop_off[i], E.Rt[i + 1], x2, coef, lit);
+  };
+  auto read_k = [&]() {
+    int k = 0;
+    CK(cudaMemcpyAsync(&k, kdev, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return (int64_t)k;
+  };
+  const double half = 0.5 * tau;
+
+  // one-site forward update of core i (< d-1): step, QR, bond back-step, push right
+  auto fwd1 = [&](int i, bool lit) {
+    expm1(i, half, lit);
+    const int64_t a = P.r[i], n = P.n[i], s = P.r[i + 1], k = std::min(a * n, s);
+    qr_forward(c, E.X[i], a, n, s, E.rbuf, E.qwork);
+    P.r[i + 1] = k;
+    left(i + 1);
+    expm0(i + 1, k, s, E.rbuf, -half, lit);
+    const int64_t q = P.n[i + 1] * P.r[i + 2];
+    push_left(c, E.rbuf, E.X[i + 1], k, s, q, E.tmp);
+    CK(cudaMemcpyAsync(E.X[i + 1], E.tmp, sizeof(double) * k * q, cudaMemcpyDeviceToDevice, c->stream));
+  };
+  // one-site backward update of core i (> 0): [step,] RQ, bond back-step, push left
+  auto bwd1 = [&](int i, bool step_core, bool lit) {
+    if (step_core) expm1(i, half, lit);
+    const int64_t a = P.r[i], n = P.n[i], s = P.r[i + 1], k = std::min(a, n * s);
+    rq_backward(c, E.X[i], a, n, s, E.rbuf, E.qwork, 0, nullptr);
+    P.r[i] = k;
+    right(i - 1);
+    expm0(i, a, k, E.rbuf, -half, lit);
+    const int64_t p = P.r[i - 1] * P.n[i - 1];
+    push_right(c, E.X[i - 1], E.rbuf, p, a, k, E.tmp);
+    CK(cudaMemcpyAsync(E.X[i - 1], E.tmp, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+  };
+  // two-site forward update of (i, i+1): step, truncated SVD (U | S V^T), back-step of core i+1
+  auto fwd2 = [&](int i, bool lit) {
+    expm2(i, half, lit);
+    const int64_t p = P.r[i] * P.n[i], q = P.n[i + 1] * P.r[i + 2];
+    CK(launch_svd_trunc(x2, p, q, 0, threshold, max_rank, swork, cbuf, sbuf, kdev, E.status, c->stream));
+    const int64_t k = read_k();
+    CK(cudaMemcpyAsync(E.X[i], cbuf, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(E.X[i + 1], sbuf, sizeof(double) * k * q, cudaMemcpyDeviceToDevice, c->stream));
+    P.r[i + 1] = k;
+    if (i < d - 2) {
+      left(i + 1);
+      expm1(i + 1, -half, lit);
+    }
+  };
+  // two-site backward update of (i, i+1): step, truncated SVD (U S | V^T), back-step of core i
+  auto bwd2 = [&](int i, bool lit) {
+    expm2(i, half, lit);
+    const int64_t p = P.r[i] * P.n[i], q = P.n[i + 1] * P.r[i + 2];
+    CK(launch_svd_trunc(x2, p, q, 1, threshold, max_rank, swork, cbuf, sbuf, kdev, E.status, c->stream));
+    const int64_t k = read_k();
+    CK(cudaMemcpyAsync(E.X[i + 1], cbuf, sizeof(double) * k * q, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(E.X[i], sbuf, sizeof(double) * p * k, cudaMemcpyDeviceToDevice, c->stream));
+    P.r[i + 1] = k;
+    if (i > 0) {
+      right(i);
+      expm1(i, -half, lit);
+    }
+  };
+  auto two_site = [&](int64_t rk, int64_t lo_dim, int64_t hi_dim) {
+    return (max_rank <= 0 || rk < max_rank) && rk < std::min(lo_dim, hi_dim);
+  };
+
+  for (int i = d - 1; i >= (kind == 2 ? 1 : 0); --i) right(i);
+  int64_t out_off = 0;
+  for (int step = 0; step < steps; ++step) {
+    if (kind == 1) {
+      for (int i = 0; i < d; ++i) {
+        if (i == 0) left(0);
+        if (i < d - 1)
+          fwd1(i, local);
+        else
+          expm1(i, tau, local);
+      }
+      for (int i = d - 1; i >= 0; --i) {
+        if (i == d - 1) right(i);
+        if (i > 0)
+          bwd1(i, i < d - 1, false);  // the reference's backward half sweep is always exact
+        else
+          expm1(0, half, false);
+      }
+    } else if (kind == 2) {
+      for (int i = 0; i + 1 < d; ++i) {
+        if (i == 0) left(0);
+        fwd2(i, local);
+      }
+      for (int i = d - 2; i >= 0; --i) {
+        if (i == d - 2) right(d - 1);
+        bwd2(i, local);
+      }
+    } else {
+      int i = 0;
+      left(0);
+      while (i < d - 1) {
+        if (two_site(P.r[i + 1], P.r[i] * P.n[i], P.n[i + 1] * P.r[i + 2])) {
+          fwd2(i, false);
+          if (i == d - 2) left(i + 1);  // the back-step, which builds it, is skipped at the last pair
+        } else {
+          fwd1(i, false);
+        }
+        ++i;
+      }
+      right(d - 1);
+      while (i > 0) {
+        if (two_site(P.r[i], P.r[i - 1] * P.n[i - 1], P.n[i] * P.r[i + 1])) {
+          --i;
+          bwd2(i, false);
+          if (i == 0) right(0);
+        } else {
+          bwd1(i, i < d - 1, false);
+          --i;
+        }
+      }
+    }
+    // normalisation: the first core carries the norm (cores 1..d-1 are right-orthonormal)
+    if (normalize == 2) {
+      const int64_t cnt = P.r[0] * P.n[0] * P.r[1];
+      QrArgs q{E.X[0], 1, 1, E.tmp, 1, 1, E.rbuf, 1, 1, cnt, 1, 1, nrm, E.qwork};
+      CK(launch_qr(q, c->stream));
+      CK(launch_scale(E.X[0], cnt, nrm, 1, c->stream));
+    } else if (normalize == 1) {
+      std::vector<std::vector<double>> h(d);
+      for (int i = 0; i < d; ++i) {
+        h[i].resize((size_t)(P.r[i] * P.n[i] * P.r[i + 1]));
+        CK(cudaMemcpyAsync(h[i].data(), E.X[i], sizeof(double) * h[i].size(), cudaMemcpyDeviceToHost, c->stream));
+      }
+      CK(cudaStreamSynchronize(c->stream));
+      const double s1 = tt_sum_host(h, P.n, P.r);
+      require(std::isfinite(s1) && s1 != 0.0, TTALS_ERR_NONFINITE, "1-norm of the state is zero or not finite");
+      double hs[2] = {s1, 0.0};
+      CK(cudaMemcpyAsync(nrm, hs, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      CK(launch_scale(E.X[0], P.r[0] * P.n[0] * P.r[1], nrm, 1, c->stream));
+      CK(cudaStreamSynchronize(c->stream));  // hs is released on return
+    }
+    for (int i = 0; i < d; ++i) {
+      const int64_t cnt = P.r[i] * P.n[i] * P.r[i + 1];
+      CK(cudaMemcpyAsync(out + out_off, E.X[i], sizeof(double) * cnt,
+                         out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream));
+      out_off += cnt;
+    }
+    if (out_ranks)
+      for (int i = 0; i <= d; ++i) out_ranks[(int64_t)step * (d + 1) + i] = P.r[i];
+  }
+  CK(cudaEventRecord(c->ev1, c->stream));
   check_status(E);
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -1779,6 +2123,15 @@ int ttals_job_finish(ttals_job* j, ttals_stats* stats) {
   });
   job_release(j);
   return st;
+}
+
+int ttals_tdvp(ttals_ctx* c, const ttals_tt* op, const ttals_tt* x0, int32_t kind, double tau, int32_t steps,
+               int32_t krylov_dim, double threshold, int64_t max_rank, int32_t normalize, double tol, double* out,
+               int64_t out_capacity, int32_t out_on_device, int64_t* out_ranks, ttals_stats* stats) {
+  return guarded(c, [&] {
+    run_tdvp(c, op, x0, kind, tau, steps, krylov_dim, threshold, max_rank, normalize, tol, out, out_capacity,
+             out_on_device, out_ranks, stats);
+  });
 }
 
 int ttals_batch_slots(ttals_ctx* c, int32_t* slots) {

@@ -25,6 +25,16 @@
 //   nonzero imaginary part ends the solve with ST_UNSUPPORTED (the real-valued
 //   cores cannot hold a complex eigenvector).
 //
+// expm_kernel: x <- exp(tau M) x for real tau, the local time step of the
+//   TDVP integrators (ode.py:1398-1616).  Two modes: "literal" runs the
+//   fixed-dimension recurrence of local_krylov (ode.py:1689-1758) exactly as
+//   written there (unnormalised start vector, three-term recurrence without
+//   reorthogonalisation, c = exp(tau T) e_1, x = sum_j c_j v_j); the other
+//   replaces scipy's expm_multiply: Lanczos with full reorthogonalisation on
+//   x / |x|, grown until the a-posteriori error beta_k |e_k^T exp(h T) e_1| is
+//   below tol |exp(h T) e_1|, with the step split into substeps h <= tau when
+//   the basis cap is reached first.
+//
 // One CTA per SM, co-resident (cooperative launch).  Vector work uses a fixed
 // chunk of elements per CTA; every scalar (dot, norm, Givens rotation, Ritz
 // value) is reduced identically in every CTA, so control flow is uniform.
@@ -32,6 +42,7 @@
 
 #include <algorithm>
 
+#include "ttals_expm.cuh"
 #include "ttals_hess.cuh"
 #include "ttals_internal.h"
 #include "ttals_tri.cuh"
@@ -718,6 +729,242 @@ cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st)
   void* args[] = {&k};
   ++launch_counter();
   return cudaLaunchCooperativeKernel((const void*)lanczos_kernel, dim3(num_sms), dim3(kKThreads), args, smem, st);
+}
+
+// ---------------------------------------------------------------------------
+// exponential action
+// ---------------------------------------------------------------------------
+
+struct ExpmK {
+  Contraction p1, p2, p3;
+  int N;
+  const double *L, *A, *R;
+  double *T1, *T2;
+  double* x;
+  double* V;
+  double* w;
+  double* partials;
+  int m, literal, max_substeps;
+  double tau, tol;
+  unsigned* bar;
+  int* status;
+  double* report;
+};
+
+// smem: al m, be m, h1 (m+2), h2 (m+2), c m, lam m, e m, rc m, rs m, Z m*m
+size_t expm_smem_bytes(int m) { return sizeof(double) * ((size_t)9 * m + 4 + (size_t)m * m); }
+
+__global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
+  extern __shared__ double sm[];
+  const int m = k.m;
+  double* al = sm;
+  double* be = al + m;
+  double* h1 = be + m;
+  double* h2 = h1 + m + 2;
+  double* cv = h2 + m + 2;
+  double* lam = cv + m;
+  double* ew = lam + m;
+  double* rc = ew + m;
+  double* rs = rc + m;
+  double* Z = rs + m;
+  __shared__ double s_h, s_err;
+  __shared__ int s_stop, s_fail;
+
+  const GridBarrier bar{k.bar, k.bar + 1};
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t N = k.N;
+  const int chunk = (int)((N + gridDim.x - 1) / gridDim.x);
+  const int e0 = (int)imin64(N, (int64_t)blockIdx.x * chunk);
+  const int e1 = (int)imin64(N, (int64_t)e0 + chunk);
+  const int ps = m + 2;
+  int rb = 0;
+  auto prow = [&](int buf) { return k.partials + ((int64_t)buf * gridDim.x + blockIdx.x) * ps; };
+  auto pbuf = [&](int buf) { return k.partials + (int64_t)buf * gridDim.x * ps; };
+  // the literal recurrence runs its m steps even past dimension N (with an
+  // unnormalised start vector it does not terminate there)
+  const int mm = k.literal ? m : (int)imin64((int64_t)m, N);
+  if (tid == 0) {
+    s_fail = 0;
+    s_err = 0.0;
+  }
+
+  // eigen-decomposition of T_nT (warp 0) and c = exp(h T) e_1 for the largest
+  // admissible h <= rem; returns through s_h / s_err / s_stop
+  auto project = [&](int nT, double bres, bool final_check, double rem) {
+    if (warp == 0) {
+      for (int i = lane; i < nT; i += 32) {
+        lam[i] = al[i];
+        ew[i] = i + 1 < nT ? be[i] : 0.0;
+      }
+      __syncwarp();
+      const bool ok = tri_ql_warp(lam, ew, nT, Z, rc, rs);
+      if (lane == 0) {
+        if (!ok) s_fail = 1;
+        double h = rem;
+        double cn = tri_expv_apply(lam, Z, nT, h, cv);
+        double err = bres * fabs(cv[nT - 1]);
+        int stop = ok && (k.literal || err <= k.tol * cn);
+        if (ok && !stop && final_check) {
+          for (int q = 0; q < 60 && err > k.tol * cn; ++q) {
+            h *= 0.5;
+            cn = tri_expv_apply(lam, Z, nT, h, cv);
+            err = bres * fabs(cv[nT - 1]);
+          }
+          stop = 1;
+        }
+        if (!ok) stop = 1;
+        if (!isfinite(cn)) s_fail = 1;
+        s_stop = stop;
+        s_h = h;
+        s_err = cn > 0.0 ? err / cn : 0.0;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  };
+
+  double rem = k.tau;
+  int substeps = 0, total_it = 0, last_nT = 0;
+  for (;;) {
+    // start vector: x itself (literal) or x / |x|
+    double scale = 1.0;
+    if (!k.literal) {
+      double sxx = 0.0;
+      for (int e = e0 + tid; e < e1; e += nt) sxx += k.x[e] * k.x[e];
+      block_partial(sxx, prow(rb));
+      if (!grid_sync(bar, k.status)) return;
+      reduce_partials(pbuf(rb), ps, 1, h1);
+      rb ^= 1;
+      scale = sqrt(h1[0]);
+      if (!(scale > 0.0)) break;  // exp(tau M) 0 = 0
+    }
+    const double inv0 = 1.0 / scale;
+    for (int e = e0 + tid; e < e1; e += nt) k.V[e] = k.x[e] * inv0;
+    if (!grid_sync(bar, k.status)) return;
+
+    int nT = 0;
+    if (tid == 0) s_stop = 0;
+    for (int j = 0; j < mm; ++j) {
+      const double* vj = k.V + (int64_t)j * N;
+      if (!apply12<double>(k.p1, k.p2, k.L, k.A, vj, k.T1, k.T2, bar, k.status)) return;
+      for (int e = e0 + tid; e < e1; e += nt) k.w[e] = apply3<double>(k.p3, k.T2, k.R, e);
+      __syncthreads();
+      double alj, bj;
+      if (k.literal) {
+        // alpha_j = w . v_j;  w -= alpha_j v_j + beta_{j-1} v_{j-1};  beta_j = |w|
+        double s = 0.0;
+        for (int e = e0 + tid; e < e1; e += nt) s += k.w[e] * vj[e];
+        block_partial(s, prow(rb));
+        if (!grid_sync(bar, k.status)) return;
+        reduce_partials(pbuf(rb), ps, 1, h1);
+        rb ^= 1;
+        alj = h1[0];
+        const double bprev = j > 0 ? be[j - 1] : 0.0;
+        const double* vp = j > 0 ? k.V + (int64_t)(j - 1) * N : vj;
+        double s2 = 0.0;
+        for (int e = e0 + tid; e < e1; e += nt) {
+          const double v = k.w[e] - alj * vj[e] - bprev * vp[e];
+          k.w[e] = v;
+          s2 += v * v;
+        }
+        block_partial(s2, prow(rb));
+        if (!grid_sync(bar, k.status)) return;
+        reduce_partials(pbuf(rb), ps, 1, h2);
+        rb ^= 1;
+        bj = sqrt(h2[0]);
+      } else {
+        // classical Gram-Schmidt against the whole basis, twice
+        chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+        if (!grid_sync(bar, k.status)) return;
+        reduce_partials(pbuf(rb), ps, j + 2, h1);
+        rb ^= 1;
+        for (int e = e0 + tid; e < e1; e += nt) {
+          double acc = k.w[e];
+          for (int q = 0; q <= j; ++q) acc -= h1[q] * k.V[(int64_t)q * N + e];
+          k.w[e] = acc;
+        }
+        __syncthreads();
+        chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+        if (!grid_sync(bar, k.status)) return;
+        reduce_partials(pbuf(rb), ps, j + 2, h2);
+        rb ^= 1;
+        double b2 = h2[j + 1];
+        for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
+        bj = sqrt(fmax(b2, 0.0));
+        alj = h1[j] + h2[j];
+        for (int e = e0 + tid; e < e1; e += nt) {
+          double acc = k.w[e];
+          for (int q = 0; q <= j; ++q) acc -= h2[q] * k.V[(int64_t)q * N + e];
+          k.w[e] = acc;
+        }
+      }
+      double tnorm = 0.0;
+      for (int i = 0; i <= j; ++i)
+        tnorm = fmax(tnorm, fabs(i == j ? alj : al[i]) + fabs(i == j ? bj : be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      // an invariant subspace (or the whole space) makes the projection exact;
+      // the literal recurrence stops only where it would divide by zero
+      const bool breakdown = k.literal ? !(bj > 0.0)
+                                       : (!(bj > 1e-14 * fmax(tnorm, 1e-300)) || j + 1 == (int)N);
+      __syncthreads();
+      if (tid == 0) {
+        al[j] = alj;
+        be[j] = bj;
+      }
+      nT = j + 1;
+      ++total_it;
+      if (!breakdown && j + 1 < mm) {
+        double* vn = k.V + (int64_t)(j + 1) * N;
+        const double inv = 1.0 / bj;
+        for (int e = e0 + tid; e < e1; e += nt) vn[e] = k.w[e] * inv;
+      }
+      __syncthreads();
+      const bool last = breakdown || nT == mm;
+      if (last || (!k.literal && (nT % 4) == 0)) {
+        project(nT, breakdown ? 0.0 : bj, last, rem);
+        if (s_stop) break;
+      }
+      if (!grid_sync(bar, k.status)) return;  // V_{j+1} complete
+    }
+    last_nT = nT;
+    // x = scale * sum_l c_l V_l
+    for (int e = e0 + tid; e < e1; e += nt) {
+      double acc = 0.0;
+      for (int l = 0; l < nT; ++l) acc += cv[l] * k.V[(int64_t)l * N + e];
+      k.x[e] = scale * acc;
+    }
+    ++substeps;
+    if (s_fail) break;
+    const double h = s_h;
+    rem = (h == rem) ? 0.0 : rem - h;
+    if (k.literal || rem == 0.0) break;
+    if (substeps >= k.max_substeps) {
+      if (blockIdx.x == 0 && tid == 0) atomicCAS(k.status, ST_OK, ST_NOCONV);
+      break;
+    }
+    if (!grid_sync(bar, k.status)) return;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    if (s_fail) atomicCAS(k.status, ST_OK, ST_NONFINITE);
+    k.report[0] = s_err;
+    k.report[1] = substeps;
+    k.report[2] = total_it;
+    k.report[3] = last_nT;
+  }
+}
+
+cudaError_t launch_expm(const ExpmLaunch& l, int num_sms, cudaStream_t st) {
+  if (l.m < 1 || l.m > 64 || l.max_substeps < 1) return cudaErrorInvalidValue;
+  Contraction p1, p2, p3;
+  local_apply_descs(l.sh, &p1, &p2, &p3);
+  ExpmK k{p1,  p2,         p3,     (int)l.sh.N(), l.L,   l.A,   l.R,      l.T1,     l.T2,     l.x,
+          l.V, l.w,        l.partials, l.m,       l.literal, l.max_substeps, l.tau, l.tol, l.bar, l.status,
+          l.report};
+  const size_t smem = expm_smem_bytes(l.m);
+  cudaError_t e = cudaFuncSetAttribute(expm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&k};
+  ++launch_counter();
+  return cudaLaunchCooperativeKernel((const void*)expm_kernel, dim3(num_sms), dim3(kKThreads), args, smem, st);
 }
 
 }  // namespace ttals

@@ -124,6 +124,26 @@ cudaError_t launch_lanczos(const LanczosLaunch& l, int num_sms, cudaStream_t st)
 size_t lanczos_partials_doubles(int m, int num_sms);
 size_t lanczos_smem_bytes(int m, int nonsym);
 
+// x <- exp(tau M) x on the local operator M (kernels_krylov.cu): literal = 1
+// runs the fixed m-dimensional recurrence of the reference's local Krylov
+// method, literal = 0 a converged Krylov approximation (relative tol) with at
+// most max_substeps substeps; m <= 64
+struct ExpmLaunch {
+  LocalShape sh;
+  const double *L, *A, *R;
+  double *T1, *T2;
+  double* x;
+  double* V;               // (m+1) x N
+  double* w;               // N
+  double* partials;        // lanczos_partials_doubles(m, num_sms)
+  int m, literal, max_substeps;
+  double tau, tol;
+  unsigned* bar;
+  int* status;
+  double* report;          // rel error estimate, substeps, iterations, basis size
+};
+cudaError_t launch_expm(const ExpmLaunch& l, int num_sms, cudaStream_t st);
+
 // rank-r orthonormal basis of an eigenvector block (kernels_evp.cu): side 0 ->
 // left basis (p x r) of M (p x q), side 1 -> right basis (r x q); tr_k > 0 reads
 // M as the transposed-and-reshaped N x tr_k block (backward sweep)

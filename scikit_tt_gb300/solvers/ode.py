@@ -16,8 +16,16 @@ step's solution; products and norms run through the device ``TT.dot`` and
   or the trapezoidal rule, step control by local error and closeness to the
   stationary state)
 
-``tt_solver='mals'`` raises ``NotImplementedError`` (two-site MALS is not on
-the device path); ``progress`` is accepted and ignored.
+* ``tdvp1site``           ode.py:1188-1288 (one-site TDVP)
+* ``tdvp2site``           ode.py:1290-1396 (two-site TDVP, truncated splits)
+* ``tdvp``                ode.py:1076-1186 (adaptive one-/two-site TDVP)
+
+``tt_solver='mals'`` runs the device two-site solver; ``progress`` is accepted
+and ignored.  The TDVP functions run every local exponential on the device
+(one persistent Krylov kernel per local step) and need a real exponent
+``-1j * step_size``: imaginary-time steps (``step_size = -1j * dt``), the
+setting of the reference's own TDVP test.  Real-time steps would need complex
+cores, which the device path does not hold; they raise ``NotImplementedError``.
 """
 
 from __future__ import annotations
@@ -26,6 +34,7 @@ from typing import List
 
 import numpy as np
 
+from .. import _lib
 from .. import tensor_train as tt
 from . import sle
 
@@ -154,3 +163,101 @@ def adaptive_step_size(operator, initial_value, initial_guess, time_end: float, 
         else:
             h = h_new
     return solution, time_steps
+
+
+# ----------------------------------------------------------------------------
+# TDVP
+# ----------------------------------------------------------------------------
+
+_TDVP_KIND = {'adaptive': 0, 'one_site': 1, 'two_site': 2}
+
+
+def _real_cores(t, what):
+    cores = []
+    for c in t.cores:
+        if np.iscomplexobj(c):
+            if np.any(np.imag(c) != 0):
+                raise NotImplementedError(f'{what}: complex cores are not supported by the device TDVP path')
+            c = np.real(c)
+        cores.append(np.asarray(c, dtype=np.float64))
+    return cores
+
+
+def _krylov_dim(local_solver):
+    """ode.py:1233-1238: no solver or 'exact' -> exact exponentials, anything
+    else -> the local Krylov method, dimension 5 unless given (the dict is
+    updated in place, as there)."""
+    if not local_solver or local_solver['method'] == 'exact':
+        return 0
+    if not local_solver.get('dimension'):
+        local_solver.setdefault('dimension', 5)
+    return int(local_solver['dimension'])
+
+
+def _run_tdvp(kind, operator, initial_value, step_size, number_of_steps, krylov_dim, threshold, max_rank,
+              normalize):
+    tau = -1j * complex(step_size)
+    if tau.imag != 0.0:
+        raise NotImplementedError('the device TDVP path needs a real exponent -1j*step_size (imaginary-time steps); '
+                                  'real-time steps need complex cores')
+    steps = int(number_of_steps)
+    op_c = _real_cores(operator, 'operator')
+    x_c = _real_cores(initial_value, 'initial_value')
+    d = len(op_c)
+    dims = [c.shape[1] for c in op_c]
+    r0 = [c.shape[0] for c in x_c] + [x_c[-1].shape[3]]
+    mr = 0 if max_rank is None or max_rank == np.inf else int(max_rank)
+    cap = list(r0)
+    if kind != 1:
+        lft = np.cumprod([1] + dims).tolist()
+        rgt = (np.cumprod(([1] + dims[::-1]))[::-1]).tolist()
+        for i in range(1, d):
+            c = min(lft[i], rgt[i])
+            if mr > 0:
+                c = min(c, mr)
+            cap[i] = max(c, r0[i])
+    step_total = sum(cap[i] * dims[i] * cap[i + 1] for i in range(d))
+    out = np.empty(max(steps * step_total, 1))
+    out_ranks = np.zeros(max(steps, 1) * (d + 1), dtype=np.int64)
+    op, x0 = _lib.Packed(op_c), _lib.Packed(x_c)
+    st = _lib.Stats()
+    _lib.check(_lib.load().ttals_tdvp(_lib.context(), op.desc, x0.desc, _TDVP_KIND[kind], float(tau.real), steps,
+                                       int(krylov_dim), float(threshold), mr, int(normalize), 0.0, _lib.dptr(out),
+                                       out.size, 0, _lib.i64ptr(out_ranks), st))
+    solution = [initial_value]
+    off = 0
+    for k in range(steps):
+        rk = out_ranks[k * (d + 1):(k + 1) * (d + 1)]
+        cores = _lib.unpack(out[off:], dims, [1] * d, rk)
+        off += sum(int(rk[i] * dims[i] * rk[i + 1]) for i in range(d))
+        solution.append(tt.TT(cores))
+    return solution
+
+
+def tdvp1site(operator, initial_value, step_size, number_of_steps: int, local_solver=None, normalize: int = 0):
+    """One-site TDVP (ode.py:1188-1288): each step a forward half sweep (local
+    exponential of every core by step/2, QR, backward step of the bond matrix)
+    and a backward half sweep (the reference always uses exact exponentials
+    there).  Returns the list of states, ``initial_value`` first."""
+    return _run_tdvp('one_site', operator, initial_value, step_size, number_of_steps, _krylov_dim(local_solver),
+                     0.0, np.inf, normalize)
+
+
+def tdvp2site(operator, initial_value, step_size, number_of_steps: int, local_solver=None, threshold=1e-12,
+              max_rank=50, normalize: int = 0):
+    """Two-site TDVP (ode.py:1290-1396): two-site local exponentials, truncated
+    SVD splits (``threshold`` relative to the largest singular value,
+    ``max_rank``), one-site backward steps."""
+    return _run_tdvp('two_site', operator, initial_value, step_size, number_of_steps, _krylov_dim(local_solver),
+                     threshold, max_rank, normalize)
+
+
+def tdvp(operator, initial_value, step_size, number_of_steps: int, threshold=1e-12, max_rank=50,
+         normalize: int = 0):
+    """Adaptive TDVP (ode.py:1076-1186): a two-site update on every bond whose
+    rank is below ``max_rank`` and below the dimensions on both sides, else a
+    one-site update.  The reference calls its update helpers without their
+    ``local_solver`` argument and stops with a TypeError; this runs the
+    evident intent with exact local exponentials."""
+    return _run_tdvp('adaptive', operator, initial_value, step_size, number_of_steps, 0, threshold, max_rank,
+                     normalize)

@@ -244,6 +244,59 @@ def mals_cases():
     mals_case('sle_mals_coupled_d5_lu', w2.op, w2.rhs, w2.x0, 1, 1e-10, 8, 'lu')
 
 
+def tdvp_case(name, fn, op, x0, step_size, steps, **kw):
+    """One TDVP run; stores the full state after every step (real parts: the
+    reference returns complex trains, which stay real for imaginary-time steps)."""
+    sol = fn(RTT([c.copy() for c in op]), RTT([c.copy() for c in x0]), step_size, steps, **kw)
+    out = {'step_im': np.array(np.imag(step_size)), 'steps': np.array(steps)}
+    for key, val in kw.items():
+        if key == 'local_solver':
+            out['krylov_dim'] = np.array(0 if val['method'] == 'exact' else val.get('dimension', 5))
+        else:
+            out[key] = np.array(-1 if val == np.inf else val)
+    pack('op', op, out)
+    pack('x0', x0, out)
+    imag = 0.0
+    for k, t in enumerate(sol):
+        full = np.asarray(t.full()).reshape(-1)
+        imag = max(imag, float(np.max(np.abs(np.imag(full)))))
+        out[f'full_{k}'] = np.real(full).copy()
+        out[f'ranks_{k}'] = np.array(t.ranks)
+    out['n_states'] = np.array(len(sol))
+    assert imag < 1e-12, imag
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'states', len(sol), 'final ranks', sol[-1].ranks, 'max imag', imag)
+
+
+def tdvp_cases():
+    """tdvp1site / tdvp2site in imaginary time on Ising chains (the setting of
+    the reference's own TDVP test), with its local Krylov method and with the
+    exact local exponential."""
+    N = 5
+    op = [c.copy() for c in rmodels.ising(N, J=1.0, h=1.2).cores]
+    init = rtt.uniform(N * [2], ranks=15).ortho()
+    init = (1 / init.norm()) * init
+    x0 = [c.copy() for c in init.cores]
+    h = -1j * 0.02
+    tdvp_case('tdvp1_ising_d5_krylov', rode.tdvp1site, op, x0, h, 30, local_solver={'method': 'local_krylov'},
+              normalize=2)
+    tdvp_case('tdvp1_ising_d5_exact', rode.tdvp1site, op, x0, h, 30, local_solver={'method': 'exact'}, normalize=2)
+    tdvp_case('tdvp2_ising_d5_krylov', rode.tdvp2site, op, x0, h, 30, local_solver={'method': 'local_krylov'},
+              normalize=2)
+    # a random initial value, rank capped at 3 (truncating two-site splits), no normalisation
+    # (normalize=1 is the sum of all entries, meant for non-negative states)
+    rng = np.random.default_rng(31)
+    N2 = 6
+    op2 = [c.copy() for c in rmodels.ising(N2, J=1.0, h=0.7).cores]
+    t2 = RTT(wl.gaussian_tt(rng, N2, 2, 2)).ortho_right()
+    t2 = (1 / t2.norm()) * t2
+    x02 = [c.copy() for c in t2.cores]
+    tdvp_case('tdvp2_ising_d6_exact_r3', rode.tdvp2site, op2, x02, -1j * 0.05, 8, local_solver={'method': 'exact'},
+              threshold=1e-12, max_rank=3)
+    tdvp_case('tdvp1_ising_d6_krylov4', rode.tdvp1site, op2, x02, -1j * 0.05, 8,
+              local_solver={'method': 'krylov', 'dimension': 4}, normalize=0)
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -276,6 +329,7 @@ def main():
     ode_cases()
     trunc_cases()
     mals_cases()
+    tdvp_cases()
 
 
 if __name__ == '__main__':
@@ -289,5 +343,7 @@ if __name__ == '__main__':
         trunc_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'mals':
         mals_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'tdvp':
+        tdvp_cases()
     else:
         main()

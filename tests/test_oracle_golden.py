@@ -95,3 +95,38 @@ def test_oracle_evp_blocks_match_reference(golden, name):
         v = O.full_vector(vecs[e])
         v = v * np.exp(-1j * np.angle(v[np.argmax(np.abs(v))]))
         assert _up_to_sign(np.real(v), z[f'vec{e}']) < 1e-8
+
+
+TDVP_CASES = ['tdvp1_ising_d5_krylov', 'tdvp1_ising_d5_exact', 'tdvp2_ising_d5_krylov', 'tdvp2_ising_d6_exact_r3',
+              'tdvp1_ising_d6_krylov4']
+
+
+def tdvp_args(z):
+    """Keyword arguments of one golden TDVP run (tau = -1j * step_size is real)."""
+    kw = {'kdim': int(z['krylov_dim'])}
+    for key in ('normalize', 'threshold', 'max_rank'):
+        if key in z:
+            kw[key] = float(z[key]) if key == 'threshold' else int(z[key])
+    return float(z['step_im']), int(z['steps']), kw
+
+
+@pytest.mark.parametrize('name', TDVP_CASES)
+def test_oracle_tdvp_matches_reference(golden, name):
+    z, cores = golden(name)
+    tau, steps, kw = tdvp_args(z)
+    fn = O.tdvp1site if name.startswith('tdvp1') else O.tdvp2site
+    states = fn(cores('op'), cores('x0'), tau, steps, **kw)
+    assert len(states) == int(z['n_states'])
+    for k, s in enumerate(states):
+        assert [c.shape[0] for c in s] + [1] == list(z[f'ranks_{k}'])
+        ref = z[f'full_{k}']
+        assert np.linalg.norm(O.full_vector(s) - ref) / np.linalg.norm(ref) < 1e-12
+
+
+def test_tdvp_refuses_real_time_steps():
+    from scikit_tt_gb300.solvers import ode
+    from scikit_tt_gb300.tensor_train import TT
+    op = TT([np.eye(2).reshape(1, 2, 2, 1)] * 3)
+    x = TT([np.ones((1, 2, 1, 1))] * 3)
+    with pytest.raises(NotImplementedError):
+        ode.tdvp1site(op, x, 0.1, 2)
