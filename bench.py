@@ -273,6 +273,23 @@ def other_workloads(lib, ctx, args):
     out['ising_d48_r64'] = {'dropin_fp64_ms': evp.last_stats['device_ms'], 'eigenvalue': val,
                             'abs_err_vs_exact': abs(val - e0), 'sweeps': its,
                             'lanczos_iterations': evp.last_stats['krylov_iterations']}
+    # two-site TDVP, Ising d=16 g=1.2 from a rank-4 state, ranks <= 16, imaginary-time steps of 0.05
+    # with exact local exponentials; the oracle runs the first two steps for time and parity
+    from scikit_tt_gb300.solvers import ode
+    wt = wl.tdvp_ising()
+    tau = float((-1j * wt.step_size).real)
+    ode.tdvp2site(T(wt.op), T(wt.x0), wt.step_size, 1, max_rank=wt.max_rank, normalize=2)
+    sol = ode.tdvp2site(T(wt.op), T(wt.x0), wt.step_size, wt.steps, max_rank=wt.max_rank, normalize=2)
+    tst = dict(ode.last_stats)
+    t0 = time.perf_counter()
+    ref = O.tdvp2site(wt.op, wt.x0, tau, 2, kdim=0, threshold=1e-12, max_rank=wt.max_rank, normalize=2)
+    cpu_s = time.perf_counter() - t0
+    out['tdvp2_ising_d16_r16'] = {
+        'steps': wt.steps, 'device_ms_per_step': tst['device_ms'] / wt.steps,
+        'oracle_cpu_ms_per_step': cpu_s * 1e3 / 2, 'local_exponentials': tst['local_solves'],
+        'krylov_iterations': tst['krylov_iterations'], 'kernel_launches': tst['kernel_launches'],
+        'final_ranks': [int(x) for x in sol[-1].ranks],
+        'rel_diff_vs_oracle_step2': O.stable_rel_diff(sol[2].cores, ref[2])}
     # 256 uneven instances (d 8..32, n in {2,4,8}, rank 4..48), 4 sweeps, one launch
     b4 = wl.batch_sle(256)
     probs = [(T(w.op), T(w.x0), T(w.rhs)) for w in b4]

@@ -257,9 +257,11 @@ struct SvdK {
   double* r;
   int* kept;         // out: k
   int* status;
+  int in_smem;       // W and Vr live in dynamic shared memory instead
 };
 
 __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
+  extern __shared__ double s_dyn[];
   __shared__ int s_a[kTrMaxGram / 2], s_b[kTrMaxGram / 2];
   __shared__ double s_sig[kTrMaxGram];
   __shared__ int s_ord[kTrMaxGram];
@@ -269,14 +271,32 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
   const bool tr = a.q > a.p;                 // work on M^T when M is wide
   const int64_t rows = tr ? a.q : a.p;       // length of a working column
   const int ncols = (int)(tr ? a.p : a.q);   // number of working columns
-  double* W = a.W;
-  double* V = a.Vr;
+  // the rotation steps re-read every column: shared memory when it fits
+  double* W = a.in_smem ? s_dyn : a.W;
+  double* V = a.in_smem ? s_dyn + rows * ncols : a.Vr;
   for (int64_t e = tid; e < rows * ncols; e += nt) {
     const int64_t c = e / rows, i = e - c * rows;
     W[e] = tr ? a.M[c * a.q + i] : a.M[i * a.q + c];
   }
   for (int64_t e = tid; e < (int64_t)ncols * ncols; e += nt) V[e] = (e / ncols == e % ncols) ? 1.0 : 0.0;
+  // |M|_F^2: columns below 1e-30 of it (singular values below 1e-15 |M|) are
+  // rounding noise that a rotation only regenerates; rotations of such pairs
+  // do not keep the sweeps going
+  __shared__ double s_red[32], s_fro2;
+  {
+    double f2 = 0.0;
+    for (int64_t e = tid; e < rows * ncols; e += nt) f2 += W[e] * W[e];
+    f2 = warp_sum(f2);
+    if (lane == 0) s_red[warp] = f2;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += s_red[w];
+      s_fro2 = t;
+    }
+  }
   __syncthreads();
+  const double live_floor = 1e-30 * s_fro2;
   const int nn = (ncols + 1) & ~1, npairs = nn / 2;
   for (int sweep = 0; sweep < 60 && ncols > 1; ++sweep) {
     if (tid == 0) s_rot = 0;
@@ -308,10 +328,22 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
         alpha = warp_sum(alpha);
         beta = warp_sum(beta);
         gamma = warp_sum(gamma);
-        if (fabs(gamma) > 1e-15 * sqrt(alpha * beta) && gamma != 0.0) {
+        // rotation angle by lane 0 only (FP64 division and square root are
+        // scarce on this part), then broadcast
+        double c = 1.0, s = 0.0;
+        int rot = 0;
+        if (lane == 0 && gamma != 0.0 && gamma * gamma > 1e-30 * alpha * beta) {
           const double zeta = (beta - alpha) / (2.0 * gamma);
-          const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+          const double t = fabs(zeta) > 1e150 ? 0.5 / zeta
+                                              : (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          c = rsqrt(1.0 + t * t);
+          s = c * t;
+          rot = 1;
+        }
+        rot = __shfl_sync(0xffffffffu, rot, 0);
+        if (rot) {
+          c = __shfl_sync(0xffffffffu, c, 0);
+          s = __shfl_sync(0xffffffffu, s, 0);
           for (int64_t i = lane; i < rows; i += 32) {
             const double x = ca[i], y = cb[i];
             ca[i] = c * x - s * y;
@@ -324,7 +356,7 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
             va[i] = c * x - s * y;
             vb[i] = s * x + c * y;
           }
-          if (lane == 0) s_rot = 1;
+          if (lane == 0 && fmin(alpha, beta) > live_floor) s_rot = 1;
         }
       }
       __syncthreads();
@@ -394,6 +426,8 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
   }
 }
 
+constexpr size_t kSvdSmemMax = 160 * 1024;  // plus ~16 KB of static shared memory
+
 size_t svd_trunc_work_doubles(int64_t p, int64_t q) {
   const int64_t n = p < q ? p : q, rows = p > q ? p : q;
   return (size_t)(rows * n + n * n + 64);
@@ -403,8 +437,15 @@ cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, do
                              double* work, double* core, double* r, int* kept, int* status, cudaStream_t st) {
   const int64_t n = p < q ? p : q, rows = p > q ? p : q;
   if (n > kTrMaxGram || n < 1) return cudaErrorInvalidValue;
-  SvdK a{M, p, q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status};
-  svd_trunc_kernel<<<1, kTrThreads, 0, st>>>(a);
+  const size_t bytes = sizeof(double) * (size_t)(rows * n + n * n);
+  const int in_smem = bytes <= kSvdSmemMax;
+  SvdK a{M, p, q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status, in_smem};
+  if (in_smem) {
+    cudaError_t e = cudaFuncSetAttribute(svd_trunc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSvdSmemMax);
+    if (e != cudaSuccess) return e;
+  }
+  svd_trunc_kernel<<<1, kTrThreads, in_smem ? bytes : 0, st>>>(a);
   ++launch_counter();
   return cudaGetLastError();
 }

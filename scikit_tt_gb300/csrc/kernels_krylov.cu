@@ -751,8 +751,8 @@ struct ExpmK {
   double* report;
 };
 
-// smem: al m, be m, h1 (m+2), h2 (m+2), c m, lam m, e m, rc m, rs m, Z m*m
-size_t expm_smem_bytes(int m) { return sizeof(double) * ((size_t)9 * m + 4 + (size_t)m * m); }
+// smem: al m, be m, h1 (m+2), h2 (m+2), c m
+size_t expm_smem_bytes(int m) { return sizeof(double) * ((size_t)5 * m + 4); }
 
 __global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
   extern __shared__ double sm[];
@@ -762,11 +762,6 @@ __global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
   double* h1 = be + m;
   double* h2 = h1 + m + 2;
   double* cv = h2 + m + 2;
-  double* lam = cv + m;
-  double* ew = lam + m;
-  double* rc = ew + m;
-  double* rs = rc + m;
-  double* Z = rs + m;
   __shared__ double s_h, s_err;
   __shared__ int s_stop, s_fail;
 
@@ -788,33 +783,26 @@ __global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
     s_err = 0.0;
   }
 
-  // eigen-decomposition of T_nT (warp 0) and c = exp(h T) e_1 for the largest
-  // admissible h <= rem; returns through s_h / s_err / s_stop
+  // c = exp(h T_nT) e_1 (warp 0) for the largest admissible h <= rem, with the
+  // a-posteriori error estimate bres |c_{nT-1}|; returns through s_h / s_err / s_stop
   auto project = [&](int nT, double bres, bool final_check, double rem) {
     if (warp == 0) {
-      for (int i = lane; i < nT; i += 32) {
-        lam[i] = al[i];
-        ew[i] = i + 1 < nT ? be[i] : 0.0;
+      bool ok = true;
+      double h = rem;
+      double cn = tri_expv_warp(al, be, nT, h, cv, &ok);
+      double err = bres * fabs(cv[nT - 1]);
+      bool stop = !ok || k.literal || err <= k.tol * cn;
+      if (!stop && final_check) {
+        for (int q = 0; q < 60 && ok && err > k.tol * cn; ++q) {
+          h *= 0.5;
+          cn = tri_expv_warp(al, be, nT, h, cv, &ok);
+          err = bres * fabs(cv[nT - 1]);
+        }
+        stop = true;
       }
-      __syncwarp();
-      const bool ok = tri_ql_warp(lam, ew, nT, Z, rc, rs);
       if (lane == 0) {
         if (!ok) s_fail = 1;
-        double h = rem;
-        double cn = tri_expv_apply(lam, Z, nT, h, cv);
-        double err = bres * fabs(cv[nT - 1]);
-        int stop = ok && (k.literal || err <= k.tol * cn);
-        if (ok && !stop && final_check) {
-          for (int q = 0; q < 60 && err > k.tol * cn; ++q) {
-            h *= 0.5;
-            cn = tri_expv_apply(lam, Z, nT, h, cv);
-            err = bres * fabs(cv[nT - 1]);
-          }
-          stop = 1;
-        }
-        if (!ok) stop = 1;
-        if (!isfinite(cn)) s_fail = 1;
-        s_stop = stop;
+        s_stop = stop ? 1 : 0;
         s_h = h;
         s_err = cn > 0.0 ? err / cn : 0.0;
       }
@@ -843,6 +831,7 @@ __global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
     if (!grid_sync(bar, k.status)) return;
 
     int nT = 0;
+    double trow = 0.0;
     if (tid == 0) s_stop = 0;
     for (int j = 0; j < mm; ++j) {
       const double* vj = k.V + (int64_t)j * N;
@@ -873,34 +862,47 @@ __global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
         rb ^= 1;
         bj = sqrt(h2[0]);
       } else {
-        // classical Gram-Schmidt against the whole basis, twice
+        // classical Gram-Schmidt against the whole basis; a second pass only
+        // when the first removed more than half of |w|^2 ("twice is enough":
+        // otherwise one pass leaves w orthogonal to working accuracy)
         chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
         if (!grid_sync(bar, k.status)) return;
         reduce_partials(pbuf(rb), ps, j + 2, h1);
         rb ^= 1;
+        // sums over q by the lanes of each warp (FP64 is scarce: no per-thread loop)
+        double sq = 0.0;
+        for (int q = lane; q <= j; q += 32) sq += h1[q] * h1[q];
+        sq = warp_sum(sq);
+        const double wn2 = h1[j + 1], rest = wn2 - sq;
         for (int e = e0 + tid; e < e1; e += nt) {
           double acc = k.w[e];
           for (int q = 0; q <= j; ++q) acc -= h1[q] * k.V[(int64_t)q * N + e];
           k.w[e] = acc;
         }
-        __syncthreads();
-        chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
-        if (!grid_sync(bar, k.status)) return;
-        reduce_partials(pbuf(rb), ps, j + 2, h2);
-        rb ^= 1;
-        double b2 = h2[j + 1];
-        for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
-        bj = sqrt(fmax(b2, 0.0));
-        alj = h1[j] + h2[j];
-        for (int e = e0 + tid; e < e1; e += nt) {
-          double acc = k.w[e];
-          for (int q = 0; q <= j; ++q) acc -= h2[q] * k.V[(int64_t)q * N + e];
-          k.w[e] = acc;
+        alj = h1[j];
+        if (rest >= 0.5 * wn2) {
+          bj = sqrt(rest);
+        } else {
+          __syncthreads();
+          chunk_dots<double>(k.V, N, j + 1, k.w, e0, e1, prow(rb));
+          if (!grid_sync(bar, k.status)) return;
+          reduce_partials(pbuf(rb), ps, j + 2, h2);
+          rb ^= 1;
+          double sq2 = 0.0;
+          for (int q = lane; q <= j; q += 32) sq2 += h2[q] * h2[q];
+          sq2 = warp_sum(sq2);
+          bj = sqrt(fmax(h2[j + 1] - sq2, 0.0));
+          alj += h2[j];
+          for (int e = e0 + tid; e < e1; e += nt) {
+            double acc = k.w[e];
+            for (int q = 0; q <= j; ++q) acc -= h2[q] * k.V[(int64_t)q * N + e];
+            k.w[e] = acc;
+          }
         }
       }
-      double tnorm = 0.0;
-      for (int i = 0; i <= j; ++i)
-        tnorm = fmax(tnorm, fabs(i == j ? alj : al[i]) + fabs(i == j ? bj : be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      // |T|_inf: running maximum over the completed rows plus the current row
+      if (j > 0) trow = fmax(trow, fabs(al[j - 1]) + fabs(be[j - 1]) + (j > 1 ? fabs(be[j - 2]) : 0.0));
+      const double tnorm = fmax(trow, fabs(alj) + fabs(bj) + (j > 0 ? fabs(be[j - 1]) : 0.0));
       // an invariant subspace (or the whole space) makes the projection exact;
       // the literal recurrence stops only where it would divide by zero
       const bool breakdown = k.literal ? !(bj > 0.0)
@@ -919,7 +921,7 @@ __global__ void __launch_bounds__(kKThreads, 1) expm_kernel(ExpmK k) {
       }
       __syncthreads();
       const bool last = breakdown || nT == mm;
-      if (last || (!k.literal && (nT % 4) == 0)) {
+      if (last || !k.literal) {
         project(nT, breakdown ? 0.0 : bj, last, rem);
         if (s_stop) break;
       }
@@ -962,9 +964,13 @@ cudaError_t launch_expm(const ExpmLaunch& l, int num_sms, cudaStream_t st) {
   const size_t smem = expm_smem_bytes(l.m);
   cudaError_t e = cudaFuncSetAttribute(expm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // TDVP's local problems are small (10^2 - 10^4 unknowns): one CTA per 64
+  // unknowns keeps ~2 us of FP64 work per contraction phase and CTA while the
+  // grid barrier, whose latency grows with the CTAs arriving, stays short
+  const int grid = (int)std::min<int64_t>(num_sms, std::max<int64_t>(1, (l.sh.N() + 63) / 64));
   void* args[] = {&k};
   ++launch_counter();
-  return cudaLaunchCooperativeKernel((const void*)expm_kernel, dim3(num_sms), dim3(kKThreads), args, smem, st);
+  return cudaLaunchCooperativeKernel((const void*)expm_kernel, dim3(grid), dim3(kKThreads), args, smem, st);
 }
 
 }  // namespace ttals

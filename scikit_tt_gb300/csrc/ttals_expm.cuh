@@ -3,12 +3,15 @@
 // projected matrix T in scikit_tt/solvers/ode.py:1750-1752 and the Krylov
 // replacement of scipy's expm_multiply, ode.py:1435 and 1525).
 //
-// tri_ql_warp: T = Z diag(d) Z^T by the implicit QL iteration with Wilkinson
-//   shifts (Bowdler, Martin, Reinsch and Wilkinson, Numer. Math. 11 (1968)).
-//   Lane 0 runs the scalar recurrence of each bulge chase and stores its
-//   rotations; the whole warp then applies them to the rows of Z.
-// tri_expv_apply: c = Z diag(exp(h d)) Z^T e_1, scaled by exp(max h d) so that
-//   only the final factor can overflow.
+// tri_expv_warp: c = exp(h T) e_1 by the truncated Taylor series with scaling
+//   (the method family of scipy's expm_multiply, Al-Mohy and Higham 2011):
+//   h T is split into s pieces with |h T / s|_inf <= 1/2, and each piece's
+//   series is cut after 16 terms (remainder <= 0.5^17 / 17! e^0.5 < 2^-60 of
+//   the piece's result, whose norm is at least e^-0.5 of its input).  One warp:
+//   lane L holds entries 2L and 2L+1 (k <= 64), a tridiagonal product is two
+//   shuffles and three FMAs per entry, so a check costs a few hundred cycles
+//   (an eigendecomposition by a serial QL chase costs 10^5 here: FP64
+//   division and square root run at a small fraction of the FMA rate).
 #pragma once
 
 #include <float.h>
@@ -17,98 +20,63 @@
 
 namespace ttals {
 
-// d: k diagonal entries, e: k-1 off-diagonal entries (+1 slot of work), both
-// overwritten (d -> eigenvalues).  Z: k x k row-major.  rc, rs: k doubles of
-// rotation storage.  Returns false when an eigenvalue needed more than 60
-// iterations (uniform over the warp).
-static __device__ __noinline__ bool tri_ql_warp(double* d, double* e, int k, double* Z, double* rc, double* rs) {
-  const int lane = threadIdx.x & 31;
-  for (int i = lane; i < k * k; i += 32) Z[i] = (i / k == i % k) ? 1.0 : 0.0;
-  if (lane == 0) e[k - 1] = 0.0;
-  __syncwarp();
-  for (int l = 0; l < k; ++l) {
-    for (int iter = 0;; ++iter) {
-      int m = l, lo = l, bad = 0;
-      if (lane == 0) {
-        for (m = l; m < k - 1; ++m) {
-          const double dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= DBL_EPSILON * dd) break;
-        }
-        if (m != l && iter >= 60) bad = 1;
-        if (m != l && !bad) {
-          double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-          double r = hypot(g, 1.0);
-          g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-          double s = 1.0, c = 1.0, p = 0.0;
-          bool split = false;
-          int i;
-          for (i = m - 1; i >= l; --i) {
-            const double f = s * e[i];
-            const double b = c * e[i];
-            r = hypot(f, g);
-            e[i + 1] = r;
-            if (r == 0.0) {
-              // the chase decoupled the matrix: restart from the split
-              d[i + 1] -= p;
-              e[m] = 0.0;
-              split = true;
-              break;
-            }
-            s = f / r;
-            c = g / r;
-            g = d[i + 1] - p;
-            r = (d[i] - g) * s + 2.0 * c * b;
-            p = s * r;
-            d[i + 1] = g + p;
-            g = c * r - b;
-            rc[i] = c;
-            rs[i] = s;
-          }
-          lo = split ? i + 1 : l;
-          if (!split) {
-            d[l] -= p;
-            e[l] = g;
-            e[m] = 0.0;
-          }
-        }
-      }
-      m = __shfl_sync(0xffffffffu, m, 0);
-      lo = __shfl_sync(0xffffffffu, lo, 0);
-      bad = __shfl_sync(0xffffffffu, bad, 0);
-      if (bad) return false;
-      if (m == l) break;
-      __syncwarp();
-      // Z <- Z G_{m-1} ... G_lo, each rotation mixing columns i and i+1
-      for (int q = lane; q < k; q += 32) {
-        double* zr = Z + q * k;
-        for (int i = m - 1; i >= lo; --i) {
-          const double f = zr[i + 1];
-          zr[i + 1] = rs[i] * zr[i] + rc[i] * f;
-          zr[i] = rc[i] * zr[i] - rs[i] * f;
-        }
-      }
-      __syncwarp();
-    }
-  }
-  __syncwarp();
-  return true;
-}
+// 1 / q for q = 0..17 (entry 0 unused)
+__device__ __constant__ const double kInvInt[18] = {0.0,       1.0,        1.0 / 2,  1.0 / 3,  1.0 / 4,  1.0 / 5,
+                                                    1.0 / 6,   1.0 / 7,    1.0 / 8,  1.0 / 9,  1.0 / 10, 1.0 / 11,
+                                                    1.0 / 12,  1.0 / 13,   1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17};
 
-// c = Z diag(exp(h lam)) Z^T e_1 (k entries), computed by lane 0.  Returns
-// |c| (2-norm).
-static __device__ __forceinline__ double tri_expv_apply(const double* lam, const double* Z, int k, double h,
-                                                        double* c) {
-  double sh = -DBL_MAX;
-  for (int q = 0; q < k; ++q) sh = fmax(sh, h * lam[q]);
-  double nrm = 0.0;
-  const double big = exp(sh);
-  for (int j = 0; j < k; ++j) {
-    double acc = 0.0;
-    for (int q = 0; q < k; ++q) acc += Z[j * k + q] * exp(h * lam[q] - sh) * Z[q];
-    c[j] = acc * big;
-    nrm += c[j] * c[j];
+// al: k diagonal entries, be: k-1 off-diagonal entries (be[i] couples i and
+// i+1).  c: k outputs (written by the lanes owning them).  Returns |c|_2 to
+// every lane; false in *ok when the scaling would need more than 2^16 pieces
+// or the result is not finite.
+static __device__ __noinline__ double tri_expv_warp(const double* al, const double* be, int k, double h, double* c,
+                                                    bool* ok) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int i0 = 2 * lane, i1 = 2 * lane + 1;
+  // local entries of h T (zero outside k)
+  const double a0 = i0 < k ? h * al[i0] : 0.0, a1 = i1 < k ? h * al[i1] : 0.0;
+  const double b0 = i0 + 1 < k ? h * be[i0] : 0.0;   // couples i0, i1
+  const double b1 = i1 + 1 < k ? h * be[i1] : 0.0;   // couples i1, i1+1 (next lane's i0)
+  const double bm = __shfl_up_sync(full, b1, 1);     // couples i0-1, i0
+  const double bmin = lane > 0 ? bm : 0.0;
+  double nrm = fmax(fabs(a0) + fabs(b0) + fabs(bmin), fabs(a1) + fabs(b0) + fabs(b1));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nrm = fmax(nrm, __shfl_xor_sync(full, nrm, o));
+  double s = ceil(2.0 * nrm);
+  if (!(s >= 1.0)) s = 1.0;
+  *ok = s <= 65536.0;
+  const int pieces = *ok ? (int)s : 1;
+  const double inv = 1.0 / (double)pieces;
+  double x0 = lane == 0 ? 1.0 : 0.0, x1 = 0.0;  // e_1
+  for (int p = 0; p < pieces; ++p) {
+    double t0 = x0, t1 = x1, s0 = x0, s1 = x1;
+    double f = inv;  // inv / q
+#pragma unroll 4
+    for (int q = 1; q <= 16; ++q) {
+      // t_q = (h T / pieces)^q e / q!, accumulated into s
+      const double left = __shfl_up_sync(full, t1, 1);    // t[i0 - 1]
+      const double right = __shfl_down_sync(full, t0, 1); // t[i1 + 1]
+      const double n0 = (a0 * t0 + b0 * t1 + (lane > 0 ? bmin * left : 0.0)) * f;
+      const double n1 = (a1 * t1 + b0 * t0 + (lane < 31 ? b1 * right : 0.0)) * f;
+      t0 = n0;
+      t1 = n1;
+      s0 += t0;
+      s1 += t1;
+      f = inv * kInvInt[q + 1];
+    }
+    x0 = s0;
+    x1 = s1;
   }
-  return sqrt(nrm);
+  if (i0 < k) c[i0] = x0;
+  if (i1 < k) c[i1] = x1;
+  double n2 = (i0 < k ? x0 * x0 : 0.0) + (i1 < k ? x1 * x1 : 0.0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(full, n2, o);
+  __syncwarp();
+  const double cn = sqrt(n2);
+  if (!isfinite(cn)) *ok = false;
+  return cn;
 }
 
 }  // namespace ttals

@@ -171,6 +171,9 @@ def adaptive_step_size(operator, initial_value, initial_guess, time_end: float, 
 
 _TDVP_KIND = {'adaptive': 0, 'one_site': 1, 'two_site': 2}
 
+# statistics of the last TDVP run (device time, launches, local exponentials)
+last_stats = {}
+
 
 def _real_cores(t, what):
     cores = []
@@ -224,6 +227,8 @@ def _run_tdvp(kind, operator, initial_value, step_size, number_of_steps, krylov_
     _lib.check(_lib.load().ttals_tdvp(_lib.context(), op.desc, x0.desc, _TDVP_KIND[kind], float(tau.real), steps,
                                        int(krylov_dim), float(threshold), mr, int(normalize), 0.0, _lib.dptr(out),
                                        out.size, 0, _lib.i64ptr(out_ranks), st))
+    global last_stats
+    last_stats = st.as_dict()
     solution = [initial_value]
     off = 0
     for k in range(steps):

@@ -116,6 +116,38 @@ def ising_evp(d=48, g=1.0, x_rank=64, repeats=6, seed=1) -> EVPInstance:
     return EVPInstance(ising_op(d, 1.0, g), x0, repeats, sigma, dict(d=d, g=g, x_rank=x_rank))
 
 
+@dataclass
+class TDVPInstance:
+    op: List[np.ndarray]
+    x0: List[np.ndarray]
+    step_size: complex
+    steps: int
+    max_rank: int
+    meta: dict = field(default_factory=dict)
+
+
+def right_orthonormal(cores: List[np.ndarray]) -> List[np.ndarray]:
+    """RQ sweep from the right (tensor_train.py:1262-1296 without truncation),
+    then the first core scaled to unit norm."""
+    cores = [c.copy() for c in cores]
+    for i in range(len(cores) - 1, 0, -1):
+        r, n, m, s = cores[i].shape
+        q, rr = np.linalg.qr(cores[i].reshape(r, n * m * s).T)
+        k = q.shape[1]
+        cores[i] = q.T.reshape(k, n, m, s)
+        cores[i - 1] = np.tensordot(cores[i - 1], rr.T, axes=(3, 0))
+    cores[0] = cores[0] / np.linalg.norm(cores[0])
+    return cores
+
+
+def tdvp_ising(d=16, g=1.2, x_rank=4, max_rank=16, steps=5, dt=0.05, seed=7) -> TDVPInstance:
+    """Imaginary-time two-site TDVP on the transverse-field Ising chain from a
+    random right-orthonormal rank-``x_rank`` state (step_size = -1j * dt)."""
+    x0 = right_orthonormal(gaussian_tt(np.random.default_rng(seed), d, 2, x_rank))
+    return TDVPInstance(ising_op(d, 1.0, g), x0, -1j * dt, steps, max_rank,
+                        dict(d=d, g=g, x_rank=x_rank, max_rank=max_rank, dt=dt))
+
+
 def reversible_markov(rng, n: int) -> np.ndarray:
     """Column-stochastic n x n transition matrix S D^-1 of a reversible chain
     (S symmetric positive, D its column sums): similar to the symmetric
