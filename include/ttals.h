@@ -213,6 +213,19 @@ int ttals_tdvp(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, int32_t k
                double* out, int64_t out_capacity, int32_t out_on_device, int64_t* out_ranks,
                ttals_stats* stats);
 
+/* Alternating ridge regression, scikit_tt/data_driven/regression.py:15 `arr`:
+ * one regression per output row.  theta: the basis functions of every mode
+ * evaluated on the data, mode i an (basis_sizes[i] x samples) row-major block,
+ * blocks back to back (regression.py:323-326); y: outputs x samples row-major;
+ * initial_guesses: one TT per output (row dims = basis sizes).  Each local
+ * step is the least-squares fit of lstsq(..., cond=rcond, lapack_driver=
+ * 'gelss') (regression.py:487) followed by the QR/RQ re-gauging.  out: the
+ * fitted trains back to back (capacity: the sum of the initial core sizes);
+ * out_ranks[outputs * (order + 1)].  Host buffers. */
+int ttals_arr(ttals_ctx* ctx, int32_t order, const int64_t* basis_sizes, int64_t samples, const double* theta,
+              int32_t outputs, const double* y, const ttals_tt* initial_guesses, int32_t repeats, double rcond,
+              double* out, int64_t out_capacity, int64_t* out_ranks, ttals_stats* stats);
+
 /* scikit_tt/tensor_train.py:422-501 (`__matmul__` / `dot`): core-wise
  * product of two trains; out has ranks a.ranks[i] * b.ranks[i]. */
 int ttals_tt_matmul(ttals_ctx* ctx, const ttals_tt* a, const ttals_tt* b, double* out_data,

@@ -696,3 +696,59 @@ def tdvp_adaptive(op, x0, tau, steps, threshold=1e-12, max_rank=50, normalize=0)
                 i -= 1
         S.finish_step(normalize, states)
     return states
+
+
+# ----------------------------------------------------------------------------
+# regression.arr (data_driven/regression.py:15-142, 297-494)
+# ----------------------------------------------------------------------------
+
+
+def arr(theta, y_data, x0s, repeats=1, rcond=1e-2):
+    """Alternating ridge regression on pre-evaluated basis values
+    ``theta[i]`` (n_i x m, regression.py:323-326); ``x0s``: one core list per
+    output row.  Returns the fitted core lists."""
+    d = len(theta)
+    m = theta[0].shape[1]
+    out = []
+    for k in range(y_data.shape[0]):
+        cores = [c.copy() for c in x0s[k]]
+        rhs = y_data[k, :]
+        sl, sr = [None] * d, [None] * d
+
+        def left(i):                                     # regression.py:297-327
+            if i == 0:
+                sl[0] = np.ones((1, m))
+            else:
+                sl[i] = np.einsum('ij,kj,ikl->lj', sl[i - 1], theta[i - 1], cores[i - 1][:, :, 0, :])
+
+        def right(i):                                    # regression.py:330-361
+            if i == d - 1:
+                sr[i] = np.ones((1, m))
+            else:
+                sr[i] = np.einsum('ikl,kj,lj->ij', cores[i + 1][:, :, 0, :], theta[i + 1], sr[i + 1])
+
+        def update(i, direction):                        # regression.py:364-494
+            a, n, s = cores[i].shape[0], theta[i].shape[0], cores[i].shape[3]
+            phi = np.einsum('ij,kj,lj->iklj', sl[i], theta[i], sr[i]).reshape(a * n * s, m)
+            x, _, _, _ = sla.lstsq(phi.T, rhs, cond=rcond, lapack_driver='gelss')
+            if direction == 'forward':
+                q, _ = sla.qr(x.reshape(a * n, s), mode='economic', check_finite=False)
+                cores[i] = q.reshape(a, n, 1, q.shape[1])
+            elif i > 0:
+                _, q = sla.rq(x.reshape(a, n * s), mode='economic', check_finite=False)
+                cores[i] = q.reshape(q.shape[0], n, 1, s)
+            else:
+                cores[i] = x.reshape(a, n, 1, s)
+
+        for i in range(d - 1, -1, -1):
+            right(i)
+        for _ in range(repeats):
+            for i in range(d):
+                left(i)
+                if i < d - 1:
+                    update(i, 'forward')
+            for i in range(d - 1, -1, -1):
+                right(i)
+                update(i, 'backward')
+        out.append(cores)
+    return out

@@ -39,7 +39,7 @@ EXPORTS = (
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
     'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_apply_f32',
-    'ttals_apply_f64emu', 'ttals_tdvp',
+    'ttals_apply_f64emu', 'ttals_tdvp', 'ttals_arr',
 )
 
 REQ_SLE = 0
@@ -103,6 +103,8 @@ def load():
         lib.ttals_evp_als.argtypes = [vp, P(TTDesc), P(TTDesc), i32, P(TTDesc), dbl, i32, i32, dbl, i32, dbl, i32,
                                       dbl, pd, pd, i32, pi64, P(i32), P(Stats)]
         lib.ttals_tt_matmul.argtypes = [vp, P(TTDesc), P(TTDesc), pd, i32]
+        lib.ttals_arr.argtypes = [vp, i32, pi64, C.c_int64, pd, i32, pd, P(TTDesc), i32, dbl, pd, C.c_int64, pi64,
+                                  P(Stats)]
         lib.ttals_tdvp.argtypes = [vp, P(TTDesc), P(TTDesc), i32, dbl, i32, i32, dbl, C.c_int64, i32, dbl, pd,
                                    C.c_int64, i32, pi64, P(Stats)]
         lib.ttals_batch_slots.argtypes = [vp, C.POINTER(i32)]

@@ -17,6 +17,8 @@
 //     by Householder QR (span(M w_1..w_r) = span(u_1..u_r)).
 #include <float.h>
 
+#include <algorithm>
+
 #include "ttals_internal.h"
 #include "ttals_qr.cuh"
 
@@ -424,6 +426,40 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
     if (a.side == 0) a.r[e] = v;
     else a.core[e] = sg > 0.0 ? v / sg : (i == j ? 1.0 : 0.0);
   }
+}
+
+// Minimum-norm least-squares solution from the truncated SVD of R (the
+// gelss step of scipy.linalg.lstsq, used by scikit_tt/data_driven/
+// regression.py:487): R (kq x N) = U S V^T with the r = *kept leading
+// singular values, c = Q^T y:  x = V S^-1 U^T c = (S V^T)^T S^-2 (U^T c).
+// U: kq x r (row-major, leading dimension r), SVt: r x N.  One CTA.
+__global__ void __launch_bounds__(1024) lstsq_combine_kernel(const double* U, const double* SVt, const double* c,
+                                                              int64_t kq, int64_t N, const int* kept, double* x) {
+  __shared__ double w[kTrMaxGram];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int r = *kept;
+  for (int i = warp; i < r; i += nw) {
+    double dot = 0.0, s2 = 0.0;
+    for (int64_t q = lane; q < kq; q += 32) dot += U[q * r + i] * c[q];
+    for (int64_t p = lane; p < N; p += 32) s2 += SVt[i * N + p] * SVt[i * N + p];
+    dot = warp_sum(dot);
+    s2 = warp_sum(s2);
+    if (lane == 0) w[i] = s2 > 0.0 ? dot / s2 : 0.0;
+  }
+  __syncthreads();
+  for (int64_t p = tid; p < N; p += nt) {
+    double acc = 0.0;
+    for (int i = 0; i < r; ++i) acc += SVt[i * N + p] * w[i];
+    x[p] = acc;
+  }
+}
+
+cudaError_t launch_lstsq_combine(const double* U, const double* SVt, const double* c, int64_t kq, int64_t N,
+                                 const int* kept, double* x, cudaStream_t st) {
+  if (std::min(kq, N) > kTrMaxGram) return cudaErrorInvalidValue;
+  lstsq_combine_kernel<<<1, 1024, 0, st>>>(U, SVt, c, kq, N, kept, x);
+  ++launch_counter();
+  return cudaGetLastError();
 }
 
 constexpr size_t kSvdSmemMax = 160 * 1024;  // plus ~16 KB of static shared memory

@@ -157,6 +157,10 @@ size_t svd_trunc_work_doubles(int64_t p, int64_t q);
 cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
                              double* work, double* core, double* r, int* kept, int* status, cudaStream_t st);
 
+// x = V S^-1 U^T c from the truncated SVD of R (kernels_evp.cu, least squares)
+cudaError_t launch_lstsq_combine(const double* U, const double* SVt, const double* c, int64_t kq, int64_t N,
+                                 const int* kept, double* x, cudaStream_t st);
+
 // failure-detection probe (kernels_basic.cu): bounded wait on *flag leaving 0
 cudaError_t launch_wait_probe(const unsigned* flag, unsigned limit, int* status, cudaStream_t st);
 

@@ -297,6 +297,66 @@ def tdvp_cases():
               local_solver={'method': 'krylov', 'dimension': 4}, normalize=0)
 
 
+def kuramoto_data(d=10, m=1000, seed=3):
+    """The Kuramoto setting of the reference's tests/test_regression.py:24-71
+    (oscillator phases from solve_ivp, derivatives as outputs), seeded."""
+    import scipy.integrate as spint
+    rng = np.random.default_rng(seed)
+    x0 = 2 * np.pi * rng.random(d) - np.pi
+    w = np.linspace(-5, 5, d)
+
+    def rhs(_, theta):
+        ti, tj = np.meshgrid(theta, theta)
+        return w + 2 / d * np.sin(tj - ti).sum(0) + 0.2 * np.sin(theta)
+
+    sol = spint.solve_ivp(rhs, [0, 100], x0, method='BDF', t_eval=np.linspace(0, 100, m))
+    x = sol.y
+    y = np.zeros((d, m))
+    for j in range(m):
+        y[:, j] = rhs(0, x[:, j])
+    return x, y, w
+
+
+def arr_case(name, x, y, basis, x0, repeats, rcond):
+    import scikit_tt.data_driven.regression as rreg
+    sol = rreg.arr(x, y, basis, RTT([c.copy() for c in x0]), repeats=repeats, rcond=rcond, progress=False)
+    theta = [np.array([[f(x[:, j]) for j in range(x.shape[1])] for f in funcs]) for funcs in basis]
+    out = {'repeats': np.array(repeats), 'rcond': np.array(rcond), 'x': x, 'y': y, 'n_out': np.array(len(sol))}
+    for i, t in enumerate(theta):
+        out[f'theta_{i}'] = t
+    out['theta_n'] = np.array(len(theta))
+    pack('x0', x0, out)
+    for k, t in enumerate(sol):
+        pack(f'sol{k}', [np.asarray(c) for c in t.cores], out)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'outputs', len(sol), 'ranks', sol[0].ranks)
+
+
+def arr_cases():
+    """regression.arr on the Kuramoto data of the reference's own test (sine and
+    cosine bases of 11 functions, rank 11), and a three-mode fit with ranks 3, 2."""
+    import scikit_tt.data_driven.transform as rtdt
+    x, y, w = kuramoto_data()
+    basis = [[rtdt.ConstantFunction(0)] + [rtdt.Sin(i, 1) for i in range(10)],
+             [rtdt.ConstantFunction(0)] + [rtdt.Cos(i, 1) for i in range(10)]]
+    x0 = [c.copy() for c in rtt.ones([11, 11], [1, 1], 11).cores]
+    arr_case('arr_kuramoto_rcond12', x, y, basis, x0, 3, 1e-12)
+    # exact coefficient tensor of the Kuramoto right-hand side (tests/test_regression.py:36, 116-137)
+    z = dict(np.load(os.path.join(HERE, 'arr_kuramoto_rcond12.npz')))
+    z['xi_exact_full'] = np.asarray(rmodels.kuramoto_coefficients(10, w).full()).reshape(-1)
+    np.savez_compressed(os.path.join(HERE, 'arr_kuramoto_rcond12.npz'), **z)
+    arr_case('arr_kuramoto_rcond2', x, y, basis, x0, 2, 1e-2)
+    rng = np.random.default_rng(41)
+    xs = rng.uniform(-1, 1, (3, 400))
+    ys = np.vstack([np.sin(2 * xs[0]) * xs[1] + 0.5 * xs[2] ** 2, np.exp(-xs[0] ** 2) - xs[1] * xs[2]])
+    basis3 = [[rtdt.ConstantFunction(0), rtdt.Identity(0), rtdt.Monomial(0, 2), rtdt.Sin(0, 2)],
+              [rtdt.ConstantFunction(1), rtdt.Identity(1), rtdt.Monomial(1, 2), rtdt.Monomial(1, 3),
+               rtdt.GaussFunction(1, 0.0, 0.5)],
+              [rtdt.ConstantFunction(2), rtdt.Identity(2), rtdt.Legendre(2, 2)]]
+    x03 = [c.copy() for c in rtt.rand([4, 5, 3], [1, 1, 1], [1, 3, 2, 1]).cores]
+    arr_case('arr_three_mode', xs, ys, basis3, x03, 3, 1e-10)
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -330,6 +390,7 @@ def main():
     trunc_cases()
     mals_cases()
     tdvp_cases()
+    arr_cases()
 
 
 if __name__ == '__main__':
@@ -345,5 +406,7 @@ if __name__ == '__main__':
         mals_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'tdvp':
         tdvp_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'arr':
+        arr_cases()
     else:
         main()

@@ -130,3 +130,48 @@ def test_tdvp_refuses_real_time_steps():
     x = TT([np.ones((1, 2, 1, 1))] * 3)
     with pytest.raises(NotImplementedError):
         ode.tdvp1site(op, x, 0.1, 2)
+
+
+ARR_CASES = ['arr_kuramoto_rcond12', 'arr_kuramoto_rcond2', 'arr_three_mode']
+
+
+def arr_inputs(z):
+    theta = [z[f'theta_{i}'] for i in range(int(z['theta_n']))]
+    x0 = [z[f'x0_{i}'] for i in range(int(z['x0_n']))]
+    refs = [[z[f'sol{k}_{i}'] for i in range(int(z[f'sol{k}_n']))] for k in range(int(z['n_out']))]
+    return theta, x0, refs
+
+
+def kuramoto_basis():
+    from scikit_tt_gb300.data_driven import transform as tdt
+    return [[tdt.ConstantFunction(0)] + [tdt.Sin(i, 1) for i in range(10)],
+            [tdt.ConstantFunction(0)] + [tdt.Cos(i, 1) for i in range(10)]]
+
+
+def three_mode_basis():
+    from scikit_tt_gb300.data_driven import transform as tdt
+    return [[tdt.ConstantFunction(0), tdt.Identity(0), tdt.Monomial(0, 2), tdt.Sin(0, 2)],
+            [tdt.ConstantFunction(1), tdt.Identity(1), tdt.Monomial(1, 2), tdt.Monomial(1, 3),
+             tdt.GaussFunction(1, 0.0, 0.5)],
+            [tdt.ConstantFunction(2), tdt.Identity(2), tdt.Legendre(2, 2)]]
+
+
+@pytest.mark.parametrize('name', ARR_CASES)
+def test_oracle_arr_matches_reference(golden, name):
+    z, _ = golden(name)
+    theta, x0, refs = arr_inputs(z)
+    sols = O.arr(theta, z['y'], [x0] * len(refs), repeats=int(z['repeats']), rcond=float(z['rcond']))
+    for s, r in zip(sols, refs):
+        v = O.full_vector(r)
+        assert np.linalg.norm(O.full_vector(s) - v) / np.linalg.norm(v) < 1e-12
+
+
+@pytest.mark.parametrize('name', ['arr_kuramoto_rcond2', 'arr_three_mode'])
+def test_basis_functions_match_reference(golden, name):
+    """The package's basis functions evaluate to the reference's values."""
+    from scikit_tt_gb300.data_driven import regression
+    z, _ = golden(name)
+    basis = kuramoto_basis() if name.startswith('arr_kuramoto') else three_mode_basis()
+    theta = regression.evaluate_basis(z['x'], basis)
+    for i, t in enumerate(theta):
+        assert np.allclose(t, z[f'theta_{i}'], rtol=1e-14, atol=1e-15)
