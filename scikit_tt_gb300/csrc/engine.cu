@@ -1209,6 +1209,12 @@ void run_tdvp(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, int kind,
 // economic QR (forward) / RQ (backward) re-gauging of sle.als, the R factor
 // discarded as the reference does.  Every step is device work; ranks follow
 // from the shapes, so nothing returns to the host inside a sweep.
+//
+// The regressions of different outputs are independent and their QR / SVD
+// kernels run on one CTA each, so up to kArrLanes of them run side by side,
+// each on its own stream with its own buffers; all host copies happen before
+// and after (a pageable copy inside a lane would stall its stream).
+constexpr int kArrLanes = 32;
 
 void run_arr(ttals_ctx* c, int d, const int64_t* nb, int64_t m, const double* theta, int nout, const double* y,
              const ttals_tt* x0s, int repeats, double rcond, double* out, int64_t out_capacity, int64_t* out_ranks,
@@ -1220,12 +1226,12 @@ void run_arr(ttals_ctx* c, int d, const int64_t* nb, int64_t m, const double* th
   require(out != nullptr, TTALS_ERR_ARG, "output buffer is null");
   std::vector<int64_t> n(nb, nb + d);
   std::vector<TTView> xv;
-  int64_t need = 0, th_total = 0, maxN = 1, maxU = 1, maxStack = 1, maxR = 1, maxQ = 1, svdw = 1, maxCore = 1,
-          maxRQ = 1;
+  int64_t th_total = 0, maxN = 1, maxU = 1, maxStack = 1, maxR = 1, maxQ = 1, svdw = 1, maxRQ = 1;
   for (int i = 0; i < d; ++i) {
     require(n[i] >= 1, TTALS_ERR_ARG, "basis sizes must be >= 1");
     th_total += n[i] * m;
   }
+  std::vector<int64_t> x_off(nout + 1, 0);
   for (int k = 0; k < nout; ++k) {
     xv.push_back(view(x0s + k, "initial_guess"));
     const TTView& v = xv.back();
@@ -1236,136 +1242,189 @@ void run_arr(ttals_ctx* c, int d, const int64_t* nb, int64_t m, const double* th
       const int64_t a = v.r[i], s = v.r[i + 1], N = a * n[i] * s, kq = std::min(m, N);
       require(std::min(kq, N) <= 1024, TTALS_ERR_UNSUPPORTED, "ARR: local problem above 1024 unknowns");
       maxN = std::max(maxN, N);
-      maxCore = std::max(maxCore, N);
       maxU = std::max(maxU, std::max(a, s) * n[i] * m);
       maxStack = std::max(maxStack, std::max(a, s) * m);
       maxR = std::max(maxR, kq * N);
       maxRQ = std::max(maxRQ, std::max(a * a, s * s));
       maxQ = std::max(maxQ, std::max(qr_work(m, N), std::max(qr_work(a * n[i], s), qr_work(n[i] * s, a))));
       svdw = std::max(svdw, (int64_t)svd_trunc_work_doubles(kq, N));
-      need += N;
     }
     require(v.r[0] == 1 && v.r[d] == 1, TTALS_ERR_ARG, "initial_guess: boundary ranks must be 1");
+    x_off[k + 1] = x_off[k] + v.total;
   }
-  require(out_capacity >= need, TTALS_ERR_ARG, "output buffer too small: need the sum of the initial core sizes");
+  require(out_capacity >= x_off[nout], TTALS_ERR_ARG, "output buffer too small: need the sum of the initial core sizes");
 
   launch_counter() = 0;
   Engine E;
   E.c = c;
   Bump B{c};
-  double *th = nullptr, *yd = nullptr, *A = nullptr, *Rb = nullptr, *U = nullptr, *cv = nullptr, *cb = nullptr,
-         *sb = nullptr, *sw = nullptr, *kept = nullptr, *qw = nullptr, *rq = nullptr;
-  std::vector<double*> X(d), Ls(d), Rs(d);
+  const int G = std::min(nout, kArrLanes);
+  struct Lane {
+    double *A = nullptr, *Rb = nullptr, *U = nullptr, *cv = nullptr, *cb = nullptr, *sb = nullptr, *sw = nullptr,
+           *kept = nullptr, *qw = nullptr, *rq = nullptr;
+    std::vector<double*> X, Ls, Rs;
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+  };
+  std::vector<Lane> lanes(G);
+  double *th = nullptr, *yd = nullptr, *x0d = nullptr, *outd = nullptr;
   B.want(&th, th_total);
   B.want(&yd, (int64_t)nout * m);
-  B.want(&A, m * maxN);
-  B.want(&Rb, maxR);
-  B.want(&U, maxU);
-  B.want(&cv, maxN);
-  B.want(&cb, maxN * maxN);
-  B.want(&sb, maxN * maxN);
-  B.want(&sw, svdw);
-  B.want(&kept, 1);
-  B.want(&qw, maxQ);
-  B.want(&rq, maxRQ);
-  for (int i = 0; i < d; ++i) {
-    B.want(&X[i], maxCore);
-    B.want(&Ls[i], maxStack);
-    B.want(&Rs[i], maxStack);
+  B.want(&x0d, x_off[nout]);
+  B.want(&outd, x_off[nout]);
+  for (Lane& L : lanes) {
+    B.want(&L.A, m * maxN);
+    B.want(&L.Rb, maxR);
+    B.want(&L.U, maxU);
+    B.want(&L.cv, maxN);
+    B.want(&L.cb, maxN * maxN);
+    B.want(&L.sb, maxN * maxN);
+    B.want(&L.sw, svdw);
+    B.want(&L.kept, 1);
+    B.want(&L.qw, maxQ);
+    B.want(&L.rq, maxRQ);
+    L.X.resize(d);
+    L.Ls.resize(d);
+    L.Rs.resize(d);
+    for (int i = 0; i < d; ++i) {
+      B.want(&L.X[i], maxN);
+      B.want(&L.Ls[i], maxStack);
+      B.want(&L.Rs[i], maxStack);
+    }
   }
   B.want(&E.status, 4);
   B.want(&E.reports, 4);
   E.solve_cap = 1;
   B.commit();
-  int* kdev = reinterpret_cast<int*>(kept);
   std::vector<int64_t> th_off(d + 1, 0);
   for (int i = 0; i < d; ++i) th_off[i + 1] = th_off[i] + n[i] * m;
+  auto Th = [&](int i) { return th + th_off[i]; };
 
   CK(cudaEventRecord(c->ev0, c->stream));
   CK(cudaMemsetAsync(E.status, 0, 4 * sizeof(int), c->stream));
   CK(cudaMemcpyAsync(th, theta, sizeof(double) * th_total, cudaMemcpyHostToDevice, c->stream));
   CK(cudaMemcpyAsync(yd, y, sizeof(double) * nout * m, cudaMemcpyHostToDevice, c->stream));
-  auto Th = [&](int i) { return th + th_off[i]; };
-  std::vector<int64_t> r;
-  // H[a, b, j] = S[a, j] theta_i[b, j]  (a < ra)
-  auto outer = [&](const double* S, int i, int64_t ra, double* H) {
-    const Ax o[3] = {{ra, m, 0, n[i] * m}, {n[i], 0, m, m}, {m, 1, 1, 1}};
-    CK(launch_contract<double>(desc_make(3, o, 0, nullptr), S, Th(i), H, 1.0, 0.0, c->stream));
-  };
-  auto left = [&](int i) {  // L_i (r_i x m), regression.py:297-327
-    if (i == 0) {
-      CK(launch_fill(Ls[0], m, 1.0, c->stream));
-      return;
+  for (int k = 0; k < nout; ++k)
+    CK(cudaMemcpyAsync(x0d + x_off[k], xv[k].data, sizeof(double) * xv[k].total,
+                       xv[k].dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  cudaEvent_t ready;
+  CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  CK(cudaEventRecord(ready, c->stream));
+  struct Cleanup {
+    std::vector<Lane>& l;
+    cudaEvent_t e;
+    ~Cleanup() {
+      for (Lane& L : l) {
+        if (L.st) cudaStreamDestroy(L.st);
+        if (L.done) cudaEventDestroy(L.done);
+      }
+      cudaEventDestroy(e);
     }
-    const int64_t a = r[i - 1], nn = n[i - 1], s = r[i];
-    outer(Ls[i - 1], i - 1, a, U);
-    const Ax o[2] = {{s, 0, 1, m}, {m, 1, 0, 1}};
-    const Ax k[2] = {{a, nn * m, nn * s, 0}, {nn, m, s, 0}};
-    CK(launch_contract<double>(desc_make(2, o, 2, k), U, X[i - 1], Ls[i], 1.0, 0.0, c->stream));
-  };
-  auto right = [&](int i) {  // R_i (r_{i+1} x m), regression.py:330-361
-    if (i == d - 1) {
-      CK(launch_fill(Rs[d - 1], m, 1.0, c->stream));
-      return;
-    }
-    const int64_t a = r[i + 1], nn = n[i + 1], s = r[i + 2];
-    const Ax o1[3] = {{a, nn * s, 0, nn * m}, {nn, s, 0, m}, {m, 0, 1, 1}};
-    const Ax k1[1] = {{s, 1, m, 0}};
-    CK(launch_contract<double>(desc_make(3, o1, 1, k1), X[i + 1], Rs[i + 1], U, 1.0, 0.0, c->stream));
-    const Ax o2[2] = {{a, nn * m, 0, m}, {m, 1, 1, 1}};
-    const Ax k2[1] = {{nn, m, m, 0}};
-    CK(launch_contract<double>(desc_make(2, o2, 1, k2), U, Th(i + 1), Rs[i], 1.0, 0.0, c->stream));
-  };
-  // least-squares core update, regression.py:364-494
-  auto solve = [&](int i, const double* yk, bool forward) {
-    const int64_t a = r[i], nn = n[i], s = r[i + 1], N = a * nn * s, kq = std::min(m, N);
-    outer(Ls[i], i, a, U);
-    // A[j, (a, b, l)] = H[a, b, j] R_i[l, j]  (Phi^T, m x N)
-    const Ax o[4] = {{m, 1, 1, N}, {a, nn * m, 0, nn * s}, {nn, m, 0, s}, {s, 0, m, 1}};
-    CK(launch_contract<double>(desc_make(4, o, 0, nullptr), U, Rs[i], A, 1.0, 0.0, c->stream));
-    QrArgs q{A, N, 1, A, kq, 1, Rb, N, 1, m, N, 0, nullptr, qw};
-    CK(launch_qr_fast(q, c->stream));
-    // c = Q^T y (kq)
-    const Ax oc[1] = {{kq, 1, 0, 1}};
-    const Ax kc[1] = {{m, kq, 1, 0}};
-    CK(launch_contract<double>(desc_make(1, oc, 1, kc), A, yk, cv, 1.0, 0.0, c->stream));
-    CK(launch_svd_trunc(Rb, kq, N, 0, rcond, 0, sw, cb, sb, kdev, E.status, c->stream));
-    CK(launch_lstsq_combine(cb, sb, cv, kq, N, kdev, X[i], c->stream));
-    if (forward) {
-      qr_forward(c, X[i], a, nn, s, rq, qw);
-      r[i + 1] = std::min(a * nn, s);
-    } else if (i > 0) {
-      rq_backward(c, X[i], a, nn, s, rq, qw, 0, nullptr);
-      r[i] = std::min(a, nn * s);
-    }
-  };
+  } cleanup{lanes, ready};
+  for (Lane& L : lanes) {
+    CK(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+    CK(cudaStreamWaitEvent(L.st, ready, 0));
+  }
 
-  int64_t off = 0;
+  std::vector<std::vector<int64_t>> rk(nout);
   for (int k = 0; k < nout; ++k) {
+    Lane& L = lanes[k % G];
+    const cudaStream_t s_ = L.st;
     const TTView& v = xv[k];
+    std::vector<int64_t>& r = rk[k];
     r = v.r;
     for (int i = 0; i < d; ++i)
-      CK(cudaMemcpyAsync(X[i], v.data + v.off[i], sizeof(double) * (v.off[i + 1] - v.off[i]),
-                         v.dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+      CK(cudaMemcpyAsync(L.X[i], x0d + x_off[k] + v.off[i], sizeof(double) * (v.off[i + 1] - v.off[i]),
+                         cudaMemcpyDeviceToDevice, s_));
     const double* yk = yd + (int64_t)k * m;
+    // H[a, b, j] = S[a, j] theta_i[b, j]  (a < ra)
+    auto outer = [&](const double* S, int i, int64_t ra, double* H) {
+      const Ax o[3] = {{ra, m, 0, n[i] * m}, {n[i], 0, m, m}, {m, 1, 1, 1}};
+      CK(launch_contract<double>(desc_make(3, o, 0, nullptr), S, Th(i), H, 1.0, 0.0, s_));
+    };
+    auto left = [&](int i) {  // L_i (r_i x m), regression.py:297-327
+      if (i == 0) {
+        CK(launch_fill(L.Ls[0], m, 1.0, s_));
+        return;
+      }
+      const int64_t a = r[i - 1], nn = n[i - 1], s = r[i];
+      outer(L.Ls[i - 1], i - 1, a, L.U);
+      const Ax o[2] = {{s, 0, 1, m}, {m, 1, 0, 1}};
+      const Ax kk[2] = {{a, nn * m, nn * s, 0}, {nn, m, s, 0}};
+      CK(launch_contract<double>(desc_make(2, o, 2, kk), L.U, L.X[i - 1], L.Ls[i], 1.0, 0.0, s_));
+    };
+    auto right = [&](int i) {  // R_i (r_{i+1} x m), regression.py:330-361
+      if (i == d - 1) {
+        CK(launch_fill(L.Rs[d - 1], m, 1.0, s_));
+        return;
+      }
+      const int64_t a = r[i + 1], nn = n[i + 1], s = r[i + 2];
+      const Ax o1[3] = {{a, nn * s, 0, nn * m}, {nn, s, 0, m}, {m, 0, 1, 1}};
+      const Ax k1[1] = {{s, 1, m, 0}};
+      CK(launch_contract<double>(desc_make(3, o1, 1, k1), L.X[i + 1], L.Rs[i + 1], L.U, 1.0, 0.0, s_));
+      const Ax o2[2] = {{a, nn * m, 0, m}, {m, 1, 1, 1}};
+      const Ax k2[1] = {{nn, m, m, 0}};
+      CK(launch_contract<double>(desc_make(2, o2, 1, k2), L.U, Th(i + 1), L.Rs[i], 1.0, 0.0, s_));
+    };
+    // least-squares core update, regression.py:364-494
+    auto solve = [&](int i, bool forward) {
+      const int64_t a = r[i], nn = n[i], s = r[i + 1], N = a * nn * s, kq = std::min(m, N);
+      outer(L.Ls[i], i, a, L.U);
+      // A[j, (a, b, l)] = H[a, b, j] R_i[l, j]  (Phi^T, m x N)
+      const Ax o[4] = {{m, 1, 1, N}, {a, nn * m, 0, nn * s}, {nn, m, 0, s}, {s, 0, m, 1}};
+      CK(launch_contract<double>(desc_make(4, o, 0, nullptr), L.U, L.Rs[i], L.A, 1.0, 0.0, s_));
+      QrArgs q{L.A, N, 1, L.A, kq, 1, L.Rb, N, 1, m, N, 0, nullptr, L.qw};
+      CK(launch_qr_fast(q, s_));
+      // c = Q^T y (kq)
+      const Ax oc[1] = {{kq, 1, 0, 1}};
+      const Ax kc[1] = {{m, kq, 1, 0}};
+      CK(launch_contract<double>(desc_make(1, oc, 1, kc), L.A, yk, L.cv, 1.0, 0.0, s_));
+      int* kdev = reinterpret_cast<int*>(L.kept);
+      CK(launch_svd_trunc(L.Rb, kq, N, 0, rcond, 0, L.sw, L.cb, L.sb, kdev, E.status, s_));
+      CK(launch_lstsq_combine(L.cb, L.sb, L.cv, kq, N, kdev, L.X[i], s_));
+      if (forward) {
+        QrArgs f{L.X[i], s, 1, L.X[i], std::min(a * nn, s), 1, L.rq, s, 1, a * nn, s, 0, nullptr, L.qw};
+        CK(launch_qr_fast(f, s_));
+        r[i + 1] = std::min(a * nn, s);
+      } else if (i > 0) {
+        const int64_t ns = nn * s, k2 = std::min(a, ns);
+        QrArgs b{L.X[i], 1, ns, L.X[i], 1, ns, L.rq, 1, k2, ns, a, 0, nullptr, L.qw};
+        CK(launch_qr_fast(b, s_));
+        r[i] = k2;
+      }
+    };
     for (int i = d - 1; i >= 0; --i) right(i);
     for (int it = 0; it < repeats; ++it) {
       for (int i = 0; i < d; ++i) {
         left(i);
-        if (i < d - 1) solve(i, yk, true);
+        if (i < d - 1) solve(i, true);
       }
       for (int i = d - 1; i >= 0; --i) {
         right(i);
-        solve(i, yk, false);
+        solve(i, false);
       }
     }
+    int64_t off = x_off[k];
     for (int i = 0; i < d; ++i) {
       const int64_t cnt = r[i] * n[i] * r[i + 1];
-      CK(cudaMemcpyAsync(out + off, X[i], sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(outd + off, L.X[i], sizeof(double) * cnt, cudaMemcpyDeviceToDevice, s_));
       off += cnt;
     }
+  }
+  for (Lane& L : lanes) {
+    CK(cudaEventRecord(L.done, L.st));
+    CK(cudaStreamWaitEvent(c->stream, L.done, 0));
+  }
+  // compact the per-output trains into out, back to back
+  int64_t off = 0;
+  for (int k = 0; k < nout; ++k) {
+    int64_t cnt = 0;
+    for (int i = 0; i < d; ++i) cnt += rk[k][i] * n[i] * rk[k][i + 1];
+    CK(cudaMemcpyAsync(out + off, outd + x_off[k], sizeof(double) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    off += cnt;
     if (out_ranks)
-      for (int i = 0; i <= d; ++i) out_ranks[(int64_t)k * (d + 1) + i] = r[i];
+      for (int i = 0; i <= d; ++i) out_ranks[(int64_t)k * (d + 1) + i] = rk[k][i];
   }
   CK(cudaEventRecord(c->ev1, c->stream));
   check_status(E);

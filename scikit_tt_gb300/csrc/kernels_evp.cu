@@ -259,7 +259,7 @@ struct SvdK {
   double* r;
   int* kept;         // out: k
   int* status;
-  int in_smem;       // W and Vr live in dynamic shared memory instead
+  int in_smem;       // 1: W in dynamic shared memory, 2: W and Vr
 };
 
 __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
   const int ncols = (int)(tr ? a.p : a.q);   // number of working columns
   // the rotation steps re-read every column: shared memory when it fits
   double* W = a.in_smem ? s_dyn : a.W;
-  double* V = a.in_smem ? s_dyn + rows * ncols : a.Vr;
+  double* V = a.in_smem == 2 ? s_dyn + rows * ncols : a.Vr;
   for (int64_t e = tid; e < rows * ncols; e += nt) {
     const int64_t c = e / rows, i = e - c * rows;
     W[e] = tr ? a.M[c * a.q + i] : a.M[i * a.q + c];
@@ -473,15 +473,17 @@ cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, do
                              double* work, double* core, double* r, int* kept, int* status, cudaStream_t st) {
   const int64_t n = p < q ? p : q, rows = p > q ? p : q;
   if (n > kTrMaxGram || n < 1) return cudaErrorInvalidValue;
-  const size_t bytes = sizeof(double) * (size_t)(rows * n + n * n);
-  const int in_smem = bytes <= kSvdSmemMax;
+  // the dots read W at every rotation step: W first, then V if both fit
+  const size_t wbytes = sizeof(double) * (size_t)(rows * n), bytes_all = wbytes + sizeof(double) * (size_t)(n * n);
+  const int in_smem = bytes_all <= kSvdSmemMax ? 2 : (wbytes <= kSvdSmemMax ? 1 : 0);
+  const size_t bytes = in_smem == 2 ? bytes_all : (in_smem == 1 ? wbytes : 0);
   SvdK a{M, p, q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status, in_smem};
   if (in_smem) {
     cudaError_t e = cudaFuncSetAttribute(svd_trunc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSvdSmemMax);
     if (e != cudaSuccess) return e;
   }
-  svd_trunc_kernel<<<1, kTrThreads, in_smem ? bytes : 0, st>>>(a);
+  svd_trunc_kernel<<<1, kTrThreads, bytes, st>>>(a);
   ++launch_counter();
   return cudaGetLastError();
 }
