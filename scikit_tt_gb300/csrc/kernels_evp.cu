@@ -259,7 +259,9 @@ struct SvdK {
   double* r;
   int* kept;         // out: k
   int* status;
-  int in_smem;       // 1: W in dynamic shared memory, 2: W and Vr
+  float* W32;        // FP32 copies for the preconditioning sweeps
+  float* V32;
+  int in_smem;       // bits: 1 W, 2 W32, 4 Vr, 8 V32 in dynamic shared memory (in that order)
 };
 
 __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
@@ -273,9 +275,17 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
   const bool tr = a.q > a.p;                 // work on M^T when M is wide
   const int64_t rows = tr ? a.q : a.p;       // length of a working column
   const int ncols = (int)(tr ? a.p : a.q);   // number of working columns
-  // the rotation steps re-read every column: shared memory when it fits
-  double* W = a.in_smem ? s_dyn : a.W;
-  double* V = a.in_smem == 2 ? s_dyn + rows * ncols : a.Vr;
+  // the rotation steps re-read every column: shared memory where it fits
+  char* sp = reinterpret_cast<char*>(s_dyn);
+  auto carve = [&](int bit, int64_t bytes) {
+    char* p = sp;
+    if (a.in_smem & bit) sp += (bytes + 7) / 8 * 8;
+    return p;
+  };
+  double* W = (a.in_smem & 1) ? reinterpret_cast<double*>(carve(1, 8 * rows * ncols)) : a.W;
+  float* W32 = (a.in_smem & 2) ? reinterpret_cast<float*>(carve(2, 4 * rows * ncols)) : a.W32;
+  double* V = (a.in_smem & 4) ? reinterpret_cast<double*>(carve(4, 8 * (int64_t)ncols * ncols)) : a.Vr;
+  float* V32 = (a.in_smem & 8) ? reinterpret_cast<float*>(carve(8, 4 * (int64_t)ncols * ncols)) : a.V32;
   for (int64_t e = tid; e < rows * ncols; e += nt) {
     const int64_t c = e / rows, i = e - c * rows;
     W[e] = tr ? a.M[c * a.q + i] : a.M[i * a.q + c];
@@ -300,6 +310,134 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
   __syncthreads();
   const double live_floor = 1e-30 * s_fro2;
   const int nn = (ncols + 1) & ~1, npairs = nn / 2;
+  // pair (ia, ib) of warp-slot pi in round-robin step `step`
+  auto pair_of = [&](int pi, int step, int& ia, int& ib) {
+    auto pos = [&](int j) { return j == 0 ? 0 : ((j - 1 + step) % (nn - 1)) + 1; };
+    ia = pos(pi);
+    ib = pos(nn - 1 - pi);
+    if (ia > ib) {
+      const int t = ia;
+      ia = ib;
+      ib = t;
+    }
+  };
+  if (ncols > 1) {
+    // Preconditioning in FP32 (57x the FP64 rate here): Jacobi sweeps on a
+    // power-of-two scaled FP32 copy until the columns are orthogonal to ~1e-6,
+    // then V = the FP32 rotations re-orthonormalised in FP64 and W = M V in
+    // FP64.  The FP64 sweeps below start from nearly orthogonal columns; their
+    // stopping rule and accuracy are unchanged.
+    double amax = 0.0;
+    for (int64_t e = tid; e < rows * ncols; e += nt) amax = fmax(amax, fabs(W[e]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if (lane == 0) s_red[warp] = amax;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t = fmax(t, s_red[w]);
+      s_red[0] = t;
+    }
+    __syncthreads();
+    const double sc = s_red[0] > 0.0 ? ldexp(1.0, -ilogb(s_red[0])) : 1.0;
+    for (int64_t e = tid; e < rows * ncols; e += nt) W32[e] = (float)(W[e] * sc);
+    for (int64_t e = tid; e < (int64_t)ncols * ncols; e += nt) V32[e] = (e / ncols == e % ncols) ? 1.f : 0.f;
+    const float live32 = (float)(1e-12 * s_fro2 * sc * sc);
+    __syncthreads();
+    for (int sweep = 0; sweep < 40; ++sweep) {
+      if (tid == 0) s_rot = 0;
+      __syncthreads();
+      for (int step = 0; step < nn - 1; ++step) {
+        for (int pi = warp; pi < npairs; pi += nw) {
+          int ia, ib;
+          pair_of(pi, step, ia, ib);
+          if (ib >= ncols) continue;
+          float* ca = W32 + (int64_t)ia * rows;
+          float* cb = W32 + (int64_t)ib * rows;
+          float al = 0.f, be = 0.f, ga = 0.f;
+          for (int64_t i = lane; i < rows; i += 32) {
+            al += ca[i] * ca[i];
+            be += cb[i] * cb[i];
+            ga += ca[i] * cb[i];
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            al += __shfl_xor_sync(0xffffffffu, al, o);
+            be += __shfl_xor_sync(0xffffffffu, be, o);
+            ga += __shfl_xor_sync(0xffffffffu, ga, o);
+          }
+          if (ga != 0.f && ga * ga > 1e-12f * al * be) {
+            const float zeta = (be - al) / (2.f * ga);
+            const float t = fabsf(zeta) > 1e18f ? 0.5f / zeta
+                                                : (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+            const float cs = rsqrtf(1.f + t * t), sn = cs * t;
+            for (int64_t i = lane; i < rows; i += 32) {
+              const float x = ca[i], y = cb[i];
+              ca[i] = cs * x - sn * y;
+              cb[i] = sn * x + cs * y;
+            }
+            float* va = V32 + (int64_t)ia * ncols;
+            float* vb = V32 + (int64_t)ib * ncols;
+            for (int i = lane; i < ncols; i += 32) {
+              const float x = va[i], y = vb[i];
+              va[i] = cs * x - sn * y;
+              vb[i] = sn * x + cs * y;
+            }
+            if (lane == 0 && fminf(al, be) > live32) s_rot = 1;
+          }
+        }
+        __syncthreads();
+      }
+      if (!s_rot) break;
+      __syncthreads();
+    }
+    // V = FP64 Gram-Schmidt (two passes) of the FP32 rotations, column by column
+    __shared__ double s_d[kTrMaxGram];
+    for (int c = 0; c < ncols; ++c) {
+      double* vc = V + (int64_t)c * ncols;
+      for (int i = tid; i < ncols; i += nt) vc[i] = (double)V32[(int64_t)c * ncols + i];
+      __syncthreads();
+      for (int pass = 0; pass < 2 && c > 0; ++pass) {
+        for (int q = warp; q < c; q += nw) {
+          const double* vq = V + (int64_t)q * ncols;
+          double dt = 0.0;
+          for (int i = lane; i < ncols; i += 32) dt += vq[i] * vc[i];
+          dt = warp_sum(dt);
+          if (lane == 0) s_d[q] = dt;
+        }
+        __syncthreads();
+        for (int i = tid; i < ncols; i += nt) {
+          double acc = vc[i];
+          for (int q = 0; q < c; ++q) acc -= s_d[q] * V[(int64_t)q * ncols + i];
+          vc[i] = acc;
+        }
+        __syncthreads();
+      }
+      double n2 = 0.0;
+      for (int i = tid; i < ncols; i += nt) n2 += vc[i] * vc[i];
+      n2 = warp_sum(n2);
+      if (lane == 0) s_red[warp] = n2;
+      __syncthreads();
+      if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t += s_red[w];
+        s_red[0] = t > 0.0 ? 1.0 / sqrt(t) : 0.0;
+      }
+      __syncthreads();
+      const double inv = s_red[0];
+      for (int i = tid; i < ncols; i += nt) vc[i] *= inv;
+      __syncthreads();
+    }
+    // W = M V (working orientation of M)
+    for (int64_t e = tid; e < rows * ncols; e += nt) {
+      const int64_t c = e / rows, i = e - c * rows;
+      const double* vc = V + c * ncols;
+      double acc = 0.0;
+      for (int q = 0; q < ncols; ++q) acc += (tr ? a.M[(int64_t)q * a.q + i] : a.M[i * a.q + q]) * vc[q];
+      W[e] = acc;
+    }
+    __syncthreads();
+  }
   for (int sweep = 0; sweep < 60 && ncols > 1; ++sweep) {
     if (tid == 0) s_rot = 0;
     __syncthreads();
@@ -462,11 +600,11 @@ cudaError_t launch_lstsq_combine(const double* U, const double* SVt, const doubl
   return cudaGetLastError();
 }
 
-constexpr size_t kSvdSmemMax = 160 * 1024;  // plus ~16 KB of static shared memory
+constexpr size_t kSvdSmemMax = 196 * 1024;  // plus ~25 KB of static shared memory
 
 size_t svd_trunc_work_doubles(int64_t p, int64_t q) {
   const int64_t n = p < q ? p : q, rows = p > q ? p : q;
-  return (size_t)(rows * n + n * n + 64);
+  return (size_t)(rows * n + n * n + (rows * n + 1) / 2 + (n * n + 1) / 2 + 64);
 }
 
 cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
@@ -474,10 +612,20 @@ cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, do
   const int64_t n = p < q ? p : q, rows = p > q ? p : q;
   if (n > kTrMaxGram || n < 1) return cudaErrorInvalidValue;
   // the dots read W at every rotation step: W first, then V if both fit
-  const size_t wbytes = sizeof(double) * (size_t)(rows * n), bytes_all = wbytes + sizeof(double) * (size_t)(n * n);
-  const int in_smem = bytes_all <= kSvdSmemMax ? 2 : (wbytes <= kSvdSmemMax ? 1 : 0);
-  const size_t bytes = in_smem == 2 ? bytes_all : (in_smem == 1 ? wbytes : 0);
-  SvdK a{M, p, q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status, in_smem};
+  // shared memory for W, then its FP32 copy, then V and its copy, while they fit
+  const size_t part[4] = {8 * (size_t)(rows * n), ((4 * (size_t)(rows * n)) + 7) / 8 * 8, 8 * (size_t)(n * n),
+                          ((4 * (size_t)(n * n)) + 7) / 8 * 8};
+  int in_smem = 0;
+  size_t bytes = 0;
+  for (int b = 0; b < 4; ++b)
+    if (bytes + part[b] <= kSvdSmemMax) {
+      bytes += part[b];
+      in_smem |= 1 << b;
+    }
+  double* w32 = work + rows * n + n * n;
+  double* v32 = w32 + (rows * n + 1) / 2;
+  SvdK a{M,    p,    q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status,
+         reinterpret_cast<float*>(w32), reinterpret_cast<float*>(v32), in_smem};
   if (in_smem) {
     cudaError_t e = cudaFuncSetAttribute(svd_trunc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSvdSmemMax);
