@@ -290,6 +290,19 @@ def other_workloads(lib, ctx, args):
         'krylov_iterations': tst['krylov_iterations'], 'kernel_launches': tst['kernel_launches'],
         'final_ranks': [int(x) for x in sol[-1].ranks],
         'rel_diff_vs_oracle_step2': O.stable_rel_diff(sol[2].cores, ref[2])}
+    # alternating ridge regression, Kuramoto d=10 (10 outputs, 1000 samples, rank 11), 10 sweeps, rcond 1e-12
+    from scikit_tt_gb300.data_driven import regression
+    wa = wl.kuramoto_arr()
+    regression.arr(wa.x, wa.y, wa.basis, T(wa.x0), repeats=1, rcond=wa.rcond)
+    xi = regression.arr(wa.x, wa.y, wa.basis, T(wa.x0), repeats=wa.repeats, rcond=wa.rcond)
+    ast = dict(regression.last_stats)
+    theta = regression.evaluate_basis(wa.x, wa.basis)
+    t0 = time.perf_counter()
+    aref = O.arr(theta, wa.y, [wa.x0] * wa.y.shape[0], repeats=wa.repeats, rcond=wa.rcond)
+    acpu = time.perf_counter() - t0
+    out['arr_kuramoto_d10_m1000'] = {
+        'device_ms': ast['device_ms'], 'oracle_cpu_ms': acpu * 1e3, 'kernel_launches': ast['kernel_launches'],
+        'max_rel_diff_vs_oracle': max(O.stable_rel_diff(a.cores, b) for a, b in zip(xi, aref))}
     # 256 uneven instances (d 8..32, n in {2,4,8}, rank 4..48), 4 sweeps, one launch
     b4 = wl.batch_sle(256)
     probs = [(T(w.op), T(w.x0), T(w.rhs)) for w in b4]

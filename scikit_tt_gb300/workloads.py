@@ -148,6 +148,41 @@ def tdvp_ising(d=16, g=1.2, x_rank=4, max_rank=16, steps=5, dt=0.05, seed=7) -> 
                         dict(d=d, g=g, x_rank=x_rank, max_rank=max_rank, dt=dt))
 
 
+@dataclass
+class ARRInstance:
+    x: np.ndarray            # samples (coordinates x samples)
+    y: np.ndarray            # outputs x samples
+    basis: list              # basis functions per mode
+    x0: List[np.ndarray]     # initial guess (one per output, copied)
+    repeats: int
+    rcond: float
+    meta: dict = field(default_factory=dict)
+
+
+def kuramoto_arr(d=10, m=1000, repeats=10, rcond=1e-12, seed=3) -> ARRInstance:
+    """Alternating ridge regression of the Kuramoto model's right-hand side
+    from d oscillator phases (the setting of the reference's ARR test): m
+    samples of one trajectory (scipy BDF), bases [1, sin x_1 .. sin x_d] and
+    [1, cos x_1 .. cos x_d], rank d+1, one regression per oscillator."""
+    import scipy.integrate as spint
+    from .data_driven import transform as tdt
+    rng = np.random.default_rng(seed)
+    x0 = 2 * np.pi * rng.random(d) - np.pi
+    w = np.linspace(-5, 5, d)
+
+    def rhs(_, theta):
+        ti, tj = np.meshgrid(theta, theta)
+        return w + 2 / d * np.sin(tj - ti).sum(0) + 0.2 * np.sin(theta)
+
+    sol = spint.solve_ivp(rhs, [0, 100], x0, method='BDF', t_eval=np.linspace(0, 100, m))
+    x = sol.y
+    y = np.stack([rhs(0, x[:, j]) for j in range(m)], axis=1)
+    basis = [[tdt.ConstantFunction(0)] + [tdt.Sin(i, 1) for i in range(d)],
+             [tdt.ConstantFunction(0)] + [tdt.Cos(i, 1) for i in range(d)]]
+    guess = [np.ones((1, d + 1, 1, d + 1)), np.ones((d + 1, d + 1, 1, 1))]
+    return ARRInstance(x, y, basis, guess, repeats, rcond, dict(d=d, m=m))
+
+
 def reversible_markov(rng, n: int) -> np.ndarray:
     """Column-stochastic n x n transition matrix S D^-1 of a reversible chain
     (S symmetric positive, D its column sums): similar to the symmetric
