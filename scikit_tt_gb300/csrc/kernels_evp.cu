@@ -383,7 +383,8 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
               va[i] = cs * x - sn * y;
               vb[i] = sn * x + cs * y;
             }
-            if (lane == 0 && fminf(al, be) > live32) s_rot = 1;
+            // a sweep whose live pairs were all within 1e-3 leaves them within ~1e-6
+            if (lane == 0 && fminf(al, be) > live32 && ga * ga > 1e-6f * al * be) s_rot = 1;
           }
         }
         __syncthreads();
@@ -428,13 +429,26 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
       for (int i = tid; i < ncols; i += nt) vc[i] *= inv;
       __syncthreads();
     }
-    // W = M V (working orientation of M)
-    for (int64_t e = tid; e < rows * ncols; e += nt) {
-      const int64_t c = e / rows, i = e - c * rows;
-      const double* vc = V + c * ncols;
-      double acc = 0.0;
-      for (int q = 0; q < ncols; ++q) acc += (tr ? a.M[(int64_t)q * a.q + i] : a.M[i * a.q + q]) * vc[q];
-      W[e] = acc;
+    // W = M V (working orientation of M): from the FP64 copy when W sits in
+    // shared memory (the global work area is free then), else from M
+    if (a.in_smem & 1) {
+      for (int64_t e = tid; e < rows * ncols; e += nt) {
+        const int64_t c = e / rows, i = e - c * rows;
+        const double* vc = V + c * ncols;
+        double acc = 0.0;
+        for (int q = 0; q < ncols; ++q) acc += W[(int64_t)q * rows + i] * vc[q];
+        a.W[e] = acc;
+      }
+      __syncthreads();
+      for (int64_t e = tid; e < rows * ncols; e += nt) W[e] = a.W[e];
+    } else {
+      for (int64_t e = tid; e < rows * ncols; e += nt) {
+        const int64_t c = e / rows, i = e - c * rows;
+        const double* vc = V + c * ncols;
+        double acc = 0.0;
+        for (int q = 0; q < ncols; ++q) acc += (tr ? a.M[(int64_t)q * a.q + i] : a.M[i * a.q + q]) * vc[q];
+        W[e] = acc;
+      }
     }
     __syncthreads();
   }
@@ -496,7 +510,9 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
             va[i] = c * x - s * y;
             vb[i] = s * x + c * y;
           }
-          if (lane == 0 && fmin(alpha, beta) > live_floor) s_rot = 1;
+          // quadratic convergence: a sweep whose live pairs were all within 1e-9
+          // (relative) leaves them within ~1e-18, so no further sweep is needed
+          if (lane == 0 && fmin(alpha, beta) > live_floor && gamma * gamma > 1e-18 * alpha * beta) s_rot = 1;
         }
       }
       __syncthreads();
