@@ -120,3 +120,21 @@ def test_tdvp_ground_state_energy():
         energy = sol[-1].transpose(conjugate=True) @ operator @ sol[-1]
         assert abs(energy - eigval) < 1e-8
     assert abs(eigval - O.ising_exact_e0(N, 1.0, 1.2)) < 1e-8
+
+
+def test_tdvp_manhattan_normalisation_and_zero_steps():
+    """normalize=1 (the sum of all entries, tensor_train.py:1334-1420) on a positive
+    state -- exp(-tau H) of the transverse-field Ising chain is entrywise positive --
+    against the oracle; number_of_steps=0 returns the initial value alone."""
+    from scikit_tt_gb300 import models
+    from scikit_tt_gb300.solvers import ode
+    rng = np.random.default_rng(9)
+    op = models.ising(5, 1.0, 0.8)
+    x0 = [rng.uniform(0.2, 1.0, (r0, 2, 1, r1)) for r0, r1 in zip([1, 2, 2, 2, 2], [2, 2, 2, 2, 1])]
+    sol = ode.tdvp1site(op, _tt(x0), -0.03j, 4, local_solver={'method': 'exact'}, normalize=1)
+    ref = O.tdvp1site([np.array(c) for c in op.cores], x0, -0.03, 4, kdim=0, normalize=1)
+    for t, r in zip(sol, ref):
+        v = O.full_vector(r)
+        assert np.linalg.norm(O.full_vector(t.cores) - v) / np.linalg.norm(v) < 1e-10
+    assert abs(np.sum(O.full_vector(sol[-1].cores)) - 1.0) < 1e-12
+    assert len(ode.tdvp2site(op, _tt(x0), -0.03j, 0)) == 1

@@ -42,3 +42,20 @@ def test_arr_kuramoto_coefficients():
     full = np.stack([O.full_vector(t.cores).reshape(11, 11) for t in xi], axis=2)
     exact = z['xi_exact_full']
     assert np.linalg.norm(full.reshape(-1) - exact) / np.linalg.norm(exact) < 1e-5
+
+
+def test_arr_single_mode_matches_oracle():
+    """One basis list (a one-core train): the fit is a single least-squares solve."""
+    from scikit_tt_gb300.data_driven import regression, transform as tdt
+    from scikit_tt_gb300.tensor_train import TT
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-2, 2, (1, 300))
+    y = np.vstack([np.exp(-x[0] ** 2), np.sin(3 * x[0])])
+    basis = [[tdt.ConstantFunction(0), tdt.Identity(0), tdt.Monomial(0, 2), tdt.GaussFunction(0, 0.0, 0.3),
+              tdt.Sin(0, 3), tdt.Cos(0, 3)]]
+    g = [rng.standard_normal((1, 6, 1, 1))]
+    sols = regression.arr(x, y, basis, TT([c.copy() for c in g]), repeats=2, rcond=1e-8)
+    refs = O.arr(regression.evaluate_basis(x, basis), y, [g, g], repeats=2, rcond=1e-8)
+    for s, r in zip(sols, refs):
+        v = O.full_vector(r)
+        assert np.linalg.norm(O.full_vector(s.cores) - v) / np.linalg.norm(v) < 1e-10
