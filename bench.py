@@ -49,6 +49,24 @@ def dist_env():
         int(os.environ.get('LOCAL_RANK', '0'))
 
 
+def rank_seeds(rank, batch):
+    """Seeds of the instances one rank solves: rank r takes r*batch .. r*batch + batch - 1,
+    so the ranks' batches are disjoint and no data crosses ranks (weak scaling)."""
+    return [rank * batch + j for j in range(batch)]
+
+
+def max_over_ranks(ms, device=None):
+    """The slowest rank's time (the job ends when its last rank does); the value
+    itself when no process group is running."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle's dense-LU ALS on a bounded sample
 # ---------------------------------------------------------------------------
@@ -369,7 +387,7 @@ def main_gpu(args):
     B = args.batch or int(slots.value)
 
     # B independent seeded instances per rank (weak scaling: each rank its own batch)
-    inst = [wl.coupled_sle(seed=rank * B + j, **WORKLOAD) for j in range(B)]
+    inst = [wl.coupled_sle(seed=s, **WORKLOAD) for s in rank_seeds(rank, B)]
     packs = [[_lib.Packed(t) for t in (w.op, w.x0, w.rhs)] for w in inst]
     dbufs = [[torch.from_numpy(p.data).to(dev) for p in pk] for pk in packs]
     dev_ops = _desc_array(_lib, [pk[0] for pk in packs], [b[0] for b in dbufs])
@@ -427,11 +445,7 @@ def main_gpu(args):
     with ClockSampler(local) as clk:
         ms_mixed, st_mixed = timed(lambda: batch(_lib.PREC_MIXED, MIXED_TOL), args.steps, args.warmup)
     torch.cuda.synchronize()
-    total_ms = float(np.sum(ms_mixed))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(np.sum(ms_mixed)), dev)
     value = world * B * args.steps / (total_ms / 1e3)
     mixed_sol = out_dev[0].cpu().numpy().copy()
     launches = int(sum(s.kernel_launches for s in st_mixed))

@@ -3,7 +3,7 @@
 Runs the unmodified scikit_tt package (imported read-only from the path in
 ``SCIKIT_TT_REF``, default ``/root/reference``) on small seeded inputs and
 stores inputs and outputs as ``.npz``.  The oracle and the device engine are
-both checked against these files; the GPU machine never needs the reference.
+both checked against these files, so the GPU tests never need the reference.
 
     python tests/golden/make_golden.py
 """
