@@ -7,15 +7,16 @@ GPU through ``libttals.so``:
 
 * ``__matmul__`` / ``dot``  -- device core products  (tensor_train.py:422-524)
 * ``ortho_left`` / ``ortho_right`` / ``ortho`` -- device Householder QR/RQ
-  sweeps (tensor_train.py:1092-1332)
+  sweeps (tensor_train.py:1092-1332); with ``threshold`` > 0 or a finite
+  ``max_rank`` a device one-sided Jacobi SVD per core with the reference's
+  rank rule (tensor_train.py:1150-1181, 1262-1296)
 * ``norm(p=2)`` -- device QR sweep with a log-carried scale
   (tensor_train.py:1334-1430; immune to the over/underflow the SVD-based
   reference meets on unnormalised trains)
 
 Structural helpers (``+``, ``-``, scalar ``*``, ``transpose``, ``copy``,
-``element``, ``full``, ``matricize``) are block copies and stay in NumPy.
-Truncated orthonormalisation (``threshold`` > 0 or finite ``max_rank``) is not
-implemented on the device and raises ``NotImplementedError``.
+``element``, ``full``, ``matricize``) and ``norm(p=1)`` are block copies and
+sums and stay in NumPy.
 """
 
 from __future__ import annotations

@@ -108,6 +108,57 @@ def ttops_case():
     print('ttops norm', out['norm'])
 
 
+def struct_case():
+    """The TT container's host-side helpers: rank-sum addition and subtraction,
+    scalar products, (partial) transposes, element access, full/matricize,
+    the 1-norm, the HOSVD constructor and the constructors of
+    tensor_train.py:1806-2032, 2144-2262."""
+    rng = np.random.default_rng(21)
+    rows, cols = [2, 3, 2, 3], [3, 2, 2, 2]
+
+    def cores(rk, rd, cd, fn=rng.standard_normal):
+        return [fn((rk[i], rd[i], cd[i], rk[i + 1])) for i in range(len(rd))]
+
+    t = cores([1, 2, 3, 2, 1], rows, [1] * 4)
+    u = cores([1, 3, 2, 2, 1], rows, [1] * 4)
+    A = cores([1, 2, 2, 3, 1], rows, cols)
+    P = cores([1, 2, 3, 2, 1], rows, [1] * 4, lambda s: rng.uniform(0.1, 1.0, s))
+    Q = cores([1, 2, 2, 2, 1], rows, cols, lambda s: rng.uniform(0.1, 1.0, s))
+    T, U, At = RTT([c.copy() for c in t]), RTT([c.copy() for c in u]), RTT([c.copy() for c in A])
+    s = T + U
+    full8 = s.full()
+    h_thr = RTT(full8.copy(), threshold=1e-10)
+    h_max = RTT(full8.copy(), max_rank=2)
+    L = np.diag([2.0, 2.0, 2.0]) - np.diag([1.0, 1.0], 1) - np.diag([1.0, 1.0], -1)
+    out = dict(
+        add_full=s.full().reshape(-1), add_ranks=np.array(s.ranks),
+        sub_full=(T - U).full().reshape(-1),
+        rmul_full=(2.5 * T).full().reshape(-1), mul_full=(T * -0.75).full().reshape(-1),
+        tr_full=At.copy().transpose().full().reshape(-1),
+        tr_part_full=At.copy().transpose(cores=[0, 2]).full().reshape(-1),
+        mat_A=At.matricize(), mat_t=T.matricize(),
+        elem_A=np.array(At.element([1, 2, 0, 1, 2, 1, 1, 0])), elem_t=np.array(T.element([1, 0, 1, 2, 0, 0, 0, 0])),
+        norm1_P=np.array(RTT([c.copy() for c in P]).norm(p=1)),
+        norm1_Q=np.array(RTT([c.copy() for c in Q]).norm(p=1)),
+        hosvd_thr_full=h_thr.full().reshape(-1), hosvd_thr_ranks=np.array(h_thr.ranks),
+        hosvd_max_full=h_max.full().reshape(-1), hosvd_max_ranks=np.array(h_max.ranks),
+        eye_full=rtt.eye([2, 3]).full().reshape(-1),
+        ones_full=rtt.ones([2, 3], [1, 2], ranks=2).full().reshape(-1),
+        unit_full=rtt.unit([2, 3, 2], [1, 2, 0]).full().reshape(-1),
+        canonical_full=rtt.canonical([2, 3, 2, 2], 3).full().reshape(-1),
+        uniform_full=rtt.uniform([2, 3, 2], ranks=2, norm=3.0).full().reshape(-1),
+        core_nested=rtt.build_core([[np.eye(3), 0], [L, np.eye(3)]]),
+        core_flat=rtt.build_core([L, np.eye(3), 2 * L]),
+        L=L)
+    pack('t', t, out)
+    pack('u', u, out)
+    pack('A', A, out)
+    pack('P', P, out)
+    pack('Q', Q, out)
+    np.savez_compressed(os.path.join(HERE, 'ttops_struct.npz'), **out)
+    print('ttops_struct add ranks', s.ranks, 'hosvd ranks', h_thr.ranks, h_max.ranks)
+
+
 def evp_block_case(name, op, x0, repeats, solver, sigma, number_ev, conv_eps=1e-10):
     """number_ev >= 1 on any operator: the eigenvalue list and one TT per eigenvector.
 
@@ -384,6 +435,7 @@ def main():
         evp_case(f'evp_ising_d{d}_eigh', w3.op, [c.copy() for c in x0o.cores], 6, 'eigh', 1.0, negate=True)
     helpers_case()
     ttops_case()
+    struct_case()
     evp_blocks()
     power_cases()
     ode_cases()
@@ -408,5 +460,7 @@ if __name__ == '__main__':
         tdvp_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'arr':
         arr_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'struct':
+        struct_case()
     else:
         main()
