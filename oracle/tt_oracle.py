@@ -149,6 +149,236 @@ def sle_als(op, x0, b, repeats=1, solver='solve'):
 
 
 # ----------------------------------------------------------------------------
+# sle.mals (sle.py:98-191, 350-472, 550-650)
+# ----------------------------------------------------------------------------
+
+
+def _merged_vec(b1, b2):
+    """Two-site right-hand side core (h, m1 m2, g) of sle.py:466-470."""
+    h, m1, _ = b1.shape
+    _, m2, g = b2.shape
+    return np.einsum('aib,bjc->aijc', b1, b2).reshape(h, m1 * m2, g)
+
+
+def _split_mals(i, sol, cores, ranks, dims, threshold, max_rank, direction):
+    """SVD split of the two-site solution, sle.py:604-650: reshape to
+    (r_i n_i) x (n_{i+1} r_{i+2}), gesvd, keep sigma_k / sigma_0 > threshold,
+    then at most max_rank.  Forward keeps U as core i; backward keeps V as
+    core i+1 and, at the first pair, U diag(s) as core 0."""
+    a, n1, n2, s = ranks[i], dims[i], dims[i + 1], ranks[i + 2]
+    u, sv, v = sla.svd(sol.reshape(a * n1, n2 * s), full_matrices=False, check_finite=False,
+                       lapack_driver='gesvd')
+    if threshold != 0:
+        keep = np.where(sv / sv[0] > threshold)[0]
+        u, sv, v = u[:, keep], sv[keep], v[keep, :]
+    if max_rank != np.inf:
+        k = int(min(u.shape[1], max_rank))
+        u, sv, v = u[:, :k], sv[:k], v[:k, :]
+    k = sv.shape[0]
+    ranks[i + 1] = k
+    if direction == 'forward':
+        cores[i] = u.reshape(a, n1, 1, k)
+    else:
+        cores[i + 1] = v.reshape(k, n2, 1, s)
+        if i == 0:
+            cores[0] = (u * sv).reshape(a, n1, 1, k)
+
+
+def sle_mals(op, x0, b, repeats=1, solver='solve', threshold=1e-12, max_rank=np.inf):
+    """Two-site MALS for ``op @ x = b`` (sle.py:98-191).  The micro system of
+    sites (i, i+1) is the one-site system of the merged site (sle.py:350-390,
+    433-472); the split follows ``_split_mals``.  Returns the core list."""
+    d = len(op)
+    cores = [c.copy() for c in x0]
+    ranks = [c.shape[0] for c in cores] + [cores[-1].shape[3]]
+    dims = [c.shape[1] for c in op]
+    sl_op, sl_b, sr_op, sr_b = [None] * d, [None] * d, [None] * d, [None] * d
+
+    def right(i):
+        if i == d - 1:
+            sr_op[i], sr_b[i] = np.ones((1, 1, 1)), np.ones((1, 1))
+        else:
+            x = cores[i + 1][:, :, 0, :]
+            sr_op[i] = stack_right_op(sr_op[i + 1], x, op[i + 1])
+            sr_b[i] = stack_right_vec(sr_b[i + 1], x, b[i + 1][:, :, 0, :])
+
+    def left(i):
+        if i == 0:
+            sl_op[i], sl_b[i] = np.ones((1, 1, 1)), np.ones((1, 1))
+        else:
+            x = cores[i - 1][:, :, 0, :]
+            sl_op[i] = stack_left_op(sl_op[i - 1], x, op[i - 1])
+            sl_b[i] = stack_left_vec(sl_b[i - 1], x, b[i - 1][:, :, 0, :])
+
+    def update(i, direction):                      # sle.py:550-603
+        mop = micro_matrix(sl_op[i], _merged_op(op[i], op[i + 1]), sr_op[i + 1])
+        mrhs = micro_vec(sl_b[i], _merged_vec(b[i][:, :, 0, :], b[i + 1][:, :, 0, :]), sr_b[i + 1])
+        if solver == 'solve':
+            sol = np.linalg.solve(mop, mrhs)
+        elif solver == 'lu':
+            sol = sla.lu_solve(sla.lu_factor(mop, check_finite=False), mrhs, check_finite=False)
+        else:
+            raise ValueError(f'unknown solver {solver!r}')
+        _split_mals(i, sol, cores, ranks, dims, threshold, max_rank, direction)
+
+    for i in range(d - 1, 0, -1):                  # sle.py:148-150
+        right(i)
+    for _ in range(repeats):                       # sle.py:156-189
+        for i in range(d - 1):
+            left(i)
+            if i < d - 2:
+                update(i, 'forward')
+        for i in range(d - 2, -1, -1):
+            right(i + 1)
+            update(i, 'backward')
+    return cores
+
+
+# ----------------------------------------------------------------------------
+# linear ODE integrators (ode.py:16-115, 249-636) and evp.power_method
+# (evp.py:182-250): compositions of sle.als / sle.mals with TT algebra.
+# Operators here are small (full vectors are used for the norms).
+# ----------------------------------------------------------------------------
+
+
+def tt_eye(dims):
+    """Identity operator, ranks 1 (tensor_train.py:1870-1893)."""
+    return [np.eye(n).reshape(1, n, n, 1) for n in dims]
+
+
+def _shifted(op, alpha):
+    """``tt.eye + alpha * op`` as a rank sum (tensor_train.py:282-344, 368-399)."""
+    return tt_add(tt_eye([c.shape[1] for c in op]), tt_scale(op, alpha))
+
+
+def _vnorm(t):
+    return float(np.linalg.norm(full_vector(t)))
+
+
+def _normalise(t, p):
+    return tt_scale(t, 1.0 / _norm_p(t, p)) if p > 0 else t
+
+
+def explicit_euler(op, x0, step_sizes, threshold=1e-12, max_rank=50, normalize=1):
+    """ode.py:16-82: x_{k+1} = (I + h A) x_k, then ``TT.ortho(threshold,
+    max_rank)`` (left sweep untruncated in rank, right sweep capped,
+    tensor_train.py:1312-1332), then division by the p-norm."""
+    sol = [x0]
+    for h in step_sizes:
+        t = tt_matmul(_shifted(op, h), sol[-1])
+        t = ortho_right(ortho_left(t, threshold), threshold, max_rank)
+        sol.append(_normalise(t, normalize))
+    return sol
+
+
+def errors_expl_euler(op, sol, step_sizes):
+    """ode.py:85-114: ||x_{k+1} - (I + h A) x_k|| / ||x_k||."""
+    return [_vnorm(tt_add(sol[k + 1], tt_scale(tt_matmul(_shifted(op, h), sol[k]), -1.0))) / _vnorm(sol[k])
+            for k, h in enumerate(step_sizes)]
+
+
+def _tt_solve(tt_solver, mop, guess, rhs, micro_solver, repeats, threshold, max_rank):
+    if tt_solver == 'als':
+        return sle_als(mop, guess, rhs, repeats=repeats, solver=micro_solver)
+    return sle_mals(mop, guess, rhs, repeats=repeats, solver=micro_solver, threshold=threshold, max_rank=max_rank)
+
+
+def implicit_euler(op, x0, guess, step_sizes, repeats=1, tt_solver='als', threshold=1e-12, max_rank=np.inf,
+                   micro_solver='solve', normalize=1):
+    """ode.py:249-330: (I - h A) x_{k+1} = x_k by ALS/MALS, warm-started from
+    the previous solution, then division by the p-norm."""
+    sol, t = [x0], guess
+    for h in step_sizes:
+        t = _tt_solve(tt_solver, _shifted(op, -h), t, sol[-1], micro_solver, repeats, threshold, max_rank)
+        t = _normalise(t, normalize)
+        sol.append(t)
+    return sol
+
+
+def errors_impl_euler(op, sol, step_sizes):
+    """ode.py:333-363: ||(I - h A) x_{k+1} - x_k|| / ||x_k||."""
+    return [_vnorm(tt_add(tt_matmul(_shifted(op, -h), sol[k + 1]), tt_scale(sol[k], -1.0))) / _vnorm(sol[k])
+            for k, h in enumerate(step_sizes)]
+
+
+def trapezoidal_rule(op, x0, guess, step_sizes, repeats=1, tt_solver='als', threshold=1e-12, max_rank=np.inf,
+                     micro_solver='solve', normalize=1):
+    """ode.py:366-451: (I - h/2 A) x_{k+1} = (I + h/2 A) x_k."""
+    sol, t = [x0], guess
+    for h in step_sizes:
+        rhs = tt_matmul(_shifted(op, 0.5 * h), sol[-1])
+        t = _tt_solve(tt_solver, _shifted(op, -0.5 * h), t, rhs, micro_solver, repeats, threshold, max_rank)
+        t = _normalise(t, normalize)
+        sol.append(t)
+    return sol
+
+
+def errors_trapezoidal(op, sol, step_sizes):
+    """ode.py:453-485: ||(I - h/2 A) x_{k+1} - (I + h/2 A) x_k|| / ||(I + h/2 A) x_k||."""
+    out = []
+    for k, h in enumerate(step_sizes):
+        fwd = tt_matmul(_shifted(op, 0.5 * h), sol[k])
+        out.append(_vnorm(tt_add(tt_matmul(_shifted(op, -0.5 * h), sol[k + 1]), tt_scale(fwd, -1.0))) / _vnorm(fwd))
+    return out
+
+
+def adaptive_step_size(op, x0, guess, time_end, step_size_first=1e-10, repeats=1, solver='solve', error_tol=1e-1,
+                       closeness_tol=0.5, step_size_min=1e-14, step_size_max=10, closeness_min=1e-3, factor_max=2,
+                       factor_safe=0.9, second_method='two_step_Euler', normalize=1):
+    """ode.py:487-636: an implicit Euler step t1 (1-norm normalised) against a
+    second method t2 (two half implicit Euler solves, both with the previous
+    state as right-hand side as the reference has it, or the trapezoidal
+    rule); a step is accepted when the local error and the relative change
+    of ||A x|| both stay inside their tolerances.  Returns (states, times)."""
+    sol, times = [x0], [0]
+    closeness_pre = _vnorm(tt_matmul(op, x0))
+    t_tmp, time, h = guess, 0, step_size_first
+    while time < time_end and closeness_pre > closeness_min and h > step_size_min:
+        t1 = _normalise(sle_als(_shifted(op, -h), t_tmp, sol[-1], repeats=repeats, solver=solver), 1)
+        if second_method == 'two_step_Euler':
+            t2 = sle_als(_shifted(op, -0.5 * h), t_tmp, sol[-1], repeats=repeats, solver=solver)
+            t2 = sle_als(_shifted(op, -0.5 * h), t2, sol[-1], repeats=repeats, solver=solver)
+        else:
+            t2 = sle_als(_shifted(op, -0.5 * h), t_tmp, tt_matmul(_shifted(op, 0.5 * h), sol[-1]), repeats=repeats,
+                         solver=solver)
+        t2 = _normalise(t2, normalize)
+        closeness = _vnorm(tt_matmul(op, t1))
+        local_error = _vnorm(tt_add(t1, tt_scale(t2, -1.0))) / _vnorm(t1)
+        closeness_difference = (closeness - closeness_pre) / closeness_pre
+        factor_local = error_tol / local_error
+        factor_closeness = closeness_tol / np.abs(closeness_difference)
+        h_new = np.amin([factor_max, factor_safe * factor_local, factor_safe * factor_closeness]) * h
+        if factor_local > 1 and factor_closeness > 1:
+            time = np.min([time + h, time_end])
+            h = np.amin([h_new, time_end - time, step_size_max])
+            sol.append(t2)
+            times.append(time)
+            t_tmp, closeness_pre = t1, closeness
+        else:
+            h = h_new
+    return sol, times
+
+
+def power_method(op, x0, op_gevp=None, repeats=10, sigma=0.999):
+    """evp.py:182-250: inverse power iteration x <- (A - sigma M)^{-1} M x by
+    one ALS sweep per step (M = I without ``op_gevp``), x <- x / ||x||, and the
+    Rayleigh quotient x^T A x (/ x^T M x).  Returns (eigenvalue, cores)."""
+    dims = [c.shape[1] for c in op]
+    mass = op_gevp if op_gevp is not None else tt_eye(dims)
+    shifted = tt_add(op, tt_scale(mass, -sigma))
+    x, val = x0, 0.0
+    for _ in range(repeats):
+        rhs = x if op_gevp is None else tt_matmul(op_gevp, x)
+        x = sle_als(shifted, x, rhs)
+        x = tt_scale(x, 1.0 / _vnorm(x))
+        v = full_vector(x)
+        val = float(v @ full_matrix(op) @ v)
+        if op_gevp is not None:
+            val /= float(v @ full_matrix(op_gevp) @ v)
+    return val, x
+
+
+# ----------------------------------------------------------------------------
 # evp.als (evp.py:17-179, 386-495)
 # ----------------------------------------------------------------------------
 

@@ -175,3 +175,54 @@ def test_basis_functions_match_reference(golden, name):
     theta = regression.evaluate_basis(z['x'], basis)
     for i, t in enumerate(theta):
         assert np.allclose(t, z[f'theta_{i}'], rtol=1e-14, atol=1e-15)
+
+
+@pytest.mark.parametrize('name', ['sle_mals_laplace_d6', 'sle_mals_laplace_d6_r4', 'sle_mals_coupled_d5_lu'])
+def test_oracle_mals_matches_reference(golden, name):
+    """Two-site MALS (sle.py:98-191): same ranks, same tensor."""
+    z, cores = golden(name)
+    mr = int(z['max_rank'])
+    sol = O.sle_mals(cores('op'), cores('x0'), cores('rhs'), repeats=int(z['repeats']), solver=str(z['solver']),
+                     threshold=float(z['threshold']), max_rank=np.inf if mr < 0 else mr)
+    assert [c.shape[0] for c in sol] + [1] == [int(r) for r in z['ranks']]
+    v = O.full_vector(sol)
+    assert np.linalg.norm(v - z['full']) / np.linalg.norm(z['full']) < 1e-12
+
+
+def test_oracle_ode_integrators_match_reference(golden):
+    """Implicit / explicit Euler, trapezoidal rule, adaptive step size and their
+    error helpers (ode.py:16-636) on a Markov generator."""
+    z, cores = golden('ode_markov')
+    op, x0, guess = cores('op'), cores('x0'), cores('guess')
+    steps = [float(h) for h in z['steps']]
+
+    def same(prefix, sol):
+        assert len(sol) == int(z[prefix + '_n'])
+        for k, s in enumerate(sol):
+            r = z[f'{prefix}_{k}']
+            assert np.linalg.norm(O.full_vector(s) - r) / np.linalg.norm(r) < 1e-12
+
+    sol = O.implicit_euler(op, x0, guess, steps)
+    same('impl', sol)
+    np.testing.assert_allclose(O.errors_impl_euler(op, sol, steps), z['impl_err'], rtol=1e-8, atol=1e-14)
+    sol = O.trapezoidal_rule(op, x0, guess, steps)
+    same('trap', sol)
+    np.testing.assert_allclose(O.errors_trapezoidal(op, sol, steps), z['trap_err'], rtol=1e-8, atol=1e-14)
+    sol = O.explicit_euler(op, x0, [0.05] * 3)
+    same('expl', sol)
+    np.testing.assert_allclose(O.errors_expl_euler(op, sol, [0.05] * 3), z['expl_err'], atol=1e-14)
+    sol, times = O.adaptive_step_size(op, x0, guess, 2.0, step_size_first=0.05)
+    same('adapt', sol)
+    np.testing.assert_allclose(times, z['adapt_times'], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize('name', ['evp_power_markov', 'evp_power_markov_gevp'])
+def test_oracle_power_method_matches_reference(golden, name):
+    """Inverse power iteration through sle.als (evp.py:182-250)."""
+    z, cores = golden(name)
+    op = cores('op')
+    gevp = O.tt_eye([c.shape[1] for c in op]) if bool(z['gevp']) else None
+    val, vec = O.power_method(op, cores('x0'), gevp, repeats=int(z['repeats']), sigma=float(z['sigma']))
+    assert abs(val - float(z['val'])) < 1e-12
+    v, r = O.full_vector(vec), z['vec0']
+    assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-12
