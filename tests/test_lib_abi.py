@@ -33,3 +33,40 @@ def test_rank_schedule_host_only():
     out = np.zeros(11, dtype=np.int64)
     assert lib.ttals_als_ranks(10, _lib.i64ptr(dims), _lib.i64ptr(xr), _lib.i64ptr(out)) == 0
     assert list(out) == [1, 4, 5, 5, 5, 5, 5, 5, 5, 4, 1]   # reference ranks after one sweep
+
+
+C_CALLER = r'''
+#include <stdio.h>
+#include "ttals.h"
+int main(void) {
+  const int64_t dims[10] = {4, 4, 4, 4, 4, 4, 4, 4, 4, 4};
+  const int64_t xr[11] = {1, 5, 5, 5, 5, 5, 5, 5, 5, 5, 1};
+  int64_t out[11];
+  if (ttals_als_ranks(10, dims, xr, out) != TTALS_OK) return 2;
+  if (ttals_als_ranks(-1, dims, xr, out) == TTALS_OK) return 3;
+  for (int i = 0; i < 11; ++i) printf("%lld ", (long long)out[i]);
+  printf("\n");
+  return 0;
+}
+'''
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """A C99 caller (what a non-Python binding compiles against) includes
+    ttals.h with -pedantic, links libttals.so and calls a host-only entry."""
+    import shutil
+    import subprocess
+    import pytest
+    from scikit_tt_gb300 import build_ext
+    if shutil.which('gcc') is None:
+        pytest.skip('no C compiler')
+    lib = build_ext.build()
+    src = tmp_path / 'caller.c'
+    src.write_text(C_CALLER)
+    exe = tmp_path / 'caller'
+    libdir = os.path.dirname(lib)
+    subprocess.run(['gcc', '-std=c99', '-Wall', '-Wextra', '-pedantic', '-Werror', '-I', os.path.join(ROOT, 'include'),
+                    str(src), '-L', libdir, '-l:libttals.so', f'-Wl,-rpath,{libdir}', '-o', str(exe)], check=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    assert res.stdout.split() == ['1', '4', '5', '5', '5', '5', '5', '5', '5', '4', '1']
