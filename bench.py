@@ -67,6 +67,22 @@ def max_over_ranks(ms, device=None):
     return float(t.item())
 
 
+def launch_traffic(batch):
+    """DRAM bytes of one batch launch from the committed ncu capture
+    (``profiles/traffic.json``: bytes of a launch of ``solves`` solves).  Every
+    solve runs on its own CTA over its own data, so a launch of ``batch``
+    solves moves batch / solves of it.  Returns (bytes or None, note)."""
+    tf = os.path.join(ROOT, 'profiles', 'traffic.json')
+    if not os.path.exists(tf):
+        return None, 'no ncu capture committed'
+    rec = json.load(open(tf))
+    solves = int(rec.get('solves', batch))
+    note = f'ncu dram__bytes_read.sum + dram__bytes_write.sum of a {solves}-solve launch'
+    if solves != batch:
+        note += f', scaled to {batch} solves'
+    return rec['batch_sle_kernel'] * batch / solves, note
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle's dense-LU ALS on a bounded sample
 # ---------------------------------------------------------------------------
@@ -496,10 +512,7 @@ def main_gpu(args):
     if os.path.exists(mp):
         bf16_peak = float(json.load(open(mp))['bf16_tflops'])
         bf16_src = 'MEASURED_PEAKS.json bf16_tflops (burst cuBLAS bf16 GEMM), of measured'
-    traffic = None
-    tf = os.path.join(ROOT, 'profiles', 'traffic.json')
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get('batch_sle_kernel')
+    traffic, traffic_note = launch_traffic(B)
 
     extra = {} if args.quick else other_workloads(lib, ctx, args)
     if rank != 0:
@@ -535,6 +548,7 @@ def main_gpu(args):
         'roofline': {'kernel': 'batch_sle_kernel (mixed)', 'bound': 'tensor',
                      'achieved': (ach64 + ach32) / 1e3, 'peak': bf16_peak, 'unit': 'TFLOP/s',
                      'frac': (ach64 + ach32) / 1e3 / bf16_peak, 'traffic': traffic,
+                     'traffic_source': traffic_note,
                      'peak_source': bf16_src,
                      'what': 'algorithmic FP64-class (stacks, residuals, QR) + FP32 (inner Krylov) flops of the '
                              'launch over its CUDA-event duration; the mixed path runs both on the tensor pipe '

@@ -53,3 +53,14 @@ def test_max_over_ranks_without_process_group():
     import bench
     assert bench.max_over_ranks(3.5) == 3.5
     assert bench.rank_seeds(0, 3) == [0, 1, 2]
+
+
+def test_launch_traffic_scales_with_batch():
+    sys.path.insert(0, ROOT)
+    import json
+    import bench
+    rec = json.load(open(os.path.join(ROOT, 'profiles', 'traffic.json')))
+    full, note = bench.launch_traffic(rec['solves'])
+    assert full == rec['batch_sle_kernel'] and 'scaled' not in note
+    part, note = bench.launch_traffic(rec['solves'] // 5)
+    assert abs(part - full * (rec['solves'] // 5) / rec['solves']) < 1.0 and 'scaled' in note
