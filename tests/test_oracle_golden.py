@@ -226,3 +226,20 @@ def test_oracle_power_method_matches_reference(golden, name):
     assert abs(val - float(z['val'])) < 1e-12
     v, r = O.full_vector(vec), z['vec0']
     assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-12
+
+
+@pytest.mark.parametrize('solver', ['solve', 'lu'])
+def test_oracle_mals_toeplitz_known_answer(golden, solver):
+    """The reference's own MALS known answer (tests/test_sle.py:61-85): the
+    Toeplitz(1..1024) system as an order-10 TT, one MALS sweep with
+    threshold 1e-14 and max_rank 10, against the dense solve (tolerance 1e-7
+    as there)."""
+    z, cores = golden('sle_toeplitz')
+    mat = sla.toeplitz(np.arange(1, 2 ** 10 + 1), np.arange(1, 2 ** 10 + 1)).astype(float)
+    from scikit_tt_gb300.tensor_train import _hosvd
+    op = _hosvd(mat.reshape([2] * 20), 0, np.inf)
+    sol = O.sle_mals(op, cores('x0'), cores('rhs'), repeats=1, solver=solver, threshold=1e-14, max_rank=10)
+    exact = np.linalg.solve(mat, np.ones(1024))
+    got = O.full_vector(sol)
+    assert np.linalg.norm(got - exact) / np.linalg.norm(exact) < 1e-7
+    assert max(c.shape[3] for c in sol) <= 10

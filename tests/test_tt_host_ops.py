@@ -66,3 +66,22 @@ def test_container_errors():
         TT(np.ones((2, 2, 2)))
     with pytest.raises(TypeError):
         TT('cores')
+
+
+def test_element_errors(golden):
+    """The element-access errors of tensor_train.py:990-1027."""
+    import pytest
+    _, cores = golden('ttops_struct')
+    A = TT(cores('A'))
+    with pytest.raises(TypeError):
+        A.element((1, 2, 0, 1, 2, 1, 1, 0))
+    with pytest.raises(TypeError):
+        A.element([1.0, 2, 0, 1, 2, 1, 1, 0])
+    with pytest.raises(ValueError):
+        A.element([1, 2, 0, 1])
+    with pytest.raises(IndexError):
+        A.element([2, 2, 0, 1, 2, 1, 1, 0])      # row index 2 of a mode of size 2
+    with pytest.raises(IndexError):
+        A.element([1, 2, 0, 1, 3, 1, 1, 0])      # column index 3 of a mode of size 3
+    with pytest.raises(IndexError):
+        A.element([1, 2, 0, -1, 2, 1, 1, 0])
