@@ -70,3 +70,24 @@ def test_header_is_plain_c_and_links(tmp_path):
     res = subprocess.run([str(exe)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
     assert res.stdout.split() == ['1', '4', '5', '5', '5', '5', '5', '5', '5', '4', '1']
+
+
+def _header_arity():
+    """Parameter count of every ttals_* declaration in the header."""
+    src = re.sub(r'/\*.*?\*/', '', open(os.path.join(ROOT, 'include', 'ttals.h')).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r'\b(ttals_[a-z_0-9]+)\s*\(([^;{]*?)\)\s*;', src, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ('', 'void') else params.count(',') + 1
+    return out
+
+
+def test_binding_matches_header_arity():
+    """The ctypes binding declares as many arguments as the header for every entry point."""
+    from scikit_tt_gb300 import build_ext, _lib
+    build_ext.build()
+    lib = _lib.load()
+    arity = _header_arity()
+    assert sorted(arity) == declared()
+    for name, n in arity.items():
+        assert len(getattr(lib, name).argtypes) == n, name
