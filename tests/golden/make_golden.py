@@ -159,6 +159,24 @@ def struct_case():
     print('ttops_struct add ranks', s.ranks, 'hosvd ranks', h_thr.ranks, h_max.ranks)
 
 
+def deflation_case():
+    """evp.als with previous eigentensors and a shift (evp.py:376-381): the
+    second-lowest Ising d=8 eigenpair, the first one deflated."""
+    w = wl.ising_evp(d=8, x_rank=16, repeats=8)
+    x0 = [c.copy() for c in RTT([c.copy() for c in w.x0]).ortho_right().cores]
+    v0, t0, _ = revp.als(RTT([c.copy() for c in w.op]), RTT([c.copy() for c in x0]), repeats=8, sigma=w.sigma)
+    t0 = (1.0 / t0.norm()) * t0
+    v1, t1, its = revp.als(RTT([c.copy() for c in w.op]), RTT([c.copy() for c in x0]), previous=[t0.copy()],
+                           shift=100.0, repeats=8, sigma=w.sigma)
+    out = {'sigma': np.array(w.sigma), 'val0': np.array(v0), 'val': np.array(v1), 'its': np.array(its),
+           'vec': np.asarray(t1.full()).reshape(-1)}
+    pack('op', w.op, out)
+    pack('x0', x0, out)
+    pack('prev', [c.copy() for c in t0.cores], out)
+    np.savez_compressed(os.path.join(HERE, 'evp_ising_d8_deflation.npz'), **out)
+    print('evp_ising_d8_deflation', v0, v1, its)
+
+
 def evp_block_case(name, op, x0, repeats, solver, sigma, number_ev, conv_eps=1e-10):
     """number_ev >= 1 on any operator: the eigenvalue list and one TT per eigenvector.
 
@@ -436,6 +454,7 @@ def main():
     helpers_case()
     ttops_case()
     struct_case()
+    deflation_case()
     evp_blocks()
     power_cases()
     ode_cases()
@@ -462,5 +481,7 @@ if __name__ == '__main__':
         arr_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'struct':
         struct_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'deflation':
+        deflation_case()
     else:
         main()

@@ -243,3 +243,16 @@ def test_oracle_mals_toeplitz_known_answer(golden, solver):
     got = O.full_vector(sol)
     assert np.linalg.norm(got - exact) / np.linalg.norm(exact) < 1e-7
     assert max(c.shape[3] for c in sol) <= 10
+
+
+def test_oracle_evp_deflation_matches_reference(golden):
+    """evp.als with a previous eigentensor and a shift (evp.py:376-381): the
+    second-lowest eigenpair of the Ising d=8 chain, as the reference finds it."""
+    z, cores = golden('evp_ising_d8_deflation')
+    val, vec, its = O.evp_als(cores('op'), cores('x0'), previous=[cores('prev')], shift=100.0, repeats=8,
+                              sigma=float(z['sigma']))
+    assert abs(val - float(z['val'])) < 1e-10
+    assert its == int(z['its'])
+    v, r = O.full_vector(vec), z['vec']
+    assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-7
+    assert abs(float(z['val']) - np.linalg.eigvalsh(O.full_matrix(cores('op')))[1]) < 1e-8
