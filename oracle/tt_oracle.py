@@ -18,6 +18,8 @@ produced by ``tests/golden/make_golden.py`` from the reference package, and
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import scipy.linalg as sla
 import scipy.sparse.linalg as spla
@@ -275,6 +277,48 @@ def errors_expl_euler(op, sol, step_sizes):
     """ode.py:85-114: ||x_{k+1} - (I + h A) x_k|| / ||x_k||."""
     return [_vnorm(tt_add(sol[k + 1], tt_scale(tt_matmul(_shifted(op, h), sol[k]), -1.0))) / _vnorm(sol[k])
             for k, h in enumerate(step_sizes)]
+
+
+def _tt_ortho(t, threshold=0.0, max_rank=np.inf):
+    """TT.ortho (tensor_train.py:1312-1332): left sweep uncapped, right sweep capped."""
+    return ortho_right(ortho_left(t, threshold), threshold, max_rank)
+
+
+def _odd_series(op, scale, step, order):
+    """scale*step*A + sum_{k=2}^{order/2} 2/(2k-1)! step^(2k-1) A^(2k-1) (ode.py:186-191, 203-208)."""
+    series = tt_scale(op, scale * step)
+    power = [c.copy() for c in op]
+    for k in range(2, order // 2 + 1):
+        power = tt_matmul(tt_matmul(power, op), op)
+        series = tt_add(series, tt_scale(power, 2 / math.factorial(2 * k - 1) * step ** (2 * k - 1)))
+    return series
+
+
+def hod(op, x0, step_size, number_of_steps, order=2, previous_value=None, op_hod=None, threshold=1e-12,
+        max_rank=50, normalize=1):
+    """Higher-order differencing, ode.py:117-247: x_{k+1} = x_{k-1} + S x_k with
+    S = 2hA + sum_k 2/(2k-1)! h^(2k-1) A^(2k-1) (order raised to even), every
+    new state re-truncated by TT.ortho(threshold, max_rank) and normalised; the
+    state before x_0 is x_0 - S_{h/2} (I - h/2 A) x_0 unless given."""
+    if order % 2:
+        order += 1
+    if op_hod is None:
+        op_hod = _tt_ortho(_odd_series(op, 2.0, step_size, order), threshold)
+    sol = [x0]
+    for i in range(number_of_steps):
+        if i == 0:
+            if previous_value is None:
+                op_first = _tt_ortho(_odd_series(op, 2.0, step_size / 2, order), threshold)
+                back = tt_matmul(_shifted(op, -0.5 * step_size), sol[0])
+                prev = tt_add(sol[0], tt_scale(tt_matmul(op_first, back), -1.0))
+            else:
+                prev = previous_value
+            prev = _tt_ortho(_normalise(prev, normalize), threshold, max_rank)
+        else:
+            prev = sol[i - 1]
+        nxt = _tt_ortho(tt_add(prev, tt_matmul(op_hod, sol[i])), threshold, max_rank)
+        sol.append(_normalise(nxt, normalize))
+    return sol
 
 
 def _tt_solve(tt_solver, mop, guess, rhs, micro_solver, repeats, threshold, max_rank):

@@ -8,6 +8,8 @@ step's solution; products and norms run through the device ``TT.dot`` and
 
 * ``explicit_euler``      ode.py:16-83   (x_{k+1} = (I + h A) x_k, re-truncated)
 * ``errors_expl_euler``   ode.py:85-115
+* ``hod``                 ode.py:117-247 (higher-order differencing,
+  x_{k+1} = x_{k-1} + 2 sinh(h A) x_k with a truncated series)
 * ``implicit_euler``      ode.py:249-331 ((I - h A) x_{k+1} = x_k)
 * ``errors_impl_euler``   ode.py:333-364
 * ``trapezoidal_rule``    ode.py:366-451 ((I - h/2 A) x_{k+1} = (I + h/2 A) x_k)
@@ -30,6 +32,7 @@ cores, which the device path does not hold; they raise ``NotImplementedError``.
 
 from __future__ import annotations
 
+import math
 from typing import List
 
 import numpy as np
@@ -53,7 +56,7 @@ def _solve(op, guess, rhs, tt_solver, micro_solver, repeats, threshold, max_rank
 
 
 def explicit_euler(operator, initial_value, step_sizes: List[float], threshold: float = 1e-12,
-                   max_rank=np.inf, normalize: int = 1, progress: bool = True) -> List:
+                   max_rank: int = 50, normalize: int = 1, progress: bool = True) -> List:
     """x_{k+1} = (I + h_k A) x_k, re-truncated by ``ortho(threshold, max_rank)``."""
     solution = [initial_value]
     for h in step_sizes:
@@ -69,6 +72,52 @@ def errors_expl_euler(operator, solution: List, step_sizes: List[float]) -> List
     """Relative residuals |x_{k+1} - (I + h A) x_k| / |x_k|."""
     return [(solution[k + 1] - _shifted(operator, step_sizes[k]).dot(solution[k])).norm() / solution[k].norm()
             for k in range(len(solution) - 1)]
+
+
+def _odd_series(operator, scale, step, order):
+    """scale*step*A + sum_{k=2}^{order/2} 2/(2k-1)! * step^(2k-1) * A^(2k-1), the
+    odd part of the exponential series the higher-order differencing scheme
+    steps with (ode.py:186-191, 203-208)."""
+    series = (scale * step) * operator.copy()
+    power = operator.copy()
+    for k in range(2, order // 2 + 1):
+        power = power.dot(operator).dot(operator)
+        series = series + (2 / math.factorial(2 * k - 1) * step ** (2 * k - 1)) * power
+    return series
+
+
+def hod(operator, initial_value, step_size: float, number_of_steps: int, order: int = 2, previous_value=None,
+        op_hod=None, threshold: float = 1e-12, max_rank: int = 50, normalize: int = 1, progress: bool = True) -> List:
+    """Higher-order differencing (ode.py:117-247): x_{k+1} = x_{k-1} + 2 sinh(h A) x_k
+    with sinh truncated after the power A^(order-1) (odd ``order`` is raised by
+    one), re-truncated by ``ortho(threshold, max_rank)`` after every step.
+    Without ``previous_value`` the state half a step back comes from one
+    explicit Euler half step and one backward application of the series at
+    h/2.  Products, truncations and 2-norms run on the device."""
+    if order % 2 != 0:
+        order += 1
+    if op_hod is None:
+        op_hod = _odd_series(operator, 2.0, step_size, order).ortho(threshold=threshold)
+    solution = [initial_value]
+    for i in range(number_of_steps):
+        if i == 0:
+            if previous_value is None:
+                # h*A + sum 2/(2k-1)! (h/2)^(2k-1) A^(2k-1); 2 * (h/2) == h exactly
+                op_first = _odd_series(operator, 2.0, step_size / 2, order).ortho(threshold=threshold)
+                back = _shifted(operator, -0.5 * step_size).dot(solution[0])
+                prev = solution[0] - op_first.dot(back)
+            else:
+                prev = previous_value
+            if normalize > 0:
+                prev = (1 / prev.norm(p=normalize)) * prev
+            prev = prev.ortho(threshold=threshold, max_rank=max_rank)
+        else:
+            prev = solution[i - 1].copy()
+        nxt = (prev + op_hod.dot(solution[i])).ortho(threshold=threshold, max_rank=max_rank)
+        if normalize > 0:
+            nxt = (1 / nxt.norm(p=normalize)) * nxt
+        solution.append(nxt.copy())
+    return solution
 
 
 def implicit_euler(operator, initial_value, initial_guess, step_sizes: List[float], repeats: int = 1,

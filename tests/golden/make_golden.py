@@ -271,6 +271,31 @@ def ode_cases():
     print('ode_markov', 'adaptive steps', len(times), times[-1], 'impl err', out['impl_err'])
 
 
+def hod_cases():
+    """Higher-order differencing (ode.py:117-247) on a small Markov generator:
+    order 2 and order 4 (operator powers), and a given previous value."""
+    rng = np.random.default_rng(13)
+    d, n = 3, 3
+    gen = RTT(wl.markov_op(d, n, 0.2, rng)) - rtt.eye([n] * d)
+    x0 = (1.0 / n ** d) * rtt.ones([n] * d, [1] * d)
+    prev = RTT([np.abs(c) + 0.1 for c in wl.gaussian_tt(rng, d, n, 2)])
+    out = {}
+    pack('op', [c.copy() for c in gen.cores], out)
+    pack('x0', [c.copy() for c in x0.cores], out)
+    pack('prev', [c.copy() for c in prev.cores], out)
+
+    def store(prefix, sol):
+        out[prefix + '_n'] = np.array(len(sol))
+        for k, t in enumerate(sol):
+            out[f'{prefix}_{k}'] = np.asarray(t.full()).reshape(-1)
+
+    store('o2', rode.hod(gen, x0, 0.1, 4, order=2, progress=False))
+    store('o4', rode.hod(gen, x0, 0.1, 4, order=3, progress=False))
+    store('o2p', rode.hod(gen, x0, 0.05, 3, order=2, previous_value=prev.copy(), normalize=2, progress=False))
+    np.savez_compressed(os.path.join(HERE, 'ode_hod.npz'), **out)
+    print('ode_hod', {k: v.shape for k, v in out.items() if k.endswith('_3')})
+
+
 def trunc_cases():
     """ortho_left / ortho_right / ortho with threshold and max_rank (SVD truncation)."""
     rng = np.random.default_rng(21)
@@ -458,6 +483,7 @@ def main():
     evp_blocks()
     power_cases()
     ode_cases()
+    hod_cases()
     trunc_cases()
     mals_cases()
     tdvp_cases()
@@ -483,5 +509,7 @@ if __name__ == '__main__':
         struct_case()
     elif len(sys.argv) > 1 and sys.argv[1] == 'deflation':
         deflation_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'hod':
+        hod_cases()
     else:
         main()

@@ -256,3 +256,17 @@ def test_oracle_evp_deflation_matches_reference(golden):
     v, r = O.full_vector(vec), z['vec']
     assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-7
     assert abs(float(z['val']) - np.linalg.eigvalsh(O.full_matrix(cores('op')))[1]) < 1e-8
+
+
+@pytest.mark.parametrize('prefix,step,steps,order,prev,normalize',
+                         [('o2', 0.1, 4, 2, False, 1), ('o4', 0.1, 4, 3, False, 1), ('o2p', 0.05, 3, 2, True, 2)])
+def test_oracle_hod_matches_reference(golden, prefix, step, steps, order, prev, normalize):
+    """Higher-order differencing (ode.py:117-247), orders 2 and 4 (an odd order is
+    raised by one), with and without a given previous value."""
+    z, cores = golden('ode_hod')
+    sol = O.hod(cores('op'), cores('x0'), step, steps, order=order,
+                previous_value=cores('prev') if prev else None, normalize=normalize)
+    assert len(sol) == int(z[prefix + '_n'])
+    for k, s in enumerate(sol):
+        r = z[f'{prefix}_{k}']
+        assert np.linalg.norm(O.full_vector(s) - r) / np.linalg.norm(r) < 1e-12
