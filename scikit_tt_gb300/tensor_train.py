@@ -15,8 +15,11 @@ GPU through ``libttals.so``:
   reference meets on unnormalised trains)
 
 Structural helpers (``+``, ``-``, scalar ``*``, ``transpose``, ``copy``,
-``element``, ``full``, ``matricize``) and ``norm(p=1)`` are block copies and
-sums and stay in NumPy.
+``element``, ``full``, ``matricize``, ``tensordot``, ``rank_tensordot``,
+``concatenate``, ``rank_transpose``, ``tt2qtt``/``qtt2tt``, ``diag``,
+``squeeze``) and ``norm(p=1)`` are block copies, small contractions and sums
+and stay in NumPy.  ``svd``/``pinv`` at a bond orthonormalise on the device
+and split the bond core (one small matrix) on the host.
 """
 
 from __future__ import annotations
@@ -176,6 +179,236 @@ class TT(object):
                                                            int(np.prod(self.col_dims[:i + 1])), self.ranks[i + 1]))
         m, n = int(np.prod(self.row_dims)), int(np.prod(self.col_dims))
         return mat.reshape(m) if n == 1 else mat.reshape(m, n)
+
+    # ------------------------------------------------ structural helpers (host)
+    def _refresh(self):
+        self.order = len(self.cores)
+        self.row_dims = [c.shape[1] for c in self.cores]
+        self.col_dims = [c.shape[2] for c in self.cores]
+        self.ranks = [c.shape[0] for c in self.cores] + [self.cores[-1].shape[3]]
+        return self
+
+    def rank_transpose(self, overwrite: bool = False) -> 'TT':
+        """The same tensor with the core order reversed and each core's two rank
+        axes swapped (tensor_train.py:862-904)."""
+        t = self if overwrite else self.copy()
+        t.cores = [np.transpose(c, (3, 1, 2, 0)) for c in reversed(t.cores)]
+        return t._refresh()
+
+    def rank_tensordot(self, matrix: np.ndarray, mode: str = 'last', overwrite: bool = False) -> 'TT':
+        """Contract ``matrix`` into the last rank axis (``t ×_last matrix``) or
+        the first (``matrix ×_first t``), tensor_train.py:703-746."""
+        if len(matrix.shape) != 2:
+            raise ValueError('argument matrix has to be 2D-Array')
+        t = self if overwrite else self.copy()
+        if mode == 'last':
+            if t.ranks[-1] != matrix.shape[0]:
+                raise ValueError('dimensions do not match')
+            t.cores[-1] = np.einsum('amnb,bc->amnc', t.cores[-1], matrix)
+        elif mode == 'first':
+            if t.ranks[0] != matrix.shape[1]:
+                raise ValueError('dimensions do not match')
+            t.cores[0] = np.einsum('ca,amnb->cmnb', matrix, t.cores[0])
+        else:
+            raise ValueError('unknown mode')
+        return t._refresh()
+
+    def concatenate(self, other: Union['TT', List[np.ndarray]], overwrite: bool = False) -> 'TT':
+        """Append the cores of ``other`` (a TT or a list of 4-D cores) after the
+        last core; the rank between them must agree (tensor_train.py:748-793)."""
+        t = self if overwrite else self.copy()
+        extra = []
+        if isinstance(other, TT):
+            extra = other.cores
+        elif isinstance(other, list):
+            if not all(c.ndim == 4 for c in other):
+                raise ValueError('list elements must be 4-dimensional arrays')
+            if any(other[i].shape[3] != other[i + 1].shape[0] for i in range(len(other) - 1)):
+                raise ValueError('List elements must be 4-dimensional arrays.')
+            extra = other
+        if extra and t.ranks[-1] != extra[0].shape[0]:
+            raise ValueError('ranks do not match!')
+        t.cores = list(t.cores) + list(extra)
+        return t._refresh()
+
+    def tensordot(self, other: 'TT', num_axes: int, mode: str = 'last-first', overwrite: bool = False) -> 'TT':
+        """Contract ``num_axes`` modes at one end of ``self`` with ``num_axes``
+        modes at one end of ``other`` (tensor_train.py:526-701).  ``mode`` names
+        the ends, ``'<self end>-<other end>'``; the contracted ends must carry
+        boundary rank 1.  The result chains what is left of both trains through
+        the contracted block: with ``self``'s remainder on the side it came from
+        and ``other``'s remainder turned (reversed, ranks swapped) where needed to
+        meet it.  The block is absorbed into ``self``'s remainder, or into
+        ``other``'s when ``self`` is contracted completely."""
+        ends = {'last-first': ('last', 'first'), 'first-last': ('first', 'last'),
+                'first-first': ('first', 'first'), 'last-last': ('last', 'last')}
+        if mode not in ends:
+            raise ValueError('unknown mode')
+        k = num_axes
+        if k > self.order or k > other.order:
+            raise ValueError('num_axes is too big')
+        se, oe = ends[mode]
+        si = list(range(self.order - k, self.order)) if se == 'last' else list(range(k))
+        oi = list(range(other.order - k, other.order)) if oe == 'last' else list(range(k))
+        if [self.row_dims[i] for i in si] != [other.row_dims[j] for j in oi] or \
+                [self.col_dims[i] for i in si] != [other.col_dims[j] for j in oi]:
+            raise ValueError('axes do not match')
+        s_bound = self.ranks[-1] if se == 'last' else self.ranks[0]
+        o_bound = other.ranks[-1] if oe == 'last' else other.ranks[0]
+        if s_bound != 1 or o_bound != 1:
+            raise ValueError(f'{se} rank of self and {oe} rank of other have to be 1')
+        # block[a, a', b, b']: self's ranks before/after the paired cores, then other's
+        block = None
+        for i, j in zip(si, oi):
+            pair = np.einsum('amnc,bmnd->acbd', self.cores[i], other.cores[j])
+            block = pair if block is None else np.einsum('acbd,cedf->aebf', block, pair)
+        bridge = block[:, 0] if se == 'last' else block[0]            # (open self rank, b, b')
+        bridge = bridge[:, :, 0] if oe == 'last' else bridge[:, 0, :]  # (open self rank, open other rank)
+
+        def turned(cores):
+            return [np.transpose(c, (3, 1, 2, 0)) for c in reversed(cores)]
+
+        s_rest = self.cores[:self.order - k] if se == 'last' else self.cores[k:]
+        o_rest = other.cores[k:] if oe == 'first' else other.cores[:other.order - k]
+        if se == 'last':    # self's remainder on the left, other's open end must face left
+            left, right = list(s_rest), list(o_rest) if oe == 'first' else turned(o_rest)
+        else:               # self's remainder on the right, other's open end must face right
+            left, right = (list(o_rest) if oe == 'last' else turned(o_rest)), list(s_rest)
+        if not left and not right:
+            cores = [bridge[:, None, None, :]]
+        elif s_rest and se == 'last':
+            left[-1] = np.einsum('amnb,bc->amnc', left[-1], bridge)
+            cores = left + right
+        elif s_rest:
+            right[0] = np.einsum('bc,bmnd->cmnd', bridge, right[0])
+            cores = left + right
+        elif se == 'last':  # self used up: absorb into other's first remaining core
+            right[0] = np.einsum('ab,bmnd->amnd', bridge, right[0])
+            cores = right
+        else:
+            left[-1] = np.einsum('cmnb,ab->cmna', left[-1], bridge)
+            cores = left
+        if overwrite:
+            self.cores = cores
+            return self._refresh()
+        return TT(cores)
+
+    def tt2qtt(self, row_dims: List[List[int]], col_dims: List[List[int]], threshold: float = 0) -> 'TT':
+        """Split every core's mode into the factors ``row_dims[i]`` x
+        ``col_dims[i]`` by successive SVDs (gesvd), singular values with
+        sigma_k / sigma_0 <= threshold dropped (tensor_train.py:1432-1516).  A
+        format conversion on the host."""
+        import scipy.linalg as sla
+        out = []
+        for i, core in enumerate(self.cores):
+            r, right = self.ranks[i], self.ranks[i + 1]
+            rest_m, rest_n = self.row_dims[i], self.col_dims[i]
+            work = core
+            for fm, fn in zip(row_dims[i][:-1], col_dims[i][:-1]):
+                rest_m, rest_n = rest_m // fm, rest_n // fn
+                mat = work.reshape(r, fm, rest_m, fn, rest_n, right).transpose(0, 1, 3, 2, 4, 5)
+                u, s, v = sla.svd(mat.reshape(r * fm * fn, rest_m * rest_n * right), full_matrices=False,
+                                  check_finite=False, lapack_driver='gesvd')
+                if threshold != 0:
+                    keep = np.where(s / s[0] > threshold)[0]
+                    u, s, v = u[:, keep], s[keep], v[keep, :]
+                out.append(u.reshape(r, fm, fn, s.shape[0]))
+                work = s[:, None] * v
+                r = s.shape[0]
+            out.append(work.reshape(r, rest_m, rest_n, right))
+        return TT(out)
+
+    def qtt2tt(self, merge_numbers: List[int]) -> 'TT':
+        """Merge groups of ``merge_numbers[k]`` consecutive cores into one core
+        each (row and column modes combined, tensor_train.py:1518-1575)."""
+        out, k = [], 0
+        for cnt in merge_numbers:
+            core = self.cores[k].copy()
+            for j in range(k + 1, k + cnt):
+                nxt = self.cores[j]
+                core = np.einsum('amnb,bpqc->ampnqc', core, nxt).reshape(
+                    core.shape[0], core.shape[1] * nxt.shape[1], core.shape[2] * nxt.shape[2], nxt.shape[3])
+            out.append(core)
+            k += cnt
+        return TT(out)
+
+    def diag(self, diag_list: List) -> 'TT':
+        """Turn the vector cores listed in ``diag_list`` into diagonal operator
+        cores, core[k, :, :, l] = diag(core[k, :, 0, l]); those cores are
+        complex, as in the reference (tensor_train.py:1719-1747)."""
+        cores = list(self.cores)
+        for i in diag_list:
+            r1, n, _, r2 = cores[i].shape
+            dc = np.zeros((r1, n, n, r2), dtype=complex)
+            idx = np.arange(n)
+            dc[:, idx, idx, :] = cores[i][:, :, 0, :]
+            cores[i] = dc
+        return TT(cores)
+
+    def squeeze(self) -> 'TT':
+        """Drop every mode with row and column dimension 1, multiplying its
+        (rank x rank) matrix into the neighbouring kept core: modes before the
+        first kept one into it from the left (row 0 of the first boundary rank),
+        every other one into the kept core before it (tensor_train.py:1749-1804).
+        ``self`` is left unchanged; a train without any kept mode squeezes to a
+        single 1 x 1 core."""
+        keep = [i for i in range(self.order) if not (self.row_dims[i] == 1 and self.col_dims[i] == 1)]
+        mats = [c[:, 0, 0, :] for c in self.cores]
+        if not keep:
+            v = mats[0][:1, :]
+            for mtx in mats[1:]:
+                v = v @ mtx
+            return TT([v.reshape(1, 1, 1, v.shape[1])])
+        cores = []
+        for pos, i in enumerate(keep):
+            core = self.cores[i]
+            if pos == 0 and i > 0:
+                lead = mats[0][:1, :]
+                for mtx in mats[1:i]:
+                    lead = lead @ mtx
+                core = np.einsum('ab,bmnc->amnc', lead, core)
+            stop = keep[pos + 1] if pos + 1 < len(keep) else self.order
+            for j in range(i + 1, stop):
+                core = core @ mats[j]
+            cores.append(core)
+        return TT(cores)
+
+    def svd(self, index: int, threshold: float = 0.0, max_rank: int = np.inf, ortho_l: bool = True,
+            ortho_r: bool = True, overwrite: bool = False):
+        """SVD of a vector train at bond ``index`` (tensor_train.py:1577-1662):
+        cores ``0..index-2`` left- and ``index..d-1`` right-orthonormalised on the
+        device (truncated by ``threshold`` / ``max_rank``), then the bond core
+        ``index-1`` split by gesvd with the same cut.  Returns ``(u, s, v)``: the
+        left train (its last rank is the bond), the singular values, the right
+        train."""
+        import scipy.linalg as sla
+        t = self if overwrite else self.copy()
+        if ortho_l:
+            t = t.ortho_left(end_index=index - 2, threshold=threshold, max_rank=max_rank)
+        if ortho_r:
+            t = t.ortho_right(end_index=index, threshold=threshold, max_rank=max_rank)
+        a, m, b = t.ranks[index - 1], t.row_dims[index - 1], t.ranks[index]
+        u, s, v = sla.svd(t.cores[index - 1].reshape(a * m, b), full_matrices=False, check_finite=False,
+                          lapack_driver='gesvd')
+        if threshold != 0:
+            keep = np.where(s / s[0] > threshold)[0]
+            u, s, v = u[:, keep], s[keep], v[keep, :]
+        if max_rank != np.inf:
+            k = int(min(s.shape[0], max_rank))
+            u, s, v = u[:, :k], s[:k], v[:k, :]
+        t.cores[index - 1] = u.reshape(a, m, 1, s.shape[0])
+        t.cores[index] = np.einsum('kb,bmnc->kmnc', v, t.cores[index])
+        t._refresh()
+        return TT(t.cores[:index]), s, TT(t.cores[index:])
+
+    def pinv(self, index: int, threshold: float = 0.0, ortho_l: bool = True, ortho_r: bool = True,
+             overwrite: bool = False) -> 'TT':
+        """Pseudo-inverse at bond ``index`` (tensor_train.py:1664-1717): the
+        trains of ``svd`` joined with 1/s in place of s."""
+        u, s, v = TT.svd(self, index, threshold=threshold, ortho_l=ortho_l, ortho_r=ortho_r, overwrite=overwrite)
+        cores = u.cores + v.cores
+        cores[index] = np.einsum('k,kmnc->kmnc', np.reciprocal(s), cores[index])
+        return TT(cores)
 
     # ------------------------------------------------------- orthonormalisation
     def _ortho(self, direction, first, last):
@@ -390,4 +623,21 @@ def build_core(matrix_list, iscomplex: bool = False) -> np.ndarray:
                 core[i, :, :, j] = e.reshape(shape)
             elif e != 0:
                 raise TypeError('Parameters in list must be either an 0 or a matrix.\n')
+    return core
+
+
+def build_core_vector(matrix_list, field_type: str = 'float') -> np.ndarray:
+    """Column core (r, m, n, 1) from a flat list of matrices, vectors (n = 1) or
+    zeros (tensor_train.py:2076-2142).  With ``field_type='complex'`` the
+    reference leaves every entry zero (it skips the copy); here the matrices
+    are copied in both cases."""
+    shape = None
+    for e in matrix_list:
+        if isinstance(e, np.ndarray):
+            shape = (e.shape[0], 1) if e.ndim == 1 else e.shape
+            break
+    core = np.zeros((len(matrix_list), shape[0], shape[1], 1), dtype=field_type)
+    for i, e in enumerate(matrix_list):
+        if isinstance(e, np.ndarray):
+            core[i, :, :, 0] = e.reshape(shape)
     return core

@@ -159,6 +159,82 @@ def struct_case():
     print('ttops_struct add ranks', s.ranks, 'hosvd ranks', h_thr.ranks, h_max.ranks)
 
 
+def container_case():
+    """The rest of the TT container (tensor_train.py:526-904, 1432-1804,
+    2076-2142): tensordot in its four modes (partial and complete on either
+    side), rank_tensordot, concatenate, rank_transpose, tt2qtt / qtt2tt, diag,
+    squeeze, svd / pinv at a bond, build_core_vector."""
+    rng = np.random.default_rng(31)
+
+    def rt(rk, rd, cd):
+        return [rng.standard_normal((rk[i], rd[i], cd[i], rk[i + 1])) for i in range(len(rd))]
+
+    a = rt([1, 2, 3, 2, 1], [2, 3, 2, 2], [1, 2, 1, 1])
+    b = rt([1, 3, 2, 1], [2, 2, 3], [1, 1, 2])
+    c = rt([1, 2, 2, 1], [2, 3, 2], [1, 2, 1])
+    out = {}
+    pack('a', a, out)
+    pack('b', b, out)
+    pack('c', c, out)
+    A, B, Cc = (lambda: RTT([x.copy() for x in a])), (lambda: RTT([x.copy() for x in b])), \
+        (lambda: RTT([x.copy() for x in c]))
+    # (self, other, num_axes, mode) -- dims must match on the contracted ends
+    e = rt([1, 1], [2], [1])
+    pack('e', e, out)
+    E = lambda: RTT([x.copy() for x in e])  # noqa: E731
+    cases = {'lf2': (A, B, 0, 2, 'last-first'), 'fl1': (B, A, 0, 1, 'first-last'),
+             'ff2': (A, Cc, 0, 2, 'first-first'), 'll1': (A, Cc, 0, 1, 'last-last'),
+             'ff_full_self': (Cc, A, 0, 3, 'first-first'), 'lf_full_self': (E, A, 0, 1, 'last-first'),
+             'fl_full_self': (E, A, 0, 1, 'first-last'), 'll_full_self': (E, A, 0, 1, 'last-last'),
+             'full_both': (A, A, 0, 4, 'last-first'), 'bad': (A, B, 0, 1, 'last-last')}
+    for key, (S, O, _, k, mode) in cases.items():
+        try:
+            r = S().tensordot(O(), k, mode=mode)
+            out[f'td_{key}_cores_n'] = np.array(r.order)
+            for i, core in enumerate(r.cores):
+                out[f'td_{key}_cores_{i}'] = core
+        except ValueError as e:
+            out[f'td_{key}_error'] = np.array(str(e))
+    out['m_last'], out['m_first'] = rng.standard_normal((1, 3)), rng.standard_normal((4, 1))
+    out['rtd_last'] = np.asarray(A().rank_tensordot(out['m_last'], mode='last').cores[-1])
+    out['rtd_first'] = np.asarray(A().rank_tensordot(out['m_first'], mode='first').cores[0])
+    cat = A().concatenate(RTT([x.copy() for x in b]))
+    out['cat_full'] = np.asarray(cat.full()).reshape(-1)
+    out['rtr_full'] = np.asarray(A().rank_transpose().full()).reshape(-1)
+    q = rt([1, 2, 3, 1], [4, 6, 2], [2, 1, 4])
+    pack('q', q, out)
+    qt = RTT([x.copy() for x in q]).tt2qtt([[2, 2], [2, 3], [2]], [[1, 2], [1, 1], [2, 2]])
+    out['qtt_ranks'] = np.array(qt.ranks)
+    out['qtt_full'] = np.asarray(qt.full()).reshape(-1)
+    qt2 = RTT([x.copy() for x in q]).tt2qtt([[2, 2], [2, 3], [2]], [[1, 2], [1, 1], [2, 2]], threshold=0.6)
+    out['qtt_thr_ranks'] = np.array(qt2.ranks)
+    out['qtt_thr_full'] = np.asarray(qt2.full()).reshape(-1)
+    back = qt.qtt2tt([2, 2, 1])
+    out['back_full'] = np.asarray(back.full()).reshape(-1)
+    out['back_rows'] = np.array(back.row_dims)
+    dg = A().diag([0, 2])
+    out['diag_full'] = np.asarray(dg.full()).reshape(-1)
+    sq = rt([1, 2, 2, 3, 2, 1], [1, 3, 1, 1, 2], [1, 1, 1, 1, 2])
+    pack('sq', sq, out)
+    s_ = RTT([x.copy() for x in sq]).squeeze()
+    out['sq_full'] = np.asarray(s_.full()).reshape(-1)
+    out['sq_rows'] = np.array(s_.row_dims)
+    v = rt([1, 3, 4, 3, 1], [3, 2, 3, 2], [1, 1, 1, 1])
+    pack('v', v, out)
+    u_, sv, w_ = RTT([x.copy() for x in v]).svd(2)
+    out['svd_s'] = sv
+    out['svd_u_full'] = np.tensordot(u_.cores[0], u_.cores[1], axes=(3, 0)).reshape(-1, u_.ranks[-1])
+    u3, sv3, _ = RTT([x.copy() for x in v]).svd(2, max_rank=2)
+    out['svd_s_r2'] = sv3
+    pv = RTT([x.copy() for x in v]).pinv(2)
+    out['pinv_full'] = np.asarray(pv.full()).reshape(-1)
+    out['bcv'] = rtt.build_core_vector([np.arange(4.0).reshape(2, 2), 0, np.eye(2)])
+    out['bcv_vec'] = rtt.build_core_vector([np.arange(3.0), 0])
+    np.savez_compressed(os.path.join(HERE, 'ttops_container.npz'), **out)
+    print('ttops_container', sorted(k for k in out if k.startswith('td_') and k.endswith('_n')),
+          [k for k in out if k.endswith('_error')], out['qtt_ranks'], out['qtt_thr_ranks'], out['svd_s'])
+
+
 def deflation_case():
     """evp.als with previous eigentensors and a shift (evp.py:376-381): the
     second-lowest Ising d=8 eigenpair, the first one deflated."""
@@ -479,6 +555,7 @@ def main():
     helpers_case()
     ttops_case()
     struct_case()
+    container_case()
     deflation_case()
     evp_blocks()
     power_cases()
@@ -511,5 +588,7 @@ if __name__ == '__main__':
         deflation_case()
     elif len(sys.argv) > 1 and sys.argv[1] == 'hod':
         hod_cases()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'container':
+        container_case()
     else:
         main()
