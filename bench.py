@@ -3,8 +3,9 @@
 
 Workload: SLE ALS on the coupled Laplacian (d=32 sites, mode size n=8,
 operator rank 4, right-hand side rank 8, solution rank 32, 4 sweeps, seeded
-inputs).  A *step* is one batch of independent solves of that workload (4 per
-SM by default) in one launch, one CTA per solve.
+inputs).  A *step* is one batch of independent solves of that workload in one
+launch, one CTA per solve; by default as many as the GPU holds resident at once
+(``ttals_batch_slots``: 5 per SM, 760 on 152 SMs).
 
 * ``value``: solves/s of the mixed-precision engine (FP32 Krylov inner solves,
   FP64 refinement residual, FP64 stacks and QR) with the inputs resident in HBM,
@@ -282,7 +283,7 @@ def other_workloads(lib, ctx, args):
     import torch
     from oracle import tt_oracle as O
     from scikit_tt_gb300 import workloads as wl
-    from scikit_tt_gb300.serving import Request, run_stream, solve_batch
+    from scikit_tt_gb300.serving import run_stream
     from scikit_tt_gb300.solvers import evp, sle
     from scikit_tt_gb300.tensor_train import TT
 

@@ -8,7 +8,6 @@ library (host-only entry point); nothing touches a GPU."""
 
 import ctypes as C
 
-import numpy as np
 import pytest
 
 from scikit_tt_gb300 import _lib, serving
