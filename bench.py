@@ -43,6 +43,7 @@ UNIT = 'solves/s'
 WORKLOAD = dict(d=32, n=8, rhs_rank=8, x_rank=32, repeats=4)
 WORKLOAD_NAME = 'coupled-Laplacian SLE ALS, d=32 n=8 op_rank=4 rhs_rank=8 x_rank=32, 4 sweeps'
 MIXED_TOL = 1e-10
+SERVE_BUDGET_BYTES = 150 * 10 ** 9   # device memory the running jobs may hold at once
 
 
 def dist_env():
@@ -365,6 +366,7 @@ def other_workloads(lib, ctx, args):
         'sle_p50_s': float(np.percentile(lat[kinds == 'sle'], 50)) if (kinds == 'sle').any() else None,
         'evp_p50_s': float(np.percentile(lat[kinds == 'evp'], 50)) if (kinds == 'evp').any() else None,
         'jobs': len(stats), 'max_local_residual': max(s['max_local_residual'] for s in stats),
+        'hbm_budget_bytes': int(os.environ.get('TTALS_BUDGET_BYTES', '0') or 0),
         'note': 'offered load exceeds one GPU: latency includes queueing'}
     torch.cuda.synchronize()
     return out
@@ -393,6 +395,8 @@ def main_gpu(args):
         dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
     torch.cuda.set_device(local)
     os.environ['TTALS_DEVICE'] = str(local)
+    # admission budget of the serving workload (150 GB of HBM); the other workloads need a few GB
+    os.environ.setdefault('TTALS_BUDGET_BYTES', str(SERVE_BUDGET_BYTES))
     dev = torch.device('cuda', local)
     lib = _lib.load()
     ctx = _lib.context()

@@ -138,7 +138,9 @@ def load():
 
 def context():
     """The process-wide engine context on the current CUDA device (created on
-    first use)."""
+    first use).  ``TTALS_DEVICE`` picks the device; ``TTALS_BUDGET_BYTES`` caps
+    the device memory the context may hold at once (arena and running jobs;
+    unset or 0: 90 % of the memory free at creation)."""
     global _ctx
     if _ctx is not None:
         return _ctx
@@ -147,7 +149,8 @@ def context():
         if _ctx is None:
             dev = int(os.environ.get('TTALS_DEVICE', '0'))
             h = C.c_void_p()
-            st = lib.ttals_create(C.byref(h), dev, 0)
+            budget = int(os.environ.get('TTALS_BUDGET_BYTES', '0') or 0)
+            st = lib.ttals_create(C.byref(h), dev, budget)
             if st != OK:
                 raise RuntimeError(f'ttals_create failed with status {st}: a CUDA device with cooperative launch '
                                    'support is required (the package has no CPU fallback)')

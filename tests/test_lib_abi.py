@@ -91,3 +91,25 @@ def test_binding_matches_header_arity():
     assert sorted(arity) == declared()
     for name, n in arity.items():
         assert len(getattr(lib, name).argtypes) == n, name
+
+
+def test_context_budget_from_environment(monkeypatch):
+    """TTALS_BUDGET_BYTES reaches ttals_create (0 when unset: 90 % of free memory)."""
+    from scikit_tt_gb300 import _lib
+    seen = []
+
+    class Fake:
+        def ttals_create(self, h, dev, budget):
+            seen.append((dev, budget))
+            return _lib.OK
+
+    monkeypatch.setattr(_lib, 'load', lambda: Fake())
+    for env, want in ((None, 0), ('150000000000', 150 * 10 ** 9)):
+        monkeypatch.setattr(_lib, '_ctx', None)
+        if env is None:
+            monkeypatch.delenv('TTALS_BUDGET_BYTES', raising=False)
+        else:
+            monkeypatch.setenv('TTALS_BUDGET_BYTES', env)
+        _lib.context()
+        assert seen[-1][1] == want
+    monkeypatch.setattr(_lib, '_ctx', None)
