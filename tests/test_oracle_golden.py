@@ -17,12 +17,14 @@ def test_oracle_sle_matches_reference(golden, name):
     assert O.stable_rel_diff(sol, ref) < 1e-12
 
 
-def test_oracle_sle_toeplitz_known_answer(golden):
+@pytest.mark.parametrize('solver', ['solve', 'lu'])
+def test_oracle_sle_toeplitz_known_answer(golden, solver):
+    """The reference's ALS known answer (tests/test_sle.py:37-59), both local solvers."""
     z, cores = golden('sle_toeplitz')
     mat = sla.toeplitz(np.arange(1, 2 ** 10 + 1), np.arange(1, 2 ** 10 + 1)).astype(float)
     from scikit_tt_gb300.tensor_train import _hosvd
     op = _hosvd(mat.reshape([2] * 20), 0, np.inf)
-    sol = O.sle_als(op, cores('x0'), cores('rhs'), repeats=1)
+    sol = O.sle_als(op, cores('x0'), cores('rhs'), repeats=1, solver=solver)
     exact = np.linalg.solve(mat, np.ones(1024))
     got = O.full_vector(sol)
     ref = O.full_vector(cores('sol'))
