@@ -155,6 +155,8 @@ def struct_case():
     pack('A', A, out)
     pack('P', P, out)
     pack('Q', Q, out)
+    np.random.seed(5)                 # tt.rand draws from NumPy's global generator, in core order
+    pack('rand', rtt.rand([2, 3, 4], [1, 2, 1], [1, 3, 2, 1]).cores, out)
     np.savez_compressed(os.path.join(HERE, 'ttops_struct.npz'), **out)
     print('ttops_struct add ranks', s.ranks, 'hosvd ranks', h_thr.ranks, h_max.ranks)
 

@@ -44,7 +44,7 @@ def test_hosvd_constructor(golden):
 
 
 def test_constructors(golden):
-    z, _ = golden('ttops_struct')
+    z, cores = golden('ttops_struct')
     L = z['L']
     np.testing.assert_allclose(tt.eye([2, 3]).full().reshape(-1), z['eye_full'], **RT)
     np.testing.assert_allclose(tt.ones([2, 3], [1, 2], ranks=2).full().reshape(-1), z['ones_full'], **RT)
@@ -53,6 +53,9 @@ def test_constructors(golden):
     np.testing.assert_allclose(tt.uniform([2, 3, 2], ranks=2, norm=3.0).full().reshape(-1), z['uniform_full'], **RT)
     np.testing.assert_array_equal(tt.build_core([[np.eye(3), 0], [L, np.eye(3)]]), z['core_nested'])
     np.testing.assert_array_equal(tt.build_core([L, np.eye(3), 2 * L]), z['core_flat'])
+    np.random.seed(5)
+    for c, r in zip(tt.rand([2, 3, 4], [1, 2, 1], [1, 3, 2, 1]).cores, cores('rand')):
+        np.testing.assert_array_equal(c, r)
 
 
 def test_container_errors():
