@@ -138,3 +138,15 @@ def test_tdvp_manhattan_normalisation_and_zero_steps():
         assert np.linalg.norm(O.full_vector(t.cores) - v) / np.linalg.norm(v) < 1e-10
     assert abs(np.sum(O.full_vector(sol[-1].cores)) - 1.0) < 1e-12
     assert len(ode.tdvp2site(op, _tt(x0), -0.03j, 0)) == 1
+
+
+@pytest.mark.parametrize('prefix,step,steps,order,prev,normalize',
+                         [('o2', 0.1, 4, 2, False, 1), ('o4', 0.1, 4, 3, False, 1), ('o2p', 0.05, 3, 2, True, 2)])
+def test_hod_matches_reference(golden, prefix, step, steps, order, prev, normalize):
+    """Higher-order differencing (ode.py:117-247) on the device: operator products
+    (A^3 at order 4), truncated orthonormalisation of operator and vector trains."""
+    from scikit_tt_gb300.solvers import ode
+    z, cores = golden('ode_hod')
+    sol = ode.hod(_tt(cores('op')), _tt(cores('x0')), step, steps, order=order,
+                  previous_value=_tt(cores('prev')) if prev else None, normalize=normalize, progress=False)
+    _close(sol, _series(z, prefix), 1e-10)
