@@ -180,6 +180,13 @@ int ttals_job_poll(ttals_job* job, int32_t* done);
  * outputs while the rest of the job keeps running. */
 int ttals_job_poll_each(ttals_job* job, int32_t* done);
 int ttals_job_fetch(ttals_job* job, int32_t index);
+/* Request `index`'s own statistics once fetched: out[0] its worst final
+ * relative residual over its local solves (linear systems: FP64 residual of
+ * the local system; eigenproblems: Ritz residual relative to the projected
+ * operator's norm), out[1] local solves, out[2] Krylov iterations, out[3]
+ * refinement cycles (SLE) or Lanczos restarts (EVP); min(cap, 4) values.
+ * No reference counterpart. */
+int ttals_job_report(ttals_job* job, int32_t index, double* out, int32_t cap);
 int ttals_job_finish(ttals_job* job, ttals_stats* stats);
 /* Device bytes a batch would reserve (admission control). */
 int ttals_batch_bytes(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int64_t* bytes);
@@ -263,13 +270,14 @@ int ttals_stack_op(ttals_ctx* ctx, int32_t left, const double* stack, const doub
  * memory (a process whose device memory is pre-reserved by its own pool, a
  * serving loop that must avoid the synchronisation of cudaMalloc/cudaFree, a
  * foreign host that only hands over buffers it owns).  No counterpart in the
- * reference.  All pointers are device pointers; the work is enqueued on the
- * context's stream and the call returns without waiting.  The intermediates
- * live in a 16 MiB static device array (2 * max(R0,R1) * max(r0,r1)^2 * n
- * doubles must fit, else TTALS_ERR_ARG).  The first call on a device looks up
- * the array's address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race. */
+ * reference.  All pointers must be device (or managed) memory of the
+ * context's device, else TTALS_ERR_ARG before anything is enqueued; the work
+ * is enqueued on the context's stream and the call returns without waiting.
+ * The intermediates live in a 16 MiB static device array (2 * max(R0,R1) *
+ * max(r0,r1)^2 * n doubles must fit, else TTALS_ERR_ARG).  The first call on
+ * a device looks up the array's address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race. */
 int ttals_stack_op_noalloc(ttals_ctx* ctx, int32_t left, const double* stack, const double* x,
                            const double* op, int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1,
                            double* out);

@@ -38,7 +38,8 @@ EXPORTS = (
     'ttals_batch_slots', 'ttals_wait_probe', 'ttals_sle_als', 'ttals_sle_mals', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_ortho_trunc', 'ttals_tt_norm',
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
-    'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_apply_f32',
+    'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_job_report',
+    'ttals_apply_f32',
     'ttals_apply_f64emu', 'ttals_tdvp', 'ttals_arr',
 )
 
@@ -127,6 +128,7 @@ def load():
         lib.ttals_apply_f32.argtypes = [vp, pf, pf, pf, pf, i64, i64, i64, i64, i64, pf]
         lib.ttals_apply_f64emu.argtypes = [vp, pd, pd, pd, pd, i64, i64, i64, i64, i64, pd]
         lib.ttals_job_fetch.argtypes = [vp, i32]
+        lib.ttals_job_report.argtypes = [vp, i32, pd, i32]
         lib.ttals_batch_bytes.argtypes = [vp, i32, P(Request), P(C.c_int64)]
         lib.ttals_stack_op_noalloc.argtypes = [vp, i32, pd, pd, pd, i64, i64, i64, i64, i64, pd]
         for name in EXPORTS:

@@ -2348,6 +2348,16 @@ int ttals_job_fetch(ttals_job* j, int32_t index) {
   });
 }
 
+int ttals_job_report(ttals_job* j, int32_t index, double* out, int32_t cap) {
+  if (!j || !out || cap < 0) return TTALS_ERR_ARG;
+  return guarded(j->c, [&] {
+    require(index >= 0 && index < (int)j->plan.in.size(), TTALS_ERR_ARG, "request index out of range");
+    require(!j->reps[index].empty(), TTALS_ERR_ARG, "request has not been fetched");
+    const std::vector<double>& rep = j->reps[index];
+    for (int k = 0; k < cap && k < 4; ++k) out[k] = rep[k];
+  });
+}
+
 int ttals_job_finish(ttals_job* j, ttals_stats* stats) {
   if (!j) return TTALS_ERR_ARG;
   ttals_ctx* c = j->c;

@@ -47,6 +47,20 @@ cudaError_t scratch_on(int device, double** out) {
   return cudaSuccess;
 }
 
+// True when `p` is memory a kernel on `device` may dereference: device memory
+// of that device or managed memory.  Pageable or pinned host memory, memory of
+// another device and unknown pointers are refused before anything is enqueued.
+// cudaPointerGetAttributes allocates nothing.
+bool device_reachable(const void* p, int device) {
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();  // a failed query leaves a (non-sticky) error behind: clear it
+    return false;
+  }
+  if (attr.type == cudaMemoryTypeManaged) return true;
+  return attr.type == cudaMemoryTypeDevice && attr.device == device;
+}
+
 }  // namespace
 
 extern "C" int ttals_stack_op_noalloc(ttals_ctx* ctx, int32_t left, const double* stack, const double* x,
@@ -57,16 +71,37 @@ extern "C" int ttals_stack_op_noalloc(ttals_ctx* ctx, int32_t left, const double
     ttals::ctx_set_error(ctx, "dimensions must be positive");
     return TTALS_ERR_ARG;
   }
+  // Each of the two intermediates holds at most max(R) * max(r)^2 * n doubles.
+  // The product is formed with overflow checks, so absurd dimensions cannot
+  // wrap around and slip under the limit.
   const int64_t rmax = r0 > r1 ? r0 : r1, Rmax = R0 > R1 ? R0 : R1;
-  const int64_t per = Rmax * rmax * rmax * n;  // each of the two intermediates
-  if (per > kScratchDoubles / 2) {
-    ttals::ctx_set_error(ctx, "ttals_stack_op_noalloc: the intermediates need " + std::to_string(2 * per) +
+  int64_t per = 0;
+  const bool wrapped = __builtin_mul_overflow(Rmax, rmax, &per) || __builtin_mul_overflow(per, rmax, &per) ||
+                       __builtin_mul_overflow(per, n, &per);
+  if (wrapped || per > kScratchDoubles / 2) {
+    ttals::ctx_set_error(ctx, "ttals_stack_op_noalloc: the intermediates need " +
+                                  (wrapped ? std::string("more than 2^63") : std::to_string(2 * per)) +
                                   " doubles, above the static scratch of " + std::to_string(kScratchDoubles) +
                                   " doubles (16 MiB); use ttals_stack_op");
     return TTALS_ERR_ARG;
   }
+  if (!stack || !x || !op || !out) {
+    ttals::ctx_set_error(ctx, "ttals_stack_op_noalloc: null pointer");
+    return TTALS_ERR_ARG;
+  }
+  const int device = ttals::ctx_device(ctx);
+  const void* ptrs[4] = {stack, x, op, out};
+  const char* names[4] = {"stack", "x", "op", "out"};
+  for (int k = 0; k < 4; ++k) {
+    if (!device_reachable(ptrs[k], device)) {
+      ttals::ctx_set_error(ctx, std::string("ttals_stack_op_noalloc: ") + names[k] +
+                                    " is not device or managed memory of the context's device "
+                                    "(this entry point takes device pointers only; ttals_stack_op takes host arrays)");
+      return TTALS_ERR_ARG;
+    }
+  }
   double* base = nullptr;
-  cudaError_t e = scratch_on(ttals::ctx_device(ctx), &base);
+  cudaError_t e = scratch_on(device, &base);
   if (e != cudaSuccess) {
     ttals::ctx_set_error(ctx, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
                                   cudaGetErrorString(e));

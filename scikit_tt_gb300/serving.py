@@ -40,6 +40,7 @@ class Request:
     solution: Optional[TT] = None
     value: Optional[float] = None
     iterations: Optional[int] = None
+    local_residual: Optional[float] = None   # worst final relative residual of its local solves
     done: float = 0.0
     _keep: list = field(default_factory=list, repr=False)
 
@@ -129,6 +130,9 @@ class Server:
             for i in range(len(reqs)):
                 if flags[i] and i not in fetched:
                     _lib.check(lib.ttals_job_fetch(h, i))
+                    rep = np.zeros(4)
+                    _lib.check(lib.ttals_job_report(h, i, _lib.dptr(rep), 4))
+                    reqs[i].local_residual = float(rep[0])
                     reqs[i]._complete()
                     reqs[i].done = clock()
                     fetched.add(i)

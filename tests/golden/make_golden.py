@@ -1,21 +1,43 @@
 """Generate the golden fixtures of ``tests/golden/`` from the reference itself.
 
-Runs the unmodified scikit_tt package (imported read-only from the path in
-``SCIKIT_TT_REF``, default ``/root/reference``) on small seeded inputs and
-stores inputs and outputs as ``.npz``.  The oracle and the device engine are
-both checked against these files, so the GPU tests never need the reference.
+Runs the unmodified scikit_tt package, imported read-only from the directory
+given by ``--reference PATH`` or the ``SCIKIT_TT_REF`` environment variable
+(one of the two is required: the directory that holds the ``scikit_tt``
+package), on seeded inputs and stores inputs and outputs as ``.npz``.  The
+oracle and the device engine are both checked against these files, so the GPU
+tests never need the reference.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference /path/to/scikit_tt_checkout [case]
 """
 
 from __future__ import annotations
 
 import os
 import sys
+import time
 
 import numpy as np
 
-REF = os.environ.get('SCIKIT_TT_REF', '/root/reference')
+
+def _reference_root():
+    """The reference checkout from ``--reference PATH`` or ``SCIKIT_TT_REF``;
+    exits with a message when neither names a directory with a scikit_tt package."""
+    root = None
+    if '--reference' in sys.argv:
+        k = sys.argv.index('--reference')
+        if k + 1 >= len(sys.argv):
+            sys.exit('make_golden.py: --reference needs a path')
+        root = sys.argv[k + 1]
+        del sys.argv[k:k + 2]
+    root = root or os.environ.get('SCIKIT_TT_REF')
+    if not root:
+        sys.exit('make_golden.py: pass --reference PATH or set SCIKIT_TT_REF to the scikit_tt checkout')
+    if not os.path.isfile(os.path.join(root, 'scikit_tt', 'solvers', 'sle.py')):
+        sys.exit(f'make_golden.py: {root} does not hold the scikit_tt package (scikit_tt/solvers/sle.py)')
+    return root
+
+
+REF = _reference_root()
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REF)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
@@ -529,6 +551,63 @@ def arr_cases():
     arr_case('arr_three_mode', xs, ys, basis3, x03, 3, 1e-10)
 
 
+def fingerprint(cores):
+    """Sum and sum of squares over all cores plus their shapes: the tests check
+    that the seeded generator still yields the inputs the reference solved."""
+    return np.array([sum(float(c.sum()) for c in cores), sum(float((c * c).sum()) for c in cores)])
+
+
+def _timed_als(w):
+    t0 = time.perf_counter()
+    sol = rsle.als(RTT([c.copy() for c in w.op]), RTT([c.copy() for c in w.x0]),
+                   RTT([c.copy() for c in w.rhs]), repeats=w.repeats, solver='solve')
+    return sol, time.perf_counter() - t0
+
+
+def headline_case():
+    """The coupled-Laplacian SLE at full size (d=32, n=8, operator rank 4, RHS
+    rank 8, guess rank 32, 4 sweeps, seed 0): the reference's own sle.als on
+    the inputs ``workloads.coupled_sle(seed=0)`` builds, which are also the
+    first instance of the benchmark's batch.  Inputs are regenerated by the
+    tests from the seed (their fingerprints are stored); the solution cores,
+    the wall time and the host's thread count are stored."""
+    from oracle import tt_oracle as orc
+    w = wl.coupled_sle(seed=0, d=32, n=8, rhs_rank=8, x_rank=32, repeats=4)
+    sol, wall = _timed_als(w)
+    res = orc.stable_residual(w.op, [np.asarray(c) for c in sol.cores], w.rhs)
+    out = {'seed': np.array(0), 'repeats': np.array(w.repeats), 'wall_s': np.array(wall),
+           'host_threads': np.array(os.cpu_count()), 'global_rel_residual': np.array(res),
+           'fp_op': fingerprint(w.op), 'fp_rhs': fingerprint(w.rhs), 'fp_x0': fingerprint(w.x0)}
+    pack('sol', sol.cores, out)
+    np.savez_compressed(os.path.join(HERE, 'sle_coupled_d32_headline.npz'), **out)
+    print('headline ranks', sol.ranks, 'wall %.1f s' % wall, 'global residual %.3e' % res)
+
+
+BATCH_SUBSET = list(range(16))   # the 16 smallest-seed instances of the uneven batch
+
+
+def batch_subset_case():
+    """The 16 smallest-seed instances of the uneven batch (instance j from
+    default_rng(1000 + j): d 8..32, n in {2,4,8}, ranks 4..48, 4 sweeps), each
+    solved by the reference's sle.als.  Stores per instance the solution cores,
+    the input fingerprints, the wall time and the global residual."""
+    from oracle import tt_oracle as orc
+    out = {'seeds': np.array(BATCH_SUBSET), 'host_threads': np.array(os.cpu_count())}
+    walls = []
+    for j in BATCH_SUBSET:
+        w = wl.batch_instance(j)
+        sol, wall = _timed_als(w)
+        walls.append(wall)
+        res = orc.stable_residual(w.op, [np.asarray(c) for c in sol.cores], w.rhs)
+        out[f'j{j}_global_rel_residual'] = np.array(res)
+        out[f'j{j}_fp_rhs'] = fingerprint(w.rhs)
+        out[f'j{j}_fp_x0'] = fingerprint(w.x0)
+        pack(f'j{j}_sol', sol.cores, out)
+        print('batch instance', j, w.meta, 'wall %.2f s' % wall, 'residual %.3e' % res, flush=True)
+    out['wall_s'] = np.array(walls)
+    np.savez_compressed(os.path.join(HERE, 'sle_batch_subset.npz'), **out)
+
+
 def main():
     # workload 1 (exact) with both local solvers
     w1 = wl.laplace_sle()
@@ -567,6 +646,8 @@ def main():
     mals_cases()
     tdvp_cases()
     arr_cases()
+    headline_case()
+    batch_subset_case()
 
 
 if __name__ == '__main__':
@@ -592,5 +673,9 @@ if __name__ == '__main__':
         hod_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'container':
         container_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'headline':
+        headline_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'batch_subset':
+        batch_subset_case()
     else:
         main()

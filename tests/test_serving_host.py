@@ -50,6 +50,10 @@ class FakeJobs:
         r.out_iterations[0] = i + 1
         return _lib.OK
 
+    def ttals_job_report(self, h, i, out, cap):
+        out[0] = 1e-12 * (i + 1)
+        return _lib.OK
+
     def ttals_job_finish(self, h, st):
         job = self.jobs.pop(h.value)
         self.in_use -= job['need']
