@@ -292,6 +292,14 @@ int ttals_apply_f32(ttals_ctx* ctx, const float* L, const float* A, const float*
  * cores (6-slice Ozaki splitting, FP32 accumulation, FP64 recombination), as
  * the mixed-precision path computes its stacks and refinement residuals.
  * Host pointers, one CTA.  No reference counterpart. */
+/* Diagnostic: D = A * Bt^T on the fifth-generation tensor cores (one
+ * tcgen05.mma tile of M = 128 rows: operands staged in shared memory, FP32
+ * accumulator in tensor memory), kind 0 BF16 or 1 TF32 inputs; A is 128 x K,
+ * Bt is N x K, out is 128 x N, all row-major host arrays.  No reference
+ * counterpart; pins the tensor-core encodings the batch kernel uses. */
+int ttals_umma_selftest(ttals_ctx* ctx, int32_t kind, int32_t N, int32_t K, const float* A, const float* Bt,
+                        float* out);
+
 int ttals_apply_f64emu(ttals_ctx* ctx, const double* L, const double* A, const double* Rt, const double* y,
                        int64_t r0, int64_t n, int64_t r1, int64_t R0, int64_t R1, double* out);
 

@@ -40,7 +40,7 @@ EXPORTS = (
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
     'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_job_report',
     'ttals_apply_f32',
-    'ttals_apply_f64emu', 'ttals_tdvp', 'ttals_arr',
+    'ttals_apply_f64emu', 'ttals_umma_selftest', 'ttals_tdvp', 'ttals_arr',
 )
 
 REQ_SLE = 0
@@ -127,6 +127,7 @@ def load():
         pf = P(C.c_float)
         lib.ttals_apply_f32.argtypes = [vp, pf, pf, pf, pf, i64, i64, i64, i64, i64, pf]
         lib.ttals_apply_f64emu.argtypes = [vp, pd, pd, pd, pd, i64, i64, i64, i64, i64, pd]
+        lib.ttals_umma_selftest.argtypes = [vp, i32, i32, i32, pf, pf, pf]
         lib.ttals_job_fetch.argtypes = [vp, i32]
         lib.ttals_job_report.argtypes = [vp, i32, pd, i32]
         lib.ttals_batch_bytes.argtypes = [vp, i32, P(Request), P(C.c_int64)]

@@ -1453,6 +1453,13 @@ struct BatchReqHost {
   int32_t* out_its = nullptr;
 };
 
+// Mixed-precision batches run on the tcgen05 kernel variant unless
+// TTALS_TENSOR_CORES=mma (warp-level mma.sync variant, kept for comparison).
+bool batch_tc_enabled() {
+  const char* v = std::getenv("TTALS_TENSOR_CORES");
+  return !(v && std::string(v) == "mma");
+}
+
 struct BatchPlan {
   std::vector<BatchReqHost> in;
   BatchSizes z{1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
@@ -1461,6 +1468,7 @@ struct BatchPlan {
   int grid = 1;
   int64_t stride = 0;
   int prec = 0;
+  int use_tc = 0;  // mixed precision on the tensor-core kernel variant
   double tol = 0.0;
   // byte layout of the device block: [regions | meta | inst | scratch | counter]
   size_t off_meta = 0, off_inst = 0, off_scratch = 0, off_next = 0, bytes = 0;
@@ -1578,7 +1586,14 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     app(Lbo, d);
     app(Rbo, d);
   }
-  P.grid = std::min(count, c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp));
+  P.use_tc = (prec == TTALS_PREC_MIXED && batch_tc_enabled()) ? 1 : 0;
+  {
+    cudaError_t e = cudaSuccess;
+    const int per_sm = batch_blocks_per_sm(kBatchM, kBatchMEvp, P.use_tc, &e);
+    require(e == cudaSuccess, TTALS_ERR_CUDA,
+            std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
+    P.grid = std::min(count, c->num_sms * per_sm);
+  }
   P.stride = batch_scratch_stride(P.z, kBatchM, kBatchMEvp);
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t o = al(sizeof(double) * P.region_total);
@@ -1643,7 +1658,7 @@ void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEve
   int* next = (int*)(mem + P.off_next);
   CK(cudaMemsetAsync(next, 0, sizeof(int), st));
   BatchArgs args{dinst, count, dmeta, next, mem + P.off_scratch, P.stride, P.z, kBatchM, kBatchMEvp,
-                 P.prec == TTALS_PREC_MIXED ? 1 : 0, P.tol, 1e-12};
+                 P.prec == TTALS_PREC_MIXED ? 1 : 0, P.tol, 1e-12, P.use_tc};
   if (k0) CK(cudaEventRecord(k0, st));
   CK(launch_batch_sle(args, P.grid, st));
   if (k1) CK(cudaEventRecord(k1, st));
@@ -2395,7 +2410,10 @@ int ttals_arr(ttals_ctx* c, int32_t order, const int64_t* basis_sizes, int64_t s
 int ttals_batch_slots(ttals_ctx* c, int32_t* slots) {
   return guarded(c, [&] {
     require(slots != nullptr, TTALS_ERR_ARG, "null output pointer");
-    *slots = c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp);
+    cudaError_t e = cudaSuccess;
+    *slots = c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp, batch_tc_enabled(), &e);
+    require(e == cudaSuccess, TTALS_ERR_CUDA,
+            std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
   });
 }
 
@@ -2712,9 +2730,39 @@ int ttals_apply_f32(ttals_ctx* c, const float* L, const float* A, const float* R
     CK(cudaMemcpyAsync(da, A, 4 * na, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dr, Rt, 4 * nr, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dy, y, 4 * N, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_apply_f32(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, reinterpret_cast<int*>(kt), c->stream));
+    CK(launch_apply_f32(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, reinterpret_cast<int*>(kt),
+                        batch_tc_enabled() ? 1 : 0, c->stream));
     CK(cudaMemcpyAsync(out, dout, 4 * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int ttals_umma_selftest(ttals_ctx* c, int32_t kind, int32_t N, int32_t K, const float* A, const float* Bt,
+                        float* out) {
+  return guarded(c, [&] {
+    require(A && Bt && out, TTALS_ERR_ARG, "null pointer");
+    require(kind == 0 || kind == 1, TTALS_ERR_ARG, "kind must be 0 (BF16) or 1 (TF32)");
+    require(N >= 16 && N <= 256 && N % 16 == 0, TTALS_ERR_ARG, "N must be a multiple of 16 in [16, 256]");
+    const int esz = kind == 0 ? 2 : 4;
+    require(K > 0 && (K * esz) % 32 == 0 && K * esz <= 512, TTALS_ERR_ARG,
+            "K must fill whole 32-byte MMA steps (K % 16 == 0 for BF16, K % 8 == 0 for TF32), at most 512 bytes");
+    const int64_t na = 128 * (int64_t)K, nb = (int64_t)N * K, nc = 128 * (int64_t)N;
+    float *da, *db, *dc, *dst;
+    Bump B{c};
+    B.want(&da, na);
+    B.want(&db, nb);
+    B.want(&dc, nc);
+    B.want(&dst, 8);
+    B.commit();
+    CK(cudaMemcpyAsync(da, A, 4 * na, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(db, Bt, 4 * nb, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(dc, 0, 4 * nc, c->stream));
+    CK(launch_umma_selftest(kind, N, K, da, db, dc, reinterpret_cast<int*>(dst), c->stream));
+    int hst = -1;
+    CK(cudaMemcpyAsync(out, dc, 4 * nc, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&hst, dst, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    require(hst == ST_OK, TTALS_ERR_TIMEOUT, "tensor-core self-test: the MMA completion wait gave up");
   });
 }
 
@@ -2742,7 +2790,8 @@ int ttals_apply_f64emu(ttals_ctx* c, const double* L, const double* A, const dou
     CK(cudaMemcpyAsync(da, A, 8 * na, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dr, Rt, 8 * nr, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(dy, y, 8 * N, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_apply_f64emu(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, oz, ozb, c->stream));
+    CK(launch_apply_f64emu(a, n, s, R0, R1, dl, da, dr, dy, t1, t2, dout, oz, ozb, batch_tc_enabled() ? 1 : 0,
+                           c->stream));
     CK(cudaMemcpyAsync(out, dout, 8 * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   });

@@ -21,6 +21,7 @@
 #include "ttals_qr.cuh"
 #include "ttals_tc.cuh"
 #include "ttals_ozaki.cuh"
+#include "ttals_tc_gemm.cuh"
 #include "ttals_tri.cuh"
 
 namespace ttals {
@@ -31,6 +32,10 @@ constexpr int kBatchThreads = 128;
 // instances overlap, and the memory-latency-bound loops get more warps to hide
 // latency behind (measured: +4 % over four CTAs per SM, with 5 x SMs requests)
 constexpr int kBatchMinBlocks = 5;
+// tensor-core variant: 256 threads (two 128-lane TMEM drain groups) and two
+// CTAs per SM, each with kTcTmemCols of the SM's 512 TMEM columns
+constexpr int kBatchThreadsTc = 256;
+constexpr int kBatchMinBlocksTc = 2;
 
 // ---------------------------------------------------------------------------
 // CTA primitives
@@ -39,12 +44,12 @@ constexpr int kBatchMinBlocks = 5;
 // Inlined body (used inside the Krylov loops); `c` must not alias C.
 template <typename T>
 __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C,
-                                                  int* ktab = nullptr) {
+                                                  int* ktab = nullptr, TcState* tc = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
-    // FP32 (inner Krylov) contractions go to the tensor cores when GEMM-shaped;
-    // the contraction-offset table lives in per-CTA global scratch (L1
-    // resident): this kernel is memory-latency bound and every KB of shared
-    // memory is taken from L1
+    // FP32 (inner Krylov) contractions go to the tensor cores when GEMM-shaped:
+    // tcgen05 (3xTF32, operands staged in shared memory, TMEM accumulator)
+    // when the CTA holds tensor memory, warp-level mma.sync otherwise
+    if (tc && ktab && cta_gemm_tf32_tc(c, A, B, C, ktab, *tc)) return;
     if (ktab && cta_gemm_tf32x3(c, A, B, C, ktab)) return;
   }
   constexpr int VW = DefaultVW<T>::value;
@@ -68,7 +73,8 @@ __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const dou
   __shared__ Contraction sc;
   if (threadIdx.x == 0) sc = cref;
   __syncthreads();
-  if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
+  if (oz && oz->tc && cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc)) return;
+  if (oz && !oz->tc && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
   cta_contract_body<double>(sc, A, B, C);
 }
 
@@ -87,11 +93,11 @@ __device__ __noinline__ void cta_contract(const Contraction& cref, const T* A, c
 // tensor-core and fallback paths instead of three inlined into the GMRES loop
 // (which otherwise spills).
 __device__ __noinline__ void cta_contract_f32(const Contraction& cref, const float* A, const float* B, float* C,
-                                              int* ktab) {
+                                              int* ktab, TcState* tc) {
   __shared__ Contraction sc;
   if (threadIdx.x == 0) sc = cref;
   __syncthreads();
-  cta_contract_body<float>(sc, A, B, C, ktab);
+  cta_contract_body<float>(sc, A, B, C, ktab, tc);
 }
 
 __device__ __forceinline__ void cta_fill(double* p, int64_t n, double v) {
@@ -147,11 +153,11 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
 template <typename T>
 __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                           const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out,
-                                          int* ktab = nullptr) {
+                                          int* ktab = nullptr, TcState* tc = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
-    cta_contract_f32(p1, L, y, T1, ktab);
-    cta_contract_f32(p2, T1, A, T2, ktab);
-    cta_contract_f32(p3, T2, R, out, ktab);
+    cta_contract_f32(p1, L, y, T1, ktab, tc);
+    cta_contract_f32(p2, T1, A, T2, ktab, tc);
+    cta_contract_f32(p3, T2, R, out, ktab, tc);
   } else {
     cta_contract_body(p1, L, y, T1, ktab);
     cta_contract_body(p2, T1, A, T2, ktab);
@@ -240,7 +246,8 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     __syncthreads();
     int jj = 0;
     for (int j = 0; j < m; ++j) {
-      cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr);
+      cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
+                    oz ? oz->tc : nullptr);
       cta_dots<TI>(V, N, j + 1, w, h1);
       // Classical Gram-Schmidt with selective reorthogonalisation (FP32 inner
       // solves): one projection suffices when it keeps at least 1/sqrt(2) of the
@@ -923,22 +930,71 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   signal_done(I.done);
 }
 
-__global__ void __launch_bounds__(kBatchThreads, kBatchMinBlocks) batch_sle_kernel(BatchArgs a) {
-  extern __shared__ double sm[];
+// Take the CTA's tensor memory and set up its completion barrier (all threads).
+__device__ __forceinline__ void tc_begin(TcState& tc, unsigned char* tiles) {
+  if ((threadIdx.x >> 5) == 0) umma::tmem_alloc(&tc.tmem, kTcTmemCols);
+  if (threadIdx.x == 0) {
+    tc.tiles = tiles;
+    tc.phase = 0;
+    tc.status = ST_OK;
+    umma::mbar_init(&tc.bar, 1);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+}
+
+// Hand the tensor memory back (all threads).  A completion wait that gave up
+// leaves MMAs possibly in flight: wait for them once more (bounded) first.
+__device__ __forceinline__ void tc_end(TcState& tc) {
+  if (tc.status != ST_OK) umma::mbar_wait(&tc.bar, tc.phase);
+  umma::fence_before_sync();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(tc.tmem, kTcTmemCols);
+}
+
+__host__ __device__ inline size_t tc_tiles_offset(size_t before) { return (before + 1023) / 1024 * 1024; }
+
+// The persistent loop of both kernel variants.  With a.use_tc the CTA holds
+// kTcTmemCols columns of tensor memory for its whole life (allocated here,
+// released on the way out whatever happened) and a 64 KB operand-tile region
+// of shared memory; its GEMM-shaped FP32 and emulated-FP64 contractions then
+// run on tcgen05.
+__device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  double* sm = reinterpret_cast<double*>(smraw);
   __shared__ int s_j;
+  __shared__ TcState s_tc;
   Scratch S = scratch_of(a, blockIdx.x);
-  S.oz.ktab = reinterpret_cast<int*>(reinterpret_cast<char*>(sm) + batch_smem_scalar_bytes(a.m, a.m_evp));
+  const size_t scal = batch_smem_scalar_bytes(a.m, a.m_evp);
+  S.oz.ktab = reinterpret_cast<int*>(smraw + scal);
+  if (a.use_tc) {
+    tc_begin(s_tc, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK));
+    S.oz.tc = &s_tc;
+  }
   for (;;) {
     if (threadIdx.x == 0) s_j = atomicAdd(a.next, 1);
     __syncthreads();
     const int j = s_j;
     __syncthreads();
-    if (j >= a.count) return;
+    if (j >= a.count) break;
     if (a.inst[j].kind == 1)
       batch_evp(a, j, S, sm);
     else
       batch_solve(a, j, S, sm);
   }
+  if (a.use_tc) tc_end(s_tc);
+}
+
+// plain FP64 (and mixed without tensor memory): 128 threads, five CTAs per SM
+__global__ void __launch_bounds__(kBatchThreads, kBatchMinBlocks) batch_sle_kernel(BatchArgs a) {
+  batch_kernel_body(a);
+}
+
+// mixed precision on tcgen05: 256 threads, two CTAs per SM (each holding half
+// of the SM's tensor memory)
+__global__ void __launch_bounds__(kBatchThreadsTc, kBatchMinBlocksTc) batch_sle_tc_kernel(BatchArgs a) {
+  batch_kernel_body(a);
 }
 
 void oz_need_site(BatchSizes& z, int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
@@ -967,6 +1023,23 @@ __global__ void __launch_bounds__(kBatchThreads) apply_f64emu_kernel(Contraction
   cta_contract_f64(p3, T2, R, out, &oz);
 }
 
+// The same on tcgen05 (256 threads, the batch kernel's tensor-core GEMMs).
+__global__ void __launch_bounds__(kBatchThreadsTc) apply_f64emu_tc_kernel(Contraction p1, Contraction p2,
+                                                                          Contraction p3, const double* L,
+                                                                          const double* A, const double* R,
+                                                                          const double* y, double* T1, double* T2,
+                                                                          double* out, OzScratch oz) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ TcState s_tc;
+  oz.ktab = reinterpret_cast<int*>(smraw);
+  tc_begin(s_tc, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK));
+  oz.tc = &s_tc;
+  cta_contract_f64(p1, L, y, T1, &oz);
+  cta_contract_f64(p2, T1, A, T2, &oz);
+  cta_contract_f64(p3, T2, R, out, &oz);
+  tc_end(s_tc);
+}
+
 size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
   BatchSizes z{};
   oz_need_site(z, a, n, s, R0, R1);
@@ -975,7 +1048,7 @@ size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, i
 
 cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const double* L,
                                 const double* A, const double* R, const double* y, double* T1, double* T2,
-                                double* out, char* ozmem, size_t ozbytes, cudaStream_t st) {
+                                double* out, char* ozmem, size_t ozbytes, int use_tc, cudaStream_t st) {
   BatchSizes z{};
   oz_need_site(z, a, n, s, R0, R1);
   auto rnd = [](int64_t b) { return (b + 255) / 256 * 256; };
@@ -998,7 +1071,14 @@ cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int
   oz.cap_c = z.oz_c;
   Contraction p1, p2, p3;
   desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
-  apply_f64emu_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
+  if (use_tc) {
+    const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + kTcSmemBytes;
+    cudaError_t e = cudaFuncSetAttribute(apply_f64emu_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    apply_f64emu_tc_kernel<<<1, kBatchThreadsTc, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
+  } else {
+    apply_f64emu_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
+  }
   ++launch_counter();
   return cudaGetLastError();
 }
@@ -1011,12 +1091,32 @@ __global__ void __launch_bounds__(kBatchThreads) apply_f32_kernel(Contraction p1
   cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
 }
 
+// The same on tcgen05 (3xTF32, 256 threads).
+__global__ void __launch_bounds__(kBatchThreadsTc) apply_f32_tc_kernel(Contraction p1, Contraction p2, Contraction p3,
+                                                                       const float* L, const float* A, const float* R,
+                                                                       const float* y, float* T1, float* T2,
+                                                                       float* out) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __shared__ TcState s_tc;
+  int* ktab = reinterpret_cast<int*>(smraw);
+  tc_begin(s_tc, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK));
+  cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab, &s_tc);
+  tc_end(s_tc);
+}
+
 cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
-                             const float* R, const float* y, float* T1, float* T2, float* out, int* ktab,
+                             const float* R, const float* y, float* T1, float* T2, float* out, int* ktab, int use_tc,
                              cudaStream_t st) {
   Contraction p1, p2, p3;
   desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
-  apply_f32_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
+  if (use_tc) {
+    const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + kTcSmemBytes;
+    cudaError_t e = cudaFuncSetAttribute(apply_f32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    apply_f32_tc_kernel<<<1, kBatchThreadsTc, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out);
+  } else {
+    apply_f32_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
+  }
   ++launch_counter();
   return cudaGetLastError();
 }
@@ -1030,8 +1130,10 @@ __host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp) {
   return sizeof(double) * (g > e ? g : e);
 }
 
-size_t batch_smem_bytes(int m, int m_evp) {
-  return batch_smem_scalar_bytes(m, m_evp) + sizeof(int) * 2 * kTcMaxK;
+size_t batch_smem_bytes(int m, int m_evp, int use_tc) {
+  const size_t base = batch_smem_scalar_bytes(m, m_evp) + sizeof(int) * 2 * kTcMaxK;
+  if (!use_tc) return base;
+  return tc_tiles_offset(base) + kTcSmemBytes;
 }
 
 int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
@@ -1042,21 +1144,36 @@ int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
          r(4 * z.opcore) + r(2 * z.oz_a) + r(2 * z.oz_b) + r(4 * z.oz_r) + r(4 * z.oz_c);
 }
 
-int batch_blocks_per_sm(int m, int m_evp) {
-  const size_t smem = batch_smem_bytes(m, m_evp);
-  cudaFuncSetAttribute(batch_sle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+int batch_threads(int use_tc) { return use_tc ? kBatchThreadsTc : kBatchThreads; }
+
+// Resident CTAs per SM of the kernel variant; *err (if given) receives the
+// first CUDA error of the query (the result is then 1).
+int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err) {
+  const size_t smem = batch_smem_bytes(m, m_evp, use_tc);
+  const void* fn = use_tc ? (const void*)batch_sle_tc_kernel : (const void*)batch_sle_kernel;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_sle_kernel, kBatchThreads, smem) != cudaSuccess ||
-      occ < 1)
-    occ = 1;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, batch_threads(use_tc), smem);
+  if (err) *err = e;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  if (occ < 1) occ = 1;
+  // each resident tensor-core CTA holds kTcTmemCols of the SM's 512 TMEM columns
+  if (use_tc && occ > (int)(512 / kTcTmemCols)) occ = (int)(512 / kTcTmemCols);
   return occ;
 }
 
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st) {
-  const size_t smem = batch_smem_bytes(a.m, a.m_evp);
-  cudaError_t e = cudaFuncSetAttribute(batch_sle_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = batch_smem_bytes(a.m, a.m_evp, a.use_tc);
+  const void* fn = a.use_tc ? (const void*)batch_sle_tc_kernel : (const void*)batch_sle_kernel;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  batch_sle_kernel<<<grid, kBatchThreads, smem, st>>>(a);
+  if (a.use_tc)
+    batch_sle_tc_kernel<<<grid, kBatchThreadsTc, smem, st>>>(a);
+  else
+    batch_sle_kernel<<<grid, kBatchThreads, smem, st>>>(a);
   ++launch_counter();
   return cudaGetLastError();
 }

@@ -47,18 +47,23 @@ struct BatchArgs {
   int prec;
   double tol;      // local linear solves
   double tol_evp;  // local eigen solves (Ritz residual relative to |T|)
+  int use_tc;      // mixed precision on tcgen05 (batch_sle_tc_kernel)
 };
 
-size_t batch_smem_bytes(int m, int m_evp);
-int batch_blocks_per_sm(int m, int m_evp);
+size_t batch_smem_bytes(int m, int m_evp, int use_tc);
+int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err = nullptr);
+int batch_threads(int use_tc);
 int64_t batch_scratch_stride(const BatchSizes& z, int m, int m_evp);
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st);
 cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const double* L,
                                 const double* A, const double* R, const double* y, double* T1, double* T2,
-                                double* out, char* ozmem, size_t ozbytes, cudaStream_t st);
+                                double* out, char* ozmem, size_t ozbytes, int use_tc, cudaStream_t st);
 size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1);
 cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
                              const float* R, const float* y, float* T1, float* T2, float* out, int* ktab,
-                             cudaStream_t st);
+                             int use_tc, cudaStream_t st);
+
+cudaError_t launch_umma_selftest(int kind, int N, int K, const float* A, const float* Bt, float* C, int* status,
+                                 cudaStream_t st);
 
 }  // namespace ttals

@@ -116,6 +116,8 @@ __device__ __forceinline__ void oz_two_sum(float& hi, float& lo, float x) {
   lo = __fadd_rn(lo, err);
 }
 
+struct TcState;  // ttals_tc_gemm.cuh
+
 struct OzScratch {
   uint16_t* as;  // S slices of A, row-major [i][k_pad]   (bf16 bits)
   uint16_t* bs;  // S slices of B, column-major [j][k_pad] (bf16 bits)
@@ -123,6 +125,7 @@ struct OzScratch {
   int* cexp;     // F_j
   int* ktab;     // 2 * kTcMaxK contraction offsets
   int64_t cap_a, cap_b, cap_r, cap_c;  // capacities (elements)
+  TcState* tc = nullptr;  // set: GEMM-shaped contractions run on tcgen05 (ttals_tc_gemm.cuh)
 };
 
 // C = contraction(A, B) with FP64-level accuracy on the BF16 tensor cores,

@@ -1,0 +1,375 @@
+// CTA-level GEMM-shaped contractions on the fifth-generation tensor cores.
+//
+// Two flavours, both staging their operands straight from the strided
+// contraction descriptors (ttals_desc.cuh, split into row / column /
+// contraction axes by gemm_split) into shared-memory tiles in the canonical
+// K-major layout (ttals_umma.cuh), with the accumulators in tensor memory:
+//
+// * cta_gemm_oz_tc: FP64-accurate C = A B from FP64 operands (emulated FP64,
+//   Ozaki-style slicing as in ttals_ozaki.cuh): each row of A (column of B) is
+//   scaled by its power-of-two maximum and cut into 6 slices of 8 bits, exact
+//   in BF16.  The 21 slice products with p + q < 6 run as tcgen05.mma
+//   kind::f16 (M = 128, N = 32, K = 16) into one FP32 accumulator per level
+//   L = p + q (6 x 32 TMEM columns).  Level sums are integers; every 64
+//   contraction steps they are drained: converted to integers, combined in
+//   64-bit fixed point (level L weighted by 2^(8 (5 - L))) and added to a
+//   per-thread running sum, which is finally turned into FP64 by bit
+//   manipulation with the scale 2^(E_i + F_j - 56) folded into the exponent.
+//   No FP64 instruction is executed (FP64 runs at 2 FMA/clk/SM on this part).
+// * cta_gemm_tf32_tc: FP32 C = A B from FP32 operands with the 3xTF32 split
+//   a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi, three tcgen05.mma kind::tf32 into
+//   one FP32 accumulator (N up to 128 columns per tile).
+//
+// One thread issues the MMAs and commits them to an mbarrier; every thread
+// waits on it (bounded), then reads its accumulator lane (row) back.
+#pragma once
+
+#include "ttals_ozaki.cuh"
+#include "ttals_umma.cuh"
+
+namespace ttals {
+
+constexpr int kTcM = 128;                 // rows per tile (TMEM lanes)
+constexpr int kTcKC = 32;                 // contraction elements per staged chunk
+constexpr int kTcOzNT = 32;               // columns per emulated-FP64 tile
+constexpr int kTcOzDrain = 2;             // chunks accumulated in TMEM between drains (64 steps)
+constexpr int kTcF32NT = 128;             // columns per 3xTF32 tile
+constexpr uint32_t kTcTmemCols = 256;     // TMEM columns held by one CTA
+constexpr int kTcSmemBytes = 64 * 1024;   // operand tiles
+
+static_assert(kOzSlices * kTcOzNT <= (int)kTcTmemCols, "level accumulators must fit the CTA's TMEM");
+static_assert(kTcF32NT <= (int)kTcTmemCols, "3xTF32 accumulator must fit the CTA's TMEM");
+static_assert(kOzSlices * kTcM * kTcKC * 2 + kOzSlices * kTcOzNT * kTcKC * 2 <= kTcSmemBytes, "Ozaki tiles");
+static_assert(2 * kTcM * kTcKC * 4 + 2 * kTcF32NT * kTcKC * 4 <= kTcSmemBytes, "3xTF32 tiles");
+
+// Per-CTA tensor-core state (lives in shared memory).
+struct TcState {
+  unsigned char* tiles;  // kTcSmemBytes, 1024-byte aligned
+  uint32_t tmem;         // TMEM base of kTcTmemCols columns
+  uint32_t phase;        // parity of the next MMA completion
+  int status;            // ST_OK; ST_TIMEOUT once a completion wait gave up (no further MMAs)
+  uint64_t bar;          // mbarrier signalled by tcgen05.commit
+};
+
+// int64 fixed point v * 2^e -> FP64, by bit manipulation (round to nearest even).
+__device__ __forceinline__ double tc_i64_to_f64(long long v, int e) {
+  if (v == 0) return 0.0;
+  const uint64_t sign = v < 0 ? 0x8000000000000000ull : 0ull;
+  const uint64_t m = v < 0 ? (uint64_t)0 - (uint64_t)v : (uint64_t)v;
+  const int msb = 63 - __clzll((long long)m);
+  uint64_t mant;
+  int ex = msb;
+  if (msb > 52) {
+    const int sh = msb - 52;
+    const uint64_t rem = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    mant = m >> sh;
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      ++mant;
+      if (mant == (1ull << 53)) {
+        mant >>= 1;
+        ++ex;
+      }
+    }
+  } else {
+    mant = m << (52 - msb);
+  }
+  const int be = ex + e + 1023;
+  if (be <= 0 || be >= 2047) {  // subnormal or overflow: rare, let FP64 handle it
+    const double dv = sign ? -(double)m : (double)m;
+    return ldexp(dv, e);
+  }
+  return __longlong_as_double((long long)(sign | ((uint64_t)be << 52) | (mant & 0xfffffffffffffull)));
+}
+
+// Contraction-offset tables koffA / koffB of c (smem, 2 * kTcMaxK ints).
+__device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
+  const int K = (int)c.ktotal;
+  for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
+    int rem = kk, oa = 0, ob = 0;
+    for (int q = c.nk - 1; q >= 0; --q) {
+      const int iq = rem % c.k_dim[q];
+      rem /= c.k_dim[q];
+      oa += iq * c.a_ks[q];
+      ob += iq * c.b_ks[q];
+    }
+    ktab[kk] = oa;
+    ktab[kTcMaxK + kk] = ob;
+  }
+}
+
+// E[i] with |x| < 2^E[i] over row i of an operand (all K); flags non-finite values.
+__device__ __forceinline__ void tc_oz_exponents(const GemmAxes& ax, const double* __restrict__ src,
+                                                const int* koff, int K, int MN, int* E, int* bad) {
+  for (int i = threadIdx.x; i < MN; i += blockDim.x) {
+    int op, dummy;
+    gemm_axes_offsets(ax, i, op, dummy);
+    unsigned long long amax = 0;
+    for (int k = 0; k < K; ++k) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(src[op + koff[k]]) & 0x7fffffffffffffffull;
+      amax = b > amax ? b : amax;
+    }
+    if (amax >= 0x7ff0000000000000ull) *bad = 1;
+    E[i] = oz_exponent_bits(amax);
+  }
+}
+
+// Rows [r0, r0 + rows) x contraction [k0, k0 + kTcKC) of an FP64 operand into
+// kOzSlices BF16 slice tiles (tile p at base + p * slice_bytes); rows >= valid
+// and k >= K are zero.  One work item = one row x 8 contraction steps (one
+// 16-byte row of a core matrix per slice).
+__device__ __forceinline__ void tc_oz_stage(const GemmAxes& ax, const double* __restrict__ src, const int* koff,
+                                            int K, int k0, int r0, int rows, int valid, const int* E,
+                                            unsigned char* base, uint32_t slice_bytes) {
+  constexpr int kbytes = kTcKC * 2;
+  const int items = rows * (kTcKC / 8);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int cc = it / rows, r = it - cc * rows;
+    const int row = r0 + r;
+    uint32_t w[kOzSlices][4];
+#pragma unroll
+    for (int p = 0; p < kOzSlices; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
+    if (row < valid) {
+      int op, dummy;
+      gemm_axes_offsets(ax, row, op, dummy);
+      const int e = E[row];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + cc * 8 + u;
+        const uint64_t b = k < K ? (uint64_t)__double_as_longlong(src[op + koff[k]]) : 0ull;
+        const uint64_t mag = oz_fixed48(b, e);
+        const uint32_t sg = (uint32_t)(b >> 48) & 0x8000u;
+#pragma unroll
+        for (int p = 0; p < kOzSlices; ++p) w[p][u >> 1] |= oz_slice_bf16(mag, sg, p) << (16 * (u & 1));
+      }
+    }
+    const uint32_t off = umma::tile_off(r, cc * 8, 2, kbytes);
+#pragma unroll
+    for (int p = 0; p < kOzSlices; ++p)
+      *reinterpret_cast<uint4*>(base + p * slice_bytes + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+  }
+}
+
+// Wait for the MMAs committed last; false (and status set) if the wait gave up.
+__device__ __forceinline__ bool tc_wait(TcState& tc) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) s_ok = 1;
+  __syncthreads();
+  if (!umma::mbar_wait(&tc.bar, tc.phase)) s_ok = 0;
+  __syncthreads();
+  umma::fence_after_sync();
+  const bool ok = s_ok != 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc.phase ^= 1u;
+    if (!ok) tc.status = ST_TIMEOUT;
+  }
+  __syncthreads();
+  return ok;
+}
+
+// shared-memory operand writes -> visible to the tensor cores; TMEM reads done
+__device__ __forceinline__ void tc_publish() {
+  umma::fence_smem_to_async();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+}
+
+// C = contraction(A, B) with FP64-level accuracy; false when not GEMM-shaped,
+// out of the scratch capacities, non-finite, or the tensor cores are unusable
+// (the caller then runs the FP64 SIMT path).
+__device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const double* __restrict__ A,
+                                               const double* __restrict__ B, double* __restrict__ C,
+                                               const OzScratch& z, int* ktab, TcState& tc) {
+  GemmAxes rows, cols;
+  // 256 threads: two 128-thread groups, each draining 16 of the 32 tile columns
+  if (blockDim.x != 256 || tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
+  const int M = rows.total, N = cols.total, K = (int)c.ktotal;
+  if (M > z.cap_r || N > z.cap_c) return false;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_bad = 0;
+  tc_k_tables(c, ktab);
+  __syncthreads();
+  const int* koffA = ktab;
+  const int* koffB = ktab + kTcMaxK;
+  tc_oz_exponents(rows, A, koffA, K, M, z.rexp, &s_bad);
+  tc_oz_exponents(cols, B, koffB, K, N, z.cexp, &s_bad);
+  __syncthreads();
+  if (s_bad) return false;
+  constexpr uint32_t a_slice = kTcM * kTcKC * 2, b_slice = kTcOzNT * kTcKC * 2;
+  constexpr uint32_t sbo = (kTcKC * 2 / 16) * 128;
+  unsigned char* ta = tc.tiles;
+  unsigned char* tb = tc.tiles + kOzSlices * a_slice;
+  const int nK = (K + kTcKC - 1) / kTcKC;
+  const int nwin = (nK + kTcOzDrain - 1) / kTcOzDrain;
+  const int sh = nwin <= 1 ? 0 : 32 - __clz(nwin - 1);  // 2^sh >= windows: the int64 sum cannot overflow
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
+  const int hh = warp >> 2;  // this thread's 16-column half of the tile
+  for (int m0 = 0; m0 < M; m0 += kTcM) {
+    for (int n0 = 0; n0 < N; n0 += kTcOzNT) {
+      const int ncols = N - n0 < kTcOzNT ? N - n0 : kTcOzNT;
+      const int ntile = (ncols + 15) & ~15;
+      const uint32_t id = umma::idesc(umma::kFmtBF16, kTcM, ntile);
+      long long acc[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[j] = 0;
+      for (int kc = 0; kc < nK; ++kc) {
+        if (nK > 1 || n0 == 0) tc_oz_stage(rows, A, koffA, K, kc * kTcKC, m0, kTcM, M, z.rexp, ta, a_slice);
+        tc_oz_stage(cols, B, koffB, K, kc * kTcKC, n0, kTcOzNT, N, z.cexp, tb, b_slice);
+        tc_publish();
+        if (threadIdx.x == 0) {
+          const bool wstart = (kc % kTcOzDrain) == 0;
+          const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
+#pragma unroll
+          for (int ks = 0; ks < kTcKC / 16; ++ks)
+#pragma unroll
+            for (int p = 0; p < kOzSlices; ++p)
+#pragma unroll
+              for (int q = 0; q < kOzSlices - p; ++q) {
+                const uint64_t da = umma::sdesc(a0 + p * a_slice + 256u * ks, 128, sbo);
+                const uint64_t db = umma::sdesc(b0 + q * b_slice + 256u * ks, 128, sbo);
+                const uint32_t acc_in = (wstart && ks == 0 && p == 0) ? 0u : 1u;
+                umma::mma_f16(umma::taddr(tc.tmem, 0, (p + q) * kTcOzNT), da, db, id, acc_in);
+              }
+          umma::commit(&tc.bar);
+        }
+        if (!tc_wait(tc)) return false;
+        if ((kc % kTcOzDrain) == kTcOzDrain - 1 || kc == nK - 1) {
+          if (hh * 16 < ntile) {  // warp-uniform
+#pragma unroll
+            for (int L = 0; L < kOzSlices; ++L) {
+              uint32_t v[16];
+              umma::ld16(umma::taddr(tc.tmem, 32 * q4, L * kTcOzNT + hh * 16), v);
+              umma::ld_wait();
+              const int lsh = 8 * (kOzSlices - 1 - L) - sh;
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const long long t = (long long)__float2int_rn(__uint_as_float(v[j]));
+                acc[j] += lsh >= 0 ? (t << lsh) : (t >> (-lsh));
+              }
+            }
+          }
+          umma::fence_before_sync();
+        }
+      }
+      // results of this tile: row m0 + 32 q4 + lane, columns n0 + 16 hh + j
+      const int row = m0 + 32 * q4 + lane;
+      if (row < M) {
+        int dummy, cr;
+        gemm_axes_offsets(rows, row, dummy, cr);
+        const int er = z.rexp[row] - 8 * (kOzSlices + 1) + sh;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = n0 + hh * 16 + j;
+          if (col < N) {
+            int cc;
+            gemm_axes_offsets(cols, col, dummy, cc);
+            C[cr + cc] = tc_i64_to_f64(acc[j], er + z.cexp[col]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  return true;
+}
+
+// Rows [r0, r0 + rows) x contraction [k0, k0 + kTcKC) of an FP32 operand as
+// TF32 head and tail tiles (hi at base, lo at base + half_bytes).
+__device__ __forceinline__ void tc_tf32_stage(const GemmAxes& ax, const float* __restrict__ src, const int* koff,
+                                              int K, int k0, int r0, int rows, int valid, unsigned char* base,
+                                              uint32_t half_bytes) {
+  constexpr int kbytes = kTcKC * 4;
+  const int items = rows * (kTcKC / 4);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int cc = it / rows, r = it - cc * rows;
+    const int row = r0 + r;
+    uint32_t hi[4] = {0u, 0u, 0u, 0u}, lo[4] = {0u, 0u, 0u, 0u};
+    if (row < valid) {
+      int op, dummy;
+      gemm_axes_offsets(ax, row, op, dummy);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + cc * 4 + u;
+        const float x = k < K ? src[op + koff[k]] : 0.f;
+        hi[u] = tf32_bits(x);
+        lo[u] = tf32_bits(x - __uint_as_float(hi[u]));
+      }
+    }
+    const uint32_t off = umma::tile_off(r, cc * 4, 4, kbytes);
+    *reinterpret_cast<uint4*>(base + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(base + half_bytes + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+  }
+}
+
+// C = contraction(A, B) in FP32 (3xTF32) on the tensor cores; false when not
+// GEMM-shaped or the tensor cores are unusable.
+__device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const float* __restrict__ A,
+                                                 const float* __restrict__ B, float* __restrict__ C, int* ktab,
+                                                 TcState& tc) {
+  GemmAxes rows, cols;
+  if (tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
+  const int M = rows.total, N = cols.total, K = (int)c.ktotal;
+  tc_k_tables(c, ktab);
+  __syncthreads();
+  const int* koffA = ktab;
+  const int* koffB = ktab + kTcMaxK;
+  constexpr uint32_t a_half = kTcM * kTcKC * 4, b_half = kTcF32NT * kTcKC * 4;
+  constexpr uint32_t sbo = (kTcKC * 4 / 16) * 128;
+  unsigned char* ta = tc.tiles;
+  unsigned char* tb = tc.tiles + 2 * a_half;
+  const int nK = (K + kTcKC - 1) / kTcKC;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
+  const int halves = blockDim.x >> 7, grp = warp >> 2;
+  for (int m0 = 0; m0 < M; m0 += kTcM) {
+    for (int n0 = 0; n0 < N; n0 += kTcF32NT) {
+      const int ncols = N - n0 < kTcF32NT ? N - n0 : kTcF32NT;
+      const int ntile = (ncols + 15) & ~15;
+      const uint32_t id = umma::idesc(umma::kFmtTF32, kTcM, ntile);
+      for (int kc = 0; kc < nK; ++kc) {
+        if (nK > 1 || n0 == 0) tc_tf32_stage(rows, A, koffA, K, kc * kTcKC, m0, kTcM, M, ta, a_half);
+        tc_tf32_stage(cols, B, koffB, K, kc * kTcKC, n0, kTcF32NT, N, tb, b_half);
+        tc_publish();
+        if (threadIdx.x == 0) {
+          const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
+          const uint32_t d = umma::taddr(tc.tmem, 0, 0);
+#pragma unroll
+          for (int ks = 0; ks < kTcKC / 8; ++ks) {
+            const uint64_t ah = umma::sdesc(a0 + 256u * ks, 128, sbo), al = umma::sdesc(a0 + a_half + 256u * ks, 128, sbo);
+            const uint64_t bh = umma::sdesc(b0 + 256u * ks, 128, sbo), bl = umma::sdesc(b0 + b_half + 256u * ks, 128, sbo);
+            umma::mma_tf32(d, al, bh, id, (kc == 0 && ks == 0) ? 0u : 1u);
+            umma::mma_tf32(d, ah, bl, id, 1u);
+            umma::mma_tf32(d, ah, bh, id, 1u);
+          }
+          umma::commit(&tc.bar);
+        }
+        if (!tc_wait(tc)) return false;
+      }
+      const int row = m0 + 32 * q4 + lane;
+      int dummy, cr = 0;
+      if (row < M) gemm_axes_offsets(rows, row, dummy, cr);
+      // each 128-thread group drains every other 16-column block
+      for (int cb = grp * 16; cb < ntile; cb += 16 * halves) {
+        uint32_t v[16];
+        umma::ld16(umma::taddr(tc.tmem, 32 * q4, cb), v);
+        umma::ld_wait();
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = n0 + cb + j;
+            if (col < N) {
+              int cc;
+              gemm_axes_offsets(cols, col, dummy, cc);
+              C[cr + cc] = __uint_as_float(v[j]);
+            }
+          }
+        }
+      }
+      umma::fence_before_sync();
+      __syncthreads();
+    }
+  }
+  return true;
+}
+
+}  // namespace ttals

@@ -47,3 +47,35 @@ def test_apply_emulated_fp64(a, n, s, R0, R1):
     # 48-bit slicing relative to row/column maxima: error ~2^-47 K max|A| max|B| per product
     assert np.abs(out - ref).max() <= 1e-13 * bound.max()
     assert np.abs(out - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+def _round_bf16(x):
+    u = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def _round_tf32(x):
+    u = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x1000) & ~np.uint64(0x1FFF)
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize('kind,N,K', [(0, 32, 32), (0, 256, 32), (0, 48, 64), (0, 16, 128),
+                                      (1, 32, 32), (1, 128, 16), (1, 64, 8), (1, 256, 64)])
+def test_umma_selftest(kind, N, K):
+    """One tcgen05.mma tile (M = 128) with shared-memory operands in the
+    canonical K-major layout and the accumulator in tensor memory, against
+    the product of the same BF16 / TF32-rounded operands in FP64."""
+    from scikit_tt_gb300 import _lib
+    lib, ctx = _lib.load(), _lib.context()
+    rng = np.random.default_rng(17 * N + K + kind)
+    A = rng.standard_normal((128, K)).astype(np.float32)
+    Bt = rng.standard_normal((N, K)).astype(np.float32)
+    out = np.full((128, N), np.nan, dtype=np.float32)
+    f = lambda x: x.ctypes.data_as(ctypes.POINTER(ctypes.c_float))  # noqa: E731
+    _lib.check(lib.ttals_umma_selftest(ctx, kind, N, K, f(A), f(Bt), f(out)))
+    rnd = _round_bf16 if kind == 0 else _round_tf32
+    ref = rnd(A).astype(np.float64) @ rnd(Bt).astype(np.float64).T
+    # FP32 accumulation of exactly rounded operands
+    assert np.abs(out - ref).max() <= 1e-5 * np.abs(ref).max()
