@@ -4,8 +4,9 @@
 Workload: SLE ALS on the coupled Laplacian (d=32 sites, mode size n=8,
 operator rank 4, right-hand side rank 8, solution rank 32, 4 sweeps, seeded
 inputs).  A *step* is one batch of independent solves of that workload in one
-launch, one CTA per solve; by default as many as the GPU holds resident at once
-(``ttals_batch_slots``: 5 per SM, 760 on 152 SMs).
+launch of the persistent batch kernel; by default five solves per SM (760 on
+152 SMs): one wave of the plain FP64 kernel (five resident CTAs per SM) and
+five of the tensor-core kernel (one CTA per SM taking solves in turn).
 
 * ``value``: solves/s of the mixed-precision engine (FP32 Krylov inner solves,
   FP64 refinement residual, FP64 stacks and QR) with the inputs resident in HBM,
@@ -469,7 +470,12 @@ def main_gpu(args):
     C = _lib.C
     slots = C.c_int32(0)
     _lib.check(lib.ttals_batch_slots(ctx, C.byref(slots)))
-    B = args.batch or int(slots.value)
+    # five solves per SM: one wave of the plain FP64 kernel (five resident CTAs
+    # per SM) and five waves of the tensor-core kernel (one CTA per SM, which
+    # takes the next solve from the work counter when it finishes one); both
+    # engines keep every SM busy on the same batch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    B = args.batch or max(int(slots.value), 5 * sms)
 
     # B independent seeded instances per rank (weak scaling: each rank its own batch)
     inst = [wl.coupled_sle(seed=s, **WORKLOAD) for s in rank_seeds(rank, B)]

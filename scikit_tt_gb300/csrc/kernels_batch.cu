@@ -32,24 +32,29 @@ constexpr int kBatchThreads = 128;
 // instances overlap, and the memory-latency-bound loops get more warps to hide
 // latency behind (measured: +4 % over four CTAs per SM, with 5 x SMs requests)
 constexpr int kBatchMinBlocks = 5;
-// tensor-core variant: 256 threads (two 128-lane TMEM drain groups) and two
-// CTAs per SM, each with kTcTmemCols of the SM's 512 TMEM columns
-constexpr int kBatchThreadsTc = 256;
-constexpr int kBatchMinBlocksTc = 2;
+// tensor-core variant: a kernel with tcgen05 instructions runs one CTA per
+// SM, which then owns the whole SM (kTcThreads threads, all TMEM columns)
+constexpr int kBatchThreadsTc = kTcThreads;
+constexpr int kBatchMinBlocksTc = 1;
 
 // ---------------------------------------------------------------------------
 // CTA primitives
 // ---------------------------------------------------------------------------
 
 // Inlined body (used inside the Krylov loops); `c` must not alias C.
-template <typename T>
+// TC: the kernel holds tensor memory and uses tcgen05.  A kernel that contains
+// any tcgen05 instruction runs one CTA per SM, so the paths without it are
+// separate instantiations (TC = false) free of tcgen05 code.
+template <typename T, bool TC = false>
 __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C,
                                                   int* ktab = nullptr, TcState* tc = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
     // FP32 (inner Krylov) contractions go to the tensor cores when GEMM-shaped:
     // tcgen05 (3xTF32, operands staged in shared memory, TMEM accumulator)
     // when the CTA holds tensor memory, warp-level mma.sync otherwise
-    if (tc && ktab && cta_gemm_tf32_tc(c, A, B, C, ktab, *tc)) return;
+    if constexpr (TC) {
+      if (tc && ktab && cta_gemm_tf32_tc(c, A, B, C, ktab, *tc)) return;
+    }
     if (ktab && cta_gemm_tf32x3(c, A, B, C, ktab)) return;
   }
   constexpr int VW = DefaultVW<T>::value;
@@ -68,13 +73,17 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
 
 // FP64 contraction; with `oz` set, GEMM-shaped ones run as emulated FP64 on the
 // BF16 tensor cores (ttals_ozaki.cuh), the rest natively.
+template <bool TC>
 __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const double* A, const double* B, double* C,
                                               const OzScratch* oz) {
   __shared__ Contraction sc;
   if (threadIdx.x == 0) sc = cref;
   __syncthreads();
-  if (oz && oz->tc && cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc)) return;
-  if (oz && !oz->tc && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
+  if constexpr (TC) {
+    if (oz && oz->tc && cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc)) return;
+  } else {
+    if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
+  }
   cta_contract_body<double>(sc, A, B, C);
 }
 
@@ -92,12 +101,13 @@ __device__ __noinline__ void cta_contract(const Contraction& cref, const T* A, c
 // Out-of-line FP32 contraction of the inner Krylov apply: one copy of the
 // tensor-core and fallback paths instead of three inlined into the GMRES loop
 // (which otherwise spills).
+template <bool TC>
 __device__ __noinline__ void cta_contract_f32(const Contraction& cref, const float* A, const float* B, float* C,
                                               int* ktab, TcState* tc) {
   __shared__ Contraction sc;
   if (threadIdx.x == 0) sc = cref;
   __syncthreads();
-  cta_contract_body<float>(sc, A, B, C, ktab, tc);
+  cta_contract_body<float, TC>(sc, A, B, C, ktab, tc);
 }
 
 __device__ __forceinline__ void cta_fill(double* p, int64_t n, double v) {
@@ -150,14 +160,14 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
 }
 
 // y -> out = M y (three contraction phases through T1, T2)
-template <typename T>
+template <typename T, bool TC = false>
 __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                           const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out,
                                           int* ktab = nullptr, TcState* tc = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
-    cta_contract_f32(p1, L, y, T1, ktab, tc);
-    cta_contract_f32(p2, T1, A, T2, ktab, tc);
-    cta_contract_f32(p3, T2, R, out, ktab, tc);
+    cta_contract_f32<TC>(p1, L, y, T1, ktab, tc);
+    cta_contract_f32<TC>(p2, T1, A, T2, ktab, tc);
+    cta_contract_f32<TC>(p3, T2, R, out, ktab, tc);
   } else {
     cta_contract_body(p1, L, y, T1, ktab);
     cta_contract_body(p2, T1, A, T2, ktab);
@@ -174,7 +184,7 @@ struct CtaSolveStats {
   int cycles, inner, status;
 };
 
-template <typename TI>
+template <typename TI, bool TC>
 __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                       const double* L64, const double* A64, const double* R64, double* T1_64,
                                       double* T2_64, const TI* Li, const TI* Ai, const TI* Ri, TI* T1i, TI* T2i,
@@ -208,9 +218,9 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     double rs = 0.0;
     if (oz) {
       // FP64-accurate residual with the products on the BF16 tensor cores
-      cta_contract_f64(p1, L64, (const double*)x, T1_64, oz);
-      cta_contract_f64(p2, (const double*)T1_64, A64, T2_64, oz);
-      cta_contract_f64(p3, (const double*)T2_64, R64, r, oz);
+      cta_contract_f64<TC>(p1, L64, (const double*)x, T1_64, oz);
+      cta_contract_f64<TC>(p2, (const double*)T1_64, A64, T2_64, oz);
+      cta_contract_f64<TC>(p3, (const double*)T2_64, R64, r, oz);
       for (int64_t e = tid; e < N; e += nt) {
         const double re = f[e] - r[e];
         r[e] = re;
@@ -246,8 +256,8 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     __syncthreads();
     int jj = 0;
     for (int j = 0; j < m; ++j) {
-      cta_apply<TI>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
-                    oz ? oz->tc : nullptr);
+      cta_apply<TI, TC>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
+                        oz ? oz->tc : nullptr);
       cta_dots<TI>(V, N, j + 1, w, h1);
       // Classical Gram-Schmidt with selective reorthogonalisation (FP32 inner
       // solves): one projection suffices when it keeps at least 1/sqrt(2) of the
@@ -552,6 +562,7 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   return s;
 }
 
+template <bool TC>
 __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double* sm) {
   const BatchInst& I = a.inst[j];
   const int d = I.d;
@@ -633,9 +644,9 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     Contraction q1, q2, q3;
     desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
     const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
-    cta_contract_f64(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
-    cta_contract_f64(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
-    cta_contract_f64(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
+    cta_contract_f64<TC>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
+    cta_contract_f64<TC>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
+    cta_contract_f64<TC>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
     cta_contract(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
     cta_contract(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
@@ -654,9 +665,9 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
     const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
-    cta_contract_f64(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
-    cta_contract_f64(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
-    cta_contract_f64(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
+    cta_contract_f64<TC>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
+    cta_contract_f64<TC>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
+    cta_contract_f64<TC>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
     cta_contract(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
     cta_contract(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
@@ -676,10 +687,10 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
       cta_to_float(S.Lf, L(i), aa * R[i] * aa);
       cta_to_float(S.Rf, Rt(i), ss * R[i + 1] * ss);
       cta_to_float(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
-      st = cta_gmres_ir<float>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
+      st = cta_gmres_ir<float, TC>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
                                S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm, &S.oz, &cr, &ci);
     } else {
-      st = cta_gmres_ir<double>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
+      st = cta_gmres_ir<double, false>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
                                 S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm, nullptr, &cr, &ci);
     }
     ph[3] += cr;
@@ -955,11 +966,12 @@ __device__ __forceinline__ void tc_end(TcState& tc) {
 
 __host__ __device__ inline size_t tc_tiles_offset(size_t before) { return (before + 1023) / 1024 * 1024; }
 
-// The persistent loop of both kernel variants.  With a.use_tc the CTA holds
+// The persistent loop of both kernel variants.  With UseTc the CTA holds
 // kTcTmemCols columns of tensor memory for its whole life (allocated here,
 // released on the way out whatever happened) and a 64 KB operand-tile region
 // of shared memory; its GEMM-shaped FP32 and emulated-FP64 contractions then
 // run on tcgen05.
+template <bool UseTc>
 __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   double* sm = reinterpret_cast<double*>(smraw);
@@ -968,7 +980,7 @@ __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
   Scratch S = scratch_of(a, blockIdx.x);
   const size_t scal = batch_smem_scalar_bytes(a.m, a.m_evp);
   S.oz.ktab = reinterpret_cast<int*>(smraw + scal);
-  if (a.use_tc) {
+  if constexpr (UseTc) {
     tc_begin(s_tc, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK));
     S.oz.tc = &s_tc;
   }
@@ -981,20 +993,19 @@ __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
     if (a.inst[j].kind == 1)
       batch_evp(a, j, S, sm);
     else
-      batch_solve(a, j, S, sm);
+      batch_solve<UseTc>(a, j, S, sm);
   }
-  if (a.use_tc) tc_end(s_tc);
+  if constexpr (UseTc) tc_end(s_tc);
 }
 
 // plain FP64 (and mixed without tensor memory): 128 threads, five CTAs per SM
 __global__ void __launch_bounds__(kBatchThreads, kBatchMinBlocks) batch_sle_kernel(BatchArgs a) {
-  batch_kernel_body(a);
+  batch_kernel_body<false>(a);
 }
 
-// mixed precision on tcgen05: 256 threads, two CTAs per SM (each holding half
-// of the SM's tensor memory)
+// mixed precision on tcgen05: one CTA per SM holding all of its tensor memory
 __global__ void __launch_bounds__(kBatchThreadsTc, kBatchMinBlocksTc) batch_sle_tc_kernel(BatchArgs a) {
-  batch_kernel_body(a);
+  batch_kernel_body<true>(a);
 }
 
 void oz_need_site(BatchSizes& z, int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
@@ -1018,9 +1029,9 @@ __global__ void __launch_bounds__(kBatchThreads) apply_f64emu_kernel(Contraction
                                                                      const double* L, const double* A,
                                                                      const double* R, const double* y, double* T1,
                                                                      double* T2, double* out, OzScratch oz) {
-  cta_contract_f64(p1, L, y, T1, &oz);
-  cta_contract_f64(p2, T1, A, T2, &oz);
-  cta_contract_f64(p3, T2, R, out, &oz);
+  cta_contract_f64<false>(p1, L, y, T1, &oz);
+  cta_contract_f64<false>(p2, T1, A, T2, &oz);
+  cta_contract_f64<false>(p3, T2, R, out, &oz);
 }
 
 // The same on tcgen05 (256 threads, the batch kernel's tensor-core GEMMs).
@@ -1034,9 +1045,9 @@ __global__ void __launch_bounds__(kBatchThreadsTc) apply_f64emu_tc_kernel(Contra
   oz.ktab = reinterpret_cast<int*>(smraw);
   tc_begin(s_tc, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK));
   oz.tc = &s_tc;
-  cta_contract_f64(p1, L, y, T1, &oz);
-  cta_contract_f64(p2, T1, A, T2, &oz);
-  cta_contract_f64(p3, T2, R, out, &oz);
+  cta_contract_f64<true>(p1, L, y, T1, &oz);
+  cta_contract_f64<true>(p2, T1, A, T2, &oz);
+  cta_contract_f64<true>(p3, T2, R, out, &oz);
   tc_end(s_tc);
 }
 
@@ -1100,7 +1111,7 @@ __global__ void __launch_bounds__(kBatchThreadsTc) apply_f32_tc_kernel(Contracti
   __shared__ TcState s_tc;
   int* ktab = reinterpret_cast<int*>(smraw);
   tc_begin(s_tc, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK));
-  cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab, &s_tc);
+  cta_apply<float, true>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab, &s_tc);
   tc_end(s_tc);
 }
 

@@ -9,8 +9,8 @@
 //   Ozaki-style slicing as in ttals_ozaki.cuh): each row of A (column of B) is
 //   scaled by its power-of-two maximum and cut into 6 slices of 8 bits, exact
 //   in BF16.  The 21 slice products with p + q < 6 run as tcgen05.mma
-//   kind::f16 (M = 128, N = 32, K = 16) into one FP32 accumulator per level
-//   L = p + q (6 x 32 TMEM columns).  Level sums are integers; every 64
+//   kind::f16 (M = 128, N = 64, K = 16) into one FP32 accumulator per level
+//   L = p + q (6 x 64 TMEM columns).  Level sums are integers; every 64
 //   contraction steps they are drained: converted to integers, combined in
 //   64-bit fixed point (level L weighted by 2^(8 (5 - L))) and added to a
 //   per-thread running sum, which is finally turned into FP64 by bit
@@ -18,7 +18,7 @@
 //   No FP64 instruction is executed (FP64 runs at 2 FMA/clk/SM on this part).
 // * cta_gemm_tf32_tc: FP32 C = A B from FP32 operands with the 3xTF32 split
 //   a b ~ a_hi b_hi + a_hi b_lo + a_lo b_hi, three tcgen05.mma kind::tf32 into
-//   one FP32 accumulator (N up to 128 columns per tile).
+//   one FP32 accumulator (N up to 256 columns per tile).
 //
 // One thread issues the MMAs and commits them to an mbarrier; every thread
 // waits on it (bounded), then reads its accumulator lane (row) back.
@@ -29,13 +29,18 @@
 
 namespace ttals {
 
+// A kernel that contains tcgen05 instructions runs one CTA per SM, so the
+// CTA owns the SM: all 512 TMEM columns, 512 threads (four 128-lane groups
+// that drain the accumulators side by side) and most of shared memory.
+constexpr int kTcThreads = 512;
+constexpr int kTcGroups = kTcThreads / 128;
 constexpr int kTcM = 128;                 // rows per tile (TMEM lanes)
 constexpr int kTcKC = 32;                 // contraction elements per staged chunk
-constexpr int kTcOzNT = 32;               // columns per emulated-FP64 tile
+constexpr int kTcOzNT = 16 * kTcGroups;   // columns per emulated-FP64 tile: 16 per drain group
 constexpr int kTcOzDrain = 2;             // chunks accumulated in TMEM between drains (64 steps)
-constexpr int kTcF32NT = 128;             // columns per 3xTF32 tile
-constexpr uint32_t kTcTmemCols = 256;     // TMEM columns held by one CTA
-constexpr int kTcSmemBytes = 64 * 1024;   // operand tiles
+constexpr int kTcF32NT = 256;             // columns per 3xTF32 tile
+constexpr uint32_t kTcTmemCols = 512;     // TMEM columns held by one CTA (all of the SM's)
+constexpr int kTcSmemBytes = 96 * 1024;   // operand tiles
 
 static_assert(kOzSlices * kTcOzNT <= (int)kTcTmemCols, "level accumulators must fit the CTA's TMEM");
 static_assert(kTcF32NT <= (int)kTcTmemCols, "3xTF32 accumulator must fit the CTA's TMEM");
@@ -182,8 +187,8 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
                                                const double* __restrict__ B, double* __restrict__ C,
                                                const OzScratch& z, int* ktab, TcState& tc) {
   GemmAxes rows, cols;
-  // 256 threads: two 128-thread groups, each draining 16 of the 32 tile columns
-  if (blockDim.x != 256 || tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
+  // kTcThreads threads: kTcGroups 128-thread groups, each draining 16 of the tile's columns
+  if (blockDim.x != kTcThreads || tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
   if (M > z.cap_r || N > z.cap_c) return false;
   __shared__ int s_bad;
@@ -204,7 +209,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
   const int nwin = (nK + kTcOzDrain - 1) / kTcOzDrain;
   const int sh = nwin <= 1 ? 0 : 32 - __clz(nwin - 1);  // 2^sh >= windows: the int64 sum cannot overflow
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
-  const int hh = warp >> 2;  // this thread's 16-column half of the tile
+  const int hh = warp >> 2;  // this thread's 16-column block of the tile
   for (int m0 = 0; m0 < M; m0 += kTcM) {
     for (int n0 = 0; n0 < N; n0 += kTcOzNT) {
       const int ncols = N - n0 < kTcOzNT ? N - n0 : kTcOzNT;
