@@ -159,6 +159,39 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
   __syncthreads();
 }
 
+// The same with every thread of the CTA: each thread keeps a partial sum per
+// vector over its own elements (four loads in flight), reduced per warp and
+// then over warps.  For the one-CTA-per-SM tensor-core kernel, where no
+// sibling CTA hides memory latency; nvec <= kWideDotsMax.
+constexpr int kWideDotsMax = 64;
+template <typename T>
+__device__ __noinline__ void cta_dots_wide(const T* V, int64_t N, int nvec, const T* w, double* out) {
+  __shared__ double part[32][kWideDotsMax + 1];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int kk = 0; kk <= nvec; ++kk) {
+    const T* xv = (kk < nvec) ? V + (int64_t)kk * N : w;
+    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+    int64_t e = tid;
+    for (; e + 3 * (int64_t)nt < N; e += 4 * (int64_t)nt) {
+      s0 += xv[e] * w[e];
+      s1 += xv[e + nt] * w[e + nt];
+      s2 += xv[e + 2 * nt] * w[e + 2 * nt];
+      s3 += xv[e + 3 * nt] * w[e + 3 * nt];
+    }
+    for (; e < N; e += nt) s0 += xv[e] * w[e];
+    double sd = ((double)s0 + (double)s1) + ((double)s2 + (double)s3);
+    sd = warp_sum(sd);
+    if (lane == 0) part[warp][kk] = sd;
+  }
+  __syncthreads();
+  for (int kk = tid; kk <= nvec; kk += nt) {
+    double t = 0.0;
+    for (int q = 0; q < nw; ++q) t += part[q][kk];
+    out[kk] = t;
+  }
+  __syncthreads();
+}
+
 // y -> out = M y (three contraction phases through T1, T2)
 template <typename T, bool TC = false>
 __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
@@ -200,8 +233,18 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
   double* h2 = h1 + m + 2;       // m+2
   __shared__ double s_res;
   __shared__ int s_flag;
+  __shared__ float s_cf[kWideDotsMax + 2];  // Gram-Schmidt / correction coefficients in TI (TC path)
   const int tid = threadIdx.x, nt = blockDim.x;
   CtaSolveStats out{1.0, 0, 0, ST_OK};
+  // the tensor-core kernel runs one CTA per SM: its vector loops use every
+  // thread, keep several loads in flight and avoid per-element FP64 work
+  constexpr bool kWide = TC && std::is_same<TI, float>::value;
+  auto dots = [&](int nv, const TI* wv, double* o) {
+    if constexpr (kWide)
+      cta_dots_wide<TI>(V, N, nv, wv, o);
+    else
+      cta_dots<TI>(V, N, nv, wv, o);
+  };
 
   double fs = 0.0;
   for (int64_t e = tid; e < N; e += nt) fs += f[e] * f[e];
@@ -248,7 +291,8 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     }
     if (out.rel <= tol) break;
     const double target = fmax(tol / out.rel, inner_floor);
-    for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(r[e] / rho);
+    const double irho = 1.0 / rho;
+    for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(r[e] * irho);
     if (tid == 0) {
       gv[0] = 1.0;
       for (int i = 1; i <= m; ++i) gv[i] = 0.0;
@@ -258,7 +302,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     for (int j = 0; j < m; ++j) {
       cta_apply<TI, TC>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
                         oz ? oz->tc : nullptr);
-      cta_dots<TI>(V, N, j + 1, w, h1);
+      dots(j + 1, w, h1);
       // Classical Gram-Schmidt with selective reorthogonalisation (FP32 inner
       // solves): one projection suffices when it keeps at least 1/sqrt(2) of the
       // norm ("twice is enough" criterion); then the projection and the
@@ -275,10 +319,21 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         if (hn > 0.0) {
           const TI inv = (TI)(1.0 / hn);
           TI* vn = V + (int64_t)(j + 1) * N;
-          for (int64_t e = tid; e < N; e += nt) {
-            TI acc = w[e];
-            for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
-            vn[e] = acc * inv;
+          if constexpr (kWide) {
+            for (int q = tid; q <= j; q += nt) s_cf[q] = (float)h1[q];
+            __syncthreads();
+            for (int64_t e = tid; e < N; e += nt) {
+              TI acc = w[e];
+#pragma unroll 4
+              for (int q = 0; q <= j; ++q) acc -= s_cf[q] * V[(int64_t)q * N + e];
+              vn[e] = acc * inv;
+            }
+          } else {
+            for (int64_t e = tid; e < N; e += nt) {
+              TI acc = w[e];
+              for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
+              vn[e] = acc * inv;
+            }
           }
         }
       } else {
@@ -288,7 +343,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
           w[e] = acc;
         }
         __syncthreads();
-        cta_dots<TI>(V, N, j + 1, w, h2);
+        dots(j + 1, w, h2);
         hn2 = h2[j + 1];
         for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
         hn = sqrt(fmax(hn2, 0.0));
@@ -352,10 +407,23 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       out.status = ST_SINGULAR;
       return out;
     }
-    for (int64_t e = tid; e < N; e += nt) {
-      double acc = 0.0;
-      for (int q = 0; q < jj; ++q) acc += yv[q] * (double)V[(int64_t)q * N + e];
-      x[e] += rho * acc;
+    if constexpr (kWide) {
+      // the correction V y is FP32-accurate by construction: sum it in FP32,
+      // one FP64 FMA per element adds it to the FP64 solution
+      for (int q = tid; q < jj; q += nt) s_cf[q] = (float)yv[q];
+      __syncthreads();
+      for (int64_t e = tid; e < N; e += nt) {
+        float acc = 0.f;
+#pragma unroll 4
+        for (int q = 0; q < jj; ++q) acc += s_cf[q] * V[(int64_t)q * N + e];
+        x[e] += rho * (double)acc;
+      }
+    } else {
+      for (int64_t e = tid; e < N; e += nt) {
+        double acc = 0.0;
+        for (int q = 0; q < jj; ++q) acc += yv[q] * (double)V[(int64_t)q * N + e];
+        x[e] += rho * acc;
+      }
     }
     __syncthreads();
     *cyc_inner += clock64() - c1;

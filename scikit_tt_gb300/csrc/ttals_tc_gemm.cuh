@@ -102,19 +102,47 @@ __device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
   }
 }
 
-// E[i] with |x| < 2^E[i] over row i of an operand (all K); flags non-finite values.
+// E[i] with |x| < 2^E[i] over row i of an operand (all K); flags non-finite
+// values.  One warp takes 8 rows at a time with its lanes along the
+// contraction, so every lane keeps 8 independent loads in flight.
 __device__ __forceinline__ void tc_oz_exponents(const GemmAxes& ax, const double* __restrict__ src,
                                                 const int* koff, int K, int MN, int* E, int* bad) {
-  for (int i = threadIdx.x; i < MN; i += blockDim.x) {
-    int op, dummy;
-    gemm_axes_offsets(ax, i, op, dummy);
-    unsigned long long amax = 0;
-    for (int k = 0; k < K; ++k) {
-      const unsigned long long b = (unsigned long long)__double_as_longlong(src[op + koff[k]]) & 0x7fffffffffffffffull;
-      amax = b > amax ? b : amax;
+  constexpr int kRows = 8;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int ib = warp * kRows; ib < MN; ib += nw * kRows) {
+    int op[kRows];
+    unsigned long long amax[kRows];
+#pragma unroll
+    for (int u = 0; u < kRows; ++u) {
+      int dummy;
+      op[u] = 0;
+      amax[u] = 0;
+      if (ib + u < MN) gemm_axes_offsets(ax, ib + u, op[u], dummy);
     }
-    if (amax >= 0x7ff0000000000000ull) *bad = 1;
-    E[i] = oz_exponent_bits(amax);
+    for (int k = lane; k < K; k += 32) {
+      const int ko = koff[k];
+#pragma unroll
+      for (int u = 0; u < kRows; ++u) {
+        if (ib + u < MN) {
+          const unsigned long long b =
+              (unsigned long long)__double_as_longlong(src[op[u] + ko]) & 0x7fffffffffffffffull;
+          amax[u] = b > amax[u] ? b : amax[u];
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kRows; ++u) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, amax[u], o);
+        amax[u] = other > amax[u] ? other : amax[u];
+      }
+      if (lane == 0 && ib + u < MN) {
+        // NaN / Inf have the all-ones exponent: larger than every finite magnitude
+        if (amax[u] >= 0x7ff0000000000000ull) *bad = 1;
+        E[ib + u] = oz_exponent_bits(amax[u]);
+      }
+    }
   }
 }
 
@@ -220,7 +248,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
       for (int j = 0; j < 16; ++j) acc[j] = 0;
       for (int kc = 0; kc < nK; ++kc) {
         if (nK > 1 || n0 == 0) tc_oz_stage(rows, A, koffA, K, kc * kTcKC, m0, kTcM, M, z.rexp, ta, a_slice);
-        tc_oz_stage(cols, B, koffB, K, kc * kTcKC, n0, kTcOzNT, N, z.cexp, tb, b_slice);
+        tc_oz_stage(cols, B, koffB, K, kc * kTcKC, n0, ntile, N, z.cexp, tb, b_slice);
         tc_publish();
         if (threadIdx.x == 0) {
           const bool wstart = (kc % kTcOzDrain) == 0;
@@ -333,7 +361,7 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
       const uint32_t id = umma::idesc(umma::kFmtTF32, kTcM, ntile);
       for (int kc = 0; kc < nK; ++kc) {
         if (nK > 1 || n0 == 0) tc_tf32_stage(rows, A, koffA, K, kc * kTcKC, m0, kTcM, M, ta, a_half);
-        tc_tf32_stage(cols, B, koffB, K, kc * kTcKC, n0, kTcF32NT, N, tb, b_half);
+        tc_tf32_stage(cols, B, koffB, K, kc * kTcKC, n0, ntile, N, tb, b_half);
         tc_publish();
         if (threadIdx.x == 0) {
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
