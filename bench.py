@@ -395,9 +395,11 @@ def other_workloads(lib, ctx, args):
     b4 = wl.batch_sle(256)
     probs = [(T(w.op), T(w.x0), T(w.rhs)) for w in b4]
     res4 = {}
+    # mixed: local systems to 1e-11, which keeps every instance of the reference-checked
+    # subset within 1e-8 of the reference (1e-10 leaves one at 2.6e-8)
     for prec in ('mixed', 'fp64'):
-        sle.als_batch(probs, repeats=4, precision=prec, tol=1e-10 if prec == 'mixed' else 0.0)
-        sols, st = sle.als_batch(probs, repeats=4, precision=prec, tol=1e-10 if prec == 'mixed' else 0.0)
+        sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
+        sols, st = sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
         res4[prec] = {'solves_per_s': 256 / (st['device_ms'] / 1e3), 'device_ms': st['device_ms'],
                       'max_local_residual': st['max_local_residual']}
     res4['mixed_over_plain'] = res4['mixed']['solves_per_s'] / res4['fp64']['solves_per_s']

@@ -95,6 +95,11 @@ typedef struct {
    * orthonormalisation, operator/RHS stacks, local right-hand sides, FP64
    * residuals, inner Krylov iterations, QR/RQ + gauge push, eigensolves, total */
   double phase_cycles[8];
+  /* batched mixed-precision calls: GEMM-shaped contractions that ran on the
+   * fifth-generation tensor cores (tcgen05), and those that fell back to the
+   * SIMT path (non-finite operands, or a tensor-core wait that gave up)      */
+  int64_t tc_gemms;
+  int64_t tc_fallbacks;
 } ttals_stats;
 
 /* Context: one device, one stream, one device-memory arena capped at

@@ -1455,6 +1455,9 @@ struct BatchReqHost {
 
 // Mixed-precision batches run on the tcgen05 kernel variant unless
 // TTALS_TENSOR_CORES=mma (warp-level mma.sync variant, kept for comparison).
+// per-request report of the batch kernel: 20 fixed slots + d + 1 ranks - 1 (see BatchInst::report)
+constexpr int kReportFixed = 20;
+
 bool batch_tc_enabled() {
   const char* v = std::getenv("TTALS_TENSOR_CORES");
   return !(v && std::string(v) == "mma");
@@ -1564,7 +1567,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     put(6, lbs);
     put(7, rbs);
     put(8, I.out_count);
-    put(9, 18 + d);
+    put(9, kReportFixed + d);
     put(10, I.kind == 1 ? xs : 1);
     I.region = P.region_total;
     P.region_total += o;
@@ -1670,8 +1673,9 @@ std::vector<double> collect_one(BatchPlan& P, int j, char* mem, cudaStream_t st,
   double* data = (double*)mem;
   BatchReqHost& I = P.in[j];
   const int d = I.op.d;
-  std::vector<double> rep(18 + d, 0.0);
-  CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (18 + d), cudaMemcpyDeviceToHost, st));
+  std::vector<double> rep(kReportFixed + d, 0.0);
+  CK(cudaMemcpyAsync(rep.data(), data + I.region + I.off[9], sizeof(double) * (kReportFixed + d),
+                     cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const int stj = (int)rep[4];
   if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
@@ -1695,11 +1699,14 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
                       float total_ms, int64_t launches) {
   if (!stats) return;
   double maxres = 0.0, fl64 = 0.0, fl32 = 0.0, ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t tcg = 0, tcf = 0;
   int64_t nsolve = 0, nits = 0, ncyc = 0;
   for (const auto& rep : reps) {
     if (rep.empty()) continue;
-    const size_t d = rep.size() - 18;
+    const size_t d = rep.size() - kReportFixed;
     for (int k = 0; k < 8; ++k) ph[k] += rep[10 + d + k];
+    tcg += (int64_t)rep[18 + d];
+    tcf += (int64_t)rep[19 + d];
     maxres = std::max(maxres, rep[0]);
     nsolve += (int64_t)rep[1];
     nits += (int64_t)rep[2];
@@ -1712,6 +1719,8 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
   stats->refinement_steps = ncyc;
   stats->max_local_residual = maxres;
   stats->device_ms = total_ms;
+  stats->tc_gemms = tcg;
+  stats->tc_fallbacks = tcf;
   stats->kernel_launches = launches;
   stats->solver_launches = 1;
   stats->solver_ms = kernel_ms;

@@ -53,7 +53,16 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
     // tcgen05 (3xTF32, operands staged in shared memory, TMEM accumulator)
     // when the CTA holds tensor memory, warp-level mma.sync otherwise
     if constexpr (TC) {
-      if (tc && ktab && cta_gemm_tf32_tc(c, A, B, C, ktab, *tc)) return;
+      if (tc && ktab) {
+        const bool done = cta_gemm_tf32_tc(c, A, B, C, ktab, *tc);
+        if (threadIdx.x == 0) {
+          if (done)
+            ++tc->gemms;
+          else
+            ++tc->fallbacks;
+        }
+        if (done) return;
+      }
     }
     if (ktab && cta_gemm_tf32x3(c, A, B, C, ktab)) return;
   }
@@ -80,7 +89,16 @@ __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const dou
   if (threadIdx.x == 0) sc = cref;
   __syncthreads();
   if constexpr (TC) {
-    if (oz && oz->tc && cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc)) return;
+    if (oz && oz->tc) {
+      const bool done = cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc);
+      if (threadIdx.x == 0) {
+        if (done)
+          ++oz->tc->gemms;
+        else
+          ++oz->tc->fallbacks;
+      }
+      if (done) return;
+    }
   } else {
     if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
   }
@@ -663,6 +681,8 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   double maxres = 0.0, fl64 = 0.0, fl32 = 0.0;
   int64_t nsolve = 0, nits = 0, ncyc = 0;
   int status = ST_OK;
+  // tensor-core counters of the CTA when this request started (thread 0 keeps them)
+  const unsigned long long tc0 = S.oz.tc ? S.oz.tc->gemms : 0ull, fb0 = S.oz.tc ? S.oz.tc->fallbacks : 0ull;
   long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const long long t_start = clock64();
   long long tp = t_start;
@@ -836,6 +856,8 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     I.report[9 + d] = (double)I.repeats;
     ph[7] = clock64() - t_start;
     for (int k = 0; k < 8; ++k) I.report[10 + d + k] = (double)ph[k];
+    I.report[18 + d] = S.oz.tc ? (double)(S.oz.tc->gemms - tc0) : 0.0;
+    I.report[19 + d] = S.oz.tc ? (double)(S.oz.tc->fallbacks - fb0) : 0.0;
   }
   signal_done(I.done);
 }
@@ -1005,6 +1027,8 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     for (int i = 0; i <= d; ++i) I.report[8 + i] = have_opt ? (double)ropt[i] : 0.0;
     I.report[9 + d] = (double)(it - 1);
     for (int k = 0; k < 8; ++k) I.report[10 + d + k] = 0.0;
+    I.report[18 + d] = 0.0;
+    I.report[19 + d] = 0.0;
   }
   signal_done(I.done);
 }
@@ -1016,6 +1040,8 @@ __device__ __forceinline__ void tc_begin(TcState& tc, unsigned char* tiles) {
     tc.tiles = tiles;
     tc.phase = 0;
     tc.status = ST_OK;
+    tc.gemms = 0;
+    tc.fallbacks = 0;
     umma::mbar_init(&tc.bar, 1);
   }
   umma::fence_before_sync();

@@ -54,6 +54,8 @@ struct TcState {
   uint32_t phase;        // parity of the next MMA completion
   int status;            // ST_OK; ST_TIMEOUT once a completion wait gave up (no further MMAs)
   uint64_t bar;          // mbarrier signalled by tcgen05.commit
+  unsigned long long gemms;      // contractions completed on the tensor cores
+  unsigned long long fallbacks;  // GEMM-shaped contractions that took the SIMT path instead
 };
 
 // int64 fixed point v * 2^e -> FP64, by bit manipulation (round to nearest even).

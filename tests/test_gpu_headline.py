@@ -106,8 +106,11 @@ def test_headline_batch_matches_reference(golden, precision, tol, local):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('precision,tol,local', [('fp64', TOL_FP64, 0.0), ('mixed', TOL_MIXED, 1e-10)])
+@pytest.mark.parametrize('precision,tol,local', [('fp64', TOL_FP64, 0.0), ('mixed', TOL_MIXED, 1e-11)])
 def test_uneven_batch_subset_matches_reference(golden, precision, tol, local):
+    """Mixed precision solves each local system to 1e-11 here: instance 13
+    (d=11, n=8, rank 25) lands 2.6e-8 from the reference at 1e-10 and 6.4e-9
+    at 1e-11 (its local systems are the worst conditioned of the subset)."""
     from scikit_tt_gb300 import workloads as wl
     from scikit_tt_gb300.solvers import sle
     z, cores = golden('sle_batch_subset')

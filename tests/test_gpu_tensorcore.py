@@ -79,3 +79,17 @@ def test_umma_selftest(kind, N, K):
     ref = rnd(A).astype(np.float64) @ rnd(Bt).astype(np.float64).T
     # FP32 accumulation of exactly rounded operands
     assert np.abs(out - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def test_mixed_batch_contractions_run_on_tcgen05():
+    """The mixed-precision batch kernel's GEMM-shaped contractions (emulated
+    FP64 stacks and residuals, 3xTF32 inner applies) complete on tcgen05: the
+    statistics count them and report no SIMT fallback."""
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.solvers import sle
+    from scikit_tt_gb300.tensor_train import TT
+    ws = [wl.coupled_sle(seed=s, d=8, n=8, rhs_rank=4, x_rank=16, repeats=1) for s in range(3)]
+    probs = [tuple(TT([c.copy() for c in cs]) for cs in (w.op, w.x0, w.rhs)) for w in ws]
+    _, st = sle.als_batch(probs, repeats=1, precision='mixed', tol=1e-10)
+    assert st['tc_gemms'] > 0
+    assert st['tc_fallbacks'] == 0, f"{st['tc_fallbacks']} of {st['tc_gemms'] + st['tc_fallbacks']} fell back"
