@@ -100,6 +100,9 @@ typedef struct {
    * SIMT path (non-finite operands, or a tensor-core wait that gave up)      */
   int64_t tc_gemms;
   int64_t tc_fallbacks;
+  /* batched calls: the part of phase_cycles[4] (inner Krylov iterations)
+   * spent applying the local operator                                      */
+  double inner_apply_cycles;
 } ttals_stats;
 
 /* Context: one device, one stream, one device-memory arena capped at

@@ -64,7 +64,7 @@ class Stats(C.Structure):
                 ('max_local_residual', C.c_double), ('device_ms', C.c_double), ('kernel_launches', C.c_int64),
                 ('solver_launches', C.c_int64), ('solver_ms', C.c_double), ('solver_flops64', C.c_double),
                 ('solver_flops32', C.c_double), ('phase_cycles', C.c_double * 8), ('tc_gemms', C.c_int64),
-                ('tc_fallbacks', C.c_int64)]
+                ('tc_fallbacks', C.c_int64), ('inner_apply_cycles', C.c_double)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}

@@ -1455,8 +1455,8 @@ struct BatchReqHost {
 
 // Mixed-precision batches run on the tcgen05 kernel variant unless
 // TTALS_TENSOR_CORES=mma (warp-level mma.sync variant, kept for comparison).
-// per-request report of the batch kernel: 20 fixed slots + d + 1 ranks - 1 (see BatchInst::report)
-constexpr int kReportFixed = 20;
+// per-request report of the batch kernel: 21 fixed slots + d (see BatchInst::report)
+constexpr int kReportFixed = 21;
 
 bool batch_tc_enabled() {
   const char* v = std::getenv("TTALS_TENSOR_CORES");
@@ -1700,6 +1700,7 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
   if (!stats) return;
   double maxres = 0.0, fl64 = 0.0, fl32 = 0.0, ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t tcg = 0, tcf = 0;
+  double iapp = 0.0;
   int64_t nsolve = 0, nits = 0, ncyc = 0;
   for (const auto& rep : reps) {
     if (rep.empty()) continue;
@@ -1707,6 +1708,7 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
     for (int k = 0; k < 8; ++k) ph[k] += rep[10 + d + k];
     tcg += (int64_t)rep[18 + d];
     tcf += (int64_t)rep[19 + d];
+    iapp += rep[20 + d];
     maxres = std::max(maxres, rep[0]);
     nsolve += (int64_t)rep[1];
     nits += (int64_t)rep[2];
@@ -1721,6 +1723,7 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
   stats->device_ms = total_ms;
   stats->tc_gemms = tcg;
   stats->tc_fallbacks = tcf;
+  stats->inner_apply_cycles = iapp;
   stats->kernel_launches = launches;
   stats->solver_launches = 1;
   stats->solver_ms = kernel_ms;

@@ -241,7 +241,8 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
                                       double* T2_64, const TI* Li, const TI* Ai, const TI* Ri, TI* T1i, TI* T2i,
                                       const double* f, double* x, double* r, TI* V, TI* w, int64_t N, int m,
                                       int max_cycles, double tol, double inner_floor, double* sm,
-                                      const OzScratch* oz, long long* cyc_res, long long* cyc_inner) {
+                                      const OzScratch* oz, long long* cyc_res, long long* cyc_inner,
+                                      long long* cyc_apply) {
   double* H = sm;                // (m+1) x m
   double* cs = H + (m + 1) * m;  // m
   double* sn = cs + m;           // m
@@ -318,8 +319,10 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     __syncthreads();
     int jj = 0;
     for (int j = 0; j < m; ++j) {
+      const long long ca0 = clock64();
       cta_apply<TI, TC>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
                         oz ? oz->tc : nullptr);
+      *cyc_apply += clock64() - ca0;
       dots(j + 1, w, h1);
       // Classical Gram-Schmidt with selective reorthogonalisation (FP32 inner
       // solves): one projection suffices when it keeps at least 1/sqrt(2) of the
@@ -682,6 +685,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   int64_t nsolve = 0, nits = 0, ncyc = 0;
   int status = ST_OK;
   // tensor-core counters of the CTA when this request started (thread 0 keeps them)
+  long long inner_apply = 0;  // cycles of the inner solves spent in local-operator applications
   const unsigned long long tc0 = S.oz.tc ? S.oz.tc->gemms : 0ull, fb0 = S.oz.tc ? S.oz.tc->fallbacks : 0ull;
   long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const long long t_start = clock64();
@@ -770,19 +774,20 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     const int m = (int)(N < a.m ? N : a.m);
     CtaSolveStats st;
     lap(2);
-    long long cr = 0, ci = 0;
+    long long cr = 0, ci = 0, capp = 0;
     if (a.prec == 1) {
       cta_to_float(S.Lf, L(i), aa * R[i] * aa);
       cta_to_float(S.Rf, Rt(i), ss * R[i + 1] * ss);
       cta_to_float(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
       st = cta_gmres_ir<float, TC>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
-                               S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm, &S.oz, &cr, &ci);
+                               S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm, &S.oz, &cr, &ci, &capp);
     } else {
       st = cta_gmres_ir<double, false>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
-                                S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm, nullptr, &cr, &ci);
+                                S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm, nullptr, &cr, &ci, &capp);
     }
     ph[3] += cr;
     ph[4] += ci;
+    inner_apply += capp;
     tp = clock64();
     ++nsolve;
     nits += st.inner;
@@ -858,6 +863,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     for (int k = 0; k < 8; ++k) I.report[10 + d + k] = (double)ph[k];
     I.report[18 + d] = S.oz.tc ? (double)(S.oz.tc->gemms - tc0) : 0.0;
     I.report[19 + d] = S.oz.tc ? (double)(S.oz.tc->fallbacks - fb0) : 0.0;
+    I.report[20 + d] = (double)inner_apply;
   }
   signal_done(I.done);
 }
@@ -1029,6 +1035,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     for (int k = 0; k < 8; ++k) I.report[10 + d + k] = 0.0;
     I.report[18 + d] = 0.0;
     I.report[19 + d] = 0.0;
+    I.report[20 + d] = 0.0;
   }
   signal_done(I.done);
 }

@@ -21,7 +21,8 @@ struct BatchInst {
   double* out;     // final cores, packed
   int* done;       // per-request completion flag in host-mapped memory (may be null)
   double* report;  // [max rel residual, local solves, Krylov its, refinement cycles, status, flops64, flops32,
-                   //  eigenvalue, ranks[d+1], sweeps run, phase cycles[8], tensor-core GEMMs, fallbacks]
+                   //  eigenvalue, ranks[d+1], sweeps run, phase cycles[8], tensor-core GEMMs, fallbacks,
+                   //  inner-solve cycles in operator applications]
 };
 
 // Largest per-CTA scratch needs over the batch (elements).

@@ -40,16 +40,20 @@ constexpr int kTcOzNT = 16 * kTcGroups;   // columns per emulated-FP64 tile: 16 
 constexpr int kTcOzDrain = 2;             // chunks accumulated in TMEM between drains (64 steps)
 constexpr int kTcF32NT = 256;             // columns per 3xTF32 tile
 constexpr uint32_t kTcTmemCols = 512;     // TMEM columns held by one CTA (all of the SM's)
-constexpr int kTcSmemBytes = 96 * 1024;   // operand tiles
+constexpr int kTcTileBytes = 96 * 1024;   // operand tiles
+// per-tile index tables after the tiles: operand offset, output offset and
+// exponent of each row (kTcM) and column (kTcF32NT) of the current tile
+constexpr int kTcTabBytes = 3 * 4 * (kTcM + kTcF32NT);
+constexpr int kTcSmemBytes = kTcTileBytes + (kTcTabBytes + 1023) / 1024 * 1024;
 
 static_assert(kOzSlices * kTcOzNT <= (int)kTcTmemCols, "level accumulators must fit the CTA's TMEM");
 static_assert(kTcF32NT <= (int)kTcTmemCols, "3xTF32 accumulator must fit the CTA's TMEM");
-static_assert(kOzSlices * kTcM * kTcKC * 2 + kOzSlices * kTcOzNT * kTcKC * 2 <= kTcSmemBytes, "Ozaki tiles");
-static_assert(2 * kTcM * kTcKC * 4 + 2 * kTcF32NT * kTcKC * 4 <= kTcSmemBytes, "3xTF32 tiles");
+static_assert(kOzSlices * kTcM * kTcKC * 2 + kOzSlices * kTcOzNT * kTcKC * 2 <= kTcTileBytes, "Ozaki tiles");
+static_assert(2 * kTcM * kTcKC * 4 + 2 * kTcF32NT * kTcKC * 4 <= kTcTileBytes, "3xTF32 tiles");
 
 // Per-CTA tensor-core state (lives in shared memory).
 struct TcState {
-  unsigned char* tiles;  // kTcSmemBytes, 1024-byte aligned
+  unsigned char* tiles;  // kTcSmemBytes, 1024-byte aligned: operand tiles, then the index tables
   uint32_t tmem;         // TMEM base of kTcTmemCols columns
   uint32_t phase;        // parity of the next MMA completion
   int status;            // ST_OK; ST_TIMEOUT once a completion wait gave up (no further MMAs)
@@ -57,6 +61,16 @@ struct TcState {
   unsigned long long gemms;      // contractions completed on the tensor cores
   unsigned long long fallbacks;  // GEMM-shaped contractions that took the SIMT path instead
 };
+
+// The index tables of the current tile (shared memory after the operand tiles).
+struct TcTables {
+  int *rop, *rco, *rex;  // rows: operand offset (-1 beyond the matrix), output offset, exponent
+  int *cop, *cco, *cex;  // columns: the same
+};
+__device__ __forceinline__ TcTables tc_tables(const TcState& tc) {
+  int* t = reinterpret_cast<int*>(tc.tiles + kTcTileBytes);
+  return TcTables{t, t + kTcM, t + 2 * kTcM, t + 3 * kTcM, t + 3 * kTcM + kTcF32NT, t + 3 * kTcM + 2 * kTcF32NT};
+}
 
 // int64 fixed point v * 2^e -> FP64, by bit manipulation (round to nearest even).
 __device__ __forceinline__ double tc_i64_to_f64(long long v, int e) {
@@ -104,30 +118,39 @@ __device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
   }
 }
 
-// E[i] with |x| < 2^E[i] over row i of an operand (all K); flags non-finite
-// values.  One warp takes 8 rows at a time with its lanes along the
-// contraction, so every lane keeps 8 independent loads in flight.
-__device__ __forceinline__ void tc_oz_exponents(const GemmAxes& ax, const double* __restrict__ src,
-                                                const int* koff, int K, int MN, int* E, int* bad) {
+// Decode rows [r0, r0 + cnt) of an axis set once per tile: operand offset
+// (-1 for rows >= valid) and output offset.
+__device__ __forceinline__ void tc_axis_table(const GemmAxes& ax, int r0, int cnt, int valid, int* op, int* co) {
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    int o = -1, c = 0;
+    if (r0 + i < valid) gemm_axes_offsets(ax, r0 + i, o, c);
+    op[i] = o;
+    co[i] = c;
+  }
+}
+
+// E[i] with |x| < 2^E[i] over the contraction of table row i; flags
+// non-finite values.  One warp takes 8 rows at a time with its lanes along
+// the contraction (8 independent loads in flight per lane).
+__device__ __forceinline__ void tc_table_exponents(const double* __restrict__ src, const int* koff, int K,
+                                                   const int* op, int cnt, int* E, int* bad) {
   constexpr int kRows = 8;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int ib = warp * kRows; ib < MN; ib += nw * kRows) {
-    int op[kRows];
+  for (int ib = warp * kRows; ib < cnt; ib += nw * kRows) {
+    int o[kRows];
     unsigned long long amax[kRows];
 #pragma unroll
     for (int u = 0; u < kRows; ++u) {
-      int dummy;
-      op[u] = 0;
+      o[u] = ib + u < cnt ? op[ib + u] : -1;
       amax[u] = 0;
-      if (ib + u < MN) gemm_axes_offsets(ax, ib + u, op[u], dummy);
     }
     for (int k = lane; k < K; k += 32) {
       const int ko = koff[k];
 #pragma unroll
       for (int u = 0; u < kRows; ++u) {
-        if (ib + u < MN) {
+        if (o[u] >= 0) {
           const unsigned long long b =
-              (unsigned long long)__double_as_longlong(src[op[u] + ko]) & 0x7fffffffffffffffull;
+              (unsigned long long)__double_as_longlong(src[o[u] + ko]) & 0x7fffffffffffffffull;
           amax[u] = b > amax[u] ? b : amax[u];
         }
       }
@@ -135,11 +158,11 @@ __device__ __forceinline__ void tc_oz_exponents(const GemmAxes& ax, const double
 #pragma unroll
     for (int u = 0; u < kRows; ++u) {
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long other = __shfl_xor_sync(0xffffffffu, amax[u], o);
+      for (int sft = 16; sft > 0; sft >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, amax[u], sft);
         amax[u] = other > amax[u] ? other : amax[u];
       }
-      if (lane == 0 && ib + u < MN) {
+      if (lane == 0 && ib + u < cnt) {
         // NaN / Inf have the all-ones exponent: larger than every finite magnitude
         if (amax[u] >= 0x7ff0000000000000ull) *bad = 1;
         E[ib + u] = oz_exponent_bits(amax[u]);
@@ -148,31 +171,34 @@ __device__ __forceinline__ void tc_oz_exponents(const GemmAxes& ax, const double
   }
 }
 
-// Rows [r0, r0 + rows) x contraction [k0, k0 + kTcKC) of an FP64 operand into
-// kOzSlices BF16 slice tiles (tile p at base + p * slice_bytes); rows >= valid
-// and k >= K are zero.  One work item = one row x 8 contraction steps (one
-// 16-byte row of a core matrix per slice).
-__device__ __forceinline__ void tc_oz_stage(const GemmAxes& ax, const double* __restrict__ src, const int* koff,
-                                            int K, int k0, int r0, int rows, int valid, const int* E,
-                                            unsigned char* base, uint32_t slice_bytes) {
+// Rows [0, rows) of the tile (operand offsets op, exponents E) x contraction
+// [k0, k0 + kTcKC) of an FP64 operand into kOzSlices BF16 slice tiles (tile p
+// at base + p * slice_bytes); rows with op < 0 and k >= K are zero.  One work
+// item = one row x 8 contraction steps (one 16-byte core-matrix row per slice);
+// consecutive threads take consecutive rows.
+__device__ __forceinline__ void tc_oz_stage(const double* __restrict__ src, const int* koff, int K, int k0,
+                                            const int* op, const int* E, int rows, unsigned char* base,
+                                            uint32_t slice_bytes) {
   constexpr int kbytes = kTcKC * 2;
   const int items = rows * (kTcKC / 8);
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
     const int cc = it / rows, r = it - cc * rows;
-    const int row = r0 + r;
+    const int o = op[r];
     uint32_t w[kOzSlices][4];
 #pragma unroll
     for (int p = 0; p < kOzSlices; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
-    if (row < valid) {
-      int op, dummy;
-      gemm_axes_offsets(ax, row, op, dummy);
-      const int e = E[row];
+    if (o >= 0) {
+      const int e = E[r];
+      uint64_t b[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = k0 + cc * 8 + u;
-        const uint64_t b = k < K ? (uint64_t)__double_as_longlong(src[op + koff[k]]) : 0ull;
-        const uint64_t mag = oz_fixed48(b, e);
-        const uint32_t sg = (uint32_t)(b >> 48) & 0x8000u;
+        b[u] = k < K ? (uint64_t)__double_as_longlong(src[o + koff[k]]) : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const uint64_t mag = oz_fixed48(b[u], e);
+        const uint32_t sg = (uint32_t)(b[u] >> 48) & 0x8000u;
 #pragma unroll
         for (int p = 0; p < kOzSlices; ++p) w[p][u >> 1] |= oz_slice_bf16(mag, sg, p) << (16 * (u & 1));
       }
@@ -211,26 +237,22 @@ __device__ __forceinline__ void tc_publish() {
 }
 
 // C = contraction(A, B) with FP64-level accuracy; false when not GEMM-shaped,
-// out of the scratch capacities, non-finite, or the tensor cores are unusable
-// (the caller then runs the FP64 SIMT path).
+// non-finite, or the tensor cores are unusable (the caller then runs the FP64
+// SIMT path, which overwrites whatever was written).
 __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const double* __restrict__ A,
                                                const double* __restrict__ B, double* __restrict__ C,
                                                const OzScratch& z, int* ktab, TcState& tc) {
+  (void)z;
   GemmAxes rows, cols;
   // kTcThreads threads: kTcGroups 128-thread groups, each draining 16 of the tile's columns
   if (blockDim.x != kTcThreads || tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
-  if (M > z.cap_r || N > z.cap_c) return false;
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
   tc_k_tables(c, ktab);
-  __syncthreads();
   const int* koffA = ktab;
   const int* koffB = ktab + kTcMaxK;
-  tc_oz_exponents(rows, A, koffA, K, M, z.rexp, &s_bad);
-  tc_oz_exponents(cols, B, koffB, K, N, z.cexp, &s_bad);
-  __syncthreads();
-  if (s_bad) return false;
+  const TcTables T = tc_tables(tc);
   constexpr uint32_t a_slice = kTcM * kTcKC * 2, b_slice = kTcOzNT * kTcKC * 2;
   constexpr uint32_t sbo = (kTcKC * 2 / 16) * 128;
   unsigned char* ta = tc.tiles;
@@ -240,31 +262,46 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
   const int sh = nwin <= 1 ? 0 : 32 - __clz(nwin - 1);  // 2^sh >= windows: the int64 sum cannot overflow
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
   const int hh = warp >> 2;  // this thread's 16-column block of the tile
+  const int rl = 32 * q4 + lane;  // this thread's row of the tile (TMEM lane)
   for (int m0 = 0; m0 < M; m0 += kTcM) {
+    tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
+    __syncthreads();
+    tc_table_exponents(A, koffA, K, T.rop, kTcM, T.rex, &s_bad);
     for (int n0 = 0; n0 < N; n0 += kTcOzNT) {
       const int ncols = N - n0 < kTcOzNT ? N - n0 : kTcOzNT;
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtBF16, kTcM, ntile);
+      tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
+      __syncthreads();
+      tc_table_exponents(B, koffB, K, T.cop, ntile, T.cex, &s_bad);
+      __syncthreads();
+      if (s_bad) return false;
       long long acc[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) acc[j] = 0;
       for (int kc = 0; kc < nK; ++kc) {
-        if (nK > 1 || n0 == 0) tc_oz_stage(rows, A, koffA, K, kc * kTcKC, m0, kTcM, M, z.rexp, ta, a_slice);
-        tc_oz_stage(cols, B, koffB, K, kc * kTcKC, n0, ntile, N, z.cexp, tb, b_slice);
+        if (nK > 1 || n0 == 0) tc_oz_stage(A, koffA, K, kc * kTcKC, T.rop, T.rex, kTcM, ta, a_slice);
+        tc_oz_stage(B, koffB, K, kc * kTcKC, T.cop, T.cex, ntile, tb, b_slice);
         tc_publish();
         if (threadIdx.x == 0) {
           const bool wstart = (kc % kTcOzDrain) == 0;
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
+          uint64_t da[kOzSlices], db[kOzSlices];
+#pragma unroll
+          for (int p = 0; p < kOzSlices; ++p) {
+            da[p] = umma::sdesc(a0 + p * a_slice, 128, sbo);
+            db[p] = umma::sdesc(b0 + p * b_slice, 128, sbo);
+          }
 #pragma unroll
           for (int ks = 0; ks < kTcKC / 16; ++ks)
 #pragma unroll
             for (int p = 0; p < kOzSlices; ++p)
 #pragma unroll
               for (int q = 0; q < kOzSlices - p; ++q) {
-                const uint64_t da = umma::sdesc(a0 + p * a_slice + 256u * ks, 128, sbo);
-                const uint64_t db = umma::sdesc(b0 + q * b_slice + 256u * ks, 128, sbo);
+                // the start-address field counts 16-byte units: +16 per 256-byte K step
                 const uint32_t acc_in = (wstart && ks == 0 && p == 0) ? 0u : 1u;
-                umma::mma_f16(umma::taddr(tc.tmem, 0, (p + q) * kTcOzNT), da, db, id, acc_in);
+                umma::mma_f16(umma::taddr(tc.tmem, 0, (p + q) * kTcOzNT), da[p] + 16u * ks, db[q] + 16u * ks, id,
+                              acc_in);
               }
           umma::commit(&tc.bar);
         }
@@ -287,20 +324,14 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
           umma::fence_before_sync();
         }
       }
-      // results of this tile: row m0 + 32 q4 + lane, columns n0 + 16 hh + j
-      const int row = m0 + 32 * q4 + lane;
-      if (row < M) {
-        int dummy, cr;
-        gemm_axes_offsets(rows, row, dummy, cr);
-        const int er = z.rexp[row] - 8 * (kOzSlices + 1) + sh;
+      // results of this tile: row m0 + rl, columns n0 + 16 hh + j
+      if (T.rop[rl] >= 0 && hh * 16 < ncols) {
+        const int cr = T.rco[rl];
+        const int er = T.rex[rl] - 8 * (kOzSlices + 1) + sh;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int col = n0 + hh * 16 + j;
-          if (col < N) {
-            int cc;
-            gemm_axes_offsets(cols, col, dummy, cc);
-            C[cr + cc] = tc_i64_to_f64(acc[j], er + z.cexp[col]);
-          }
+          const int cl = hh * 16 + j;
+          if (cl < ncols) C[cr + T.cco[cl]] = tc_i64_to_f64(acc[j], er + T.cex[cl]);
         }
       }
       __syncthreads();
@@ -309,26 +340,28 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
   return true;
 }
 
-// Rows [r0, r0 + rows) x contraction [k0, k0 + kTcKC) of an FP32 operand as
-// TF32 head and tail tiles (hi at base, lo at base + half_bytes).
-__device__ __forceinline__ void tc_tf32_stage(const GemmAxes& ax, const float* __restrict__ src, const int* koff,
-                                              int K, int k0, int r0, int rows, int valid, unsigned char* base,
-                                              uint32_t half_bytes) {
+// Rows [0, rows) of the tile (operand offsets op) x contraction [k0, k0 + kTcKC)
+// of an FP32 operand as TF32 head and tail tiles (hi at base, lo at
+// base + half_bytes); rows with op < 0 and k >= K are zero.
+__device__ __forceinline__ void tc_tf32_stage(const float* __restrict__ src, const int* koff, int K, int k0,
+                                              const int* op, int rows, unsigned char* base, uint32_t half_bytes) {
   constexpr int kbytes = kTcKC * 4;
   const int items = rows * (kTcKC / 4);
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
     const int cc = it / rows, r = it - cc * rows;
-    const int row = r0 + r;
+    const int o = op[r];
     uint32_t hi[4] = {0u, 0u, 0u, 0u}, lo[4] = {0u, 0u, 0u, 0u};
-    if (row < valid) {
-      int op, dummy;
-      gemm_axes_offsets(ax, row, op, dummy);
+    if (o >= 0) {
+      float x[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int k = k0 + cc * 4 + u;
-        const float x = k < K ? src[op + koff[k]] : 0.f;
-        hi[u] = tf32_bits(x);
-        lo[u] = tf32_bits(x - __uint_as_float(hi[u]));
+        x[u] = k < K ? src[o + koff[k]] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        hi[u] = tf32_bits(x[u]);
+        lo[u] = tf32_bits(x[u] - __uint_as_float(hi[u]));
       }
     }
     const uint32_t off = umma::tile_off(r, cc * 4, 4, kbytes);
@@ -346,9 +379,9 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
   if (tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
   tc_k_tables(c, ktab);
-  __syncthreads();
   const int* koffA = ktab;
   const int* koffB = ktab + kTcMaxK;
+  const TcTables T = tc_tables(tc);
   constexpr uint32_t a_half = kTcM * kTcKC * 4, b_half = kTcF32NT * kTcKC * 4;
   constexpr uint32_t sbo = (kTcKC * 4 / 16) * 128;
   unsigned char* ta = tc.tiles;
@@ -356,47 +389,47 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
   const int nK = (K + kTcKC - 1) / kTcKC;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
   const int halves = blockDim.x >> 7, grp = warp >> 2;
+  const int rl = 32 * q4 + lane;
   for (int m0 = 0; m0 < M; m0 += kTcM) {
+    tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
     for (int n0 = 0; n0 < N; n0 += kTcF32NT) {
       const int ncols = N - n0 < kTcF32NT ? N - n0 : kTcF32NT;
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtTF32, kTcM, ntile);
+      tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
+      __syncthreads();
       for (int kc = 0; kc < nK; ++kc) {
-        if (nK > 1 || n0 == 0) tc_tf32_stage(rows, A, koffA, K, kc * kTcKC, m0, kTcM, M, ta, a_half);
-        tc_tf32_stage(cols, B, koffB, K, kc * kTcKC, n0, ntile, N, tb, b_half);
+        if (nK > 1 || n0 == 0) tc_tf32_stage(A, koffA, K, kc * kTcKC, T.rop, kTcM, ta, a_half);
+        tc_tf32_stage(B, koffB, K, kc * kTcKC, T.cop, ntile, tb, b_half);
         tc_publish();
         if (threadIdx.x == 0) {
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
           const uint32_t d = umma::taddr(tc.tmem, 0, 0);
+          const uint64_t ah = umma::sdesc(a0, 128, sbo), al = umma::sdesc(a0 + a_half, 128, sbo);
+          const uint64_t bh = umma::sdesc(b0, 128, sbo), bl = umma::sdesc(b0 + b_half, 128, sbo);
 #pragma unroll
           for (int ks = 0; ks < kTcKC / 8; ++ks) {
-            const uint64_t ah = umma::sdesc(a0 + 256u * ks, 128, sbo), al = umma::sdesc(a0 + a_half + 256u * ks, 128, sbo);
-            const uint64_t bh = umma::sdesc(b0 + 256u * ks, 128, sbo), bl = umma::sdesc(b0 + b_half + 256u * ks, 128, sbo);
-            umma::mma_tf32(d, al, bh, id, (kc == 0 && ks == 0) ? 0u : 1u);
-            umma::mma_tf32(d, ah, bl, id, 1u);
-            umma::mma_tf32(d, ah, bh, id, 1u);
+            const uint64_t st = 16u * ks;  // start-address field: 256 bytes per K step
+            umma::mma_tf32(d, al + st, bh + st, id, (kc == 0 && ks == 0) ? 0u : 1u);
+            umma::mma_tf32(d, ah + st, bl + st, id, 1u);
+            umma::mma_tf32(d, ah + st, bh + st, id, 1u);
           }
           umma::commit(&tc.bar);
         }
         if (!tc_wait(tc)) return false;
       }
-      const int row = m0 + 32 * q4 + lane;
-      int dummy, cr = 0;
-      if (row < M) gemm_axes_offsets(rows, row, dummy, cr);
+      const bool live = T.rop[rl] >= 0;
+      const int cr = T.rco[rl];
       // each 128-thread group drains every other 16-column block
       for (int cb = grp * 16; cb < ntile; cb += 16 * halves) {
         uint32_t v[16];
         umma::ld16(umma::taddr(tc.tmem, 32 * q4, cb), v);
         umma::ld_wait();
-        if (row < M) {
+        if (live) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int col = n0 + cb + j;
-            if (col < N) {
-              int cc;
-              gemm_axes_offsets(cols, col, dummy, cc);
-              C[cr + cc] = __uint_as_float(v[j]);
-            }
+            const int cl = cb + j;
+            if (cl < ncols) C[cr + T.cco[cl]] = __uint_as_float(v[j]);
           }
         }
       }
