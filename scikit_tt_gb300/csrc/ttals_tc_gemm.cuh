@@ -210,22 +210,35 @@ __device__ __forceinline__ void tc_oz_stage(const double* __restrict__ src, cons
   }
 }
 
-// Wait for the MMAs committed last; false (and status set) if the wait gave up.
-__device__ __forceinline__ bool tc_wait(TcState& tc) {
-  __shared__ int s_ok;
-  if (threadIdx.x == 0) s_ok = 1;
-  __syncthreads();
-  if (!umma::mbar_wait(&tc.bar, tc.phase)) s_ok = 0;
+// Completion waits of one GEMM call: every thread tracks the mbarrier phase in
+// a register (all threads wait for the same commits in the same order) and
+// one barrier per wait publishes whether any thread gave up.
+struct TcWaiter {
+  uint32_t phase;
+  int* fail;  // shared flag, cleared at the start of the call
+};
+__device__ __forceinline__ TcWaiter tc_waiter_begin(TcState& tc) {
+  __shared__ int s_fail;
+  if (threadIdx.x == 0) s_fail = 0;
+  return TcWaiter{tc.phase, &s_fail};
+}
+// Wait for the MMAs committed last (all threads); false (status set) if the wait gave up.
+__device__ __forceinline__ bool tc_wait(TcState& tc, TcWaiter& w) {
+  if (!umma::mbar_wait(&tc.bar, w.phase)) *w.fail = 1;
+  w.phase ^= 1u;
   __syncthreads();
   umma::fence_after_sync();
-  const bool ok = s_ok != 0;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    tc.phase ^= 1u;
-    if (!ok) tc.status = ST_TIMEOUT;
+  if (*w.fail) {
+    if (threadIdx.x == 0) tc.status = ST_TIMEOUT;
+    return false;
   }
+  return true;
+}
+// End of a GEMM call: the parity of the next completion goes back to the state.
+__device__ __forceinline__ void tc_waiter_end(TcState& tc, const TcWaiter& w) {
   __syncthreads();
-  return ok;
+  if (threadIdx.x == 0) tc.phase = w.phase;
+  __syncthreads();
 }
 
 // shared-memory operand writes -> visible to the tensor cores; TMEM reads done
@@ -263,19 +276,30 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
   const int hh = warp >> 2;  // this thread's 16-column block of the tile
   const int rl = 32 * q4 + lane;  // this thread's row of the tile (TMEM lane)
+  TcWaiter wt = tc_waiter_begin(tc);
+  const bool one_n = N <= kTcOzNT;  // column tables and exponents stay valid across row tiles
   for (int m0 = 0; m0 < M; m0 += kTcM) {
+    const bool cols_now = one_n && m0 == 0;  // the single column tile, decoded once
     tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
+    if (cols_now) tc_axis_table(cols, 0, (N + 15) & ~15, N, T.cop, T.cco);
     __syncthreads();
     tc_table_exponents(A, koffA, K, T.rop, kTcM, T.rex, &s_bad);
+    if (cols_now) tc_table_exponents(B, koffB, K, T.cop, (N + 15) & ~15, T.cex, &s_bad);
     for (int n0 = 0; n0 < N; n0 += kTcOzNT) {
       const int ncols = N - n0 < kTcOzNT ? N - n0 : kTcOzNT;
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtBF16, kTcM, ntile);
-      tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
+      if (!one_n) {
+        __syncthreads();  // the previous tile's store has read the column tables
+        tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
+        __syncthreads();
+        tc_table_exponents(B, koffB, K, T.cop, ntile, T.cex, &s_bad);
+      }
       __syncthreads();
-      tc_table_exponents(B, koffB, K, T.cop, ntile, T.cex, &s_bad);
-      __syncthreads();
-      if (s_bad) return false;
+      if (s_bad) {
+        tc_waiter_end(tc, wt);
+        return false;
+      }
       long long acc[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) acc[j] = 0;
@@ -305,7 +329,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
               }
           umma::commit(&tc.bar);
         }
-        if (!tc_wait(tc)) return false;
+        if (!tc_wait(tc, wt)) return false;
         if ((kc % kTcOzDrain) == kTcOzDrain - 1 || kc == nK - 1) {
           if (hh * 16 < ntile) {  // warp-uniform
 #pragma unroll
@@ -337,6 +361,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
       __syncthreads();
     }
   }
+  tc_waiter_end(tc, wt);
   return true;
 }
 
@@ -390,13 +415,15 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
   const int halves = blockDim.x >> 7, grp = warp >> 2;
   const int rl = 32 * q4 + lane;
+  TcWaiter wt = tc_waiter_begin(tc);
+  const bool one_n = N <= kTcF32NT;
   for (int m0 = 0; m0 < M; m0 += kTcM) {
     tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
     for (int n0 = 0; n0 < N; n0 += kTcF32NT) {
       const int ncols = N - n0 < kTcF32NT ? N - n0 : kTcF32NT;
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtTF32, kTcM, ntile);
-      tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
+      if (!one_n || m0 == 0) tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
       __syncthreads();
       for (int kc = 0; kc < nK; ++kc) {
         if (nK > 1 || n0 == 0) tc_tf32_stage(A, koffA, K, kc * kTcKC, T.rop, kTcM, ta, a_half);
@@ -416,7 +443,7 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
           }
           umma::commit(&tc.bar);
         }
-        if (!tc_wait(tc)) return false;
+        if (!tc_wait(tc, wt)) return false;
       }
       const bool live = T.rop[rl] >= 0;
       const int cr = T.rco[rl];
@@ -437,6 +464,7 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
       __syncthreads();
     }
   }
+  tc_waiter_end(tc, wt);
   return true;
 }
 
