@@ -398,10 +398,12 @@ def other_workloads(lib, ctx, args):
     # mixed: local systems to 1e-11, which keeps every instance of the reference-checked
     # subset within 1e-8 of the reference (1e-10 leaves one at 2.6e-8)
     for prec in ('mixed', 'fp64'):
-        sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
+        for _ in range(3 if prec == 'mixed' else 2):   # the engine autotuner's trials
+            sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
         sols, st = sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
         res4[prec] = {'solves_per_s': 256 / (st['device_ms'] / 1e3), 'device_ms': st['device_ms'],
-                      'max_local_residual': st['max_local_residual']}
+                      'max_local_residual': st['max_local_residual'],
+                      'tensor_cores_tcgen05': bool(st['batch_tensor_cores']), 'ctas_per_sm': st['batch_ctas_per_sm']}
     res4['mixed_over_plain'] = res4['mixed']['solves_per_s'] / res4['fp64']['solves_per_s']
     out['batch256_uneven'] = res4
     # serving: Poisson arrivals at 2000/s (80 % SLE from the uneven distribution, 20 % Ising EVP
@@ -514,9 +516,15 @@ def main_gpu(args):
                                                st))
         return st
 
-    def timed(fn, steps, warmup):
+    tuning = []  # (precision, tensor cores, CTAs per SM, kernel ms per solve) of the warm-up calls
+
+    def timed(fn, steps, warmup, prec_name=None):
         for _ in range(warmup):
-            fn()
+            st = fn()
+            if prec_name:
+                tuning.append({'precision': prec_name, 'tensor_cores': int(st.batch_tensor_cores),
+                               'ctas_per_sm': int(st.batch_ctas_per_sm), 'ms_per_solve': st.solver_ms / B
+                               if st.solver_ms > 0 else st.device_ms / B})
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         stats = []
@@ -536,7 +544,9 @@ def main_gpu(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        ms_mixed, st_mixed = timed(lambda: batch(_lib.PREC_MIXED, MIXED_TOL), args.steps, args.warmup)
+        # the warm-up steps are also the engine autotuner's trials (one per candidate variant)
+        ms_mixed, st_mixed = timed(lambda: batch(_lib.PREC_MIXED, MIXED_TOL), args.steps, max(args.warmup, 3),
+                                   'mixed')
     torch.cuda.synchronize()
     total_ms = max_over_ranks(float(np.sum(ms_mixed)), dev)
     value = world * B * args.steps / (total_ms / 1e3)
@@ -544,7 +554,7 @@ def main_gpu(args):
     launches = int(sum(s.kernel_launches for s in st_mixed))
 
     # plain FP64 on the same batch
-    ms_plain_b, st_plain_b = timed(lambda: batch(_lib.PREC_FP64, 0.0), 1, 1)
+    ms_plain_b, st_plain_b = timed(lambda: batch(_lib.PREC_FP64, 0.0), 1, 2, 'fp64')
     plain_batch_value = B / (float(np.mean(ms_plain_b)) / 1e3)
     plain_sol = out_dev[0].cpu().numpy().copy()
 
@@ -613,6 +623,14 @@ def main_gpu(args):
                        'max_local_residual': st_plain_b[-1].max_local_residual,
                        'achieved_fp64_gflops': plain_ach64},
         'mixed_over_plain_batched': value / world / plain_batch_value,
+        'engine': {'mixed': {'tensor_cores_tcgen05': bool(st_mixed[-1].batch_tensor_cores),
+                             'ctas_per_sm': int(st_mixed[-1].batch_ctas_per_sm),
+                             'tc_gemms_per_step': int(st_mixed[-1].tc_gemms)},
+                   'plain_fp64': {'ctas_per_sm': int(st_plain_b[-1].batch_ctas_per_sm)},
+                   'autotuner_trials': tuning,
+                   'what': 'the engine times each launch variant once per workload bucket (the warm-up '
+                           'steps) and runs the fastest: the tcgen05 kernel (one CTA per SM) or the '
+                           'warp-MMA kernel at full occupancy or one CTA per SM less'},
         'dropin_single_solve': {'fp64_ms': float(np.mean(ms_drop64)), 'mixed_ms': float(np.mean(ms_dropmx)),
                                 'fp64_solves_per_s': 1e3 / float(np.mean(ms_drop64)),
                                 'mixed_solves_per_s': 1e3 / float(np.mean(ms_dropmx)),

@@ -103,6 +103,11 @@ typedef struct {
   /* batched calls: the part of phase_cycles[4] (inner Krylov iterations)
    * spent applying the local operator                                      */
   double inner_apply_cycles;
+  /* batched calls: the launch variant the engine used (chosen by its
+   * autotuner unless fixed by ttals_set_batch_variant): 1 = tensor-core
+   * kernel (tcgen05), 0 = SIMT / warp-MMA kernel; and its CTAs per SM       */
+  int32_t batch_tensor_cores;
+  int32_t batch_ctas_per_sm;
 } ttals_stats;
 
 /* Context: one device, one stream, one device-memory arena capped at
@@ -158,6 +163,16 @@ int ttals_sle_mals(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const
  * (SMs x resident CTAs per SM): a batch of this size keeps every SM busy.  No
  * reference counterpart. */
 int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
+
+/* Launch variant of the batched calls (ttals_sle_als_batch, ttals_solve_batch,
+ * ttals_submit).  -1 (default): autotuned -- per workload bucket (precision,
+ * request kinds, largest local system, stack and operator core) the first
+ * batches try each candidate once (every one of them solves its batch in
+ * full), later ones use the fastest by kernel time per solve.  Candidates,
+ * mixed precision: 0 tensor-core kernel (one CTA per SM), 1 warp-MMA kernel
+ * at full occupancy, 2 the same with one CTA per SM less; plain FP64: 0 full
+ * occupancy, 1 one CTA per SM less.  No reference counterpart. */
+int ttals_set_batch_variant(ttals_ctx* ctx, int32_t variant);
 
 /* Batched scikit_tt/solvers/sle.py:10 `als`: `count` independent systems
  * (each with its own order, mode sizes and ranks) solved in one launch, one

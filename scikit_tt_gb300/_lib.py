@@ -35,7 +35,7 @@ EVP_SOLVERS = {'eig': 0, 'eigs': 1, 'eigh': 2}
 # every symbol include/ttals.h declares
 EXPORTS = (
     'ttals_create', 'ttals_destroy', 'ttals_last_error', 'ttals_set_stream', 'ttals_als_ranks',
-    'ttals_batch_slots', 'ttals_wait_probe', 'ttals_sle_als', 'ttals_sle_mals', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_ortho_trunc', 'ttals_tt_norm',
+    'ttals_batch_slots', 'ttals_set_batch_variant', 'ttals_wait_probe', 'ttals_sle_als', 'ttals_sle_mals', 'ttals_evp_als', 'ttals_tt_matmul', 'ttals_tt_ortho', 'ttals_tt_ortho_trunc', 'ttals_tt_norm',
     'ttals_stack_op', 'ttals_micro_matrix', 'ttals_set_profiling', 'ttals_measure_peaks',
     'ttals_stack_op_noalloc', 'ttals_sle_als_batch', 'ttals_solve_batch', 'ttals_submit', 'ttals_job_poll',
     'ttals_job_finish', 'ttals_batch_bytes', 'ttals_job_poll_each', 'ttals_job_fetch', 'ttals_job_report',
@@ -64,7 +64,8 @@ class Stats(C.Structure):
                 ('max_local_residual', C.c_double), ('device_ms', C.c_double), ('kernel_launches', C.c_int64),
                 ('solver_launches', C.c_int64), ('solver_ms', C.c_double), ('solver_flops64', C.c_double),
                 ('solver_flops32', C.c_double), ('phase_cycles', C.c_double * 8), ('tc_gemms', C.c_int64),
-                ('tc_fallbacks', C.c_int64), ('inner_apply_cycles', C.c_double)]
+                ('tc_fallbacks', C.c_int64), ('inner_apply_cycles', C.c_double),
+                ('batch_tensor_cores', C.c_int32), ('batch_ctas_per_sm', C.c_int32)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}
@@ -110,6 +111,7 @@ def load():
         lib.ttals_tdvp.argtypes = [vp, P(TTDesc), P(TTDesc), i32, dbl, i32, i32, dbl, C.c_int64, i32, dbl, pd,
                                    C.c_int64, i32, pi64, P(Stats)]
         lib.ttals_batch_slots.argtypes = [vp, C.POINTER(i32)]
+        lib.ttals_set_batch_variant.argtypes = [vp, i32]
         lib.ttals_wait_probe.argtypes = [vp, i32, C.c_uint32, C.POINTER(i32)]
         lib.ttals_tt_ortho.argtypes = [vp, P(TTDesc), i32, i32, i32, pd, i32, pi64]
         lib.ttals_tt_ortho_trunc.argtypes = [vp, P(TTDesc), i32, i32, i32, C.c_double, pi64, pd, i32, pi64]

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -47,6 +48,14 @@ struct ttals_ctx {
   bool profiling = false;
   std::vector<cudaEvent_t> evpool;  // event pairs around local-solve launches
   size_t inflight = 0;               // device bytes held by submitted jobs
+  // batch-engine autotuner: per workload bucket, kernel milliseconds per solve
+  // of each candidate variant (tried on the first batches of the bucket)
+  struct Tune {
+    int trials = 0;
+    double ms[4] = {0, 0, 0, 0};
+  };
+  std::map<std::string, Tune> tune;
+  int batch_variant = -1;  // -1: autotuned; otherwise the candidate index to use
 };
 
 namespace {
@@ -1472,12 +1481,41 @@ struct BatchPlan {
   int64_t stride = 0;
   int prec = 0;
   int use_tc = 0;  // mixed precision on the tensor-core kernel variant
+  int variant = 0;  // index into batch_candidates(prec)
+  int per_sm = 1;   // resident CTAs per SM of the launch
   double tol = 0.0;
   // byte layout of the device block: [regions | meta | inst | scratch | counter]
   size_t off_meta = 0, off_inst = 0, off_scratch = 0, off_next = 0, bytes = 0;
 };
 
-BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol) {
+// Candidate launch variants of the batch kernel for one precision: the
+// tensor-core kernel (tcgen05, one CTA per SM) and the SIMT / warp-MMA kernel
+// at its full occupancy and one CTA per SM less.
+struct BatchVariant {
+  int use_tc;
+  int less;  // CTAs per SM below the occupancy maximum
+};
+std::vector<BatchVariant> batch_candidates(int prec) {
+  std::vector<BatchVariant> v;
+  if (prec == TTALS_PREC_MIXED && batch_tc_enabled()) v.push_back({1, 0});
+  v.push_back({0, 0});
+  v.push_back({0, 1});
+  return v;
+}
+
+// Bucket of a planned batch for the autotuner: precision, request kinds and
+// the largest per-site sizes (local unknowns, stack, operator core).
+std::string tune_key(const BatchPlan& P) {
+  int evp = 0;
+  for (const auto& I : P.in) evp |= I.kind == 1;
+  return std::to_string(P.prec) + "|" + std::to_string(evp) + "|" + std::to_string(P.z.N) + "|" +
+         std::to_string(P.z.stack) + "|" + std::to_string(P.z.opcore);
+}
+
+// trial: the plan may try an untested candidate (synchronous batches, which
+// time themselves); otherwise (serving jobs, size queries) it takes the
+// bucket's fastest candidate once known, else the warp-MMA kernel at full occupancy.
+BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, bool trial = false) {
   require(count >= 1, TTALS_ERR_ARG, "count must be >= 1");
   require(reqs != nullptr, TTALS_ERR_ARG, "null request array");
   require(prec == TTALS_PREC_FP64 || prec == TTALS_PREC_MIXED, TTALS_ERR_ARG, "unknown precision mode");
@@ -1589,12 +1627,29 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     app(Lbo, d);
     app(Rbo, d);
   }
-  P.use_tc = (prec == TTALS_PREC_MIXED && batch_tc_enabled()) ? 1 : 0;
+  // launch variant: forced by the context, else the autotuner's choice for
+  // this bucket (its first batches try every candidate once)
   {
+    const std::vector<BatchVariant> cand = batch_candidates(prec);
+    int pick = 0;
+    if (c->batch_variant >= 0) {
+      pick = std::min<int>(c->batch_variant, (int)cand.size() - 1);
+    } else {
+      const ttals_ctx::Tune& t = c->tune[tune_key(P)];
+      if (t.trials < (int)cand.size()) {
+        pick = trial ? t.trials : (cand[0].use_tc ? 1 : 0);
+      } else {
+        for (int k = 1; k < (int)cand.size(); ++k)
+          if (t.ms[k] < t.ms[pick]) pick = k;
+      }
+    }
+    P.variant = pick;
+    P.use_tc = cand[pick].use_tc;
     cudaError_t e = cudaSuccess;
-    const int per_sm = batch_blocks_per_sm(kBatchM, kBatchMEvp, P.use_tc, &e);
+    const int per_sm = std::max(1, batch_blocks_per_sm(kBatchM, kBatchMEvp, P.use_tc, &e) - cand[pick].less);
     require(e == cudaSuccess, TTALS_ERR_CUDA,
             std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
+    P.per_sm = per_sm;
     P.grid = std::min(count, c->num_sms * per_sm);
   }
   P.stride = batch_scratch_stride(P.z, kBatchM, kBatchMEvp);
@@ -1743,7 +1798,7 @@ void collect_plan(BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_s
 void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, int out_dev,
                     ttals_stats* st) {
   launch_counter() = 0;
-  BatchPlan P = plan_batch(c, count, reqs, prec, tol);
+  BatchPlan P = plan_batch(c, count, reqs, prec, tol, true);
   char* mem = nullptr;
   Bump B{c};
   B.want(&mem, (int64_t)P.bytes);
@@ -1756,7 +1811,18 @@ void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec
   float kms = 0.f, tms = 0.f;
   CK(cudaEventElapsedTime(&kms, k0, k1));
   CK(cudaEventElapsedTime(&tms, c->ev0, c->ev1));
+  if (c->batch_variant < 0) {
+    ttals_ctx::Tune& t = c->tune[tune_key(P)];
+    if (t.trials < (int)batch_candidates(prec).size() && P.variant == t.trials) {
+      t.ms[t.trials] = (double)kms / count;
+      ++t.trials;
+    }
+  }
   collect_plan(P, mem, c->stream, out_dev, st, kms, tms, launch_counter());
+  if (st) {
+    st->batch_tensor_cores = P.use_tc;
+    st->batch_ctas_per_sm = P.per_sm;
+  }
 }
 
 void run_sle_batch(ttals_ctx* c, int count, const ttals_tt* ops, const ttals_tt* x0s, const ttals_tt* rhss,
@@ -2416,6 +2482,13 @@ int ttals_arr(ttals_ctx* c, int32_t order, const int64_t* basis_sizes, int64_t s
   return guarded(c, [&] {
     run_arr(c, order, basis_sizes, samples, theta, outputs, y, initial_guesses, repeats, rcond, out, out_capacity,
             out_ranks, stats);
+  });
+}
+
+int ttals_set_batch_variant(ttals_ctx* c, int32_t variant) {
+  return guarded(c, [&] {
+    require(variant >= -1 && variant <= 3, TTALS_ERR_ARG, "variant must be -1 (autotuned) or a candidate index");
+    c->batch_variant = variant;
   });
 }
 
