@@ -27,6 +27,11 @@
 namespace ttals {
 
 constexpr int kMaxOrderB = 256;
+// Lanczos restarts per local eigensolve (64-vector basis, restarted from the
+// Ritz vector): most sites converge in one or two; a site whose wanted
+// eigenvalue sits close to the next one needs many more (40 left a served
+// Ising request at a 1.4e-8 Ritz residual)
+constexpr int kBatchEvpRestarts = 200;
 constexpr int kBatchThreads = 128;
 // five CTAs per SM (102 registers a thread): FP32 and FP64 phases of different
 // instances overlap, and the memory-latency-bound loops get more warps to hide
@@ -955,7 +960,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     // previous sweep's core, FP64 Lanczos converges in ~12 steps per site, and
     // an FP32 Lanczos pre-stage (then FP64 polish) measured 2.8x slower.
     const CtaEigStats st = cta_lanczos<double>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m,
-                                               I.mode, I.sigma, 40, a.tol_evp, sm);
+                                               I.mode, I.sigma, kBatchEvpRestarts, a.tol_evp, sm);
     theta = st.theta;
     nits += st.its;
     nrst += st.restarts;

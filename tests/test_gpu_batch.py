@@ -77,3 +77,36 @@ def test_batch_many_instances_more_than_sms():
     for k in (0, 151, 152, 399):
         a, x, b = inst[k]
         assert O.stable_rel_diff(sols[k].cores, O.sle_als(a, x, b, repeats=1)) < 1e-10
+
+
+def test_batch_autotuner_tries_each_variant_then_keeps_the_fastest():
+    """The engine's autotuner: per workload bucket the first mixed-precision
+    batches run the tcgen05 kernel, the warp-MMA kernel at full occupancy and
+    at one CTA per SM less (each solving its batch in full), then it keeps
+    the fastest by kernel time per solve; a fixed variant is honoured."""
+    from scikit_tt_gb300 import _lib
+    from scikit_tt_gb300.solvers import sle
+    lib, ctx = _lib.load(), _lib.context()
+    inst = _instances()[:4]
+    probs = [(_tt(a), _tt(x), _tt(b)) for a, x, b in inst]
+    refs = [O.sle_als(a, x, b, repeats=1) for a, x, b in inst]
+    seen = []
+    try:
+        # a bucket no other test uses: seven instances of the fourth shape
+        probs7 = [probs[3]] * 7
+        for _ in range(4):
+            sols, st = sle.als_batch(probs7, repeats=1, precision='mixed', tol=1e-10)
+            seen.append((st['batch_tensor_cores'], st['batch_ctas_per_sm'], st['solver_ms']))
+            assert O.stable_rel_diff(sols[0].cores, refs[3]) < 1e-8
+        variants = [(t, c) for t, c, _ in seen[:3]]
+        assert variants[0][0] == 1 and variants[1][0] == 0 and variants[2][0] == 0
+        assert variants[2][1] == variants[1][1] - 1
+        best = min(range(3), key=lambda k: seen[k][2])
+        assert (seen[3][0], seen[3][1]) == variants[best]
+        _lib.check(lib.ttals_set_batch_variant(ctx, 1))
+        sols, st = sle.als_batch(probs, repeats=1, precision='mixed', tol=1e-10)
+        assert st['batch_tensor_cores'] == 0
+        for sol, ref in zip(sols, refs):
+            assert O.stable_rel_diff(sol.cores, ref) < 1e-8
+    finally:
+        _lib.check(lib.ttals_set_batch_variant(ctx, -1))
