@@ -171,7 +171,8 @@ int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
  * full), later ones use the fastest by kernel time per solve.  Candidates,
  * mixed precision: 0 tensor-core kernel (one CTA per SM), 1 warp-MMA kernel
  * at full occupancy, 2 the same with one CTA per SM less; plain FP64: 0 full
- * occupancy, 1 one CTA per SM less.  No reference counterpart. */
+ * occupancy, 1 one CTA per SM less.  -2 forgets every bucket's timings and
+ * autotunes afresh.  No reference counterpart. */
 int ttals_set_batch_variant(ttals_ctx* ctx, int32_t variant);
 
 /* Batched scikit_tt/solvers/sle.py:10 `als`: `count` independent systems

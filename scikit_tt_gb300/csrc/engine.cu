@@ -2487,8 +2487,10 @@ int ttals_arr(ttals_ctx* c, int32_t order, const int64_t* basis_sizes, int64_t s
 
 int ttals_set_batch_variant(ttals_ctx* c, int32_t variant) {
   return guarded(c, [&] {
-    require(variant >= -1 && variant <= 3, TTALS_ERR_ARG, "variant must be -1 (autotuned) or a candidate index");
-    c->batch_variant = variant;
+    require(variant >= -2 && variant <= 3, TTALS_ERR_ARG,
+            "variant must be -2 (forget the tuning), -1 (autotuned) or a candidate index");
+    if (variant == -2) c->tune.clear();
+    c->batch_variant = variant < 0 ? -1 : variant;
   });
 }
 
