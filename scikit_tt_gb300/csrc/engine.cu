@@ -56,6 +56,9 @@ struct ttals_ctx {
   };
   std::map<std::string, Tune> tune;
   int batch_variant = -1;  // -1: autotuned; otherwise the candidate index to use
+  // pinned host staging of the per-request reports of a synchronous batch
+  double* pinned = nullptr;
+  size_t pinned_cap = 0;  // doubles
 };
 
 namespace {
@@ -1788,10 +1791,50 @@ void fill_batch_stats(const std::vector<std::vector<double>>& reps, ttals_stats*
 }
 
 // After the stream finished: copy every request's outputs and fill the statistics.
-void collect_plan(BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_stats* stats, float kernel_ms,
-                  float total_ms, int64_t launches) {
-  std::vector<std::vector<double>> reps(P.in.size());
-  for (size_t j = 0; j < P.in.size(); ++j) reps[j] = collect_one(P, (int)j, mem, st, out_dev);
+// All requests of a finished synchronous batch at once: every report is
+// copied into the context's pinned staging buffer with one synchronisation,
+// checked, then every solution is copied out with one more.
+void collect_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, int out_dev, ttals_stats* stats,
+                  float kernel_ms, float total_ms, int64_t launches) {
+  double* data = (double*)mem;
+  const size_t n = P.in.size();
+  std::vector<size_t> roff(n + 1, 0);
+  for (size_t j = 0; j < n; ++j) roff[j + 1] = roff[j] + kReportFixed + P.in[j].op.d;
+  if (c->pinned_cap < roff[n]) {
+    if (c->pinned) CK(cudaFreeHost(c->pinned));
+    c->pinned = nullptr;
+    c->pinned_cap = 0;
+    CK(cudaHostAlloc((void**)&c->pinned, sizeof(double) * roff[n], cudaHostAllocDefault));
+    c->pinned_cap = roff[n];
+  }
+  for (size_t j = 0; j < n; ++j) {
+    const BatchReqHost& I = P.in[j];
+    CK(cudaMemcpyAsync(c->pinned + roff[j], data + I.region + I.off[9], sizeof(double) * (roff[j + 1] - roff[j]),
+                       cudaMemcpyDeviceToHost, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  std::vector<std::vector<double>> reps(n);
+  for (size_t j = 0; j < n; ++j) {
+    BatchReqHost& I = P.in[j];
+    const int d = I.op.d;
+    std::vector<double>& rep = reps[j];
+    rep.assign(c->pinned + roff[j], c->pinned + roff[j + 1]);
+    const int stj = (int)rep[4];
+    if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
+    if (stj == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in request " + std::to_string(j)};
+    if (stj != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(stj)};
+    int64_t cnt = 0;
+    for (int i = 0; i < d; ++i) {
+      const int64_t ri = (int64_t)rep[8 + i], rn = (int64_t)rep[9 + i];
+      require(ri == I.fin[i] && rn == I.fin[i + 1], TTALS_ERR_CUDA, "rank schedule mismatch in a batched request");
+      cnt += ri * I.op.m[i] * rn;
+    }
+    CK(cudaMemcpyAsync(I.out, data + I.region + I.off[8], sizeof(double) * cnt,
+                       out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (I.out_val) *I.out_val = rep[7];
+    if (I.out_its) *I.out_its = (int32_t)rep[9 + d];
+  }
+  CK(cudaStreamSynchronize(st));
   fill_batch_stats(reps, stats, kernel_ms, total_ms, launches);
 }
 
@@ -1818,7 +1861,7 @@ void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec
       ++t.trials;
     }
   }
-  collect_plan(P, mem, c->stream, out_dev, st, kms, tms, launch_counter());
+  collect_plan(c, P, mem, c->stream, out_dev, st, kms, tms, launch_counter());
   if (st) {
     st->batch_tensor_cores = P.use_tc;
     st->batch_ctas_per_sm = P.per_sm;
@@ -2276,6 +2319,7 @@ int ttals_destroy(ttals_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->arena) cudaFree(c->arena);
+  if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (auto e : c->evpool) cudaEventDestroy(e);
