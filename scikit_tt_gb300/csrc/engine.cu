@@ -24,6 +24,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <sstream>
+#include <memory>
 #include <map>
 #include <string>
 #include <vector>
@@ -59,6 +61,9 @@ struct ttals_ctx {
   // pinned host staging of the per-request reports of a synchronous batch
   double* pinned = nullptr;
   size_t pinned_cap = 0;  // doubles
+  // instantiated CUDA graphs of single-solve SLE sweeps, by launch layout
+  std::map<std::string, std::shared_ptr<void>> graphs;
+  std::map<std::string, int> ungraphable;  // layouts whose capture failed
 };
 
 namespace {
@@ -517,65 +522,27 @@ void download_x(Engine& E, double* out, int out_dev, int64_t* out_ranks, int k_l
     for (int i = 0; i <= P.d; ++i) out_ranks[i] = P.r[i];
 }
 
-void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttals_tt* b_t, int repeats, int solver,
-             int prec, double tol, double* out, int out_dev, int64_t* out_ranks, ttals_stats* st) {
-  TTView op = view(op_t, "operator"), x0 = view(x_t, "initial_guess"), b = view(b_t, "right_hand_side");
-  validate_square_op(op);
-  validate_vec(x0, op, "initial_guess");
-  validate_vec(b, op, "right_hand_side");
-  require(solver == TTALS_SLE_SOLVE || solver == TTALS_SLE_LU, TTALS_ERR_ARG, "solver must be 'solve' or 'lu'");
-  require(prec == TTALS_PREC_FP64 || prec == TTALS_PREC_MIXED, TTALS_ERR_ARG, "unknown precision mode");
-  require(repeats >= 0, TTALS_ERR_ARG, "repeats must be >= 0");
-  require(out != nullptr, TTALS_ERR_ARG, "output buffer is null");
-  if (tol <= 0) tol = (prec == TTALS_PREC_FP64) ? 1e-13 : 1e-10;
+bool sle_graphs_enabled() {
+  const char* v = std::getenv("TTALS_GRAPHS");
+  return !(v && std::string(v) == "0");
+}
 
-  launch_counter() = 0;
-  Engine E;
-  E.c = c;
-  E.prec = prec;
+// A captured single-solve sweep: the executable graph, the host-side engine
+// state the sweep leaves behind, and the kernels it launches.
+struct SleGraph {
+  cudaGraphExec_t exec;
+  Engine after;
+  int64_t launches;
+};
+
+// The ALS sweeps of sle.als (scikit_tt/solvers/sle.py:47-95) on the prepared
+// engine: initial right stacks, then `repeats` forward and backward half
+// sweeps with local solves, QR/RQ re-gauging and gauge pushes.  Enqueued
+// without host round trips (the ranks follow the economic QR/RQ rule).
+void sle_sweeps(Engine& E, int repeats, double tol) {
+  ttals_ctx* c = E.c;
   auto& P = E.P;
-  P.d = op.d;
-  P.n = op.m;
-  P.R = op.r;
-  P.rx0 = x0.r;
-  P.cap = ro_ranks(P.n, P.rx0);
-  P.r = P.cap;
   const int d = P.d;
-  E.op_off = op.off;
-  E.rhs_off = b.off;
-  E.rb = b.r;
-
-  Bump B{c};
-  alloc_common(E, B, op.total, b.total, x0.total, 1);
-  E.Lb.resize(d);
-  E.Rb.resize(d);
-  for (int i = 0; i < d; ++i) {
-    B.want(&E.Lb[i], E.rb[i] * P.cap[i]);
-    B.want(&E.Rb[i], E.rb[i + 1] * P.cap[i + 1]);
-    E.maxU = std::max(E.maxU, P.cap[i] * P.n[i] * std::max(E.rb[i], E.rb[i + 1]));
-    E.maxU = std::max(E.maxU, P.cap[i + 1] * P.n[i] * E.rb[i + 1]);
-  }
-  B.want(&E.U, E.maxU);
-  if (prec == TTALS_PREC_MIXED) {
-    B.want(&E.opf, op.total);
-    B.want(&E.Lf, E.maxStackOp);
-    B.want(&E.Rf, E.maxStackOp);
-    B.want(&E.T1f, E.maxT);
-    B.want(&E.T2f, E.maxT);
-    B.want(&E.Vf, (int64_t)(E.m + 1) * E.maxN);
-    B.want(&E.wf, E.maxN);
-  }
-  B.commit();
-
-  CK(cudaEventRecord(c->ev0, c->stream));
-  upload(c, E.op, op);
-  upload(c, E.rhs, b);
-  upload(c, E.x0, x0);
-  init_barrier(E);
-  if (prec == TTALS_PREC_MIXED) CK(launch_to_float(E.op, E.opf, op.total, c->stream));
-  std::vector<int64_t> x0_off = x0.off;
-  ortho_initial(E, x0_off);
-
   auto Aop = [&](int i) { return E.op + E.op_off[i]; };
   auto Bc = [&](int i) { return E.rhs + E.rhs_off[i]; };
   auto right = [&](int i) {
@@ -632,6 +599,133 @@ void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttal
       }
     }
   }
+}
+
+void run_sle(ttals_ctx* c, const ttals_tt* op_t, const ttals_tt* x_t, const ttals_tt* b_t, int repeats, int solver,
+             int prec, double tol, double* out, int out_dev, int64_t* out_ranks, ttals_stats* st) {
+  TTView op = view(op_t, "operator"), x0 = view(x_t, "initial_guess"), b = view(b_t, "right_hand_side");
+  validate_square_op(op);
+  validate_vec(x0, op, "initial_guess");
+  validate_vec(b, op, "right_hand_side");
+  require(solver == TTALS_SLE_SOLVE || solver == TTALS_SLE_LU, TTALS_ERR_ARG, "solver must be 'solve' or 'lu'");
+  require(prec == TTALS_PREC_FP64 || prec == TTALS_PREC_MIXED, TTALS_ERR_ARG, "unknown precision mode");
+  require(repeats >= 0, TTALS_ERR_ARG, "repeats must be >= 0");
+  require(out != nullptr, TTALS_ERR_ARG, "output buffer is null");
+  if (tol <= 0) tol = (prec == TTALS_PREC_FP64) ? 1e-13 : 1e-10;
+
+  launch_counter() = 0;
+  Engine E;
+  E.c = c;
+  E.prec = prec;
+  auto& P = E.P;
+  P.d = op.d;
+  P.n = op.m;
+  P.R = op.r;
+  P.rx0 = x0.r;
+  P.cap = ro_ranks(P.n, P.rx0);
+  P.r = P.cap;
+  const int d = P.d;
+  E.op_off = op.off;
+  E.rhs_off = b.off;
+  E.rb = b.r;
+
+  Bump B{c};
+  alloc_common(E, B, op.total, b.total, x0.total, 1);
+  E.Lb.resize(d);
+  E.Rb.resize(d);
+  for (int i = 0; i < d; ++i) {
+    B.want(&E.Lb[i], E.rb[i] * P.cap[i]);
+    B.want(&E.Rb[i], E.rb[i + 1] * P.cap[i + 1]);
+    E.maxU = std::max(E.maxU, P.cap[i] * P.n[i] * std::max(E.rb[i], E.rb[i + 1]));
+    E.maxU = std::max(E.maxU, P.cap[i + 1] * P.n[i] * E.rb[i + 1]);
+  }
+  B.want(&E.U, E.maxU);
+  if (prec == TTALS_PREC_MIXED) {
+    B.want(&E.opf, op.total);
+    B.want(&E.Lf, E.maxStackOp);
+    B.want(&E.Rf, E.maxStackOp);
+    B.want(&E.T1f, E.maxT);
+    B.want(&E.T2f, E.maxT);
+    B.want(&E.Vf, (int64_t)(E.m + 1) * E.maxN);
+    B.want(&E.wf, E.maxN);
+  }
+  B.commit();
+
+  CK(cudaEventRecord(c->ev0, c->stream));
+  upload(c, E.op, op);
+  upload(c, E.rhs, b);
+  upload(c, E.x0, x0);
+  // The sweep below is enqueued without host round trips; it is captured in
+  // a CUDA graph once per launch layout (arena, shapes, options) and replayed
+  // by later calls with the same layout, together with the host-side engine
+  // state it leaves behind.
+  std::string gkey;
+  const bool graphs = !c->profiling && sle_graphs_enabled();
+  if (graphs) {
+    std::ostringstream k;
+    k << (const void*)c->arena << '|' << c->arena_cap << '|' << prec << '|' << tol << '|' << repeats << '|' << solver
+      << '|' << d;
+    for (int i = 0; i < d; ++i) k << ',' << P.n[i] << ':' << P.R[i] << ':' << P.rx0[i] << ':' << E.rb[i];
+    k << ',' << P.R[d] << ':' << E.rb[d] << '|' << op.total << '|' << b.total << '|' << x0.total;
+    gkey = k.str();
+    auto it = c->graphs.find(gkey);
+    if (it != c->graphs.end()) {
+      const SleGraph* g = static_cast<const SleGraph*>(it->second.get());
+      CK(cudaGraphLaunch(g->exec, c->stream));
+      E = g->after;
+      launch_counter() += g->launches;
+      CK(cudaEventRecord(c->ev1, c->stream));
+      download_x(E, out, out_dev, out_ranks);
+      check_status(E);
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+      fill_stats(E, st, ms);
+      return;
+    }
+  }
+  const Engine before = E;
+  const int64_t launches0 = launch_counter();
+  auto enqueue = [&]() {
+    init_barrier(E);
+    if (prec == TTALS_PREC_MIXED) CK(launch_to_float(E.op, E.opf, op.total, c->stream));
+    std::vector<int64_t> x0_off = x0.off;
+    ortho_initial(E, x0_off);
+    sle_sweeps(E, repeats, tol);
+  };
+  bool done = false;
+  if (graphs && c->ungraphable.find(gkey) == c->ungraphable.end()) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      try {
+        enqueue();
+      } catch (const Fail&) {
+        e = cudaErrorStreamCaptureUnsupported;  // a launch refused capture: plain launches below
+      }
+      const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+      if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e == cudaSuccess) {
+      CK(cudaGraphLaunch(ex, c->stream));
+      if (c->graphs.size() >= 8) c->graphs.erase(c->graphs.begin());
+      c->graphs[gkey] = std::shared_ptr<void>(new SleGraph{ex, E, launch_counter() - launches0}, [](void* p) {
+        SleGraph* sg = static_cast<SleGraph*>(p);
+        cudaGraphExecDestroy(sg->exec);
+        delete sg;
+      });
+      done = true;
+    } else {
+      if (ex) cudaGraphExecDestroy(ex);
+      cudaGetLastError();
+      c->ungraphable[gkey] = 1;
+      E = before;
+      launch_counter() = launches0;
+    }
+  }
+  if (!done) enqueue();
   CK(cudaEventRecord(c->ev1, c->stream));
   download_x(E, out, out_dev, out_ranks);
   check_status(E);

@@ -142,3 +142,17 @@ def test_mals_matches_reference(golden, name):
         assert list(sol.ranks) == list(z['ranks'])
     else:
         assert max(abs(a - b) for a, b in zip(sol.ranks, z['ranks'])) <= 2
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', TOL_FP64), ('mixed', TOL_MIXED)])
+def test_sle_graph_replay_uses_new_inputs(precision, tol):
+    """The single-solve sweep is captured in a CUDA graph on its first call and
+    replayed by later calls with the same shapes: every call must solve its own
+    inputs (three different seeds, identical shapes)."""
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.solvers import sle
+    for seed in (11, 12, 13):
+        w = wl.coupled_sle(d=7, n=4, rhs_rank=3, x_rank=6, repeats=2, seed=seed)
+        sol, _ = sle.als_ex(_tt(w.op), _tt(w.x0), _tt(w.rhs), repeats=w.repeats, precision=precision)
+        ref = O.sle_als(w.op, w.x0, w.rhs, repeats=w.repeats)
+        assert O.stable_rel_diff(sol.cores, ref) < tol
