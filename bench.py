@@ -567,6 +567,10 @@ def main_gpu(args):
         _lib.check(lib.ttals_sle_als(ctx, dev_ops[0], dev_x0s[0], dev_rhs[0], WORKLOAD['repeats'], 0, prec, tol,
                                      C.cast(out1.data_ptr(), C.POINTER(C.c_double)), 1, _lib.i64ptr(out_ranks), st))
         return st
+    # plain launches first (TTALS_GRAPHS=0), then the CUDA-graph replay of the captured sweep
+    os.environ['TTALS_GRAPHS'] = '0'
+    ms_drop64_nog, _ = timed(lambda: single(_lib.PREC_FP64, 0.0), 2, 1)
+    os.environ['TTALS_GRAPHS'] = '1'
     ms_drop64, _ = timed(lambda: single(_lib.PREC_FP64, 0.0), 3, 1)
     ms_dropmx, _ = timed(lambda: single(_lib.PREC_MIXED, MIXED_TOL), 3, 1)
 
@@ -632,6 +636,8 @@ def main_gpu(args):
                            'steps) and runs the fastest: the tcgen05 kernel (one CTA per SM) or the '
                            'warp-MMA kernel at full occupancy or one CTA per SM less'},
         'dropin_single_solve': {'fp64_ms': float(np.mean(ms_drop64)), 'mixed_ms': float(np.mean(ms_dropmx)),
+                                'fp64_ms_plain_launches': float(np.mean(ms_drop64_nog)),
+                                'cuda_graph': 'the sweep is captured once per launch layout and replayed',
                                 'fp64_solves_per_s': 1e3 / float(np.mean(ms_drop64)),
                                 'mixed_solves_per_s': 1e3 / float(np.mean(ms_dropmx)),
                                 'what': 'one solve spread over the whole GPU (cooperative kernels)'},
