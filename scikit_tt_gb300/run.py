@@ -2,6 +2,7 @@
 
     python -m scikit_tt_gb300.run coupled --precision mixed --repeats 1
     python -m scikit_tt_gb300.run ising --repeats 2
+    python -m scikit_tt_gb300.run tdvp --d 8 --count 1
 
 Used for profiling (one warm-up solve, then ``--count`` measured solves).
 """
@@ -18,7 +19,7 @@ from .tensor_train import TT
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('workload', choices=['laplace', 'coupled', 'ising'])
+    ap.add_argument('workload', choices=['laplace', 'coupled', 'ising', 'tdvp'])
     ap.add_argument('--precision', default='fp64', choices=['fp64', 'mixed'])
     ap.add_argument('--repeats', type=int, default=None)
     ap.add_argument('--d', type=int, default=None)
@@ -32,6 +33,15 @@ def main():
         kw['d'] = a.d
     if a.rank:
         kw['x_rank'] = a.rank
+    if a.workload == 'tdvp':
+        # two-site imaginary-time TDVP on the Ising chain (Krylov exponentials, Jacobi SVD splits)
+        from .solvers import ode
+        w = wl.tdvp_ising(**({'d': a.d} if a.d else {}), **({'max_rank': a.rank} if a.rank else {}))
+        for k in range(a.count + 1):
+            ode.tdvp2site(TT([c.copy() for c in w.op]), TT([c.copy() for c in w.x0]), w.step_size, w.steps,
+                          max_rank=w.max_rank, normalize=2)
+        print(json.dumps(ode.last_stats))
+        return
     if a.workload == 'ising':
         w = wl.ising_evp(**kw)
         rep = a.repeats or w.repeats
