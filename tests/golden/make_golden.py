@@ -583,6 +583,52 @@ def headline_case():
     print('headline ranks', sol.ranks, 'wall %.1f s' % wall, 'global residual %.3e' % res)
 
 
+def triple_well_case():
+    """The reference's own eigenproblem known answer (tests/test_evp.py:16-150):
+    the Ulam transfer operator of the triple-well data shipped with the
+    reference (examples/data/triple_well_transitions.npz, coarse-grained as the
+    test does) in TT format, built by the reference's ulam_2d; the rank-15 ones
+    guess, right-orthonormalised; the reference's evp.als with eig, eigs and
+    eigh (symmetrised operator), number_ev=3, 10 sweeps, eig with the identity
+    operator_gevp, and power_method; and the dense eigs answers the test
+    compares with.  Eigenvectors are stored as full vectors."""
+    import scipy.sparse.linalg as splin
+    import scikit_tt.data_driven.ulam as rulam
+    tr = np.load(os.path.join(REF, 'examples', 'data', 'triple_well_transitions.npz'))['transitions']
+    tr = np.int64(np.ceil(np.true_divide(tr, 2)))
+    op = rulam.ulam_2d(tr, [25, 25], 2000)
+    x0 = rtt.ones(op.row_dims, [1] * op.order, ranks=15).ortho_right()
+    out = {}
+    pack('op', [c.copy() for c in op.cores], out)
+    pack('x0', [c.copy() for c in x0.cores], out)
+    mat = op.matricize()
+    vals, vecs = splin.eigs(mat, k=3)
+    out['mat_vals'], out['mat_vecs'] = np.real(vals), np.real(vecs)
+    sym = 0.5 * (op + op.transpose())
+    symmat = 0.5 * (mat + mat.transpose())
+    svals, svecs = splin.eigs(symmat, k=3)
+    out['sym_vals'], out['sym_vecs'] = np.real(svals), np.real(svecs)
+    pack('sym', [c.copy() for c in sym.cores], out)
+
+    def cp(t):
+        return RTT([c.copy() for c in t.cores])
+    for solver in ('eig', 'eigs', 'eigh'):
+        A = sym if solver == 'eigh' else op
+        v, t, its = revp.als(cp(A), cp(x0), number_ev=3, repeats=10, solver=solver)
+        out[f'{solver}_vals'] = np.array(v)
+        out[f'{solver}_vecs'] = np.stack([t[k].matricize() for k in range(3)])
+        out[f'{solver}_its'] = np.array(its)
+        print('triple well', solver, v, its)
+    v1, t1, _ = revp.als(cp(op), cp(x0), operator_gevp=rtt.eye(op.row_dims), repeats=10)
+    out['gevp_val'] = np.array(v1)
+    out['gevp_vec'] = t1.matricize()
+    pv, pt = revp.power_method(cp(op), cp(x0))
+    out['power_val'] = np.array(pv)
+    out['power_vec'] = pt.matricize()
+    print('triple well gevp', v1, 'power', pv)
+    np.savez_compressed(os.path.join(HERE, 'evp_triple_well.npz'), **out)
+
+
 BATCH_SUBSET = list(range(16))   # the 16 smallest-seed instances of the uneven batch
 
 
@@ -646,6 +692,7 @@ def main():
     mals_cases()
     tdvp_cases()
     arr_cases()
+    triple_well_case()
     headline_case()
     batch_subset_case()
 
@@ -673,6 +720,8 @@ if __name__ == '__main__':
         hod_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'container':
         container_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'triple_well':
+        triple_well_case()
     elif len(sys.argv) > 1 and sys.argv[1] == 'headline':
         headline_case()
     elif len(sys.argv) > 1 and sys.argv[1] == 'batch_subset':

@@ -134,3 +134,47 @@ def test_power_method_matches_reference(golden, name):
                                 sigma=float(z['sigma']))
     assert abs(val - float(z['val'])) < 1e-10
     assert _same_up_to_sign(O.full_vector(vec.cores), z['vec0']) < 1e-7
+
+
+def _vec_err(u, v):
+    u, v = np.asarray(u).ravel(), np.asarray(v).ravel()
+    return min(np.linalg.norm(u - v), np.linalg.norm(u + v)) / np.linalg.norm(v)
+
+
+@pytest.mark.parametrize('solver', ['eig', 'eigs', 'eigh'])
+def test_triple_well_known_answer(golden, solver):
+    """The reference's own eigenproblem test (tests/test_evp.py:16-150) on the
+    device: the Ulam transfer operator of the triple-well data, rank-15 ones
+    guess, number_ev=3, 10 sweeps.  Its assertions (eigenvalues within 5e-3 and
+    eigenvectors within 5e-2 of the dense eigs answer), and agreement with the
+    reference's own evp.als result to 1e-8 (eigenvalues) / 1e-6 (vectors)."""
+    from scikit_tt_gb300.solvers import evp
+    z, cores = golden('evp_triple_well')
+    op = _tt(cores('sym') if solver == 'eigh' else cores('op'))
+    vals, vecs, _ = evp.als(op, _tt(cores('x0')), number_ev=3, repeats=10, solver=solver)
+    mv = z['sym_vals'] if solver == 'eigh' else z['mat_vals']
+    mx = z['sym_vecs'] if solver == 'eigh' else z['mat_vecs']
+    idx = np.argsort(mv) if solver == 'eigs' else np.argsort(mv)[::-1]
+    mv, mx = mv[idx], mx[:, idx]
+    for i in range(3):
+        assert abs(mv[i] - vals[i]) / mv[i] < 5e-3
+        assert _vec_err(vecs[i].matricize(), mx[:, i]) < 5e-2
+        assert abs(vals[i] - z[f'{solver}_vals'][i]) <= 1e-8 * abs(z[f'{solver}_vals'][i])
+        assert _vec_err(vecs[i].matricize(), z[f'{solver}_vecs'][i]) < 1e-6
+
+
+def test_triple_well_identity_gevp_and_power_method(golden):
+    """The same test's number_ev=1 solve with the identity operator_gevp and the
+    inverse power method, against the reference's results and the dense answer."""
+    from scikit_tt_gb300.solvers import evp
+    from scikit_tt_gb300 import tensor_train as tt
+    z, cores = golden('evp_triple_well')
+    op = _tt(cores('op'))
+    val, vec, _ = evp.als(op, _tt(cores('x0')), operator_gevp=tt.eye(op.row_dims), repeats=10)
+    assert abs(val - float(z['gevp_val'])) <= 1e-8 * abs(float(z['gevp_val']))
+    assert _vec_err(vec.matricize(), z['gevp_vec']) < 1e-6
+    pv, pvec = evp.power_method(_tt(cores('op')), _tt(cores('x0')))
+    top = z['mat_vals'][np.argmax(z['mat_vals'])]
+    assert abs(pv - top) / abs(top) < 5e-3
+    assert abs(pv - float(z['power_val'])) <= 1e-8 * abs(float(z['power_val']))
+    assert _vec_err(pvec.matricize(), z['power_vec']) < 1e-6
