@@ -4,9 +4,10 @@
 Workload: SLE ALS on the coupled Laplacian (d=32 sites, mode size n=8,
 operator rank 4, right-hand side rank 8, solution rank 32, 4 sweeps, seeded
 inputs).  A *step* is one batch of independent solves of that workload in one
-launch of the persistent batch kernel; by default five solves per SM (760 on
-152 SMs): one wave of the plain FP64 kernel (five resident CTAs per SM) and
-five of the tensor-core kernel (one CTA per SM taking solves in turn).
+launch of the persistent batch kernel; by default ten solves per SM (1520 on
+152 SMs): two full waves of the warp-MMA kernel (five resident CTAs per SM)
+and five of the tensor-core kernel (one CTA per SM running two solves side by
+side), so that neither launch variant ends on a part-filled wave.
 
 * ``value``: solves/s of the mixed-precision engine (FP32 Krylov inner solves,
   FP64 refinement residual, FP64 stacks and QR) with the inputs resident in HBM,
@@ -14,7 +15,8 @@ five of the tensor-core kernel (one CTA per SM taking solves in turn).
 * ``e2e``: the same batch through the C ABI with host buffers (host->device
   copies of all trains and the device->host copy of the solutions inside the
   timed region), wall clock.
-* ``plain_fp64``: the plain FP64 engine on the same batch; ``dropin_single_solve``:
+* ``plain_fp64``: the plain FP64 engine on the first five solves per SM of the
+  batch (one full wave of its kernel); ``dropin_single_solve``:
   one solve spread over the whole GPU (the drop-in for a single ``sle.als``
   call), plain FP64 and mixed.
 * ``cpu_baseline``: the CPU oracle (a NumPy restatement of the reference's
@@ -474,12 +476,12 @@ def main_gpu(args):
     C = _lib.C
     slots = C.c_int32(0)
     _lib.check(lib.ttals_batch_slots(ctx, C.byref(slots)))
-    # five solves per SM: one wave of the plain FP64 kernel (five resident CTAs
-    # per SM) and five waves of the tensor-core kernel (one CTA per SM, which
-    # takes the next solve from the work counter when it finishes one); both
-    # engines keep every SM busy on the same batch
+    # ten solves per SM: two waves of the warp-MMA kernel (five resident CTAs
+    # per SM) and five of the tensor-core kernel (two solves side by side on
+    # each SM's one CTA); both variants keep every SM busy to the last wave
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    B = args.batch or max(int(slots.value), 5 * sms)
+    B = args.batch or max(int(slots.value), 10 * sms)
+    B_plain = min(B, 5 * sms)   # one full wave of the plain FP64 kernel
 
     # B independent seeded instances per rank (weak scaling: each rank its own batch)
     inst = [wl.coupled_sle(seed=s, **WORKLOAD) for s in rank_seeds(rank, B)]
@@ -507,10 +509,11 @@ def main_gpu(args):
     reps = (C.c_int32 * B)(*([WORKLOAD['repeats']] * B))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    def batch(prec, tol, on_device=True):
+    def batch(prec, tol, on_device=True, count=B):
         st = _lib.Stats()
         if on_device:
-            _lib.check(lib.ttals_sle_als_batch(ctx, B, dev_ops, dev_x0s, dev_rhs, reps, prec, tol, dev_ptrs, 1, st))
+            _lib.check(lib.ttals_sle_als_batch(ctx, count, dev_ops, dev_x0s, dev_rhs, reps, prec, tol, dev_ptrs, 1,
+                                               st))
         else:
             _lib.check(lib.ttals_sle_als_batch(ctx, B, host_ops, host_x0s, host_rhs, reps, prec, tol, host_ptrs, 0,
                                                st))
@@ -518,13 +521,13 @@ def main_gpu(args):
 
     tuning = []  # (precision, tensor cores, CTAs per SM, kernel ms per solve) of the warm-up calls
 
-    def timed(fn, steps, warmup, prec_name=None):
+    def timed(fn, steps, warmup, prec_name=None, count=B):
         for _ in range(warmup):
             st = fn()
             if prec_name:
                 tuning.append({'precision': prec_name, 'tensor_cores': int(st.batch_tensor_cores),
-                               'ctas_per_sm': int(st.batch_ctas_per_sm), 'ms_per_solve': st.solver_ms / B
-                               if st.solver_ms > 0 else st.device_ms / B})
+                               'ctas_per_sm': int(st.batch_ctas_per_sm), 'ms_per_solve': st.solver_ms / count
+                               if st.solver_ms > 0 else st.device_ms / count})
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         stats = []
@@ -553,9 +556,9 @@ def main_gpu(args):
     mixed_sol = out_dev[0].cpu().numpy().copy()
     launches = int(sum(s.kernel_launches for s in st_mixed))
 
-    # plain FP64 on the same batch
-    ms_plain_b, st_plain_b = timed(lambda: batch(_lib.PREC_FP64, 0.0), 1, 2, 'fp64')
-    plain_batch_value = B / (float(np.mean(ms_plain_b)) / 1e3)
+    # plain FP64 on one full wave of its kernel (the batch's first solves)
+    ms_plain_b, st_plain_b = timed(lambda: batch(_lib.PREC_FP64, 0.0, count=B_plain), 1, 2, 'fp64', count=B_plain)
+    plain_batch_value = B_plain / (float(np.mean(ms_plain_b)) / 1e3)
     plain_sol = out_dev[0].cpu().numpy().copy()
 
     # the single-instance drop-in (whole GPU on one solve), plain FP64 and mixed
@@ -618,12 +621,13 @@ def main_gpu(args):
         'dtype': 'f32 Krylov (3xTF32) + f64 refinement residuals and stacks (6-slice BF16 emulation) + f64 QR',
         'data': 'synthetic (seeded N(0,1) trains)',
         'config': {'workload': WORKLOAD_NAME, 'precision': 'mixed', 'local_tol': MIXED_TOL,
-                   'batch_per_gpu': B, 'step': f'{B} independent solves in one launch (one CTA per solve)',
+                   'batch_per_gpu': B, 'step': f'{B} independent solves in one launch (one solve per CTA, or per 256-thread group '
+                           'of the tensor-core kernel)',
                    'l2': 'flushed between steps (256 MiB write); batch working set > L2',
                    'parallelism': f'instances sharded over {world} GPU(s)'},
         'latency_ms': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99)),
                        'note': 'per batch step; every solve of the batch completes within it'},
-        'plain_fp64': {'value': plain_batch_value, 'unit': UNIT, 'what': 'same batch, plain FP64 engine',
+        'plain_fp64': {'value': plain_batch_value, 'unit': UNIT, 'what': f'plain FP64 engine on the batch\'s first {B_plain} solves (one wave)',
                        'max_local_residual': st_plain_b[-1].max_local_residual,
                        'achieved_fp64_gflops': plain_ach64},
         'mixed_over_plain_batched': value / world / plain_batch_value,

@@ -160,8 +160,9 @@ int ttals_sle_mals(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, const
                    int32_t out_on_device, int64_t* out_ranks, int64_t* out_capacity, ttals_stats* stats);
 
 /* Number of requests one batched launch runs at the same time on this device
- * (SMs x resident CTAs per SM): a batch of this size keeps every SM busy.  No
- * reference counterpart. */
+ * (SMs x resident CTAs per SM x solves per CTA, for the default launch
+ * variant): a batch of this size keeps every SM busy.  No reference
+ * counterpart. */
 int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
 
 /* Launch variant of the batched calls (ttals_sle_als_batch, ttals_solve_batch,
@@ -169,7 +170,8 @@ int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
  * request kinds, largest local system, stack and operator core) the first
  * batches try each candidate once (every one of them solves its batch in
  * full), later ones use the fastest by kernel time per solve.  Candidates,
- * mixed precision: 0 tensor-core kernel (one CTA per SM), 1 warp-MMA kernel
+ * mixed precision: 0 tensor-core kernel (one CTA per SM running two requests
+ * side by side, one per 256-thread group), 1 warp-MMA kernel
  * at full occupancy, 2 the same with one CTA per SM less; plain FP64: 0 full
  * occupancy, 1 one CTA per SM less.  -2 forgets every bucket's timings and
  * autotunes afresh.  No reference counterpart. */
@@ -177,14 +179,14 @@ int ttals_set_batch_variant(ttals_ctx* ctx, int32_t variant);
 
 /* Batched scikit_tt/solvers/sle.py:10 `als`: `count` independent systems
  * (each with its own order, mode sizes and ranks) solved in one launch, one
- * CTA per system.  out_data[j] receives system j's cores with the ranks
+ * CTA per system (one 256-thread group of a CTA on the tensor-core variant).  out_data[j] receives system j's cores with the ranks
  * ttals_als_ranks gives; all systems use `precision` and `tol`. */
 int ttals_sle_als_batch(ttals_ctx* ctx, int32_t count, const ttals_tt* ops, const ttals_tt* x0s,
                         const ttals_tt* rhss, const int32_t* repeats, int32_t precision, double tol,
                         double* const* out_data, int32_t out_on_device, ttals_stats* stats);
 
 /* Mixed batch of SLE and EVP requests (each `als` of sle.py:10 / evp.py:17),
- * one CTA per request, synchronous.  Outputs follow out_on_device. */
+ * one CTA (or CTA group) per request, synchronous.  Outputs follow out_on_device. */
 int ttals_solve_batch(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, int32_t precision, double tol,
                       int32_t out_on_device, ttals_stats* stats);
 

@@ -1580,6 +1580,7 @@ struct BatchPlan {
   int use_tc = 0;  // mixed precision on the tensor-core kernel variant
   int variant = 0;  // index into batch_candidates(prec)
   int per_sm = 1;   // resident CTAs per SM of the launch
+  int spc = 1;      // solves one CTA runs side by side
   double tol = 0.0;
   // byte layout of the device block: [regions | meta | inst | scratch | counter]
   size_t off_meta = 0, off_inst = 0, off_scratch = 0, off_next = 0, bytes = 0;
@@ -1747,7 +1748,8 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     require(e == cudaSuccess, TTALS_ERR_CUDA,
             std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
     P.per_sm = per_sm;
-    P.grid = std::min(count, c->num_sms * per_sm);
+    P.spc = batch_solves_per_cta(P.use_tc);
+    P.grid = std::min((count + P.spc - 1) / P.spc, c->num_sms * per_sm);
   }
   P.stride = batch_scratch_stride(P.z, kBatchM, kBatchMEvp);
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -1757,7 +1759,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
   P.off_inst = o;
   o += al(sizeof(BatchInst) * count);
   P.off_scratch = o;
-  o += (size_t)P.stride * P.grid;
+  o += (size_t)P.stride * P.grid * P.spc;  // one scratch slot per group of every CTA
   P.off_next = o;
   o += 256;
   P.bytes = o;
@@ -2636,7 +2638,8 @@ int ttals_batch_slots(ttals_ctx* c, int32_t* slots) {
   return guarded(c, [&] {
     require(slots != nullptr, TTALS_ERR_ARG, "null output pointer");
     cudaError_t e = cudaSuccess;
-    *slots = c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp, batch_tc_enabled(), &e);
+    const int tc = batch_tc_enabled();
+    *slots = c->num_sms * batch_blocks_per_sm(kBatchM, kBatchMEvp, tc, &e) * batch_solves_per_cta(tc);
     require(e == cudaSuccess, TTALS_ERR_CUDA,
             std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
   });

@@ -39,8 +39,11 @@ constexpr int kBatchThreads = 128;
 // latency behind (measured: +4 % over four CTAs per SM, with 5 x SMs requests)
 constexpr int kBatchMinBlocks = 5;
 // tensor-core variant: a kernel with tcgen05 instructions runs one CTA per
-// SM, which then owns the whole SM (kTcThreads threads, all TMEM columns)
-constexpr int kBatchThreadsTc = kTcThreads;
+// SM, which then owns the whole SM.  It runs two solves side by side, one per
+// 256-thread group (each with half of the TMEM columns, its own operand tiles
+// and named barriers), so that one solve's latency-bound phases (Krylov
+// vector loops, QR, waits on MMA completion) overlap the other's products.
+constexpr int kBatchThreadsTc = kGroupThreads * kGroups<true>;
 constexpr int kBatchMinBlocksTc = 1;
 
 // ---------------------------------------------------------------------------
@@ -51,6 +54,8 @@ constexpr int kBatchMinBlocksTc = 1;
 // TC: the kernel holds tensor memory and uses tcgen05.  A kernel that contains
 // any tcgen05 instruction runs one CTA per SM, so the paths without it are
 // separate instantiations (TC = false) free of tcgen05 code.
+// TC also selects the two-group form (every CTA routine below runs on the
+// calling group: gtid / gsize / gsync of ttals_device.cuh).
 template <typename T, bool TC = false>
 __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C,
                                                   int* ktab = nullptr, TcState* tc = nullptr) {
@@ -61,7 +66,7 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
     if constexpr (TC) {
       if (tc && ktab) {
         const bool done = cta_gemm_tf32_tc(c, A, B, C, ktab, *tc);
-        if (threadIdx.x == 0) {
+        if (gtid<TC>() == 0) {
           if (done)
             ++tc->gemms;
           else
@@ -70,20 +75,20 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
         if (done) return;
       }
     }
-    if (ktab && cta_gemm_tf32x3(c, A, B, C, ktab)) return;
+    if (ktab && cta_gemm_tf32x3<TC>(c, A, B, C, ktab)) return;
   }
   constexpr int VW = DefaultVW<T>::value;
   if (contract_vec_ok<T, VW>(c, B, C)) {
-    for (int64_t e = (int64_t)threadIdx.x * VW; e < c.total; e += (int64_t)blockDim.x * VW)
+    for (int64_t e = (int64_t)gtid<TC>() * VW; e < c.total; e += (int64_t)gsize<TC>() * VW)
       contract_vec_elem<T, VW>(c, A, B, C, e);
   } else {
-    for (int64_t e = threadIdx.x; e < c.total; e += blockDim.x) {
+    for (int64_t e = gtid<TC>(); e < c.total; e += gsize<TC>()) {
       int64_t ao, bo, co;
       contract_offsets(c, e, ao, bo, co);
       C[co] = contract_sum(c, A, B, ao, bo);
     }
   }
-  __syncthreads();
+  gsync<TC>();
 }
 
 // FP64 contraction; with `oz` set, GEMM-shaped ones run as emulated FP64 on the
@@ -91,13 +96,14 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
 template <bool TC>
 __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const double* A, const double* B, double* C,
                                               const OzScratch* oz) {
-  __shared__ Contraction sc;
-  if (threadIdx.x == 0) sc = cref;
-  __syncthreads();
+  __shared__ Contraction sc_g[kGroups<TC>];
+  Contraction& sc = sc_g[gidx<TC>()];
+  if (gtid<TC>() == 0) sc = cref;
+  gsync<TC>();
   if constexpr (TC) {
     if (oz && oz->tc) {
       const bool done = cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc);
-      if (threadIdx.x == 0) {
+      if (gtid<TC>() == 0) {
         if (done)
           ++oz->tc->gemms;
         else
@@ -108,18 +114,19 @@ __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const dou
   } else {
     if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
   }
-  cta_contract_body<double>(sc, A, B, C);
+  cta_contract_body<double, TC>(sc, A, B, C);
 }
 
 // Out-of-line version for the per-site bookkeeping (stacks, pushes): keeps the
 // register pressure of the instance driver low.  The descriptor is copied to
 // shared memory so that stores to C cannot alias it.
-template <typename T>
+template <typename T, bool G = false>
 __device__ __noinline__ void cta_contract(const Contraction& cref, const T* A, const T* B, T* C) {
-  __shared__ Contraction sc;
-  if (threadIdx.x == 0) sc = cref;
-  __syncthreads();
-  cta_contract_body<T>(sc, A, B, C);
+  __shared__ Contraction sc_g[kGroups<G>];
+  Contraction& sc = sc_g[gidx<G>()];
+  if (gtid<G>() == 0) sc = cref;
+  gsync<G>();
+  cta_contract_body<T, G>(sc, A, B, C);
 }
 
 // Out-of-line FP32 contraction of the inner Krylov apply: one copy of the
@@ -128,35 +135,41 @@ __device__ __noinline__ void cta_contract(const Contraction& cref, const T* A, c
 template <bool TC>
 __device__ __noinline__ void cta_contract_f32(const Contraction& cref, const float* A, const float* B, float* C,
                                               int* ktab, TcState* tc) {
-  __shared__ Contraction sc;
-  if (threadIdx.x == 0) sc = cref;
-  __syncthreads();
+  __shared__ Contraction sc_g[kGroups<TC>];
+  Contraction& sc = sc_g[gidx<TC>()];
+  if (gtid<TC>() == 0) sc = cref;
+  gsync<TC>();
   cta_contract_body<float, TC>(sc, A, B, C, ktab, tc);
 }
 
+template <bool G = false>
 __device__ __forceinline__ void cta_fill(double* p, int64_t n, double v) {
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = v;
-  __syncthreads();
+  for (int64_t i = gtid<G>(); i < n; i += gsize<G>()) p[i] = v;
+  gsync<G>();
 }
+template <bool G = false>
 __device__ __forceinline__ void cta_copy(double* d, const double* s, int64_t n) {
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
-  __syncthreads();
+  for (int64_t i = gtid<G>(); i < n; i += gsize<G>()) d[i] = s[i];
+  gsync<G>();
 }
+template <bool G = false>
 __device__ __forceinline__ void cta_to_float(float* d, const double* s, int64_t n) {
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = (float)s[i];
-  __syncthreads();
+  for (int64_t i = gtid<G>(); i < n; i += gsize<G>()) d[i] = (float)s[i];
+  gsync<G>();
 }
 
-// sum over the CTA, returned to every thread
+// sum over the CTA (the group), returned to every thread
+template <bool G = false>
 __device__ __forceinline__ double cta_sum(double v) {
-  __shared__ double red[32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ double red_g[kGroups<G>][32];
+  double* red = red_g[gidx<G>()];
+  const int lane = gtid<G>() & 31, warp = gtid<G>() >> 5, nw = gsize<G>() >> 5;
   v = warp_sum(v);
   if (lane == 0) red[warp] = v;
-  __syncthreads();
+  gsync<G>();
   double s = 0.0;
   for (int w = 0; w < nw; ++w) s += red[w];
-  __syncthreads();
+  gsync<G>();
   return s;
 }
 
@@ -164,9 +177,9 @@ __device__ __forceinline__ double cta_sum(double v) {
 // Dots accumulate in the vectors' own precision (FP32 for the inner solver:
 // its Gram-Schmidt only needs inner-solver accuracy, and FP64 arithmetic is
 // 57x slower on this part); lane partial sums keep the rounding error ~sqrt(N).
-template <typename T>
+template <typename T, bool G = false>
 __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const T* w, double* out) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = gtid<G>() & 31, warp = gtid<G>() >> 5, nw = gsize<G>() >> 5;
   for (int kk = warp; kk <= nvec; kk += nw) {
     const T* xv = (kk < nvec) ? V + (int64_t)kk * N : w;
     T s0 = T(0), s1 = T(0);
@@ -180,7 +193,7 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
     s = warp_sum(s);
     if (lane == 0) out[kk] = s;
   }
-  __syncthreads();
+  gsync<G>();
 }
 
 // The same with every thread of the CTA: each thread keeps a partial sum per
@@ -188,10 +201,12 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
 // then over warps.  For the one-CTA-per-SM tensor-core kernel, where no
 // sibling CTA hides memory latency; nvec <= kWideDotsMax.
 constexpr int kWideDotsMax = 64;
-template <typename T>
+template <typename T, bool G = false>
 __device__ __noinline__ void cta_dots_wide(const T* V, int64_t N, int nvec, const T* w, double* out) {
-  __shared__ double part[32][kWideDotsMax + 1];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  constexpr int kWarps = G ? kGroupThreads / 32 : 32;
+  __shared__ double part_g[kGroups<G>][kWarps][kWideDotsMax + 1];
+  double(*part)[kWideDotsMax + 1] = part_g[gidx<G>()];
+  const int tid = gtid<G>(), nt = gsize<G>(), lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   for (int kk = 0; kk <= nvec; ++kk) {
     const T* xv = (kk < nvec) ? V + (int64_t)kk * N : w;
     T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
@@ -207,13 +222,13 @@ __device__ __noinline__ void cta_dots_wide(const T* V, int64_t N, int nvec, cons
     sd = warp_sum(sd);
     if (lane == 0) part[warp][kk] = sd;
   }
-  __syncthreads();
+  gsync<G>();
   for (int kk = tid; kk <= nvec; kk += nt) {
     double t = 0.0;
     for (int q = 0; q < nw; ++q) t += part[q][kk];
     out[kk] = t;
   }
-  __syncthreads();
+  gsync<G>();
 }
 
 // y -> out = M y (three contraction phases through T1, T2)
@@ -226,9 +241,9 @@ __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contracti
     cta_contract_f32<TC>(p2, T1, A, T2, ktab, tc);
     cta_contract_f32<TC>(p3, T2, R, out, ktab, tc);
   } else {
-    cta_contract_body(p1, L, y, T1, ktab);
-    cta_contract_body(p2, T1, A, T2, ktab);
-    cta_contract_body(p3, T2, R, out, ktab);
+    cta_contract_body<T, TC>(p1, L, y, T1, ktab);
+    cta_contract_body<T, TC>(p2, T1, A, T2, ktab);
+    cta_contract_body<T, TC>(p3, T2, R, out, ktab);
   }
 }
 
@@ -256,27 +271,30 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
   double* yv = gv + m + 1;       // m
   double* h1 = yv + m;           // m+2
   double* h2 = h1 + m + 2;       // m+2
-  __shared__ double s_res;
-  __shared__ int s_flag;
-  __shared__ float s_cf[kWideDotsMax + 2];  // Gram-Schmidt / correction coefficients in TI (TC path)
-  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ double s_res_g[kGroups<TC>];
+  __shared__ int s_flag_g[kGroups<TC>];
+  __shared__ float s_cf_g[kGroups<TC>][kWideDotsMax + 2];  // Gram-Schmidt / correction coefficients in TI (TC path)
+  double& s_res = s_res_g[gidx<TC>()];
+  int& s_flag = s_flag_g[gidx<TC>()];
+  float* s_cf = s_cf_g[gidx<TC>()];
+  const int tid = gtid<TC>(), nt = gsize<TC>();
   CtaSolveStats out{1.0, 0, 0, ST_OK};
   // the tensor-core kernel runs one CTA per SM: its vector loops use every
   // thread, keep several loads in flight and avoid per-element FP64 work
   constexpr bool kWide = TC && std::is_same<TI, float>::value;
   auto dots = [&](int nv, const TI* wv, double* o) {
     if constexpr (kWide)
-      cta_dots_wide<TI>(V, N, nv, wv, o);
+      cta_dots_wide<TI, TC>(V, N, nv, wv, o);
     else
-      cta_dots<TI>(V, N, nv, wv, o);
+      cta_dots<TI, TC>(V, N, nv, wv, o);
   };
 
   double fs = 0.0;
   for (int64_t e = tid; e < N; e += nt) fs += f[e] * f[e];
-  const double fnorm = sqrt(cta_sum(fs));
+  const double fnorm = sqrt(cta_sum<TC>(fs));
   if (!(fnorm > 0.0)) {
     for (int64_t e = tid; e < N; e += nt) x[e] = 0.0;
-    __syncthreads();
+    gsync<TC>();
     out.rel = 0.0;
     if (!(fnorm == 0.0)) out.status = ST_NONFINITE;
     return out;
@@ -295,8 +313,8 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         rs += re * re;
       }
     } else {
-      cta_contract_body(p1, L64, (const double*)x, T1_64);
-      cta_contract_body(p2, (const double*)T1_64, A64, T2_64);
+      cta_contract_body<double, TC>(p1, L64, (const double*)x, T1_64);
+      cta_contract_body<double, TC>(p2, (const double*)T1_64, A64, T2_64);
       for (int64_t e = tid; e < N; e += nt) {
         int64_t ao, bo, co;
         contract_offsets(p3, e, ao, bo, co);
@@ -305,7 +323,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         rs += re * re;
       }
     }
-    const double rho = sqrt(cta_sum(rs));
+    const double rho = sqrt(cta_sum<TC>(rs));
     *cyc_res += clock64() - c0;
     const long long c1 = clock64();
     out.rel = rho / fnorm;
@@ -322,7 +340,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       gv[0] = 1.0;
       for (int i = 1; i <= m; ++i) gv[i] = 0.0;
     }
-    __syncthreads();
+    gsync<TC>();
     int jj = 0;
     for (int j = 0; j < m; ++j) {
       const long long ca0 = clock64();
@@ -348,7 +366,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
           TI* vn = V + (int64_t)(j + 1) * N;
           if constexpr (kWide) {
             for (int q = tid; q <= j; q += nt) s_cf[q] = (float)h1[q];
-            __syncthreads();
+            gsync<TC>();
             for (int64_t e = tid; e < N; e += nt) {
               TI acc = w[e];
 #pragma unroll 4
@@ -369,7 +387,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
           for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
           w[e] = acc;
         }
-        __syncthreads();
+        gsync<TC>();
         dots(j + 1, w, h2);
         hn2 = h2[j + 1];
         for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
@@ -409,7 +427,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         s_res = fabs(gv[j + 1]);
         s_flag = (hn <= 1e-300) ? 1 : 0;
       }
-      __syncthreads();
+      gsync<TC>();
       jj = j + 1;
       ++out.inner;
       if (s_res <= target || s_flag) break;
@@ -429,7 +447,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       }
       s_flag = bad;
     }
-    __syncthreads();
+    gsync<TC>();
     if (s_flag) {
       out.status = ST_SINGULAR;
       return out;
@@ -438,7 +456,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       // the correction V y is FP32-accurate by construction: sum it in FP32,
       // one FP64 FMA per element adds it to the FP64 solution
       for (int q = tid; q < jj; q += nt) s_cf[q] = (float)yv[q];
-      __syncthreads();
+      gsync<TC>();
       for (int64_t e = tid; e < N; e += nt) {
         float acc = 0.f;
 #pragma unroll 4
@@ -452,7 +470,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         x[e] += rho * acc;
       }
     }
-    __syncthreads();
+    gsync<TC>();
     *cyc_inner += clock64() - c1;
   }
   return out;
@@ -471,7 +489,7 @@ struct CtaEigStats {
 // TI: arithmetic of the operator, basis and products (double, or float for
 // the first stage of the mixed-precision eigensolve).  x (in: start vector,
 // out: Ritz vector) and all scalars stay FP64.
-template <typename TI>
+template <typename TI, bool G = false>
 __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                                const TI* L, const TI* A, const TI* R, TI* T1, TI* T2, double* x,
                                                TI* V, TI* w, int64_t N, int m, int mode, double sigma,
@@ -483,9 +501,12 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   double* z = h2 + m + 2;
   double* twk = z + m;
   int* piv = (int*)(twk + 5 * m + 8);
-  __shared__ double s_theta, s_res;
-  __shared__ int s_conv;
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ double s_theta_g[kGroups<G>], s_res_g[kGroups<G>];
+  __shared__ int s_conv_g[kGroups<G>];
+  double& s_theta = s_theta_g[gidx<G>()];
+  double& s_res = s_res_g[gidx<G>()];
+  int& s_conv = s_conv_g[gidx<G>()];
+  const int tid = gtid<G>(), nt = gsize<G>(), lane = tid & 31, warp = tid >> 5;
   CtaEigStats out{0.0, 0.0, 0, 0, ST_OK};
   if (tid == 0) {
     s_conv = 0;
@@ -494,23 +515,23 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   }
   double xs = 0.0;
   for (int64_t e = tid; e < N; e += nt) xs += x[e] * x[e];
-  const double xn = sqrt(cta_sum(xs));
+  const double xn = sqrt(cta_sum<G>(xs));
   const bool ok = xn > 0.0 && isfinite(xn);
   for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(ok ? x[e] / xn : 1.0 / sqrt((double)N));
-  __syncthreads();
+  gsync<G>();
   const int mm = (int)(N < m ? N : m);
   for (;;) {
     int nT = 0;
     for (int j = 0; j < mm; ++j) {
-      cta_apply<TI>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
-      cta_dots<TI>(V, N, j + 1, w, h1);
+      cta_apply<TI, G>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
+      cta_dots<TI, G>(V, N, j + 1, w, h1);
       for (int64_t e = tid; e < N; e += nt) {
         double acc = (double)w[e];
         for (int q = 0; q <= j; ++q) acc -= h1[q] * (double)V[(int64_t)q * N + e];
         w[e] = (TI)acc;
       }
-      __syncthreads();
-      cta_dots<TI>(V, N, j + 1, w, h2);
+      gsync<G>();
+      cta_dots<TI, G>(V, N, j + 1, w, h2);
       double b2 = h2[j + 1];
       for (int q = 0; q <= j; ++q) b2 -= h2[q] * h2[q];
       const double bj = sqrt(fmax(b2, 0.0));
@@ -527,7 +548,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
           vn[e] = (TI)(acc * inv);
         }
       }
-      __syncthreads();
+      gsync<G>();
       ++out.its;
       nT = j + 1;
       double tnorm = 0.0;
@@ -564,7 +585,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
             s_conv = (s_res <= tol) || breakdown;
           }
         }
-        __syncthreads();
+        gsync<G>();
         if (s_conv || nT == mm) break;
       } else if (breakdown) {
         break;
@@ -576,14 +597,14 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
       for (int l = 0; l < nT; ++l) acc += z[l] * (double)V[(int64_t)l * N + e];
       x[e] = acc;
     }
-    __syncthreads();
+    gsync<G>();
     if (s_conv || out.restarts >= max_restarts) break;
     ++out.restarts;
     double s2 = 0.0;
     for (int64_t e = tid; e < N; e += nt) s2 += x[e] * x[e];
-    const double nrm = sqrt(cta_sum(s2));
+    const double nrm = sqrt(cta_sum<G>(s2));
     for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(nrm > 0.0 ? x[e] / nrm : 1.0 / sqrt((double)N));
-    __syncthreads();
+    gsync<G>();
   }
   out.theta = s_theta;
   out.res = s_res;
@@ -591,17 +612,19 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   return out;
 }
 
-__device__ __noinline__ void cta_qr(const QrArgs& q) { cta_householder_qr(q); }
+template <bool G = false>
+__device__ __noinline__ void cta_qr(const QrArgs& q) { cta_householder_qr<G>(q); }
 
 // Make this request's outputs visible to the host and to copy engines, then
 // raise its completion flag (host-mapped memory).
+template <bool G = false>
 __device__ __forceinline__ void signal_done(int* flag) {
-  __syncthreads();
-  if (threadIdx.x == 0 && flag) {
+  gsync<G>();
+  if (gtid<G>() == 0 && flag) {
     __threadfence_system();
     asm volatile("st.release.sys.global.s32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
   }
-  __syncthreads();
+  gsync<G>();
 }
 
 // ---------------------------------------------------------------------------
@@ -675,10 +698,11 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   const int64_t* Rt_off = L_off + d;
   const int64_t* Lb_off = Rt_off + d;
   const int64_t* Rb_off = Lb_off + d;
-  __shared__ int64_t r[kMaxOrderB + 1];
-  for (int i = threadIdx.x; i <= d; i += blockDim.x) r[i] = cap[i];
-  __syncthreads();
-  const int tid = threadIdx.x;
+  __shared__ int64_t r_g[kGroups<TC>][kMaxOrderB + 1];
+  int64_t* r = r_g[gidx<TC>()];
+  const int tid = gtid<TC>();
+  for (int i = tid; i <= d; i += gsize<TC>()) r[i] = cap[i];
+  gsync<TC>();
   auto X = [&](int i) { return I.X + X_off[i]; };
   auto L = [&](int i) { return I.L + L_off[i]; };
   auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
@@ -717,15 +741,15 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_qr(q);
+      cta_qr<TC>(q);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
-      cta_contract(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
+      cta_contract<double, TC>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
       cur = outb;
       cur_left = rx0[i - 1];
       cur_right = k;
     }
-    cta_copy(X(0), cur, n[0] * cur_right);
+    cta_copy<TC>(X(0), cur, n[0] * cur_right);
   }
   lap(0);
 
@@ -735,7 +759,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         Rt(i)[0] = 1.0;
         Rb(i)[0] = 1.0;
       }
-      __syncthreads();
+      gsync<TC>();
       return;
     }
     const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
@@ -746,8 +770,8 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     cta_contract_f64<TC>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
     cta_contract_f64<TC>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
-    cta_contract(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
-    cta_contract(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
+    cta_contract<double, TC>(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
+    cta_contract<double, TC>(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
     lap(1);
   };
   auto left = [&](int i) {
@@ -756,7 +780,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         L(i)[0] = 1.0;
         Lb(i)[0] = 1.0;
       }
-      __syncthreads();
+      gsync<TC>();
       return;
     }
     const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
@@ -767,14 +791,14 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     cta_contract_f64<TC>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
     cta_contract_f64<TC>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
-    cta_contract(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
-    cta_contract(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
+    cta_contract<double, TC>(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
+    cta_contract<double, TC>(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
     lap(1);
   };
   auto solve = [&](int i) {
     const int64_t aa = r[i], nn = n[i], ss = r[i + 1], N = aa * nn * ss;
-    cta_contract(desc_vec_u_left(aa, nn, rb[i], rb[i + 1]), (const double*)Lb(i), B(i), S.U);
-    cta_contract(desc_micro_f(aa, nn, ss, rb[i + 1]), (const double*)S.U, (const double*)Rb(i), S.f);
+    cta_contract<double, TC>(desc_vec_u_left(aa, nn, rb[i], rb[i + 1]), (const double*)Lb(i), B(i), S.U);
+    cta_contract<double, TC>(desc_micro_f(aa, nn, ss, rb[i + 1]), (const double*)S.U, (const double*)Rb(i), S.f);
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
     const int m = (int)(N < a.m ? N : a.m);
@@ -782,13 +806,13 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     lap(2);
     long long cr = 0, ci = 0, capp = 0;
     if (a.prec == 1) {
-      cta_to_float(S.Lf, L(i), aa * R[i] * aa);
-      cta_to_float(S.Rf, Rt(i), ss * R[i + 1] * ss);
-      cta_to_float(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
+      cta_to_float<TC>(S.Lf, L(i), aa * R[i] * aa);
+      cta_to_float<TC>(S.Rf, Rt(i), ss * R[i + 1] * ss);
+      cta_to_float<TC>(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
       st = cta_gmres_ir<float, TC>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
                                S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm, &S.oz, &cr, &ci, &capp);
     } else {
-      st = cta_gmres_ir<double, false>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
+      st = cta_gmres_ir<double, TC>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
                                 S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm, nullptr, &cr, &ci, &capp);
     }
     ph[3] += cr;
@@ -820,13 +844,13 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_qr(q);
+        cta_qr<TC>(q);
         fl64 += qr_fl((double)(aa * nn), (double)ss);
         const int64_t qq = n[i + 1] * r[i + 2];
-        cta_contract(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
-        cta_copy(X(i + 1), S.tmp0, k * qq);
+        cta_contract<double, TC>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
+        cta_copy<TC>(X(i + 1), S.tmp0, k * qq);
         if (tid == 0) r[i + 1] = k;
-        __syncthreads();
+        gsync<TC>();
         lap(5);
       }
     }
@@ -836,13 +860,13 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_qr(q);
+        cta_qr<TC>(q);
         fl64 += qr_fl((double)ns, (double)aa);
         const int64_t p = r[i - 1] * n[i - 1];
-        cta_contract(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
-        cta_copy(X(i - 1), S.tmp0, p * k);
+        cta_contract<double, TC>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
+        cta_copy<TC>(X(i - 1), S.tmp0, p * k);
         if (tid == 0) r[i] = k;
-        __syncthreads();
+        gsync<TC>();
         lap(5);
       }
     }
@@ -851,7 +875,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   int64_t off = 0;
   for (int i = 0; i < d; ++i) {
     const int64_t cnt = r[i] * n[i] * r[i + 1];
-    for (int64_t e = tid; e < cnt; e += blockDim.x) I.out[off + e] = X(i)[e];
+    for (int64_t e = tid; e < cnt; e += gsize<TC>()) I.out[off + e] = X(i)[e];
     off += cnt;
   }
   if (tid == 0) {
@@ -871,13 +895,14 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     I.report[19 + d] = S.oz.tc ? (double)(S.oz.tc->fallbacks - fb0) : 0.0;
     I.report[20 + d] = (double)inner_apply;
   }
-  signal_done(I.done);
+  signal_done<TC>(I.done);
 }
 
 // ---------------------------------------------------------------------------
 // one eigenproblem instance (evp.py:17-179, symmetric, number_ev == 1)
 // ---------------------------------------------------------------------------
 
+template <bool G = false>
 __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch& S, double* sm) {
   const BatchInst& I = a.inst[j];
   const int d = I.d;
@@ -892,11 +917,13 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   const int64_t* X_off = x0_off + d;
   const int64_t* L_off = X_off + d;
   const int64_t* Rt_off = L_off + d;
-  __shared__ int64_t r[kMaxOrderB + 1];
-  __shared__ int64_t ropt[kMaxOrderB + 1];
-  for (int i = threadIdx.x; i <= d; i += blockDim.x) r[i] = cap[i];
-  __syncthreads();
-  const int tid = threadIdx.x;
+  __shared__ int64_t r_g[kGroups<G>][kMaxOrderB + 1];
+  __shared__ int64_t ropt_g[kGroups<G>][kMaxOrderB + 1];
+  int64_t* r = r_g[gidx<G>()];
+  int64_t* ropt = ropt_g[gidx<G>()];
+  const int tid = gtid<G>();
+  for (int i = tid; i <= d; i += gsize<G>()) r[i] = cap[i];
+  gsync<G>();
   auto X = [&](int i) { return I.X + X_off[i]; };
   auto Xo = [&](int i) { return I.Xopt + X_off[i]; };
   auto L = [&](int i) { return I.L + L_off[i]; };
@@ -913,42 +940,42 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_qr(q);
+      cta_qr<G>(q);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
-      cta_contract(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
+      cta_contract<double, G>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
       cur = outb;
       cur_left = rx0[i - 1];
       cur_right = k;
     }
-    cta_copy(X(0), cur, n[0] * cur_right);
+    cta_copy<G>(X(0), cur, n[0] * cur_right);
   }
   auto right = [&](int i) {
     if (i == d - 1) {
       if (tid == 0) Rt(i)[0] = 1.0;
-      __syncthreads();
+      gsync<G>();
       return;
     }
     const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
     Contraction q1, q2, q3;
     desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
-    cta_contract(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1);
-    cta_contract(q2, (const double*)S.T1, A(i + 1), S.T2);
-    cta_contract(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i));
+    cta_contract<double, G>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1);
+    cta_contract<double, G>(q2, (const double*)S.T1, A(i + 1), S.T2);
+    cta_contract<double, G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i));
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
   };
   auto left = [&](int i) {
     if (i == 0) {
       if (tid == 0) L(i)[0] = 1.0;
-      __syncthreads();
+      gsync<G>();
       return;
     }
     const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
-    cta_contract(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1);
-    cta_contract(p2, (const double*)S.T1, A(i - 1), S.T2);
-    cta_contract(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i));
+    cta_contract<double, G>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1);
+    cta_contract<double, G>(p2, (const double*)S.T1, A(i - 1), S.T2);
+    cta_contract<double, G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i));
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
   };
   auto solve = [&](int i) {
@@ -960,7 +987,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     // Eigen solves stay FP64 in both precision modes: warm-started from the
     // previous sweep's core, FP64 Lanczos converges in ~12 steps per site, and
     // an FP32 Lanczos pre-stage (then FP64 polish) measured 2.8x slower.
-    const CtaEigStats st = cta_lanczos<double>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m,
+    const CtaEigStats st = cta_lanczos<double, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m,
                                                I.mode, I.sigma, kBatchEvpRestarts, a.tol_evp, sm);
     theta = st.theta;
     nits += st.its;
@@ -982,12 +1009,12 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_qr(q);
+        cta_qr<G>(q);
         const int64_t qq = n[i + 1] * r[i + 2];
-        cta_contract(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
-        cta_copy(X(i + 1), S.tmp0, k * qq);
+        cta_contract<double, G>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
+        cta_copy<G>(X(i + 1), S.tmp0, k * qq);
         if (tid == 0) r[i + 1] = k;
-        __syncthreads();
+        gsync<G>();
       }
     }
     for (int i = d - 1; i >= 0; --i) {
@@ -996,12 +1023,12 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_qr(q);
+        cta_qr<G>(q);
         const int64_t p = r[i - 1] * n[i - 1];
-        cta_contract(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
-        cta_copy(X(i - 1), S.tmp0, p * k);
+        cta_contract<double, G>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
+        cta_copy<G>(X(i - 1), S.tmp0, p * k);
         if (tid == 0) r[i] = k;
-        __syncthreads();
+        gsync<G>();
       }
     }
     ++it;
@@ -1009,9 +1036,9 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     if (fabs(lam - I.sigma) < fabs(val_opt - I.sigma)) {
       val_opt = lam;
       have_opt = true;
-      for (int i = 0; i < d; ++i) cta_copy(Xo(i), X(i), r[i] * n[i] * r[i + 1]);
-      for (int i = tid; i <= d; i += blockDim.x) ropt[i] = r[i];
-      __syncthreads();
+      for (int i = 0; i < d; ++i) cta_copy<G>(Xo(i), X(i), r[i] * n[i] * r[i + 1]);
+      for (int i = tid; i <= d; i += gsize<G>()) ropt[i] = r[i];
+      gsync<G>();
     }
     double diff = 0.0;
     const int nl = nh < 3 ? nh : 3;
@@ -1024,7 +1051,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   int64_t off = 0;
   for (int i = 0; i < d; ++i) {
     const int64_t cnt = have_opt ? ropt[i] * n[i] * ropt[i + 1] : 0;
-    for (int64_t e = tid; e < cnt; e += blockDim.x) I.out[off + e] = Xo(i)[e];
+    for (int64_t e = tid; e < cnt; e += gsize<G>()) I.out[off + e] = Xo(i)[e];
     off += cnt;
   }
   if (tid == 0) {
@@ -1043,66 +1070,89 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     I.report[19 + d] = 0.0;
     I.report[20 + d] = 0.0;
   }
-  signal_done(I.done);
+  signal_done<G>(I.done);
 }
 
-// Take the CTA's tensor memory and set up its completion barrier (all threads).
-__device__ __forceinline__ void tc_begin(TcState& tc, unsigned char* tiles) {
-  if ((threadIdx.x >> 5) == 0) umma::tmem_alloc(&tc.tmem, kTcTmemCols);
-  if (threadIdx.x == 0) {
-    tc.tiles = tiles;
-    tc.phase = 0;
-    tc.status = ST_OK;
-    tc.gemms = 0;
-    tc.fallbacks = 0;
-    umma::mbar_init(&tc.bar, 1);
+// Take the CTA's tensor memory (all threads of the CTA): warp 0 allocates the
+// SM's 512 columns once, each of the `groups` groups gets kTcTmemCols of them
+// and its own completion barrier and operand tiles (tiles + g * tile_stride).
+__device__ __forceinline__ void tc_begin(TcState* tc, int groups, unsigned char* tiles, size_t tile_stride) {
+  __shared__ uint32_t s_tmem;
+  if ((threadIdx.x >> 5) == 0) umma::tmem_alloc(&s_tmem, kTcCtaTmemCols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (threadIdx.x < (unsigned)groups) {
+    TcState& t = tc[threadIdx.x];
+    t.tmem = s_tmem + kTcTmemCols * threadIdx.x;  // column offset in the low half
+    t.tiles = tiles + tile_stride * threadIdx.x;
+    t.phase = 0;
+    t.status = ST_OK;
+    t.gemms = 0;
+    t.fallbacks = 0;
+    umma::mbar_init(&t.bar, 1);
   }
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
 }
 
-// Hand the tensor memory back (all threads).  A completion wait that gave up
-// leaves MMAs possibly in flight: wait for them once more (bounded) first.
-__device__ __forceinline__ void tc_end(TcState& tc) {
-  if (tc.status != ST_OK) umma::mbar_wait(&tc.bar, tc.phase);
+// Hand the tensor memory back (all threads of the CTA, after every group is
+// done).  A completion wait that gave up leaves MMAs possibly in flight: wait
+// for them once more (bounded) first.
+__device__ __forceinline__ void tc_end(TcState* tc, int groups) {
+  if (threadIdx.x < (unsigned)groups && tc[threadIdx.x].status != ST_OK)
+    umma::mbar_wait(&tc[threadIdx.x].bar, tc[threadIdx.x].phase);
   umma::fence_before_sync();
   __syncthreads();
-  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(tc.tmem, kTcTmemCols);
+  umma::fence_after_sync();
+  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(tc[0].tmem, kTcCtaTmemCols);
 }
 
 __host__ __device__ inline size_t tc_tiles_offset(size_t before) { return (before + 1023) / 1024 * 1024; }
 
-// The persistent loop of both kernel variants.  With UseTc the CTA holds
-// kTcTmemCols columns of tensor memory for its whole life (allocated here,
-// released on the way out whatever happened) and a 64 KB operand-tile region
-// of shared memory; its GEMM-shaped FP32 and emulated-FP64 contractions then
-// run on tcgen05.
+// Dynamic shared memory of one group: GMRES / Lanczos scalars, the
+// contraction-offset table, and (tensor-core variant) the operand tiles.
+__host__ __device__ size_t batch_group_smem_bytes(int m, int m_evp, int use_tc) {
+  const size_t base = batch_smem_scalar_bytes(m, m_evp) + sizeof(int) * 2 * kTcMaxK;
+  return use_tc ? tc_tiles_offset(base) + kTcSmemBytes : base;
+}
+
+// The persistent loop of both kernel variants.  Each group (the whole CTA, or
+// each of the tensor-core kernel's two) takes requests from the work counter
+// and solves them with its own scratch slot and shared-memory region.  With
+// UseTc the CTA holds all TMEM columns for its whole life (allocated here,
+// released on the way out whatever happened); its GEMM-shaped FP32 and
+// emulated-FP64 contractions then run on tcgen05.
 template <bool UseTc>
 __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
   extern __shared__ __align__(1024) unsigned char smraw[];
-  double* sm = reinterpret_cast<double*>(smraw);
-  __shared__ int s_j;
-  __shared__ TcState s_tc;
-  Scratch S = scratch_of(a, blockIdx.x);
+  constexpr int NG = kGroups<UseTc>;
+  __shared__ int s_j[NG];
+  __shared__ TcState s_tc[NG];
+  const int g = gidx<UseTc>();
+  const size_t gbytes = batch_group_smem_bytes(a.m, a.m_evp, UseTc ? 1 : 0);
+  unsigned char* mine = smraw + gbytes * g;
+  double* sm = reinterpret_cast<double*>(mine);
+  Scratch S = scratch_of(a, (int)blockIdx.x * NG + g);
   const size_t scal = batch_smem_scalar_bytes(a.m, a.m_evp);
-  S.oz.ktab = reinterpret_cast<int*>(smraw + scal);
+  S.oz.ktab = reinterpret_cast<int*>(mine + scal);
   if constexpr (UseTc) {
-    tc_begin(s_tc, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK));
-    S.oz.tc = &s_tc;
+    tc_begin(s_tc, NG, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK), gbytes);
+    S.oz.tc = &s_tc[g];
   }
   for (;;) {
-    if (threadIdx.x == 0) s_j = atomicAdd(a.next, 1);
-    __syncthreads();
-    const int j = s_j;
-    __syncthreads();
+    if (gtid<UseTc>() == 0) s_j[g] = atomicAdd(a.next, 1);
+    gsync<UseTc>();
+    const int j = s_j[g];
+    gsync<UseTc>();
     if (j >= a.count) break;
     if (a.inst[j].kind == 1)
-      batch_evp(a, j, S, sm);
+      batch_evp<UseTc>(a, j, S, sm);
     else
       batch_solve<UseTc>(a, j, S, sm);
   }
-  if constexpr (UseTc) tc_end(s_tc);
+  if constexpr (UseTc) tc_end(s_tc, NG);
 }
 
 // plain FP64 (and mixed without tensor memory): 128 threads, five CTAs per SM
@@ -1141,8 +1191,8 @@ __global__ void __launch_bounds__(kBatchThreads) apply_f64emu_kernel(Contraction
   cta_contract_f64<false>(p3, T2, R, out, &oz);
 }
 
-// The same on tcgen05 (256 threads, the batch kernel's tensor-core GEMMs).
-__global__ void __launch_bounds__(kBatchThreadsTc) apply_f64emu_tc_kernel(Contraction p1, Contraction p2,
+// The same on tcgen05 (one 256-thread group, the batch kernel's tensor-core GEMMs).
+__global__ void __launch_bounds__(kGroupThreads) apply_f64emu_tc_kernel(Contraction p1, Contraction p2,
                                                                           Contraction p3, const double* L,
                                                                           const double* A, const double* R,
                                                                           const double* y, double* T1, double* T2,
@@ -1150,12 +1200,12 @@ __global__ void __launch_bounds__(kBatchThreadsTc) apply_f64emu_tc_kernel(Contra
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ TcState s_tc;
   oz.ktab = reinterpret_cast<int*>(smraw);
-  tc_begin(s_tc, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK));
+  tc_begin(&s_tc, 1, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK), 0);
   oz.tc = &s_tc;
   cta_contract_f64<true>(p1, L, y, T1, &oz);
   cta_contract_f64<true>(p2, T1, A, T2, &oz);
   cta_contract_f64<true>(p3, T2, R, out, &oz);
-  tc_end(s_tc);
+  tc_end(&s_tc, 1);
 }
 
 size_t apply_f64emu_scratch_bytes(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
@@ -1193,7 +1243,7 @@ cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int
     const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + kTcSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(apply_f64emu_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    apply_f64emu_tc_kernel<<<1, kBatchThreadsTc, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
+    apply_f64emu_tc_kernel<<<1, kGroupThreads, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
   } else {
     apply_f64emu_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
   }
@@ -1209,17 +1259,17 @@ __global__ void __launch_bounds__(kBatchThreads) apply_f32_kernel(Contraction p1
   cta_apply<float>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
 }
 
-// The same on tcgen05 (3xTF32, 256 threads).
-__global__ void __launch_bounds__(kBatchThreadsTc) apply_f32_tc_kernel(Contraction p1, Contraction p2, Contraction p3,
+// The same on tcgen05 (3xTF32, one 256-thread group).
+__global__ void __launch_bounds__(kGroupThreads) apply_f32_tc_kernel(Contraction p1, Contraction p2, Contraction p3,
                                                                        const float* L, const float* A, const float* R,
                                                                        const float* y, float* T1, float* T2,
                                                                        float* out) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ TcState s_tc;
   int* ktab = reinterpret_cast<int*>(smraw);
-  tc_begin(s_tc, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK));
+  tc_begin(&s_tc, 1, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK), 0);
   cta_apply<float, true>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab, &s_tc);
-  tc_end(s_tc);
+  tc_end(&s_tc, 1);
 }
 
 cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const float* L, const float* A,
@@ -1231,7 +1281,7 @@ cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_
     const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + kTcSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(apply_f32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    apply_f32_tc_kernel<<<1, kBatchThreadsTc, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out);
+    apply_f32_tc_kernel<<<1, kGroupThreads, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out);
   } else {
     apply_f32_kernel<<<1, kBatchThreads, 0, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab);
   }
@@ -1249,10 +1299,10 @@ __host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp) {
 }
 
 size_t batch_smem_bytes(int m, int m_evp, int use_tc) {
-  const size_t base = batch_smem_scalar_bytes(m, m_evp) + sizeof(int) * 2 * kTcMaxK;
-  if (!use_tc) return base;
-  return tc_tiles_offset(base) + kTcSmemBytes;
+  return batch_group_smem_bytes(m, m_evp, use_tc) * (use_tc ? kGroups<true> : 1);
 }
+
+int batch_solves_per_cta(int use_tc) { return use_tc ? kGroups<true> : 1; }
 
 int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
   const int m = mg > m_evp ? mg : m_evp;
@@ -1278,8 +1328,8 @@ int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err) {
     return 1;
   }
   if (occ < 1) occ = 1;
-  // each resident tensor-core CTA holds kTcTmemCols of the SM's 512 TMEM columns
-  if (use_tc && occ > (int)(512 / kTcTmemCols)) occ = (int)(512 / kTcTmemCols);
+  // a resident tensor-core CTA holds all of the SM's 512 TMEM columns
+  if (use_tc && occ > (int)(512 / kTcCtaTmemCols)) occ = (int)(512 / kTcCtaTmemCols);
   return occ;
 }
 

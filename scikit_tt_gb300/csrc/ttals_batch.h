@@ -54,6 +54,8 @@ struct BatchArgs {
 size_t batch_smem_bytes(int m, int m_evp, int use_tc);
 int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err = nullptr);
 int batch_threads(int use_tc);
+// independent solves one CTA of the variant runs side by side (scratch slots per CTA)
+int batch_solves_per_cta(int use_tc);
 int64_t batch_scratch_stride(const BatchSizes& z, int m, int m_evp);
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st);
 cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1, const double* L,

@@ -18,6 +18,45 @@
 
 namespace ttals {
 
+// Thread groups of the batch kernels.  The tensor-core variant runs two
+// independent solves per CTA, one per group of kGroupThreads threads, each
+// with its own named barrier (ids 1 and 2), shared state and tensor memory,
+// so that one group's memory round trips overlap the other's work.  Every
+// other kernel is one group: the whole CTA (barrier 0).  G = true selects the
+// two-group form; code instantiated with G = true never uses a CTA-wide
+// barrier.
+constexpr int kGroupThreads = 256;
+template <bool G>
+constexpr int kGroups = G ? 2 : 1;
+template <bool G>
+__device__ __forceinline__ int gtid() {
+  if constexpr (G)
+    return (int)(threadIdx.x & (kGroupThreads - 1));
+  else
+    return (int)threadIdx.x;
+}
+template <bool G>
+__device__ __forceinline__ int gsize() {
+  if constexpr (G)
+    return kGroupThreads;
+  else
+    return (int)blockDim.x;
+}
+template <bool G>
+__device__ __forceinline__ int gidx() {
+  if constexpr (G)
+    return (int)(threadIdx.x / kGroupThreads);
+  else
+    return 0;
+}
+template <bool G>
+__device__ __forceinline__ void gsync() {
+  if constexpr (G)
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x / kGroupThreads)), "n"(kGroupThreads) : "memory");
+  else
+    __syncthreads();
+}
+
 constexpr int kMaxOut = 6;
 constexpr int kMaxK = 3;
 

@@ -10,6 +10,8 @@
 
 namespace ttals {
 
+// G: the two-group form of the batch kernels (ttals_device.cuh); false: the whole CTA.
+template <bool G = false>
 __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
   const int64_t rows = a.rows, cols = a.cols;
   const int64_t k = rows < cols ? rows : cols;
@@ -17,16 +19,20 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
   double* Vh = W + rows * cols;
   double* Qw = Vh + rows * k;
   double* tau = Qw + rows * k;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = gtid<G>(), nt = gsize<G>();
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  __shared__ double red[32];
-  __shared__ double s_alpha, s_tau, s_v0;
+  __shared__ double red_g[kGroups<G>][32];
+  __shared__ double s_alpha_g[kGroups<G>], s_tau_g[kGroups<G>], s_v0_g[kGroups<G>];
+  double* red = red_g[gidx<G>()];
+  double& s_alpha = s_alpha_g[gidx<G>()];
+  double& s_tau = s_tau_g[gidx<G>()];
+  double& s_v0 = s_v0_g[gidx<G>()];
 
   for (int64_t e = tid; e < rows * cols; e += nt) {
     const int64_t i = e % rows, c = e / rows;
     W[e] = a.in[i * a.ris + c * a.rjs];
   }
-  __syncthreads();
+  gsync<G>();
 
   for (int64_t j = 0; j < k; ++j) {
     const double* col = W + j * rows;
@@ -34,7 +40,7 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
     for (int64_t i = j + tid; i < rows; i += nt) s += col[i] * col[i];
     s = warp_sum(s);
     if (lane == 0) red[warp] = s;
-    __syncthreads();
+    gsync<G>();
     if (tid == 0) {
       double tot = 0.0;
       for (int w = 0; w < nw; ++w) tot += red[w];
@@ -50,10 +56,10 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
       }
       tau[j] = s_tau;
     }
-    __syncthreads();
+    gsync<G>();
     double* v = Vh + j * rows;
     for (int64_t i = j + tid; i < rows; i += nt) v[i] = (i == j) ? s_v0 : col[i];
-    __syncthreads();
+    gsync<G>();
     const double tj = s_tau;
     for (int64_t c = j + 1 + warp; c < cols; c += nw) {
       double* wc = W + c * rows;
@@ -62,9 +68,9 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
       dot = warp_sum(dot) * tj;
       for (int64_t i = j + lane; i < rows; i += 32) wc[i] -= dot * v[i];
     }
-    __syncthreads();
+    gsync<G>();
     if (tid == 0) W[j * rows + j] = s_alpha;
-    __syncthreads();
+    gsync<G>();
   }
 
   // R (k x cols, upper trapezoidal) and optional normalisation
@@ -77,10 +83,10 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
     }
     s = warp_sum(s);
     if (lane == 0) red[warp] = s;
-    __syncthreads();
+    gsync<G>();
     double tot = 0.0;
     for (int w = 0; w < nw; ++w) tot += red[w];
-    __syncthreads();
+    gsync<G>();
     const double nrm = sqrt(tot);
     if (a.rnorm && tid == 0) *a.rnorm = nrm;
     rscale = (nrm > 0.0) ? 1.0 / nrm : 1.0;
@@ -97,7 +103,7 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
     const int64_t i = e % rows, c = e / rows;
     Qw[e] = (i == c) ? 1.0 : 0.0;
   }
-  __syncthreads();
+  gsync<G>();
   for (int64_t j = k - 1; j >= 0; --j) {
     const double* v = Vh + j * rows;
     const double tj = tau[j];
@@ -108,13 +114,13 @@ __device__ __forceinline__ void cta_householder_qr(const QrArgs& a) {
       dot = warp_sum(dot) * tj;
       for (int64_t i = j + lane; i < rows; i += 32) qc[i] -= dot * v[i];
     }
-    __syncthreads();
+    gsync<G>();
   }
   for (int64_t e = tid; e < rows * k; e += nt) {
     const int64_t i = e % rows, c = e / rows;
     a.q[i * a.qis + c * a.qjs] = Qw[e];
   }
-  __syncthreads();
+  gsync<G>();
 }
 
 }  // namespace ttals

@@ -92,9 +92,11 @@ __host__ __device__ __forceinline__ bool gemm_split(const Contraction& c, GemmAx
   return rows.n > 0 && cols.n > 0;
 }
 
-// C = contraction(A, B) on the tensor cores, executed by the whole CTA.
+// C = contraction(A, B) on the tensor cores, executed by the whole CTA (G:
+// by the calling group of the two-group form, ttals_device.cuh).
 // ktab: 2 * kTcMaxK ints of shared memory.  Returns false (nothing done) when
 // the contraction is not GEMM-shaped; the caller then uses the SIMT path.
+template <bool G = false>
 __device__ __forceinline__ bool cta_gemm_tf32x3(const Contraction& c, const float* __restrict__ A,
                                                 const float* __restrict__ B, float* __restrict__ C, int* ktab) {
   GemmAxes rows, cols;
@@ -102,7 +104,7 @@ __device__ __forceinline__ bool cta_gemm_tf32x3(const Contraction& c, const floa
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
   int* koffA = ktab;
   int* koffB = ktab + kTcMaxK;
-  for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
+  for (int kk = gtid<G>(); kk < K; kk += gsize<G>()) {
     int rem = kk, oa = 0, ob = 0;
     for (int q = c.nk - 1; q >= 0; --q) {
       const int iq = rem % c.k_dim[q];
@@ -113,8 +115,8 @@ __device__ __forceinline__ bool cta_gemm_tf32x3(const Contraction& c, const floa
     koffA[kk] = oa;
     koffB[kk] = ob;
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  gsync<G>();
+  const int lane = gtid<G>() & 31, warp = gtid<G>() >> 5, nw = gsize<G>() >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int tilesM = (M + 15) >> 4, tilesN = (N + 7) >> 3;
   for (int tile = warp; tile < tilesM * tilesN; tile += nw) {
@@ -162,7 +164,7 @@ __device__ __forceinline__ bool cta_gemm_tf32x3(const Contraction& c, const floa
     if (v1 && cc0 < N) C[cr1 + ccol0] = acc[2];
     if (v1 && cc1 < N) C[cr1 + ccol1] = acc[3];
   }
-  __syncthreads();
+  gsync<G>();
   return true;
 }
 

@@ -29,18 +29,21 @@
 
 namespace ttals {
 
-// A kernel that contains tcgen05 instructions runs one CTA per SM, so the
-// CTA owns the SM: all 512 TMEM columns, 512 threads (four 128-lane groups
-// that drain the accumulators side by side) and most of shared memory.
-constexpr int kTcThreads = 512;
-constexpr int kTcGroups = kTcThreads / 128;
-constexpr int kTcM = 128;                 // rows per tile (TMEM lanes)
-constexpr int kTcKC = 32;                 // contraction elements per staged chunk
-constexpr int kTcOzNT = 16 * kTcGroups;   // columns per emulated-FP64 tile: 16 per drain group
-constexpr int kTcOzDrain = 2;             // chunks accumulated in TMEM between drains (64 steps)
-constexpr int kTcF32NT = 256;             // columns per 3xTF32 tile
-constexpr uint32_t kTcTmemCols = 512;     // TMEM columns held by one CTA (all of the SM's)
-constexpr int kTcTileBytes = 96 * 1024;   // operand tiles
+// A kernel that contains tcgen05 instructions runs one CTA per SM.  That CTA
+// runs two independent solves, one per thread group (kGroupThreads threads,
+// ttals_device.cuh); each group holds half of the SM's 512 TMEM columns and
+// its own operand tiles, and drains its accumulators with two 128-lane
+// sub-groups side by side.  All functions here work on the calling group.
+constexpr int kTcThreads = kGroupThreads;        // threads of one group
+constexpr int kTcGroups = kTcThreads / 128;      // 128-lane drain sub-groups of a group
+constexpr int kTcM = 128;                        // rows per tile (TMEM lanes)
+constexpr int kTcKC = 32;                        // contraction elements per staged chunk
+constexpr int kTcOzNT = 16 * kTcGroups;          // columns per emulated-FP64 tile: 16 per drain sub-group
+constexpr int kTcOzDrain = 2;                    // chunks accumulated in TMEM between drains (64 steps)
+constexpr int kTcF32NT = 128;                    // columns per 3xTF32 tile
+constexpr uint32_t kTcTmemCols = 256;            // TMEM columns held by one group
+constexpr uint32_t kTcCtaTmemCols = 512;         // TMEM columns allocated by the CTA (all of the SM's)
+constexpr int kTcTileBytes = 64 * 1024;          // operand tiles of one group
 // per-tile index tables after the tiles: operand offset, output offset and
 // exponent of each row (kTcM) and column (kTcF32NT) of the current tile
 constexpr int kTcTabBytes = 3 * 4 * (kTcM + kTcF32NT);
@@ -51,10 +54,10 @@ static_assert(kTcF32NT <= (int)kTcTmemCols, "3xTF32 accumulator must fit the CTA
 static_assert(kOzSlices * kTcM * kTcKC * 2 + kOzSlices * kTcOzNT * kTcKC * 2 <= kTcTileBytes, "Ozaki tiles");
 static_assert(2 * kTcM * kTcKC * 4 + 2 * kTcF32NT * kTcKC * 4 <= kTcTileBytes, "3xTF32 tiles");
 
-// Per-CTA tensor-core state (lives in shared memory).
+// Per-group tensor-core state (lives in shared memory).
 struct TcState {
   unsigned char* tiles;  // kTcSmemBytes, 1024-byte aligned: operand tiles, then the index tables
-  uint32_t tmem;         // TMEM base of kTcTmemCols columns
+  uint32_t tmem;         // TMEM base of the group's kTcTmemCols columns
   uint32_t phase;        // parity of the next MMA completion
   int status;            // ST_OK; ST_TIMEOUT once a completion wait gave up (no further MMAs)
   uint64_t bar;          // mbarrier signalled by tcgen05.commit
@@ -105,7 +108,7 @@ __device__ __forceinline__ double tc_i64_to_f64(long long v, int e) {
 // Contraction-offset tables koffA / koffB of c (smem, 2 * kTcMaxK ints).
 __device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
   const int K = (int)c.ktotal;
-  for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
+  for (int kk = gtid<true>(); kk < K; kk += gsize<true>()) {
     int rem = kk, oa = 0, ob = 0;
     for (int q = c.nk - 1; q >= 0; --q) {
       const int iq = rem % c.k_dim[q];
@@ -121,7 +124,7 @@ __device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
 // Decode rows [r0, r0 + cnt) of an axis set once per tile: operand offset
 // (-1 for rows >= valid) and output offset.
 __device__ __forceinline__ void tc_axis_table(const GemmAxes& ax, int r0, int cnt, int valid, int* op, int* co) {
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+  for (int i = gtid<true>(); i < cnt; i += gsize<true>()) {
     int o = -1, c = 0;
     if (r0 + i < valid) gemm_axes_offsets(ax, r0 + i, o, c);
     op[i] = o;
@@ -135,7 +138,7 @@ __device__ __forceinline__ void tc_axis_table(const GemmAxes& ax, int r0, int cn
 __device__ __forceinline__ void tc_table_exponents(const double* __restrict__ src, const int* koff, int K,
                                                    const int* op, int cnt, int* E, int* bad) {
   constexpr int kRows = 8;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = gtid<true>() & 31, warp = gtid<true>() >> 5, nw = gsize<true>() >> 5;
   for (int ib = warp * kRows; ib < cnt; ib += nw * kRows) {
     int o[kRows];
     unsigned long long amax[kRows];
@@ -181,7 +184,7 @@ __device__ __forceinline__ void tc_oz_stage(const double* __restrict__ src, cons
                                             uint32_t slice_bytes) {
   constexpr int kbytes = kTcKC * 2;
   const int items = rows * (kTcKC / 8);
-  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+  for (int it = gtid<true>(); it < items; it += gsize<true>()) {
     const int cc = it / rows, r = it - cc * rows;
     const int o = op[r];
     uint32_t w[kOzSlices][4];
@@ -218,34 +221,35 @@ struct TcWaiter {
   int* fail;  // shared flag, cleared at the start of the call
 };
 __device__ __forceinline__ TcWaiter tc_waiter_begin(TcState& tc) {
-  __shared__ int s_fail;
-  if (threadIdx.x == 0) s_fail = 0;
-  return TcWaiter{tc.phase, &s_fail};
+  __shared__ int s_fail[2];
+  int* f = &s_fail[gidx<true>()];
+  if (gtid<true>() == 0) *f = 0;
+  return TcWaiter{tc.phase, f};
 }
 // Wait for the MMAs committed last (all threads); false (status set) if the wait gave up.
 __device__ __forceinline__ bool tc_wait(TcState& tc, TcWaiter& w) {
   if (!umma::mbar_wait(&tc.bar, w.phase)) *w.fail = 1;
   w.phase ^= 1u;
-  __syncthreads();
+  gsync<true>();
   umma::fence_after_sync();
   if (*w.fail) {
-    if (threadIdx.x == 0) tc.status = ST_TIMEOUT;
+    if (gtid<true>() == 0) tc.status = ST_TIMEOUT;
     return false;
   }
   return true;
 }
 // End of a GEMM call: the parity of the next completion goes back to the state.
 __device__ __forceinline__ void tc_waiter_end(TcState& tc, const TcWaiter& w) {
-  __syncthreads();
-  if (threadIdx.x == 0) tc.phase = w.phase;
-  __syncthreads();
+  gsync<true>();
+  if (gtid<true>() == 0) tc.phase = w.phase;
+  gsync<true>();
 }
 
 // shared-memory operand writes -> visible to the tensor cores; TMEM reads done
 __device__ __forceinline__ void tc_publish() {
   umma::fence_smem_to_async();
   umma::fence_before_sync();
-  __syncthreads();
+  gsync<true>();
   umma::fence_after_sync();
 }
 
@@ -257,11 +261,12 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
                                                const OzScratch& z, int* ktab, TcState& tc) {
   (void)z;
   GemmAxes rows, cols;
-  // kTcThreads threads: kTcGroups 128-thread groups, each draining 16 of the tile's columns
-  if (blockDim.x != kTcThreads || tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
+  // a group of kTcThreads threads: kTcGroups 128-thread sub-groups, each draining 16 of the tile's columns
+  if (tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
-  __shared__ int s_bad;
-  if (threadIdx.x == 0) s_bad = 0;
+  __shared__ int s_bad_g[2];
+  int& s_bad = s_bad_g[gidx<true>()];
+  if (gtid<true>() == 0) s_bad = 0;
   tc_k_tables(c, ktab);
   const int* koffA = ktab;
   const int* koffB = ktab + kTcMaxK;
@@ -273,7 +278,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
   const int nK = (K + kTcKC - 1) / kTcKC;
   const int nwin = (nK + kTcOzDrain - 1) / kTcOzDrain;
   const int sh = nwin <= 1 ? 0 : 32 - __clz(nwin - 1);  // 2^sh >= windows: the int64 sum cannot overflow
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
+  const int warp = gtid<true>() >> 5, lane = gtid<true>() & 31, q4 = warp & 3;
   const int hh = warp >> 2;  // this thread's 16-column block of the tile
   const int rl = 32 * q4 + lane;  // this thread's row of the tile (TMEM lane)
   TcWaiter wt = tc_waiter_begin(tc);
@@ -282,7 +287,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
     const bool cols_now = one_n && m0 == 0;  // the single column tile, decoded once
     tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
     if (cols_now) tc_axis_table(cols, 0, (N + 15) & ~15, N, T.cop, T.cco);
-    __syncthreads();
+    gsync<true>();
     tc_table_exponents(A, koffA, K, T.rop, kTcM, T.rex, &s_bad);
     if (cols_now) tc_table_exponents(B, koffB, K, T.cop, (N + 15) & ~15, T.cex, &s_bad);
     for (int n0 = 0; n0 < N; n0 += kTcOzNT) {
@@ -290,12 +295,12 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtBF16, kTcM, ntile);
       if (!one_n) {
-        __syncthreads();  // the previous tile's store has read the column tables
+        gsync<true>();  // the previous tile's store has read the column tables
         tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
-        __syncthreads();
+        gsync<true>();
         tc_table_exponents(B, koffB, K, T.cop, ntile, T.cex, &s_bad);
       }
-      __syncthreads();
+      gsync<true>();
       if (s_bad) {
         tc_waiter_end(tc, wt);
         return false;
@@ -307,7 +312,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
         if (nK > 1 || n0 == 0) tc_oz_stage(A, koffA, K, kc * kTcKC, T.rop, T.rex, kTcM, ta, a_slice);
         tc_oz_stage(B, koffB, K, kc * kTcKC, T.cop, T.cex, ntile, tb, b_slice);
         tc_publish();
-        if (threadIdx.x == 0) {
+        if (gtid<true>() == 0) {
           const bool wstart = (kc % kTcOzDrain) == 0;
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
           uint64_t da[kOzSlices], db[kOzSlices];
@@ -358,7 +363,7 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
           if (cl < ncols) C[cr + T.cco[cl]] = tc_i64_to_f64(acc[j], er + T.cex[cl]);
         }
       }
-      __syncthreads();
+      gsync<true>();
     }
   }
   tc_waiter_end(tc, wt);
@@ -372,7 +377,7 @@ __device__ __forceinline__ void tc_tf32_stage(const float* __restrict__ src, con
                                               const int* op, int rows, unsigned char* base, uint32_t half_bytes) {
   constexpr int kbytes = kTcKC * 4;
   const int items = rows * (kTcKC / 4);
-  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+  for (int it = gtid<true>(); it < items; it += gsize<true>()) {
     const int cc = it / rows, r = it - cc * rows;
     const int o = op[r];
     uint32_t hi[4] = {0u, 0u, 0u, 0u}, lo[4] = {0u, 0u, 0u, 0u};
@@ -412,8 +417,8 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
   unsigned char* ta = tc.tiles;
   unsigned char* tb = tc.tiles + 2 * a_half;
   const int nK = (K + kTcKC - 1) / kTcKC;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q4 = warp & 3;
-  const int halves = blockDim.x >> 7, grp = warp >> 2;
+  const int warp = gtid<true>() >> 5, lane = gtid<true>() & 31, q4 = warp & 3;
+  const int halves = gsize<true>() >> 7, grp = warp >> 2;
   const int rl = 32 * q4 + lane;
   TcWaiter wt = tc_waiter_begin(tc);
   const bool one_n = N <= kTcF32NT;
@@ -424,12 +429,12 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtTF32, kTcM, ntile);
       if (!one_n || m0 == 0) tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
-      __syncthreads();
+      gsync<true>();
       for (int kc = 0; kc < nK; ++kc) {
         if (nK > 1 || n0 == 0) tc_tf32_stage(A, koffA, K, kc * kTcKC, T.rop, kTcM, ta, a_half);
         tc_tf32_stage(B, koffB, K, kc * kTcKC, T.cop, ntile, tb, b_half);
         tc_publish();
-        if (threadIdx.x == 0) {
+        if (gtid<true>() == 0) {
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
           const uint32_t d = umma::taddr(tc.tmem, 0, 0);
           const uint64_t ah = umma::sdesc(a0, 128, sbo), al = umma::sdesc(a0 + a_half, 128, sbo);
@@ -461,7 +466,7 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
         }
       }
       umma::fence_before_sync();
-      __syncthreads();
+      gsync<true>();
     }
   }
   tc_waiter_end(tc, wt);
