@@ -72,20 +72,23 @@ def max_over_ranks(ms, device=None):
     return float(t.item())
 
 
-def launch_traffic(batch):
-    """DRAM bytes of one batch launch from the committed ncu capture
-    (``profiles/traffic.json``: bytes of a launch of ``solves`` solves).  Every
-    solve runs on its own CTA over its own data, so a launch of ``batch``
-    solves moves batch / solves of it.  Returns (bytes or None, note)."""
+def launch_traffic(batch, kernel):
+    """DRAM bytes of one launch of ``kernel`` from the committed ncu capture
+    (``profiles/traffic.json``: per kernel, the bytes of a launch of ``solves``
+    solves).  Every solve runs on its own CTA (or CTA group) over its own data,
+    so a launch of ``batch`` solves moves batch / solves of it.  Returns
+    (bytes or None, note)."""
     tf = os.path.join(ROOT, 'profiles', 'traffic.json')
     if not os.path.exists(tf):
         return None, 'no ncu capture committed'
-    rec = json.load(open(tf))
-    solves = int(rec.get('solves', batch))
-    note = f'ncu dram__bytes_read.sum + dram__bytes_write.sum of a {solves}-solve launch'
+    rec = json.load(open(tf)).get(kernel)
+    if not isinstance(rec, dict):
+        return None, f'no ncu capture of {kernel} committed'
+    solves = int(rec['solves'])
+    note = f'ncu dram__bytes_read.sum + dram__bytes_write.sum of a {solves}-solve launch of {kernel}'
     if solves != batch:
         note += f', scaled to {batch} solves'
-    return rec['batch_sle_kernel'] * batch / solves, note
+    return rec['bytes'] * batch / solves, note
 
 
 # ---------------------------------------------------------------------------
@@ -586,12 +589,14 @@ def main_gpu(args):
     parity = headline_parity({'mixed': tm, 'plain_fp64': tp}, inst[0]) if rank == 0 else None
 
     # end to end: the same batch through the C ABI with host buffers
-    e2e_ms = []
+    e2e_ms, e2e_parts = [], []
     batch(_lib.PREC_MIXED, MIXED_TOL, on_device=False)
     for _ in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
-        batch(_lib.PREC_MIXED, MIXED_TOL, on_device=False)
+        st_e = batch(_lib.PREC_MIXED, MIXED_TOL, on_device=False)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        # engine events: uploads + kernel (device_ms) and the kernel alone (solver_ms)
+        e2e_parts.append((st_e.device_ms, st_e.solver_ms))
     h2d = sum(p.data.nbytes for pk in packs for p in pk)
     d2h = out_host.numel() * out_host.element_size()
 
@@ -607,7 +612,7 @@ def main_gpu(args):
     if os.path.exists(mp):
         bf16_peak = float(json.load(open(mp))['bf16_tflops'])
         bf16_src = 'MEASURED_PEAKS.json bf16_tflops (burst cuBLAS bf16 GEMM), of measured'
-    traffic, traffic_note = launch_traffic(B)
+    traffic, traffic_note = launch_traffic(B, 'batch_sle_tc_kernel' if sm_.batch_tensor_cores else 'batch_sle_kernel')
 
     extra = {} if args.quick else other_workloads(lib, ctx, args)
     if rank != 0:
@@ -652,9 +657,15 @@ def main_gpu(args):
         'headline_parity': parity,
         'max_local_residual': max(s.max_local_residual for s in st_mixed),
         'e2e': {'value': B / (float(np.mean(e2e_ms)) / 1e3), 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
-                'd2h_bytes_per_step': int(d2h), 'ms_per_step': float(np.mean(e2e_ms))},
+                'd2h_bytes_per_step': int(d2h), 'ms_per_step': float(np.mean(e2e_ms)),
+                'breakdown_ms': {'wall': float(np.mean(e2e_ms)),
+                                 'uploads_and_kernel': float(np.mean([p[0] for p in e2e_parts])),
+                                 'kernel': float(np.mean([p[1] for p in e2e_parts])),
+                                 'note': 'engine CUDA events; wall minus uploads_and_kernel is host planning, '
+                                         'result collection and the device-to-host copies'}},
         'gpu_launches': launches,
-        'roofline': {'kernel': 'batch_sle_kernel (mixed)', 'bound': 'tensor',
+        'roofline': {'kernel': ('batch_sle_tc_kernel' if sm_.batch_tensor_cores else 'batch_sle_kernel') + ' (mixed)',
+                     'bound': 'tensor',
                      'achieved': (ach64 + ach32) / 1e3, 'peak': bf16_peak, 'unit': 'TFLOP/s',
                      'frac': (ach64 + ach32) / 1e3 / bf16_peak, 'traffic': traffic,
                      'traffic_source': traffic_note,

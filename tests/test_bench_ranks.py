@@ -59,8 +59,13 @@ def test_launch_traffic_scales_with_batch():
     sys.path.insert(0, ROOT)
     import json
     import bench
-    rec = json.load(open(os.path.join(ROOT, 'profiles', 'traffic.json')))
-    full, note = bench.launch_traffic(rec['solves'])
-    assert full == rec['batch_sle_kernel'] and 'scaled' not in note
-    part, note = bench.launch_traffic(rec['solves'] // 5)
-    assert abs(part - full * (rec['solves'] // 5) / rec['solves']) < 1.0 and 'scaled' in note
+    recs = json.load(open(os.path.join(ROOT, 'profiles', 'traffic.json')))
+    kernels = [k for k, v in recs.items() if isinstance(v, dict)]
+    assert 'batch_sle_kernel' in kernels
+    for k in kernels:
+        rec = recs[k]
+        full, note = bench.launch_traffic(rec['solves'], k)
+        assert full == rec['bytes'] and 'scaled' not in note and k in note
+        part, note = bench.launch_traffic(rec['solves'] // 5, k)
+        assert abs(part - full * (rec['solves'] // 5) / rec['solves']) < 1.0 and 'scaled' in note
+    assert bench.launch_traffic(10, 'no_such_kernel')[0] is None
