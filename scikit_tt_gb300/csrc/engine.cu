@@ -1581,6 +1581,7 @@ struct BatchPlan {
   int variant = 0;  // index into batch_candidates(prec)
   int per_sm = 1;   // resident CTAs per SM of the launch
   int spc = 1;      // solves one CTA runs side by side
+  std::vector<int> caller;  // the caller's index of each planned request (the plan may reorder them)
   double tol = 0.0;
   // byte layout of the device block: [regions | meta | inst | scratch | counter]
   size_t off_meta = 0, off_inst = 0, off_scratch = 0, off_next = 0, bytes = 0;
@@ -1684,7 +1685,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
       P.z.core = std::max(P.z.core, std::max(a * nn * s, rx0[i] * nn * std::max(I.cap[i + 1], rx0[i + 1])));
       P.z.stack = std::max(P.z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
       P.z.opcore = std::max(P.z.opcore, R[i] * nn * nn * R[i + 1]);
-      if (prec == TTALS_PREC_MIXED && I.kind == 0) oz_need_site(P.z, a, nn, s, R[i], R[i + 1]);
+      if (prec == TTALS_PREC_MIXED) oz_need_site(P.z, a, nn, s, R[i], R[i + 1]);
     }
     require(P.z.T < (int64_t(1) << 31) && P.z.N * (kBatchMEvp + 1) < (int64_t(1) << 31), TTALS_ERR_UNSUPPORTED,
             "a request exceeds the 32-bit index range of the batch kernel");
@@ -1749,7 +1750,9 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
             std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
     P.per_sm = per_sm;
     P.spc = batch_solves_per_cta(P.use_tc);
-    P.grid = std::min((count + P.spc - 1) / P.spc, c->num_sms * per_sm);
+    // every SM gets a CTA even when the groups outnumber the requests: a
+    // request alone on an SM runs faster than one that shares it
+    P.grid = std::min(count, c->num_sms * per_sm);
   }
   P.stride = batch_scratch_stride(P.z, kBatchM, kBatchMEvp);
   auto al = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -1916,8 +1919,9 @@ void collect_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, int ou
     std::vector<double>& rep = reps[j];
     rep.assign(c->pinned + roff[j], c->pinned + roff[j + 1]);
     const int stj = (int)rep[4];
-    if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(j)};
-    if (stj == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in request " + std::to_string(j)};
+    const int cj = j < P.caller.size() ? P.caller[j] : (int)j;
+    if (stj == ST_NONFINITE) throw Fail{TTALS_ERR_NONFINITE, "non-finite value in request " + std::to_string(cj)};
+    if (stj == ST_SINGULAR) throw Fail{TTALS_ERR_SINGULAR, "singular local system in request " + std::to_string(cj)};
     if (stj != ST_OK) throw Fail{TTALS_ERR_CUDA, "device status " + std::to_string(stj)};
     int64_t cnt = 0;
     for (int i = 0; i < d; ++i) {
@@ -1934,10 +1938,40 @@ void collect_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, int ou
   fill_batch_stats(reps, stats, kernel_ms, total_ms, launches);
 }
 
+// Relative device work of a request (ordering only): local-operator flops of
+// every site at the initial guess's ranks, times the sweeps; an eigenproblem
+// counts 4x (FP64 Lanczos with full reorthogonalisation).  0 for a malformed
+// request (plan_batch reports it).
+double request_work(const ttals_request& q) {
+  const ttals_tt& op = q.op;
+  const ttals_tt& x = q.x0;
+  if (op.order < 1 || x.order != op.order || !op.ranks || !op.row_dims || !x.ranks) return 0.0;
+  double w = 0.0;
+  for (int i = 0; i < op.order; ++i) {
+    const double a = (double)x.ranks[i], s = (double)x.ranks[i + 1], n = (double)op.row_dims[i];
+    const double R0 = (double)op.ranks[i], R1 = (double)op.ranks[i + 1];
+    w += a * a * R0 * n * s + a * s * n * n * R0 * R1 + a * n * s * s * R1;
+  }
+  return w * (q.repeats > 0 ? q.repeats : 1) * (q.kind == TTALS_REQ_EVP ? 4.0 : 1.0);
+}
+
 void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, int out_dev,
                     ttals_stats* st) {
   launch_counter() = 0;
-  BatchPlan P = plan_batch(c, count, reqs, prec, tol, true);
+  // largest requests first: the batch kernel hands the first requests to
+  // distinct SMs, so the longest solves start at once instead of lengthening
+  // the launch's tail (outputs go to each request's own pointers)
+  std::vector<int> order(count > 0 ? count : 0);
+  std::vector<double> work(order.size());
+  for (int j = 0; j < count; ++j) {
+    order[j] = j;
+    work[j] = reqs ? request_work(reqs[j]) : 0.0;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work[x] > work[y]; });
+  std::vector<ttals_request> sorted(order.size());
+  for (size_t j = 0; j < order.size(); ++j) sorted[j] = reqs[order[j]];
+  BatchPlan P = plan_batch(c, count, reqs ? sorted.data() : reqs, prec, tol, true);
+  P.caller = order;
   char* mem = nullptr;
   Bump B{c};
   B.want(&mem, (int64_t)P.bytes);

@@ -92,7 +92,11 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
 }
 
 // FP64 contraction; with `oz` set, GEMM-shaped ones run as emulated FP64 on the
-// BF16 tensor cores (ttals_ozaki.cuh), the rest natively.
+// BF16 tensor cores (ttals_ozaki.cuh), the rest natively.  A contraction over
+// fewer than kOzMinK elements stays native: measured on a batch of 32 Ising
+// eigenproblems (whose middle contraction has K = 6) 16 % faster than
+// emulating it, and no change on the SLE batches.
+constexpr int kOzMinK = 16;
 template <bool TC>
 __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const double* A, const double* B, double* C,
                                               const OzScratch* oz) {
@@ -100,6 +104,7 @@ __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const dou
   Contraction& sc = sc_g[gidx<TC>()];
   if (gtid<TC>() == 0) sc = cref;
   gsync<TC>();
+  if (sc.ktotal < kOzMinK) oz = nullptr;
   if constexpr (TC) {
     if (oz && oz->tc) {
       const bool done = cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc);
@@ -493,7 +498,8 @@ template <typename TI, bool G = false>
 __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                                const TI* L, const TI* A, const TI* R, TI* T1, TI* T2, double* x,
                                                TI* V, TI* w, int64_t N, int m, int mode, double sigma,
-                                               int max_restarts, double tol, double* sm) {
+                                               int max_restarts, double tol, double* sm,
+                                               const OzScratch* oz = nullptr) {
   double* al = sm;
   double* be = al + m;
   double* h1 = be + m;
@@ -523,7 +529,18 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   for (;;) {
     int nT = 0;
     for (int j = 0; j < mm; ++j) {
-      cta_apply<TI, G>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
+      if constexpr (std::is_same<TI, double>::value) {
+        if (oz) {
+          // FP64-accurate products on the tensor cores (emulated FP64)
+          cta_contract_f64<G>(p1, L, V + (int64_t)j * N, T1, oz);
+          cta_contract_f64<G>(p2, T1, A, T2, oz);
+          cta_contract_f64<G>(p3, T2, R, w, oz);
+        } else {
+          cta_apply<TI, G>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
+        }
+      } else {
+        cta_apply<TI, G>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
+      }
       cta_dots<TI, G>(V, N, j + 1, w, h1);
       for (int64_t e = tid; e < N; e += nt) {
         double acc = (double)w[e];
@@ -612,8 +629,19 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   return out;
 }
 
+// QR of a core; with a shared-memory region (the group's tensor-core tiles,
+// idle between GEMMs) large enough for the matrix, in shared memory.
 template <bool G = false>
-__device__ __noinline__ void cta_qr(const QrArgs& q) { cta_householder_qr<G>(q); }
+__device__ __noinline__ void cta_qr(const QrArgs& q, unsigned char* shm = nullptr, int64_t shm_doubles = 0) {
+  if constexpr (G) {  // only the tensor-core kernel's groups have such a region
+    const int64_t k = q.rows < q.cols ? q.rows : q.cols;
+    if (shm && q.rows * q.cols <= shm_doubles && k <= kQrSharedMaxK) {
+      cta_householder_qr_shared<G>(q, reinterpret_cast<double*>(shm));
+      return;
+    }
+  }
+  cta_householder_qr<G>(q);
+}
 
 // Make this request's outputs visible to the host and to copy engines, then
 // raise its completion flag (host-mapped memory).
@@ -703,6 +731,12 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   const int tid = gtid<TC>();
   for (int i = tid; i <= d; i += gsize<TC>()) r[i] = cap[i];
   gsync<TC>();
+  // the group's tensor-core tiles hold the QR factorisations between GEMMs;
+  // in mixed precision the gauge pushes run as emulated FP64 on tcgen05 (on
+  // the warp-MMA kernel they stay native)
+  unsigned char* qsh = S.oz.tc ? S.oz.tc->tiles : nullptr;
+  constexpr int64_t qcap = kTcSmemBytes / 8;
+  const OzScratch* ozp = (TC && a.prec == 1) ? &S.oz : nullptr;
   auto X = [&](int i) { return I.X + X_off[i]; };
   auto L = [&](int i) { return I.L + L_off[i]; };
   auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
@@ -741,10 +775,10 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_qr<TC>(q);
+      cta_qr<TC>(q, qsh, qcap);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
-      cta_contract<double, TC>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
+      cta_contract_f64<TC>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb, ozp);
       cur = outb;
       cur_left = rx0[i - 1];
       cur_right = k;
@@ -844,10 +878,10 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_qr<TC>(q);
+        cta_qr<TC>(q, qsh, qcap);
         fl64 += qr_fl((double)(aa * nn), (double)ss);
         const int64_t qq = n[i + 1] * r[i + 2];
-        cta_contract<double, TC>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
+        cta_contract_f64<TC>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0, ozp);
         cta_copy<TC>(X(i + 1), S.tmp0, k * qq);
         if (tid == 0) r[i + 1] = k;
         gsync<TC>();
@@ -860,10 +894,10 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_qr<TC>(q);
+        cta_qr<TC>(q, qsh, qcap);
         fl64 += qr_fl((double)ns, (double)aa);
         const int64_t p = r[i - 1] * n[i - 1];
-        cta_contract<double, TC>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
+        cta_contract_f64<TC>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0, ozp);
         cta_copy<TC>(X(i - 1), S.tmp0, p * k);
         if (tid == 0) r[i] = k;
         gsync<TC>();
@@ -926,6 +960,9 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   gsync<G>();
   auto X = [&](int i) { return I.X + X_off[i]; };
   auto Xo = [&](int i) { return I.Xopt + X_off[i]; };
+  const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
+  unsigned char* qsh = S.oz.tc ? S.oz.tc->tiles : nullptr;
+  constexpr int64_t qcap = kTcSmemBytes / 8;
   auto L = [&](int i) { return I.L + L_off[i]; };
   auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
   auto A = [&](int i) { return I.op + op_off[i]; };
@@ -940,7 +977,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_qr<G>(q);
+      cta_qr<G>(q, qsh, qcap);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
       cta_contract<double, G>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
@@ -959,9 +996,9 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
     Contraction q1, q2, q3;
     desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
-    cta_contract<double, G>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1);
-    cta_contract<double, G>(q2, (const double*)S.T1, A(i + 1), S.T2);
-    cta_contract<double, G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i));
+    cta_contract_f64<G>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
+    cta_contract_f64<G>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
+    cta_contract_f64<G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
   };
   auto left = [&](int i) {
@@ -973,9 +1010,9 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
-    cta_contract<double, G>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1);
-    cta_contract<double, G>(p2, (const double*)S.T1, A(i - 1), S.T2);
-    cta_contract<double, G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i));
+    cta_contract_f64<G>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
+    cta_contract_f64<G>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
+    cta_contract_f64<G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
   };
   auto solve = [&](int i) {
@@ -984,11 +1021,13 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
     const int m = (int)(N < a.m_evp ? N : a.m_evp);
     const double fa = apply_fl((double)aa, (double)nn, (double)ss, (double)R[i], (double)R[i + 1]);
-    // Eigen solves stay FP64 in both precision modes: warm-started from the
-    // previous sweep's core, FP64 Lanczos converges in ~12 steps per site, and
-    // an FP32 Lanczos pre-stage (then FP64 polish) measured 2.8x slower.
+    // Eigen solves stay FP64-accurate in both precision modes: warm-started
+    // from the previous sweep's core, FP64 Lanczos converges in ~12 steps per
+    // site, and an FP32 Lanczos pre-stage (then FP64 polish) measured 2.8x
+    // slower.  In mixed precision their products (and the stacks) run as
+    // emulated FP64 on the tensor cores.
     const CtaEigStats st = cta_lanczos<double, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m,
-                                               I.mode, I.sigma, kBatchEvpRestarts, a.tol_evp, sm);
+                                               I.mode, I.sigma, kBatchEvpRestarts, a.tol_evp, sm, oz);
     theta = st.theta;
     nits += st.its;
     nrst += st.restarts;
@@ -1009,7 +1048,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_qr<G>(q);
+        cta_qr<G>(q, qsh, qcap);
         const int64_t qq = n[i + 1] * r[i + 2];
         cta_contract<double, G>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
         cta_copy<G>(X(i + 1), S.tmp0, k * qq);
@@ -1023,7 +1062,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_qr<G>(q);
+        cta_qr<G>(q, qsh, qcap);
         const int64_t p = r[i - 1] * n[i - 1];
         cta_contract<double, G>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
         cta_copy<G>(X(i - 1), S.tmp0, p * k);
@@ -1141,8 +1180,17 @@ __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
     tc_begin(s_tc, NG, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK), gbytes);
     S.oz.tc = &s_tc[g];
   }
+  bool first = true;
   for (;;) {
-    if (gtid<UseTc>() == 0) s_j[g] = atomicAdd(a.next, 1);
+    if (gtid<UseTc>() == 0) {
+      // every group's first request is fixed: requests 0 .. grid-1 (the
+      // largest, in the host's order) go to distinct CTAs, the next grid pair
+      // with them in reverse order (largest with smallest); later ones come
+      // from the work counter
+      const int grid = (int)gridDim.x, b = (int)blockIdx.x;
+      s_j[g] = first ? ((g & 1) ? (g + 1) * grid - 1 - b : g * grid + b) : NG * grid + atomicAdd(a.next, 1);
+    }
+    first = false;
     gsync<UseTc>();
     const int j = s_j[g];
     gsync<UseTc>();

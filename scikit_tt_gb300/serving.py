@@ -5,7 +5,9 @@
 arrive, grouped into jobs launched on their own streams while earlier jobs
 still run (so their work overlaps on the device), and admitted only while
 the device-memory budget holds; each request's latency is measured from its
-arrival to its completion.
+arrival to its completion.  Admission is per CTA slot in effect: a job's CTA
+exits once its job has no request left, and the hardware scheduler gives its
+SM to the CTAs of the jobs launched after it.
 """
 
 from __future__ import annotations
@@ -68,6 +70,19 @@ class Request:
         self._keep = [op, x0, rhs, out, val, its, ranks, dims]
         return r
 
+    def work_estimate(self) -> float:
+        """Relative device work: flops of the local-operator application at
+        every site (ranks of the initial guess, operator ranks, mode sizes),
+        times the sweeps; an eigenproblem counts 4x (FP64 Lanczos with full
+        reorthogonalisation, against the mixed-precision GMRES of a system)."""
+        r = [c.shape[0] for c in self.x0] + [1]
+        R = [c.shape[0] for c in self.op] + [1]
+        w = 0.0
+        for i, c in enumerate(self.op):
+            n, a, s, R0, R1 = c.shape[1], r[i], r[i + 1], R[i], R[i + 1]
+            w += a * a * R0 * n * s + a * s * n * n * R0 * R1 + a * n * s * s * R1
+        return w * max(1, int(self.repeats)) * (4.0 if self.kind == 'evp' else 1.0)
+
     def _complete(self):
         _, _, _, out, val, its, ranks, dims = self._keep
         self.solution = TT(_lib.unpack(out, dims, [1] * len(dims), ranks))
@@ -105,7 +120,10 @@ class Server:
 
     def _launch(self, clock):
         lib, ctx = _lib.load(), _lib.context()
-        take = self.queue[:self.max_batch]
+        # first come, first served across jobs; inside a job the largest
+        # requests first (the job's CTAs take requests in index order, so the
+        # longest ones start at once instead of extending the job's tail)
+        take = sorted(self.queue[:self.max_batch], key=lambda r: r.work_estimate(), reverse=True)
         arr = (_lib.Request * len(take))(*[r._descriptor() for r in take])
         h = C.c_void_p()
         st = lib.ttals_submit(ctx, len(take), arr, self.prec, self.tol, C.byref(h))

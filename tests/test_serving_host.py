@@ -1,6 +1,7 @@
 """Host logic of the continuous-batching server on CPU, against a fake of the
 asynchronous job API (ttals_submit / ttals_job_poll_each / ttals_job_fetch /
-ttals_job_finish): requests are grouped first come first served, a job the
+ttals_job_finish): requests are grouped first come first served (largest
+first inside a job), a job the
 memory budget cannot hold (TTALS_ERR_NOMEM) waits until running jobs release
 theirs, at most ``max_jobs`` jobs run at once, and each request completes on
 its own, in the order its CTA finishes.  The rank rule comes from the real
@@ -99,15 +100,19 @@ def test_budget_admission_and_per_request_completion(fake):
     assert f.nomem > 0 and f.peak == 4 and f.running_max == 2
     assert len(srv.finished) == 7 and len(srv.stats) == 3
     assert sorted(s['local_solves'] for s in srv.stats) == [1, 3, 3]   # in the order jobs finish
-    # first come, first served: requests 0-2 in job 1, 3-5 in job 2, 6 in job 3
-    for j, r in enumerate(reqs):
-        job, idx = divmod(j, 3)
-        assert r.solution.cores[0].reshape(-1)[0] == 1000.0 * (job + 1) + idx
-        if r.kind == 'evp':
-            assert r.value == -float(idx) and r.iterations == idx + 1
+    # first come, first served across jobs: requests 0-2 in job 1, 3-5 in job 2, 6 in job 3;
+    # inside a job the largest request first (the eigenproblem of each three here)
+    for job in range(3):
+        members = reqs[3 * job:3 * job + 3]
+        order = sorted(members, key=lambda r: r.work_estimate(), reverse=True)
+        assert order[0].kind == 'evp' or len(members) == 1
+        for idx, r in enumerate(order):
+            assert r.solution.cores[0].reshape(-1)[0] == 1000.0 * (job + 1) + idx
+            if r.kind == 'evp':
+                assert r.value == -float(idx) and r.iterations == idx + 1
     # within a job, requests complete in the order their CTAs finish (last first here)
-    pos = {id(r): j for j, r in enumerate(reqs)}
-    assert [pos[id(r)] for r in srv.finished[:3]] == [2, 1, 0]
+    first = sorted(reqs[:3], key=lambda r: r.work_estimate(), reverse=True)
+    assert [id(r) for r in srv.finished[:3]] == [id(r) for r in first[::-1]]
     assert all(r.done > 0 for r in reqs)
 
 
