@@ -697,7 +697,7 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--batch', type=int, default=0, help='solves per step and GPU (default: resident CTAs x SMs)')
     ap.add_argument('--quick', action='store_true', help='headline only (skip the other workloads)')
-    ap.add_argument('--serve-window', type=float, default=0.1, help='seconds of Poisson arrivals to replay')
+    ap.add_argument('--serve-window', type=float, default=1.0, help='seconds of Poisson arrivals to replay')
     args = ap.parse_args()
     if args.impl == 'reference':
         run_reference(args)
