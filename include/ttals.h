@@ -53,6 +53,10 @@ typedef struct ttals_job ttals_job;
 /* request kinds of the batched / served entry points */
 #define TTALS_REQ_SLE 0 /* scikit_tt/solvers/sle.py:10 als */
 #define TTALS_REQ_EVP 1 /* scikit_tt/solvers/evp.py:17 als (symmetric, number_ev == 1) */
+/* scikit_tt/solvers/evp.py:17 als with operator_gevp (evp.py:272-287, 314-329,
+ * 367-368): A x = lambda B x with A symmetric and B symmetric positive
+ * definite, number_ev == 1; the request's rhs carries operator_gevp */
+#define TTALS_REQ_GEVP 2
 
 typedef struct {
   int32_t order;
@@ -66,7 +70,8 @@ typedef struct {
 /* One ALS problem of a batch.  out_data receives the solution cores (ranks
  * from ttals_als_ranks; for EVP the best sweep's eigentensor, evp.py:151-155);
  * out_value the eigenvalue and out_iterations the sweeps run (EVP, may be
- * NULL).  rhs is ignored for EVP. */
+ * NULL).  rhs is ignored for EVP; for GEVP it is operator_gevp (an operator
+ * train with the operator's mode sizes). */
 typedef struct {
   int32_t kind;
   ttals_tt op, x0, rhs;

@@ -45,6 +45,7 @@ EXPORTS = (
 
 REQ_SLE = 0
 REQ_EVP = 1
+REQ_GEVP = 2
 
 
 class TTDesc(C.Structure):

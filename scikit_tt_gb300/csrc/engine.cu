@@ -1606,7 +1606,7 @@ std::vector<BatchVariant> batch_candidates(int prec) {
 // the largest per-site sizes (local unknowns, stack, operator core).
 std::string tune_key(const BatchPlan& P) {
   int evp = 0;
-  for (const auto& I : P.in) evp |= I.kind == 1;
+  for (const auto& I : P.in) evp |= I.kind;
   return std::to_string(P.prec) + "|" + std::to_string(evp) + "|" + std::to_string(P.z.N) + "|" +
          std::to_string(P.z.stack) + "|" + std::to_string(P.z.opcore);
 }
@@ -1625,8 +1625,9 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
   for (int j = 0; j < count; ++j) {
     const ttals_request& q = reqs[j];
     BatchReqHost& I = P.in[j];
-    require(q.kind == TTALS_REQ_SLE || q.kind == TTALS_REQ_EVP, TTALS_ERR_ARG, "unknown request kind");
-    I.kind = q.kind == TTALS_REQ_EVP ? 1 : 0;
+    require(q.kind == TTALS_REQ_SLE || q.kind == TTALS_REQ_EVP || q.kind == TTALS_REQ_GEVP, TTALS_ERR_ARG,
+            "unknown request kind");
+    I.kind = q.kind == TTALS_REQ_GEVP ? 2 : (q.kind == TTALS_REQ_EVP ? 1 : 0);
     I.op = view(&q.op, "operator");
     I.x0 = view(&q.x0, "initial_guess");
     validate_square_op(I.op);
@@ -1641,11 +1642,20 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
       I.mode = q.solver == TTALS_EVP_EIGH ? 0 : 1;
       I.sigma = q.sigma;
       I.conv_eps = q.conv_eps;
-      I.b = TTView();
-      I.b.d = I.op.d;
-      I.b.r.assign(I.op.d + 1, 1);
-      I.b.off.assign(I.op.d + 1, 0);
-      I.b.total = 0;
+      if (I.kind == 2) {
+        // operator_gevp travels in the rhs slot: its cores, ranks and stacks
+        // take the places of the right-hand side's
+        I.b = view(&q.rhs, "operator_gevp");
+        validate_square_op(I.b);
+        require(I.b.d == I.op.d && I.b.m == I.op.m, TTALS_ERR_ARG,
+                "operator_gevp must have the operator's order and mode sizes");
+      } else {
+        I.b = TTView();
+        I.b.d = I.op.d;
+        I.b.r.assign(I.op.d + 1, 1);
+        I.b.off.assign(I.op.d + 1, 0);
+        I.b.total = 0;
+      }
     }
     require(q.repeats >= 1, TTALS_ERR_ARG, "repeats must be >= 1 in a batch");
     require(q.out_data != nullptr, TTALS_ERR_ARG, "request without an output buffer");
@@ -1672,12 +1682,14 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
       Rto[i] = rts;
       rts += s * R[i + 1] * s;
       Lbo[i] = lbs;
-      lbs += rb[i] * a;
+      lbs += I.kind == 2 ? a * rb[i] * a : rb[i] * a;  // operator_gevp stacks / RHS stacks
       Rbo[i] = rbs;
-      rbs += rb[i + 1] * s;
+      rbs += I.kind == 2 ? s * rb[i + 1] * s : rb[i + 1] * s;
       I.out_count += I.fin[i] * nn * I.fin[i + 1];
       P.z.N = std::max(P.z.N, a * nn * s);
-      P.z.T = std::max(P.z.T, std::max(R[i], R[i + 1]) * std::max(a, s) * std::max(a, s) * nn);
+      const int64_t Rm = I.kind == 2 ? std::max(std::max(R[i], R[i + 1]), std::max(rb[i], rb[i + 1]))
+                                     : std::max(R[i], R[i + 1]);
+      P.z.T = std::max(P.z.T, Rm * std::max(a, s) * std::max(a, s) * nn);
       P.z.U = std::max(P.z.U, std::max(a, s) * nn * std::max(rb[i], rb[i + 1]));
       P.z.R = std::max(P.z.R, std::max(std::max(a, s) * std::max(a, s), rx0[i] * rx0[i]));
       P.z.Q = std::max(P.z.Q,
@@ -1686,6 +1698,12 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
       P.z.stack = std::max(P.z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
       P.z.opcore = std::max(P.z.opcore, R[i] * nn * nn * R[i + 1]);
       if (prec == TTALS_PREC_MIXED) oz_need_site(P.z, a, nn, s, R[i], R[i + 1]);
+      if (I.kind == 2) {
+        P.z.Ng = std::max(P.z.Ng, a * nn * s);
+        P.z.stack = std::max(P.z.stack, std::max(a * rb[i] * a, s * rb[i + 1] * s));
+        P.z.opcore = std::max(P.z.opcore, rb[i] * nn * nn * rb[i + 1]);
+        if (prec == TTALS_PREC_MIXED) oz_need_site(P.z, a, nn, s, rb[i], rb[i + 1]);
+      }
     }
     require(P.z.T < (int64_t(1) << 31) && P.z.N * (kBatchMEvp + 1) < (int64_t(1) << 31), TTALS_ERR_UNSUPPORTED,
             "a request exceeds the 32-bit index range of the batch kernel");
@@ -1705,7 +1723,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     put(7, rbs);
     put(8, I.out_count);
     put(9, kReportFixed + d);
-    put(10, I.kind == 1 ? xs : 1);
+    put(10, I.kind != 0 ? xs : 1);
     I.region = P.region_total;
     P.region_total += o;
     I.meta_off = (int64_t)P.meta.size();
@@ -1745,7 +1763,8 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     P.variant = pick;
     P.use_tc = cand[pick].use_tc;
     cudaError_t e = cudaSuccess;
-    const int per_sm = std::max(1, batch_blocks_per_sm(kBatchM, kBatchMEvp, P.use_tc, &e) - cand[pick].less);
+    const int per_sm =
+        std::max(1, batch_blocks_per_sm(kBatchM, kBatchMEvp, P.use_tc, &e, P.z.Ng > 0 ? 1 : 0) - cand[pick].less);
     require(e == cudaSuccess, TTALS_ERR_CUDA,
             std::string("occupancy query of the batch kernel failed: ") + cudaGetErrorString(e));
     P.per_sm = per_sm;
@@ -1812,7 +1831,7 @@ void launch_plan(ttals_ctx* c, BatchPlan& P, char* mem, cudaStream_t st, cudaEve
                            v.dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
     };
     up((double*)hinst[j].op, I.op);
-    if (I.kind == 0) up((double*)hinst[j].rhs, I.b);
+    if (I.kind != 1) up((double*)hinst[j].rhs, I.b);  // right-hand side, or operator_gevp
     up((double*)hinst[j].x0, I.x0);
   }
   int* next = (int*)(mem + P.off_next);
@@ -1952,7 +1971,7 @@ double request_work(const ttals_request& q) {
     const double R0 = (double)op.ranks[i], R1 = (double)op.ranks[i + 1];
     w += a * a * R0 * n * s + a * s * n * n * R0 * R1 + a * n * s * s * R1;
   }
-  return w * (q.repeats > 0 ? q.repeats : 1) * (q.kind == TTALS_REQ_EVP ? 4.0 : 1.0);
+  return w * (q.repeats > 0 ? q.repeats : 1) * (q.kind != TTALS_REQ_SLE ? 4.0 : 1.0);
 }
 
 void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, int out_dev,

@@ -629,6 +629,207 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   return out;
 }
 
+// ---------------------------------------------------------------------------
+// CTA Lanczos for the generalised symmetric-definite local problem
+// A x = lambda B x (evp.py:418-439 with micro_op_gevp): Lanczos on B^{-1} A,
+// which is self-adjoint in the B inner product, with B-orthonormal basis V
+// (and its images BV = B V kept beside it), two B-orthogonalisation passes,
+// and each B^{-1} applied by an FP64 GMRES solve with the mass operator's
+// local operator (stacks LB, RB).  The tridiagonal matrix and the selection
+// rules are those of cta_lanczos.  The returned vector is normalised as the
+// reference's local solver returns it: x^T B x = 1 for 'eigh' (mode 0,
+// scipy.linalg.eigh with b), |x| = 1 otherwise (scipy.linalg.eig with b).
+// ---------------------------------------------------------------------------
+
+template <bool G>
+__device__ __noinline__ CtaEigStats cta_glanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
+                                                const Contraction& q1, const Contraction& q2, const Contraction& q3,
+                                                const double* L, const double* A, const double* R,
+                                                const double* LB, const double* B, const double* RB, double* T1,
+                                                double* T2, double* x, double* V, double* BV, double* w, double* y,
+                                                double* gV, double* gr, double* gw, int64_t N, int m, int mg,
+                                                int mode, double sigma, int max_restarts, double tol, double* sm,
+                                                double* smg, const OzScratch* oz, int64_t* inner_its) {
+  double* al = sm;
+  double* be = al + m;
+  double* h1 = be + m;
+  double* h2 = h1 + m + 2;
+  double* z = h2 + m + 2;
+  double* twk = z + m;
+  int* piv = (int*)(twk + 5 * m + 8);
+  __shared__ double s_theta_g[kGroups<G>], s_res_g[kGroups<G>];
+  __shared__ int s_conv_g[kGroups<G>];
+  double& s_theta = s_theta_g[gidx<G>()];
+  double& s_res = s_res_g[gidx<G>()];
+  int& s_conv = s_conv_g[gidx<G>()];
+  const int tid = gtid<G>(), nt = gsize<G>(), lane = tid & 31, warp = tid >> 5;
+  CtaEigStats out{0.0, 0.0, 0, 0, ST_OK};
+  auto applyA = [&](const double* src, double* dst) {
+    cta_contract_f64<G>(p1, L, src, T1, oz);
+    cta_contract_f64<G>(p2, T1, A, T2, oz);
+    cta_contract_f64<G>(p3, T2, R, dst, oz);
+  };
+  auto applyB = [&](const double* src, double* dst) {
+    cta_contract_f64<G>(q1, LB, src, T1, oz);
+    cta_contract_f64<G>(q2, T1, B, T2, oz);
+    cta_contract_f64<G>(q3, T2, RB, dst, oz);
+  };
+  // B-normalise v (its image Bv computed into bv); false if v^T B v is not positive
+  auto bnormalise = [&](double* v, double* bv) {
+    applyB(v, bv);
+    double sb = 0.0;
+    for (int64_t e = tid; e < N; e += nt) sb += v[e] * bv[e];
+    const double nb2 = cta_sum<G>(sb);
+    if (!(nb2 > 0.0) || !isfinite(nb2)) return false;
+    const double inv = 1.0 / sqrt(nb2);
+    for (int64_t e = tid; e < N; e += nt) {
+      v[e] *= inv;
+      bv[e] *= inv;
+    }
+    gsync<G>();
+    return true;
+  };
+  if (tid == 0) {
+    s_conv = 0;
+    s_theta = 0.0;
+    s_res = 0.0;
+  }
+  for (int64_t e = tid; e < N; e += nt) V[e] = x[e];
+  gsync<G>();
+  if (!bnormalise(V, BV)) {
+    for (int64_t e = tid; e < N; e += nt) V[e] = 1.0;
+    gsync<G>();
+    if (!bnormalise(V, BV)) {
+      out.status = ST_SINGULAR;  // the mass operator is not positive definite
+      return out;
+    }
+  }
+  const int mm = (int)(N < m ? N : m);
+  for (;;) {
+    int nT = 0;
+    for (int j = 0; j < mm; ++j) {
+      applyA(V + (int64_t)j * N, w);
+      // y = B^{-1} w (zero start), FP64 to 1e-13
+      for (int64_t e = tid; e < N; e += nt) y[e] = 0.0;
+      gsync<G>();
+      long long c0 = 0, c1 = 0, c2 = 0;
+      const CtaSolveStats gs = cta_gmres_ir<double, G>(q1, q2, q3, LB, B, RB, T1, T2, LB, B, RB, T1, T2, w, y, gr, gV,
+                                                       gw, N, (int)(N < mg ? N : mg), 60, 1e-13, 0.0, smg, nullptr,
+                                                       &c0, &c1, &c2);
+      *inner_its += gs.inner;
+      if (gs.status != ST_OK) {
+        out.status = gs.status;
+        return out;
+      }
+      // two B-orthogonalisation passes: <v_q, y>_B = (B v_q)^T y
+      cta_dots<double, G>(BV, N, j + 1, y, h1);
+      for (int64_t e = tid; e < N; e += nt) {
+        double acc = y[e];
+        for (int q = 0; q <= j; ++q) acc -= h1[q] * V[(int64_t)q * N + e];
+        y[e] = acc;
+      }
+      gsync<G>();
+      cta_dots<double, G>(BV, N, j + 1, y, h2);
+      for (int64_t e = tid; e < N; e += nt) {
+        double acc = y[e];
+        for (int q = 0; q <= j; ++q) acc -= h2[q] * V[(int64_t)q * N + e];
+        y[e] = acc;
+      }
+      gsync<G>();
+      applyB(y, gw);  // B y
+      double sb = 0.0;
+      for (int64_t e = tid; e < N; e += nt) sb += y[e] * gw[e];
+      const double bj = sqrt(fmax(cta_sum<G>(sb), 0.0));
+      if (tid == 0) {
+        al[j] = h1[j] + h2[j];
+        be[j] = bj;
+      }
+      if (bj > 0.0 && j + 1 < mm) {
+        double* vn = V + (int64_t)(j + 1) * N;
+        double* bvn = BV + (int64_t)(j + 1) * N;
+        const double inv = 1.0 / bj;
+        for (int64_t e = tid; e < N; e += nt) {
+          vn[e] = y[e] * inv;
+          bvn[e] = gw[e] * inv;
+        }
+      }
+      gsync<G>();
+      ++out.its;
+      nT = j + 1;
+      double tnorm = 0.0;
+      for (int i = 0; i < nT; ++i)
+        tnorm = fmax(tnorm, fabs(al[i]) + fabs(be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      const bool breakdown = !(bj > 1e-14 * fmax(tnorm, 1e-300));
+      if ((nT % 4) == 0 || nT == mm || breakdown) {
+        if (warp == 0) {
+          double lo = 1e300, hi = -1e300;
+          for (int i = 0; i < nT; ++i) {
+            const double rad = (i > 0 ? fabs(be[i - 1]) : 0.0) + (i < nT - 1 ? fabs(be[i]) : 0.0);
+            lo = fmin(lo, al[i] - rad);
+            hi = fmax(hi, al[i] + rad);
+          }
+          const double pivmin = 1e-300 + DBL_MIN * fmax(1.0, tnorm * tnorm);
+          lo -= 1e-12 * fmax(1.0, tnorm);
+          hi += 1e-12 * fmax(1.0, tnorm);
+          int sel;
+          if (mode == 0) {
+            sel = nT - 1;
+          } else if (mode == 2) {
+            sel = 0;
+          } else {
+            const int below = sturm_count(al, be, nT, sigma, pivmin);
+            const double vdn = below > 0 ? tri_eigval(al, be, nT, below - 1, lo, hi, pivmin) : 0.0;
+            const double vup = below < nT ? tri_eigval(al, be, nT, below, lo, hi, pivmin) : 0.0;
+            sel = (below > 0 && (below >= nT || fabs(vdn - sigma) <= fabs(vup - sigma))) ? below - 1 : below;
+          }
+          const double th = tri_eigval(al, be, nT, sel, lo, hi, pivmin);
+          if (lane == 0) {
+            tri_eigvec(al, be, nT, th, fmax(tnorm, 1e-300), z, twk, piv);
+            s_theta = th;
+            s_res = bj * fabs(z[nT - 1]) / fmax(tnorm, 1e-300);
+            s_conv = (s_res <= tol) || breakdown;
+          }
+        }
+        gsync<G>();
+        if (s_conv || nT == mm) break;
+      } else if (breakdown) {
+        break;
+      }
+    }
+    // Ritz vector x = V z and its image B x = BV z (into w)
+    for (int64_t e = tid; e < N; e += nt) {
+      double acc = 0.0, bacc = 0.0;
+      for (int l = 0; l < nT; ++l) {
+        acc += z[l] * V[(int64_t)l * N + e];
+        bacc += z[l] * BV[(int64_t)l * N + e];
+      }
+      x[e] = acc;
+      w[e] = bacc;
+    }
+    gsync<G>();
+    if (s_conv || out.restarts >= max_restarts) break;
+    ++out.restarts;
+    for (int64_t e = tid; e < N; e += nt) V[e] = x[e];
+    gsync<G>();
+    if (!bnormalise(V, BV)) {
+      out.status = ST_SINGULAR;
+      return out;
+    }
+  }
+  // the reference's normalisation of the local eigenvector
+  double s2 = 0.0;
+  for (int64_t e = tid; e < N; e += nt) s2 += mode == 0 ? x[e] * w[e] : x[e] * x[e];
+  const double nrm2 = cta_sum<G>(s2);
+  if (nrm2 > 0.0 && isfinite(nrm2)) {
+    const double inv = 1.0 / sqrt(nrm2);
+    for (int64_t e = tid; e < N; e += nt) x[e] *= inv;
+  }
+  gsync<G>();
+  out.theta = s_theta;
+  out.res = s_res;
+  return out;
+}
+
 // QR of a core; with a shared-memory region (the group's tensor-core tiles,
 // idle between GEMMs) large enough for the matrix, in shared memory.
 template <bool G = false>
@@ -659,11 +860,17 @@ __device__ __forceinline__ void signal_done(int* flag) {
 // one instance
 // ---------------------------------------------------------------------------
 
-__host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp);
+__host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp, int gevp);
+__host__ __device__ inline size_t batch_lanczos_doubles(int m_evp) {
+  return (size_t)10 * m_evp + 12 + m_evp / 2 + 1;  // Lanczos arrays + pivots
+}
 
 struct Scratch {
   double *T1, *T2, *U, *f, *r, *w, *V, *rbuf, *qwork, *tmp0, *tmp1;
   float *Vf, *wf, *T1f, *T2f, *Lf, *Rf, *Af;
+  // generalised eigenproblems: B-images of the Lanczos basis, the inner
+  // GMRES basis and vectors (sized only when the batch holds such a request)
+  double *BV, *gV, *gy, *gr, *gw;
   OzScratch oz;
 };
 
@@ -696,6 +903,11 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   s.Lf = (float*)take(4 * z.stack);
   s.Rf = (float*)take(4 * z.stack);
   s.Af = (float*)take(4 * z.opcore);
+  s.BV = (double*)take(8 * (int64_t)(a.m_evp + 1) * z.Ng);
+  s.gV = (double*)take(8 * (int64_t)(a.m + 1) * z.Ng);
+  s.gy = (double*)take(8 * z.Ng);
+  s.gr = (double*)take(8 * z.Ng);
+  s.gw = (double*)take(8 * z.Ng);
   s.oz.as = (uint16_t*)take(2 * z.oz_a);
   s.oz.bs = (uint16_t*)take(2 * z.oz_b);
   s.oz.rexp = (int*)take(4 * z.oz_r);
@@ -943,14 +1155,18 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   const int64_t* M = a.meta + I.meta_off;
   const int64_t* n = M;
   const int64_t* R = n + d;
-  const int64_t* rb = R + d + 1;
+  const int64_t* rb = R + d + 1;  // generalised problems: ranks of operator_gevp
   const int64_t* rx0 = rb + d + 1;
   const int64_t* cap = rx0 + d + 1;
   const int64_t* op_off = cap + d + 1;
+  const int64_t* rhs_off = op_off + d;  // ... its cores
   const int64_t* x0_off = op_off + 2 * d;
   const int64_t* X_off = x0_off + d;
   const int64_t* L_off = X_off + d;
   const int64_t* Rt_off = L_off + d;
+  const int64_t* Lb_off = Rt_off + d;   // ... and its stacks
+  const int64_t* Rb_off = Lb_off + d;
+  const bool gevp = I.kind == 2;
   __shared__ int64_t r_g[kGroups<G>][kMaxOrderB + 1];
   __shared__ int64_t ropt_g[kGroups<G>][kMaxOrderB + 1];
   int64_t* r = r_g[gidx<G>()];
@@ -966,8 +1182,13 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   auto L = [&](int i) { return I.L + L_off[i]; };
   auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
   auto A = [&](int i) { return I.op + op_off[i]; };
+  auto Bg = [&](int i) { return I.rhs + rhs_off[i]; };
+  auto LB = [&](int i) { return I.Lb + Lb_off[i]; };
+  auto RB = [&](int i) { return I.Rb + Rb_off[i]; };
+  int64_t ginner = 0;  // inner mass-operator GMRES iterations
   double fl64 = 0.0, fl32 = 0.0, maxres = 0.0, theta = 0.0;
   int64_t nsolve = 0, nits = 0, nrst = 0;
+  int evp_status = ST_OK;
   auto apply_fl = [&](double aa, double nn, double ss, double r0, double r1) {
     return 2 * aa * aa * r0 * nn * ss + 2 * aa * ss * nn * nn * r0 * r1 + 2 * aa * nn * ss * ss * r1;
   };
@@ -989,7 +1210,10 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   }
   auto right = [&](int i) {
     if (i == d - 1) {
-      if (tid == 0) Rt(i)[0] = 1.0;
+      if (tid == 0) {
+        Rt(i)[0] = 1.0;
+        if (gevp) RB(i)[0] = 1.0;
+      }
       gsync<G>();
       return;
     }
@@ -1000,10 +1224,20 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     cta_contract_f64<G>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
     cta_contract_f64<G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
+    if (gevp) {  // evp.py:314-329
+      desc_right(aa, nn, ss, rb[i + 1], rb[i + 2], &q1, &q2, &q3);
+      cta_contract_f64<G>(q1, (const double*)RB(i + 1), (const double*)X(i + 1), S.T1, oz);
+      cta_contract_f64<G>(q2, (const double*)S.T1, Bg(i + 1), S.T2, oz);
+      cta_contract_f64<G>(q3, (const double*)X(i + 1), (const double*)S.T2, RB(i), oz);
+      fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)rb[i + 1], (double)rb[i + 2]);
+    }
   };
   auto left = [&](int i) {
     if (i == 0) {
-      if (tid == 0) L(i)[0] = 1.0;
+      if (tid == 0) {
+        L(i)[0] = 1.0;
+        if (gevp) LB(i)[0] = 1.0;
+      }
       gsync<G>();
       return;
     }
@@ -1014,6 +1248,13 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     cta_contract_f64<G>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
     cta_contract_f64<G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
+    if (gevp) {  // evp.py:272-287
+      desc_apply(aa, nn, ss, rb[i - 1], rb[i], &p1, &p2, &p3);
+      cta_contract_f64<G>(p1, (const double*)LB(i - 1), (const double*)X(i - 1), S.T1, oz);
+      cta_contract_f64<G>(p2, (const double*)S.T1, Bg(i - 1), S.T2, oz);
+      cta_contract_f64<G>(desc_left_p3(aa, nn, ss, rb[i]), (const double*)S.T2, (const double*)X(i - 1), LB(i), oz);
+      fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)rb[i - 1], (double)rb[i]);
+    }
   };
   auto solve = [&](int i) {
     const int64_t aa = r[i], nn = n[i], ss = r[i + 1], N = aa * nn * ss;
@@ -1026,8 +1267,18 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     // site, and an FP32 Lanczos pre-stage (then FP64 polish) measured 2.8x
     // slower.  In mixed precision their products (and the stacks) run as
     // emulated FP64 on the tensor cores.
-    const CtaEigStats st = cta_lanczos<double, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m,
-                                               I.mode, I.sigma, kBatchEvpRestarts, a.tol_evp, sm, oz);
+    CtaEigStats st;
+    if (gevp) {
+      Contraction g1, g2, g3;
+      desc_apply(aa, nn, ss, rb[i], rb[i + 1], &g1, &g2, &g3);
+      st = cta_glanczos<G>(p1, p2, p3, g1, g2, g3, L(i), A(i), Rt(i), LB(i), Bg(i), RB(i), S.T1, S.T2, X(i), S.V,
+                           S.BV, S.w, S.gy, S.gV, S.gr, S.gw, N, m, a.m, I.mode, I.sigma, kBatchEvpRestarts,
+                           a.tol_evp, sm, sm + batch_lanczos_doubles(a.m_evp), oz, &ginner);
+      if (st.status != ST_OK && evp_status == ST_OK) evp_status = st.status;
+    } else {
+      st = cta_lanczos<double, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m, I.mode, I.sigma,
+                                  kBatchEvpRestarts, a.tol_evp, sm, oz);
+    }
     theta = st.theta;
     nits += st.its;
     nrst += st.restarts;
@@ -1041,7 +1292,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   double val_opt = INFINITY;
   int it = 1;
   bool conv = false, have_opt = false;
-  while (it <= I.repeats && !conv) {
+  while (it <= I.repeats && !conv && evp_status == ST_OK) {
     for (int i = 0; i < d; ++i) {
       left(i);
       if (i < d - 1) {
@@ -1096,9 +1347,9 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   if (tid == 0) {
     I.report[0] = maxres;
     I.report[1] = (double)nsolve;
-    I.report[2] = (double)nits;
+    I.report[2] = (double)(nits + ginner);
     I.report[3] = (double)nrst;
-    I.report[4] = (double)ST_OK;
+    I.report[4] = (double)evp_status;
     I.report[5] = fl64;
     I.report[6] = fl32;
     I.report[7] = val_opt;
@@ -1152,8 +1403,8 @@ __host__ __device__ inline size_t tc_tiles_offset(size_t before) { return (befor
 
 // Dynamic shared memory of one group: GMRES / Lanczos scalars, the
 // contraction-offset table, and (tensor-core variant) the operand tiles.
-__host__ __device__ size_t batch_group_smem_bytes(int m, int m_evp, int use_tc) {
-  const size_t base = batch_smem_scalar_bytes(m, m_evp) + sizeof(int) * 2 * kTcMaxK;
+__host__ __device__ size_t batch_group_smem_bytes(int m, int m_evp, int use_tc, int gevp) {
+  const size_t base = batch_smem_scalar_bytes(m, m_evp, gevp) + sizeof(int) * 2 * kTcMaxK;
   return use_tc ? tc_tiles_offset(base) + kTcSmemBytes : base;
 }
 
@@ -1170,11 +1421,12 @@ __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
   __shared__ int s_j[NG];
   __shared__ TcState s_tc[NG];
   const int g = gidx<UseTc>();
-  const size_t gbytes = batch_group_smem_bytes(a.m, a.m_evp, UseTc ? 1 : 0);
+  const int gevp = a.sizes.Ng > 0 ? 1 : 0;
+  const size_t gbytes = batch_group_smem_bytes(a.m, a.m_evp, UseTc ? 1 : 0, gevp);
   unsigned char* mine = smraw + gbytes * g;
   double* sm = reinterpret_cast<double*>(mine);
   Scratch S = scratch_of(a, (int)blockIdx.x * NG + g);
-  const size_t scal = batch_smem_scalar_bytes(a.m, a.m_evp);
+  const size_t scal = batch_smem_scalar_bytes(a.m, a.m_evp, gevp);
   S.oz.ktab = reinterpret_cast<int*>(mine + scal);
   if constexpr (UseTc) {
     tc_begin(s_tc, NG, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK), gbytes);
@@ -1195,7 +1447,7 @@ __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
     const int j = s_j[g];
     gsync<UseTc>();
     if (j >= a.count) break;
-    if (a.inst[j].kind == 1)
+    if (a.inst[j].kind != 0)
       batch_evp<UseTc>(a, j, S, sm);
     else
       batch_solve<UseTc>(a, j, S, sm);
@@ -1340,14 +1592,16 @@ cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_
 // dynamic shared memory: the GMRES / Lanczos scalars, then one contraction-offset
 // table shared by the FP32 tensor-core apply and the emulated-FP64 contractions
 // (never used at the same time); the rest of the SM's 256 KB stays L1
-__host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp) {
+// (gevp: the Lanczos arrays and, after them, those of the inner GMRES solves
+// with the mass operator, both live at once)
+__host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp, int gevp) {
   const size_t g = (size_t)(m + 1) * m + 2 * m + (m + 1) + m + 2 * (m + 2);
-  const size_t e = (size_t)10 * m_evp + 12 + m_evp / 2 + 1;  // Lanczos arrays + pivots
-  return sizeof(double) * (g > e ? g : e);
+  const size_t e = batch_lanczos_doubles(m_evp);
+  return sizeof(double) * (gevp ? g + e : (g > e ? g : e));
 }
 
-size_t batch_smem_bytes(int m, int m_evp, int use_tc) {
-  return batch_group_smem_bytes(m, m_evp, use_tc) * (use_tc ? kGroups<true> : 1);
+size_t batch_smem_bytes(int m, int m_evp, int use_tc, int gevp) {
+  return batch_group_smem_bytes(m, m_evp, use_tc, gevp) * (use_tc ? kGroups<true> : 1);
 }
 
 int batch_solves_per_cta(int use_tc) { return use_tc ? kGroups<true> : 1; }
@@ -1357,15 +1611,16 @@ int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
   auto r = [](int64_t b) { return (b + 255) / 256 * 256; };
   return r(8 * z.T) * 2 + r(8 * z.U) + r(8 * z.N) * 3 + r(8 * (int64_t)(m + 1) * z.N) + r(8 * z.R) + r(8 * z.Q) +
          r(8 * z.core) * 2 + r(4 * (int64_t)(m + 1) * z.N) + r(4 * z.N) + r(4 * z.T) * 2 + r(4 * z.stack) * 2 +
-         r(4 * z.opcore) + r(2 * z.oz_a) + r(2 * z.oz_b) + r(4 * z.oz_r) + r(4 * z.oz_c);
+         r(4 * z.opcore) + r(8 * (int64_t)(m_evp + 1) * z.Ng) + r(8 * (int64_t)(mg + 1) * z.Ng) + r(8 * z.Ng) * 3 +
+         r(2 * z.oz_a) + r(2 * z.oz_b) + r(4 * z.oz_r) + r(4 * z.oz_c);
 }
 
 int batch_threads(int use_tc) { return use_tc ? kBatchThreadsTc : kBatchThreads; }
 
 // Resident CTAs per SM of the kernel variant; *err (if given) receives the
 // first CUDA error of the query (the result is then 1).
-int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err) {
-  const size_t smem = batch_smem_bytes(m, m_evp, use_tc);
+int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err, int gevp) {
+  const size_t smem = batch_smem_bytes(m, m_evp, use_tc, gevp);
   const void* fn = use_tc ? (const void*)batch_sle_tc_kernel : (const void*)batch_sle_kernel;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
@@ -1382,7 +1637,7 @@ int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err) {
 }
 
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st) {
-  const size_t smem = batch_smem_bytes(a.m, a.m_evp, a.use_tc);
+  const size_t smem = batch_smem_bytes(a.m, a.m_evp, a.use_tc, a.sizes.Ng > 0 ? 1 : 0);
   const void* fn = a.use_tc ? (const void*)batch_sle_tc_kernel : (const void*)batch_sle_kernel;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

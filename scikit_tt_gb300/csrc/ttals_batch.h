@@ -28,6 +28,7 @@ struct BatchInst {
 // Largest per-CTA scratch needs over the batch (elements).
 struct BatchSizes {
   int64_t T, U, N, R, Q, core, stack, opcore;
+  int64_t Ng;  // N when the batch holds a generalised eigenproblem, else 0 (its extra scratch)
   int64_t oz_a, oz_b, oz_r, oz_c;  // emulated-FP64 GEMM scratch: slice arrays and exponent vectors
 };
 
@@ -51,8 +52,8 @@ struct BatchArgs {
   int use_tc;      // mixed precision on tcgen05 (batch_sle_tc_kernel)
 };
 
-size_t batch_smem_bytes(int m, int m_evp, int use_tc);
-int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err = nullptr);
+size_t batch_smem_bytes(int m, int m_evp, int use_tc, int gevp = 0);
+int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err = nullptr, int gevp = 0);
 int batch_threads(int use_tc);
 // independent solves one CTA of the variant runs side by side (scratch slots per CTA)
 int batch_solves_per_cta(int use_tc);

@@ -28,7 +28,9 @@ _PREC = {'fp64': _lib.PREC_FP64, 'mixed': _lib.PREC_MIXED}
 @dataclass
 class Request:
     """One ALS problem.  kind 'sle': ``op @ x = rhs`` (sle.py:10); kind 'evp':
-    eigenpair of the symmetric ``op`` (evp.py:17)."""
+    eigenpair of the symmetric ``op`` (evp.py:17); kind 'gevp': eigenpair of
+    ``op x = lambda rhs x`` with ``rhs`` the symmetric positive definite
+    ``operator_gevp`` (evp.py:17 with operator_gevp)."""
     kind: str
     op: List[np.ndarray]
     x0: List[np.ndarray]
@@ -49,7 +51,7 @@ class Request:
     def _descriptor(self):
         lib = _lib.load()
         op, x0 = _lib.Packed(self.op), _lib.Packed(self.x0)
-        rhs = _lib.Packed(self.rhs) if self.kind == 'sle' else x0
+        rhs = _lib.Packed(self.rhs) if self.kind in ('sle', 'gevp') else x0
         dims = np.array([c.shape[1] for c in self.op], dtype=np.int64)
         ranks = np.zeros(len(dims) + 1, dtype=np.int64)
         _lib.check(lib.ttals_als_ranks(len(dims), _lib.i64ptr(dims), _lib.i64ptr(x0.ranks), _lib.i64ptr(ranks)))
@@ -57,7 +59,7 @@ class Request:
         val = np.zeros(1)
         its = np.zeros(1, dtype=np.int32)
         r = _lib.Request()
-        r.kind = _lib.REQ_SLE if self.kind == 'sle' else _lib.REQ_EVP
+        r.kind = {'sle': _lib.REQ_SLE, 'evp': _lib.REQ_EVP, 'gevp': _lib.REQ_GEVP}[self.kind]
         r.op, r.x0, r.rhs = op.desc, x0.desc, rhs.desc
         r.repeats = int(self.repeats)
         solver = self.solver or ('solve' if self.kind == 'sle' else 'eig')
@@ -81,12 +83,12 @@ class Request:
         for i, c in enumerate(self.op):
             n, a, s, R0, R1 = c.shape[1], r[i], r[i + 1], R[i], R[i + 1]
             w += a * a * R0 * n * s + a * s * n * n * R0 * R1 + a * n * s * s * R1
-        return w * max(1, int(self.repeats)) * (4.0 if self.kind == 'evp' else 1.0)
+        return w * max(1, int(self.repeats)) * (1.0 if self.kind == 'sle' else 4.0)
 
     def _complete(self):
         _, _, _, out, val, its, ranks, dims = self._keep
         self.solution = TT(_lib.unpack(out, dims, [1] * len(dims), ranks))
-        if self.kind == 'evp':
+        if self.kind != 'sle':
             self.value = float(val[0])
             self.iterations = int(its[0])
         self._keep = []

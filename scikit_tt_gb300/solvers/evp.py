@@ -15,8 +15,14 @@ singular directions as in evp.py:455-486, and the last sweep's eigenvalues and
 eigentensors are returned (evp.py:170-177).
 
 Implemented: ``number_ev`` 1..8, ``previous`` / ``shift`` deflation,
-``operator_gevp`` equal to the identity train.  Generalised problems with
-another ``operator_gevp``, ``'eigh'`` on a nonsymmetric operator and wanted
+``operator_gevp`` equal to the identity train, and generalised problems
+``A x = lambda B x`` with a symmetric operator and a symmetric positive
+definite ``operator_gevp`` (``number_ev == 1``, no ``previous``): those run as
+one request of the batched engine (``ttals_solve_batch``, request kind
+``TTALS_REQ_GEVP``), whose local solver is Lanczos on ``B^{-1} A`` in the B
+inner product with FP64 GMRES solves for ``B^{-1}`` (evp.py:272-287,
+314-329, 367-368 and the ``b=`` / ``M=`` local solves of evp.py:410-439).
+Other generalised problems, ``'eigh'`` on a nonsymmetric operator and wanted
 eigenvalues with a nonzero imaginary part raise ``NotImplementedError``.
 """
 
@@ -69,6 +75,37 @@ def _is_symmetric(op: TT) -> bool:
     return nrm > 0 and _host_norm((op - op.transpose()).cores) <= 1e-12 * nrm
 
 
+def _gevp_als(operator, initial_guess, operator_gevp, repeats, conv_eps, solver, sigma):
+    """Generalised symmetric-definite problem through the batched engine (one
+    request on one CTA, FP64).  Returns the reference's ``(eigenvalue,
+    eigentensor, iterations)`` for ``number_ev == 1``."""
+    global last_stats
+    lib = _lib.load()
+    op, x0, og = _lib.Packed(operator.cores), _lib.Packed(initial_guess.cores), _lib.Packed(operator_gevp.cores)
+    dims = np.array(operator.row_dims, dtype=np.int64)
+    ranks = np.zeros(operator.order + 1, dtype=np.int64)
+    _lib.check(lib.ttals_als_ranks(operator.order, _lib.i64ptr(dims), _lib.i64ptr(x0.ranks), _lib.i64ptr(ranks)))
+    out = np.empty(max(1, int(sum(ranks[i] * dims[i] * ranks[i + 1] for i in range(operator.order)))))
+    val = np.zeros(1)
+    its = np.zeros(1, dtype=np.int32)
+    r = _lib.Request()
+    r.kind = _lib.REQ_GEVP
+    r.op, r.x0, r.rhs = op.desc, x0.desc, og.desc
+    r.repeats = int(repeats)
+    r.solver = _lib.EVP_SOLVERS[solver]
+    r.sigma = float(sigma)
+    r.conv_eps = float(conv_eps)
+    r.out_data = _lib.dptr(out)
+    r.out_value = _lib.dptr(val)
+    r.out_iterations = its.ctypes.data_as(_lib.C.POINTER(_lib.C.c_int32))
+    arr = (_lib.Request * 1)(r)
+    st = _lib.Stats()
+    _lib.check(lib.ttals_solve_batch(_lib.context(), 1, arr, _lib.PREC_FP64, 0.0, 0, st))
+    last_stats = st.as_dict()
+    cores = _lib.unpack(out, operator.row_dims, [1] * operator.order, ranks)
+    return np.float64(val[0]), TT(cores), int(its[0])
+
+
 def als(operator: 'TT', initial_guess: 'TT', previous: List['TT'] = [], shift: float = 0,
         operator_gevp: 'TT' = None, number_ev: int = 1, repeats: int = 1, conv_eps: float = 1e-10,
         solver: str = 'eig', sigma: float = 1, real: bool = True):
@@ -77,8 +114,17 @@ def als(operator: 'TT', initial_guess: 'TT', previous: List['TT'] = [], shift: f
     if solver not in _lib.EVP_SOLVERS:
         raise ValueError("solver must be 'eig', 'eigs' or 'eigh'")
     if not _is_identity(operator_gevp):
-        raise NotImplementedError('generalised eigenproblems (operator_gevp other than the identity) are not '
-                                  'implemented on the device path')
+        if operator_gevp.row_dims != operator.row_dims or operator_gevp.col_dims != operator.col_dims:
+            raise ValueError('operator_gevp must have the dimensions of operator')
+        if number_ev != 1 or len(previous) > 0:
+            raise NotImplementedError('generalised eigenproblems support number_ev == 1 without previous on the '
+                                      'device path')
+        if not (_is_symmetric(operator) and _is_symmetric(operator_gevp)):
+            raise NotImplementedError('generalised eigenproblems need a symmetric operator and a symmetric '
+                                      'positive definite operator_gevp on the device path')
+        if repeats < 1:
+            return np.inf, None, 0
+        return _gevp_als(operator, initial_guess, operator_gevp, repeats, conv_eps, solver, sigma)
     if solver == 'eigh' and not _is_symmetric(operator):
         raise NotImplementedError("solver='eigh' needs a symmetric operator")
     if not 1 <= number_ev <= 8:

@@ -632,6 +632,38 @@ def triple_well_case():
 BATCH_SUBSET = list(range(16))   # the 16 smallest-seed instances of the uneven batch
 
 
+def gevp_case(name, op, gevp, x0, repeats, solver, sigma, conv_eps=1e-10):
+    """evp.als with a non-identity operator_gevp (evp.py:272-287, 314-329, 367-368, 410-439)."""
+    val, vec, its = revp.als(RTT([c.copy() for c in op]), RTT([c.copy() for c in x0]),
+                             operator_gevp=RTT([c.copy() for c in gevp]), repeats=repeats, solver=solver,
+                             sigma=sigma, conv_eps=conv_eps)
+    out = {'repeats': np.array(repeats), 'solver': np.array(solver), 'sigma': np.array(sigma),
+           'conv_eps': np.array(conv_eps), 'val': np.array(val), 'its': np.array(its)}
+    pack('op', op, out)
+    pack('gevp', gevp, out)
+    pack('x0', x0, out)
+    pack('vec', vec.cores, out)
+    # the dense pencil's eigenvalues, for the eigenvalues the ALS approaches
+    A = RTT([c.copy() for c in op]).matricize()
+    B = RTT([c.copy() for c in gevp]).matricize()
+    out['pencil_vals'] = np.sort(sla.eigh(A, B, eigvals_only=True))
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print(name, 'val', val, 'its', its, 'pencil ends', out['pencil_vals'][[0, -1]])
+
+
+def gevp_cases():
+    """Ising d=6 (g=1.2) against the SPD mass operator sum_i L_i + I (L = [[2,-1],[-1,2]]),
+    right-orthonormal rank-4 guess: the lowest generalised eigenpair ('eig', sigma below the
+    spectrum) and the largest ('eigh')."""
+    d = 6
+    op = wl.ising_op(d, 1.0, 1.2)
+    gevp = wl.laplace_op(d, 2, h=1.0, shift=1.0)
+    rng = np.random.default_rng(11)
+    x0 = [c.copy() for c in RTT(wl.gaussian_tt(rng, d, 2, 4)).ortho_right().cores]
+    gevp_case('evp_gevp_ising_d6_eig', op, gevp, x0, 4, 'eig', -3.0)
+    gevp_case('evp_gevp_ising_d6_eigh', op, gevp, x0, 4, 'eigh', 1.0)
+
+
 def batch_subset_case():
     """The 16 smallest-seed instances of the uneven batch (instance j from
     default_rng(1000 + j): d 8..32, n in {2,4,8}, ranks 4..48, 4 sweeps), each
@@ -724,6 +756,8 @@ if __name__ == '__main__':
         triple_well_case()
     elif len(sys.argv) > 1 and sys.argv[1] == 'headline':
         headline_case()
+    elif len(sys.argv) > 1 and sys.argv[1] == 'gevp':
+        gevp_cases()
     elif len(sys.argv) > 1 and sys.argv[1] == 'batch_subset':
         batch_subset_case()
     else:

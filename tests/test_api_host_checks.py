@@ -47,14 +47,22 @@ def test_evp_checks():
     x0 = TT([np.ones((1, 2, 1, 2)), np.ones((2, 2, 1, 2)), np.ones((2, 2, 1, 2)), np.ones((2, 2, 1, 1))])
     with pytest.raises(ValueError):
         evp.als(H, x0, solver='lobpcg')
+    M = 2.0 * TT([np.eye(2).reshape(1, 2, 2, 1) for _ in range(4)])
+    # generalised problems run with number_ev == 1, no deflation, symmetric operators
     with pytest.raises(NotImplementedError):
-        evp.als(H, x0, operator_gevp=2.0 * TT([np.eye(2).reshape(1, 2, 2, 1) for _ in range(4)]))
+        evp.als(H, x0, operator_gevp=M, number_ev=2)
+    with pytest.raises(NotImplementedError):
+        evp.als(H, x0, previous=[x0], operator_gevp=M)
     with pytest.raises(NotImplementedError):
         evp.als(H, x0, number_ev=9)
     rng = np.random.default_rng(0)
     N = TT([rng.standard_normal((1, 2, 2, 1)) for _ in range(4)])
     with pytest.raises(NotImplementedError):
         evp.als(N, x0, solver='eigh')
+    with pytest.raises(NotImplementedError):
+        evp.als(H, x0, operator_gevp=N)
+    with pytest.raises(ValueError):
+        evp.als(H, x0, operator_gevp=TT([2 * np.eye(3).reshape(1, 3, 3, 1) for _ in range(4)]))
 
 
 def test_identity_gevp_is_accepted():

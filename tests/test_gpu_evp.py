@@ -183,3 +183,43 @@ def test_triple_well_identity_gevp_and_power_method(golden):
     assert abs(pv - top) / abs(top) < 5e-3
     assert abs(pv - float(z['power_val'])) <= 1e-8 * abs(float(z['power_val']))
     assert _vec_err(pvec.matricize(), z['power_vec']) < 1e-6
+
+
+@pytest.mark.parametrize('name', ['evp_gevp_ising_d6_eig', 'evp_gevp_ising_d6_eigh'])
+def test_gevp_matches_reference(golden, name):
+    """Generalised problem A x = lambda B x with an SPD mass operator (evp.py:272-287,
+    314-329, 367-368 and the b= local solves of evp.py:423-439): the reference's
+    eigenvalue to 1e-9 and eigentensor to 1e-6 up to sign (unit 2-norm for 'eig',
+    unit B-norm for 'eigh', as the reference's local solvers return them)."""
+    from scikit_tt_gb300.solvers import evp
+    z, cores = golden(name)
+    val, vec, its = evp.als(_tt(cores('op')), _tt(cores('x0')), operator_gevp=_tt(cores('gevp')),
+                            repeats=int(z['repeats']), solver=str(z['solver']), sigma=float(z['sigma']),
+                            conv_eps=float(z['conv_eps']))
+    ref = float(z['val'])
+    assert abs(val - ref) <= 1e-9 * max(1.0, abs(ref))
+    assert its == int(z['its'])
+    assert _vec_err(vec.matricize(), _tt(cores('vec')).matricize()) < 1e-6
+    assert evp.last_stats['local_solves'] > 0
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_gevp_in_a_mixed_batch(golden, precision):
+    """A generalised request beside a linear system and a standard eigenproblem in one
+    launch: each matches its own reference result."""
+    from scikit_tt_gb300 import workloads as wl
+    from scikit_tt_gb300.serving import Request, solve_batch
+    zg, cg = golden('evp_gevp_ising_d6_eig')
+    w = wl.laplace_sle(d=6, n=2, rhs_rank=2, x_rank=3, repeats=2, seed=4)
+    we = wl.ising_evp(d=6, g=0.8, x_rank=3, repeats=3, seed=2)
+    reqs = [Request('gevp', cg('op'), cg('x0'), cg('gevp'), repeats=int(zg['repeats']), solver='eig',
+                    sigma=float(zg['sigma']), conv_eps=float(zg['conv_eps'])),
+            Request('sle', w.op, w.x0, w.rhs, repeats=w.repeats),
+            Request('evp', we.op, we.x0, repeats=we.repeats, sigma=we.sigma)]
+    solve_batch(reqs, precision=precision)
+    assert abs(reqs[0].value - float(zg['val'])) <= 1e-9 * max(1.0, abs(float(zg['val'])))
+    assert _vec_err(reqs[0].solution.matricize(), _tt(cg('vec')).matricize()) < 1e-6
+    tol = 1e-10 if precision == 'fp64' else 1e-8
+    assert O.stable_rel_diff(reqs[1].solution.cores, O.sle_als(w.op, w.x0, w.rhs, repeats=w.repeats)) < tol
+    ref_val, _, _ = O.evp_als(we.op, O.ortho_right(we.x0), repeats=we.repeats, sigma=we.sigma)
+    assert abs(reqs[2].value - ref_val) < 1e-9

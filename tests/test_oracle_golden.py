@@ -46,6 +46,22 @@ def test_oracle_evp_matches_reference(golden, name):
     assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-7
 
 
+@pytest.mark.parametrize('name', ['evp_gevp_ising_d6_eig', 'evp_gevp_ising_d6_eigh'])
+def test_oracle_gevp_matches_reference(golden, name):
+    """Generalised problem (operator_gevp = SPD mass operator): the oracle's
+    stacks and dense local pencil solve against the reference's result, and
+    the eigenvalue against the dense pencil's extreme eigenvalue."""
+    z, cores = golden(name)
+    val, vec, its = O.evp_als(cores('op'), cores('x0'), op_gevp=cores('gevp'), repeats=int(z['repeats']),
+                              solver=str(z['solver']), sigma=float(z['sigma']), conv_eps=float(z['conv_eps']))
+    assert abs(val - float(z['val'])) < 1e-10
+    assert its == int(z['its'])
+    want = z['pencil_vals'][0] if str(z['solver']) == 'eig' else z['pencil_vals'][-1]
+    assert abs(val - want) < 1e-7      # rank-4 ALS after four sweeps
+    v, r = O.full_vector(vec), O.full_vector(cores('vec'))
+    assert min(np.linalg.norm(v - r), np.linalg.norm(v + r)) / np.linalg.norm(r) < 1e-7
+
+
 def test_oracle_ising_free_fermion():
     # E0 of the d=12 chain from free fermions vs the dense spectrum
     op = wl.ising_op(8, 1.0, 1.0)
