@@ -224,9 +224,11 @@ int ttals_batch_bytes(ttals_ctx* ctx, int32_t count, const ttals_request* reqs, 
 
 /* scikit_tt/solvers/evp.py:17 `als(operator, initial_guess, previous, shift,
  * operator_gevp=None, number_ev, repeats, conv_eps, solver, sigma, real)` for
- * symmetric operators.  out_vals[number_ev]; out_data as for ttals_sle_als
- * (for number_ev > 1 core 0 carries a trailing axis of length number_ev, the
- * 5-D core of evp.py:492-493).  *iterations as evp.py:177. */
+ * symmetric operators (operator_gevp = identity; a symmetric positive
+ * definite operator_gevp goes through ttals_solve_batch, TTALS_REQ_GEVP).
+ * out_vals[number_ev]; out_data as for ttals_sle_als (for number_ev > 1 core
+ * 0 carries a trailing axis of length number_ev, the 5-D core of
+ * evp.py:492-493).  *iterations as evp.py:177. */
 int ttals_evp_als(ttals_ctx* ctx, const ttals_tt* op, const ttals_tt* x0, int32_t n_previous,
                   const ttals_tt* previous, double shift, int32_t number_ev, int32_t repeats,
                   double conv_eps, int32_t solver, double sigma, int32_t precision, double tol,
