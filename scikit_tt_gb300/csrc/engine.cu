@@ -1698,6 +1698,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
       P.z.stack = std::max(P.z.stack, std::max(a * R[i] * a, s * R[i + 1] * s));
       P.z.opcore = std::max(P.z.opcore, R[i] * nn * nn * R[i + 1]);
       if (prec == TTALS_PREC_MIXED) oz_need_site(P.z, a, nn, s, R[i], R[i + 1]);
+      if (I.kind != 0) P.z.Q = std::max<int64_t>(P.z.Q, 2 * kBatchMEvp * kBatchMEvp);  // thick-restart matrices
       if (I.kind == 2) {
         P.z.Ng = std::max(P.z.Ng, a * nn * s);
         P.z.stack = std::max(P.z.stack, std::max(a * rb[i] * a, s * rb[i + 1] * s));

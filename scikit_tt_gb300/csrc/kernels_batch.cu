@@ -486,6 +486,98 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
 // (see lanczos_kernel for the grid version and the selection rules)
 // ---------------------------------------------------------------------------
 
+// Symmetric eigen-decomposition of H (n x n, leading dimension ld, n <= 64)
+// by the group: cyclic Jacobi with the round-robin parallel ordering (n/2
+// disjoint rotations per round, each applied to the columns of H and Z, then
+// to the rows of H), until the off-diagonal mass is below 1e-32 of the total
+// (at most 30 sweeps).  On return H's diagonal holds the eigenvalues and Z's
+// columns the eigenvectors.
+constexpr int kSymEigMax = 64;
+template <bool G>
+__device__ __noinline__ void cta_sym_eig(double* H, double* Z, int n, int ld) {
+  __shared__ int ra_g[kGroups<G>][kSymEigMax / 2], rb_g[kGroups<G>][kSymEigMax / 2];
+  __shared__ double rc_g[kGroups<G>][kSymEigMax / 2], rs_g[kGroups<G>][kSymEigMax / 2];
+  int* ra = ra_g[gidx<G>()];
+  int* rb = rb_g[gidx<G>()];
+  double* rc = rc_g[gidx<G>()];
+  double* rs = rs_g[gidx<G>()];
+  const int tid = gtid<G>(), nt = gsize<G>();
+  const int npl = n + (n & 1), npairs = npl / 2;
+  for (int idx = tid; idx < n * n; idx += nt) {
+    const int r = idx / n, c = idx - r * n;
+    Z[r * ld + c] = r == c ? 1.0 : 0.0;
+  }
+  gsync<G>();
+  if (n < 2) return;
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    double so = 0.0, st = 0.0;
+    for (int idx = tid; idx < n * n; idx += nt) {
+      const int r = idx / n, c = idx - r * n;
+      const double v = H[r * ld + c];
+      st += v * v;
+      if (r < c) so += v * v;
+    }
+    so = cta_sum<G>(so);
+    st = cta_sum<G>(st);
+    if (!(so > 1e-32 * st)) break;
+    for (int round = 0; round < npl - 1; ++round) {
+      if (tid < npairs) {
+        const int pk = tid, qk = npl - 1 - tid;
+        int a = pk == 0 ? 0 : 1 + (pk - 1 + round) % (npl - 1);
+        int b = 1 + (qk - 1 + round) % (npl - 1);
+        if (a > b) {
+          const int t = a;
+          a = b;
+          b = t;
+        }
+        double c = 1.0, sn = 0.0;
+        if (b < n) {
+          const double apq = H[a * ld + b];
+          if (fabs(apq) > 1e-300) {
+            const double theta = (H[b * ld + b] - H[a * ld + a]) / (2.0 * apq);
+            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+            c = 1.0 / sqrt(fma(t, t, 1.0));
+            sn = t * c;
+          }
+        }
+        ra[tid] = (b < n && sn != 0.0) ? a : -1;
+        rb[tid] = b;
+        rc[tid] = c;
+        rs[tid] = sn;
+      }
+      gsync<G>();
+      for (int idx = tid; idx < npairs * n; idx += nt) {
+        const int k = idx / n, i = idx - k * n;
+        const int a = ra[k];
+        if (a < 0) continue;
+        const int b = rb[k];
+        const double c = rc[k], sn = rs[k];
+        const double ha = H[i * ld + a], hb = H[i * ld + b];
+        H[i * ld + a] = c * ha - sn * hb;
+        H[i * ld + b] = sn * ha + c * hb;
+        const double za = Z[i * ld + a], zb = Z[i * ld + b];
+        Z[i * ld + a] = c * za - sn * zb;
+        Z[i * ld + b] = sn * za + c * zb;
+      }
+      gsync<G>();
+      for (int idx = tid; idx < npairs * n; idx += nt) {
+        const int k = idx / n, i = idx - k * n;
+        const int a = ra[k];
+        if (a < 0) continue;
+        const int b = rb[k];
+        const double c = rc[k], sn = rs[k];
+        const double ha = H[a * ld + i], hb = H[b * ld + i];
+        H[a * ld + i] = c * ha - sn * hb;
+        H[b * ld + i] = sn * ha + c * hb;
+      }
+      gsync<G>();
+    }
+  }
+}
+
+// Ritz vectors kept by a thick restart of the CTA Lanczos
+constexpr int kLanczosKeep = 8;
+
 struct CtaEigStats {
   double theta, res;
   int its, restarts, status;
@@ -499,7 +591,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
                                                const TI* L, const TI* A, const TI* R, TI* T1, TI* T2, double* x,
                                                TI* V, TI* w, int64_t N, int m, int mode, double sigma,
                                                int max_restarts, double tol, double* sm,
-                                               const OzScratch* oz = nullptr) {
+                                               const OzScratch* oz = nullptr, double* dense = nullptr) {
   double* al = sm;
   double* be = al + m;
   double* h1 = be + m;
@@ -526,9 +618,21 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
   for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(ok ? x[e] / xn : 1.0 / sqrt((double)N));
   gsync<G>();
   const int mm = (int)(N < m ? N : m);
+  // thick restarts (after a first cycle without convergence): kk Ritz vectors
+  // kept in V[0, kk), their values th and couplings bb to V[kk]
+  __shared__ double th_g[kGroups<G>][kLanczosKeep], bb_g[kGroups<G>][kLanczosKeep];
+  __shared__ int sel_g[kGroups<G>][kLanczosKeep];
+  __shared__ int s_keep_g[kGroups<G>];
+  double* th = th_g[gidx<G>()];
+  double* bb = bb_g[gidx<G>()];
+  int* selk = sel_g[gidx<G>()];
+  int& s_keep = s_keep_g[gidx<G>()];
+  const bool can_thick = dense != nullptr && mm > kLanczosKeep + 1;
+  bool thick = false;
+  int kk = 0;
   for (;;) {
-    int nT = 0;
-    for (int j = 0; j < mm; ++j) {
+    int nT = kk;
+    for (int j = kk; j < mm; ++j) {
       if constexpr (std::is_same<TI, double>::value) {
         if (oz) {
           // FP64-accurate products on the tensor cores (emulated FP64)
@@ -556,7 +660,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
         al[j] = h1[j] + h2[j];
         be[j] = bj;
       }
-      if (bj > 0.0 && j + 1 < mm) {
+      if (bj > 0.0 && (j + 1 < mm || can_thick)) {
         TI* vn = V + (int64_t)(j + 1) * N;
         const double inv = 1.0 / bj;
         for (int64_t e = tid; e < N; e += nt) {
@@ -569,9 +673,13 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
       ++out.its;
       nT = j + 1;
       double tnorm = 0.0;
-      for (int i = 0; i < nT; ++i)
-        tnorm = fmax(tnorm, fabs(al[i]) + fabs(be[i]) + (i > 0 ? fabs(be[i - 1]) : 0.0));
+      for (int i = kk; i < nT; ++i)
+        tnorm = fmax(tnorm, fabs(al[i]) + fabs(be[i]) + (i > kk ? fabs(be[i - 1]) : 0.0));
       const bool breakdown = !(bj > 1e-14 * fmax(tnorm, 1e-300));
+      if (thick) {
+        if (breakdown) break;
+        continue;
+      }
       if ((nT % 4) == 0 || nT == mm || breakdown) {
         if (warp == 0) {
           double lo = 1e300, hi = -1e300;
@@ -608,20 +716,106 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
         break;
       }
     }
-    // Ritz vector
-    for (int64_t e = tid; e < N; e += nt) {
-      double acc = 0.0;
-      for (int l = 0; l < nT; ++l) acc += z[l] * (double)V[(int64_t)l * N + e];
-      x[e] = acc;
+    if (!thick) {
+      if (s_conv || out.restarts >= max_restarts || !can_thick || nT < mm) {
+        // Ritz vector of the tridiagonal matrix
+        for (int64_t e = tid; e < N; e += nt) {
+          double acc = 0.0;
+          for (int l = 0; l < nT; ++l) acc += z[l] * (double)V[(int64_t)l * N + e];
+          x[e] = acc;
+        }
+        gsync<G>();
+        if (s_conv || out.restarts >= max_restarts || nT < mm) break;
+        // a basis too small for thick restarts: restart from the Ritz vector
+        ++out.restarts;
+        double s2 = 0.0;
+        for (int64_t e = tid; e < N; e += nt) s2 += x[e] * x[e];
+        const double nrm = sqrt(cta_sum<G>(s2));
+        for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(nrm > 0.0 ? x[e] / nrm : 1.0 / sqrt((double)N));
+        gsync<G>();
+        continue;
+      }
+      thick = true;  // the first cycle did not converge: thick restarts from here on
+    }
+    // Projected matrix of the cycle: kept Ritz values on the diagonal, their
+    // couplings to V[kk] (arrow), the cycle's tridiagonal part; its
+    // eigen-decomposition (Jacobi) gives the Ritz pairs of the whole basis.
+    double* H = dense;
+    double* Z = dense + (int64_t)m * m;
+    for (int idx = tid; idx < nT * nT; idx += nt) {
+      const int r = idx / nT, c = idx - r * nT;
+      double v = 0.0;
+      if (r == c) v = r < kk ? th[r] : al[r];
+      else if (r < kk && c == kk) v = bb[r];
+      else if (c < kk && r == kk) v = bb[c];
+      else if (r >= kk && c >= kk && (r == c + 1 || c == r + 1)) v = be[r < c ? r : c];
+      H[r * m + c] = v;
     }
     gsync<G>();
-    if (s_conv || out.restarts >= max_restarts) break;
-    ++out.restarts;
-    double s2 = 0.0;
-    for (int64_t e = tid; e < N; e += nt) s2 += x[e] * x[e];
-    const double nrm = sqrt(cta_sum<G>(s2));
-    for (int64_t e = tid; e < N; e += nt) V[e] = (TI)(nrm > 0.0 ? x[e] / nrm : 1.0 / sqrt((double)N));
+    cta_sym_eig<G>(H, Z, nT, m);
+    const double blast = be[nT - 1];
+    if (tid == 0) {
+      // wanted pair and the kLanczosKeep best by the selection rule
+      double tn = 0.0;
+      for (int i = 0; i < nT; ++i) tn = fmax(tn, fabs(H[i * m + i]));
+      const int kkeep = nT - 1 < kLanczosKeep ? nT - 1 : kLanczosKeep;
+      for (int q = 0; q < kkeep; ++q) {
+        int best = -1;
+        double bkey = 0.0;
+        for (int i = 0; i < nT; ++i) {
+          bool used = false;
+          for (int u = 0; u < q; ++u) used |= selk[u] == i;
+          if (used) continue;
+          const double t = H[i * m + i];
+          const double key = mode == 0 ? -t : (mode == 2 ? t : fabs(t - sigma));
+          if (best < 0 || key < bkey) {
+            best = i;
+            bkey = key;
+          }
+        }
+        selk[q] = best;
+      }
+      s_keep = kkeep;
+      s_theta = H[selk[0] * m + selk[0]];
+      s_res = fabs(blast * Z[(nT - 1) * m + selk[0]]) / fmax(tn, 1e-300);
+      s_conv = s_res <= tol;
+    }
     gsync<G>();
+    if (s_conv || out.restarts >= max_restarts || nT < mm) {
+      const int w0 = selk[0];
+      for (int64_t e = tid; e < N; e += nt) {
+        double acc = 0.0;
+        for (int l = 0; l < nT; ++l) acc += Z[l * m + w0] * (double)V[(int64_t)l * N + e];
+        x[e] = acc;
+      }
+      gsync<G>();
+      break;
+    }
+    ++out.restarts;
+    // new basis: V[0, k) = V Z[:, sel] (element by element, so in place), V[k] = V[nT]
+    const int k = s_keep;
+    for (int64_t e = tid; e < N; e += nt) {
+      double acc[kLanczosKeep];
+#pragma unroll
+      for (int i = 0; i < kLanczosKeep; ++i) acc[i] = 0.0;
+      for (int l = 0; l < nT; ++l) {
+        const double v = (double)V[(int64_t)l * N + e];
+#pragma unroll
+        for (int i = 0; i < kLanczosKeep; ++i)
+          if (i < k) acc[i] += Z[l * m + selk[i]] * v;
+      }
+      const TI cont = V[(int64_t)nT * N + e];
+#pragma unroll
+      for (int i = 0; i < kLanczosKeep; ++i)
+        if (i < k) V[(int64_t)i * N + e] = (TI)acc[i];
+      V[(int64_t)k * N + e] = cont;
+    }
+    if (tid < k) {
+      th[tid] = H[selk[tid] * m + selk[tid]];
+      bb[tid] = blast * Z[(nT - 1) * m + selk[tid]];
+    }
+    gsync<G>();
+    kk = k;
   }
   out.theta = s_theta;
   out.res = s_res;
@@ -1276,8 +1470,10 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
                            a.tol_evp, sm, sm + batch_lanczos_doubles(a.m_evp), oz, &ginner);
       if (st.status != ST_OK && evp_status == ST_OK) evp_status = st.status;
     } else {
+      // thick restarts use the group's idle tile memory (tensor-core kernel) or
+      // the QR work area for the projected matrix and its eigenvectors
       st = cta_lanczos<double, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m, I.mode, I.sigma,
-                                  kBatchEvpRestarts, a.tol_evp, sm, oz);
+                                  kBatchEvpRestarts, a.tol_evp, sm, oz, qsh ? (double*)qsh : S.qwork);
     }
     theta = st.theta;
     nits += st.its;
