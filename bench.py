@@ -403,12 +403,13 @@ def other_workloads(lib, ctx, args):
     # mixed: local systems to 1e-11, which keeps every instance of the reference-checked
     # subset within 1e-8 of the reference (1e-10 leaves one at 2.6e-8)
     for prec in ('mixed', 'fp64'):
-        for _ in range(3 if prec == 'mixed' else 2):   # the engine autotuner's trials
+        for _ in range(4 if prec == 'mixed' else 2):   # the engine autotuner's trials
             sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
         sols, st = sle.als_batch(probs, repeats=4, precision=prec, tol=1e-11 if prec == 'mixed' else 0.0)
         res4[prec] = {'solves_per_s': 256 / (st['device_ms'] / 1e3), 'device_ms': st['device_ms'],
                       'max_local_residual': st['max_local_residual'],
-                      'tensor_cores_tcgen05': bool(st['batch_tensor_cores']), 'ctas_per_sm': st['batch_ctas_per_sm']}
+                      'tensor_cores_tcgen05': bool(st['batch_tensor_cores']), 'ctas_per_sm': st['batch_ctas_per_sm'],
+                      'solves_per_cta': st['batch_solves_per_cta']}
     res4['mixed_over_plain'] = res4['mixed']['solves_per_s'] / res4['fp64']['solves_per_s']
     out['batch256_uneven'] = res4
     # serving: Poisson arrivals at 2000/s (80 % SLE from the uneven distribution, 20 % Ising EVP
@@ -529,6 +530,7 @@ def main_gpu(args):
             st = fn()
             if prec_name:
                 tuning.append({'precision': prec_name, 'tensor_cores': int(st.batch_tensor_cores),
+                               'solves_per_cta': int(st.batch_solves_per_cta),
                                'ctas_per_sm': int(st.batch_ctas_per_sm), 'ms_per_solve': st.solver_ms / count
                                if st.solver_ms > 0 else st.device_ms / count})
         torch.cuda.synchronize()
@@ -551,7 +553,7 @@ def main_gpu(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         # the warm-up steps are also the engine autotuner's trials (one per candidate variant)
-        ms_mixed, st_mixed = timed(lambda: batch(_lib.PREC_MIXED, MIXED_TOL), args.steps, max(args.warmup, 3),
+        ms_mixed, st_mixed = timed(lambda: batch(_lib.PREC_MIXED, MIXED_TOL), args.steps, max(args.warmup, 4),
                                    'mixed')
     torch.cuda.synchronize()
     total_ms = max_over_ranks(float(np.sum(ms_mixed)), dev)
@@ -612,7 +614,9 @@ def main_gpu(args):
     if os.path.exists(mp):
         bf16_peak = float(json.load(open(mp))['bf16_tflops'])
         bf16_src = 'MEASURED_PEAKS.json bf16_tflops (burst cuBLAS bf16 GEMM), of measured'
-    traffic, traffic_note = launch_traffic(B, 'batch_sle_tc_kernel' if sm_.batch_tensor_cores else 'batch_sle_kernel')
+    kname = ('batch_sle_tc_kernel' if sm_.batch_solves_per_cta == 2 else 'batch_sle_tc1_kernel') \
+        if sm_.batch_tensor_cores else 'batch_sle_kernel'
+    traffic, traffic_note = launch_traffic(B, kname)
 
     extra = {} if args.quick else other_workloads(lib, ctx, args)
     if rank != 0:
@@ -638,12 +642,13 @@ def main_gpu(args):
         'mixed_over_plain_batched': value / world / plain_batch_value,
         'engine': {'mixed': {'tensor_cores_tcgen05': bool(st_mixed[-1].batch_tensor_cores),
                              'ctas_per_sm': int(st_mixed[-1].batch_ctas_per_sm),
+                             'solves_per_cta': int(st_mixed[-1].batch_solves_per_cta),
                              'tc_gemms_per_step': int(st_mixed[-1].tc_gemms)},
                    'plain_fp64': {'ctas_per_sm': int(st_plain_b[-1].batch_ctas_per_sm)},
                    'autotuner_trials': tuning,
                    'what': 'the engine times each launch variant once per workload bucket (the warm-up '
-                           'steps) and runs the fastest: the tcgen05 kernel (one CTA per SM) or the '
-                           'warp-MMA kernel at full occupancy or one CTA per SM less'},
+                           'steps) and runs the fastest: the tcgen05 kernel (one CTA per SM, two solves '
+                           'per CTA or one) or the warp-MMA kernel at full occupancy or one CTA per SM less'},
         'dropin_single_solve': {'fp64_ms': float(np.mean(ms_drop64)), 'mixed_ms': float(np.mean(ms_dropmx)),
                                 'fp64_ms_plain_launches': float(np.mean(ms_drop64_nog)),
                                 'cuda_graph': 'the sweep is captured once per launch layout and replayed',
@@ -664,7 +669,7 @@ def main_gpu(args):
                                  'note': 'engine CUDA events; wall minus uploads_and_kernel is host planning, '
                                          'result collection and the device-to-host copies'}},
         'gpu_launches': launches,
-        'roofline': {'kernel': ('batch_sle_tc_kernel' if sm_.batch_tensor_cores else 'batch_sle_kernel') + ' (mixed)',
+        'roofline': {'kernel': kname + ' (mixed)',
                      'bound': 'tensor',
                      'achieved': (ach64 + ach32) / 1e3, 'peak': bf16_peak, 'unit': 'TFLOP/s',
                      'frac': (ach64 + ach32) / 1e3 / bf16_peak, 'traffic': traffic,

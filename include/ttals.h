@@ -113,6 +113,9 @@ typedef struct {
    * kernel (tcgen05), 0 = SIMT / warp-MMA kernel; and its CTAs per SM       */
   int32_t batch_tensor_cores;
   int32_t batch_ctas_per_sm;
+  /* ... and the solves one of its CTAs runs side by side (2 on the
+   * tensor-core kernel's two-group variant, else 1)                        */
+  int32_t batch_solves_per_cta;
 } ttals_stats;
 
 /* Context: one device, one stream, one device-memory arena capped at
@@ -176,9 +179,10 @@ int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
  * batches try each candidate once (every one of them solves its batch in
  * full), later ones use the fastest by kernel time per solve.  Candidates,
  * mixed precision: 0 tensor-core kernel (one CTA per SM running two requests
- * side by side, one per 256-thread group), 1 warp-MMA kernel
- * at full occupancy, 2 the same with one CTA per SM less; plain FP64: 0 full
- * occupancy, 1 one CTA per SM less.  -2 forgets every bucket's timings and
+ * side by side, one per 256-thread group), 1 the tensor-core kernel running
+ * one request on all 512 threads, 2 warp-MMA kernel at full occupancy, 3 the
+ * same with one CTA per SM less; plain FP64: 0 full occupancy, 1 one CTA per
+ * SM less.  -2 forgets every bucket's timings and
  * autotunes afresh.  No reference counterpart. */
 int ttals_set_batch_variant(ttals_ctx* ctx, int32_t variant);
 

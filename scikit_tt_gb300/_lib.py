@@ -66,7 +66,8 @@ class Stats(C.Structure):
                 ('solver_launches', C.c_int64), ('solver_ms', C.c_double), ('solver_flops64', C.c_double),
                 ('solver_flops32', C.c_double), ('phase_cycles', C.c_double * 8), ('tc_gemms', C.c_int64),
                 ('tc_fallbacks', C.c_int64), ('inner_apply_cycles', C.c_double),
-                ('batch_tensor_cores', C.c_int32), ('batch_ctas_per_sm', C.c_int32)]
+                ('batch_tensor_cores', C.c_int32), ('batch_ctas_per_sm', C.c_int32),
+                ('batch_solves_per_cta', C.c_int32)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_}

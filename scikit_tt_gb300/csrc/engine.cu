@@ -1588,15 +1588,18 @@ struct BatchPlan {
 };
 
 // Candidate launch variants of the batch kernel for one precision: the
-// tensor-core kernel (tcgen05, one CTA per SM) and the SIMT / warp-MMA kernel
-// at its full occupancy and one CTA per SM less.
+// tensor-core kernel (tcgen05, one CTA per SM) with two solves per CTA or one,
+// and the SIMT / warp-MMA kernel at its full occupancy and one CTA per SM less.
 struct BatchVariant {
-  int use_tc;
-  int less;  // CTAs per SM below the occupancy maximum
+  int use_tc;  // 0 none, 1 two solves per CTA, 2 one solve per CTA
+  int less;    // CTAs per SM below the occupancy maximum
 };
 std::vector<BatchVariant> batch_candidates(int prec) {
   std::vector<BatchVariant> v;
-  if (prec == TTALS_PREC_MIXED && batch_tc_enabled()) v.push_back({1, 0});
+  if (prec == TTALS_PREC_MIXED && batch_tc_enabled()) {
+    v.push_back({1, 0});
+    v.push_back({2, 0});
+  }
   v.push_back({0, 0});
   v.push_back({0, 1});
   return v;
@@ -1755,7 +1758,10 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     } else {
       const ttals_ctx::Tune& t = c->tune[tune_key(P)];
       if (t.trials < (int)cand.size()) {
-        pick = trial ? t.trials : (cand[0].use_tc ? 1 : 0);
+        // untested bucket outside a timed batch: the warp-MMA kernel at full occupancy
+        int plain = 0;
+        while (plain + 1 < (int)cand.size() && cand[plain].use_tc != 0) ++plain;
+        pick = trial ? t.trials : plain;
       } else {
         for (int k = 1; k < (int)cand.size(); ++k)
           if (t.ms[k] < t.ms[pick]) pick = k;
@@ -2013,8 +2019,9 @@ void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec
   }
   collect_plan(c, P, mem, c->stream, out_dev, st, kms, tms, launch_counter());
   if (st) {
-    st->batch_tensor_cores = P.use_tc;
+    st->batch_tensor_cores = P.use_tc != 0 ? 1 : 0;
     st->batch_ctas_per_sm = P.per_sm;
+    st->batch_solves_per_cta = P.spc;
   }
 }
 

@@ -56,7 +56,7 @@ constexpr int kBatchMinBlocksTc = 1;
 // separate instantiations (TC = false) free of tcgen05 code.
 // TC also selects the two-group form (every CTA routine below runs on the
 // calling group: gtid / gsize / gsync of ttals_device.cuh).
-template <typename T, bool TC = false>
+template <typename T, bool TC = false, bool G = TC>
 __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T* A, const T* B, T* C,
                                                   int* ktab = nullptr, TcState* tc = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
@@ -65,8 +65,8 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
     // when the CTA holds tensor memory, warp-level mma.sync otherwise
     if constexpr (TC) {
       if (tc && ktab) {
-        const bool done = cta_gemm_tf32_tc(c, A, B, C, ktab, *tc);
-        if (gtid<TC>() == 0) {
+        const bool done = cta_gemm_tf32_tc<G>(c, A, B, C, ktab, *tc);
+        if (gtid<G>() == 0) {
           if (done)
             ++tc->gemms;
           else
@@ -75,20 +75,20 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
         if (done) return;
       }
     }
-    if (ktab && cta_gemm_tf32x3<TC>(c, A, B, C, ktab)) return;
+    if (ktab && cta_gemm_tf32x3<G>(c, A, B, C, ktab)) return;
   }
   constexpr int VW = DefaultVW<T>::value;
   if (contract_vec_ok<T, VW>(c, B, C)) {
-    for (int64_t e = (int64_t)gtid<TC>() * VW; e < c.total; e += (int64_t)gsize<TC>() * VW)
+    for (int64_t e = (int64_t)gtid<G>() * VW; e < c.total; e += (int64_t)gsize<G>() * VW)
       contract_vec_elem<T, VW>(c, A, B, C, e);
   } else {
-    for (int64_t e = gtid<TC>(); e < c.total; e += gsize<TC>()) {
+    for (int64_t e = gtid<G>(); e < c.total; e += gsize<G>()) {
       int64_t ao, bo, co;
       contract_offsets(c, e, ao, bo, co);
       C[co] = contract_sum(c, A, B, ao, bo);
     }
   }
-  gsync<TC>();
+  gsync<G>();
 }
 
 // FP64 contraction; with `oz` set, GEMM-shaped ones run as emulated FP64 on the
@@ -97,18 +97,18 @@ __device__ __forceinline__ void cta_contract_body(const Contraction& c, const T*
 // eigenproblems (whose middle contraction has K = 6) 16 % faster than
 // emulating it, and no change on the SLE batches.
 constexpr int kOzMinK = 16;
-template <bool TC>
+template <bool TC, bool G = TC>
 __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const double* A, const double* B, double* C,
                                               const OzScratch* oz) {
-  __shared__ Contraction sc_g[kGroups<TC>];
-  Contraction& sc = sc_g[gidx<TC>()];
-  if (gtid<TC>() == 0) sc = cref;
-  gsync<TC>();
+  __shared__ Contraction sc_g[kGroups<G>];
+  Contraction& sc = sc_g[gidx<G>()];
+  if (gtid<G>() == 0) sc = cref;
+  gsync<G>();
   if (sc.ktotal < kOzMinK) oz = nullptr;
   if constexpr (TC) {
     if (oz && oz->tc) {
-      const bool done = cta_gemm_oz_tc(sc, A, B, C, *oz, oz->ktab, *oz->tc);
-      if (gtid<TC>() == 0) {
+      const bool done = cta_gemm_oz_tc<G>(sc, A, B, C, *oz, oz->ktab, *oz->tc);
+      if (gtid<G>() == 0) {
         if (done)
           ++oz->tc->gemms;
         else
@@ -119,7 +119,7 @@ __device__ __noinline__ void cta_contract_f64(const Contraction& cref, const dou
   } else {
     if (oz && cta_gemm_ozaki(sc, A, B, C, *oz, oz->ktab)) return;
   }
-  cta_contract_body<double, TC>(sc, A, B, C);
+  cta_contract_body<double, TC, G>(sc, A, B, C);
 }
 
 // Out-of-line version for the per-site bookkeeping (stacks, pushes): keeps the
@@ -137,14 +137,14 @@ __device__ __noinline__ void cta_contract(const Contraction& cref, const T* A, c
 // Out-of-line FP32 contraction of the inner Krylov apply: one copy of the
 // tensor-core and fallback paths instead of three inlined into the GMRES loop
 // (which otherwise spills).
-template <bool TC>
+template <bool TC, bool G = TC>
 __device__ __noinline__ void cta_contract_f32(const Contraction& cref, const float* A, const float* B, float* C,
                                               int* ktab, TcState* tc) {
-  __shared__ Contraction sc_g[kGroups<TC>];
-  Contraction& sc = sc_g[gidx<TC>()];
-  if (gtid<TC>() == 0) sc = cref;
-  gsync<TC>();
-  cta_contract_body<float, TC>(sc, A, B, C, ktab, tc);
+  __shared__ Contraction sc_g[kGroups<G>];
+  Contraction& sc = sc_g[gidx<G>()];
+  if (gtid<G>() == 0) sc = cref;
+  gsync<G>();
+  cta_contract_body<float, TC, G>(sc, A, B, C, ktab, tc);
 }
 
 template <bool G = false>
@@ -237,18 +237,18 @@ __device__ __noinline__ void cta_dots_wide(const T* V, int64_t N, int nvec, cons
 }
 
 // y -> out = M y (three contraction phases through T1, T2)
-template <typename T, bool TC = false>
+template <typename T, bool TC = false, bool G = TC>
 __device__ __forceinline__ void cta_apply(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                           const T* L, const T* A, const T* R, const T* y, T* T1, T* T2, T* out,
                                           int* ktab = nullptr, TcState* tc = nullptr) {
   if constexpr (std::is_same<T, float>::value) {
-    cta_contract_f32<TC>(p1, L, y, T1, ktab, tc);
-    cta_contract_f32<TC>(p2, T1, A, T2, ktab, tc);
-    cta_contract_f32<TC>(p3, T2, R, out, ktab, tc);
+    cta_contract_f32<TC, G>(p1, L, y, T1, ktab, tc);
+    cta_contract_f32<TC, G>(p2, T1, A, T2, ktab, tc);
+    cta_contract_f32<TC, G>(p3, T2, R, out, ktab, tc);
   } else {
-    cta_contract_body<T, TC>(p1, L, y, T1, ktab);
-    cta_contract_body<T, TC>(p2, T1, A, T2, ktab);
-    cta_contract_body<T, TC>(p3, T2, R, out, ktab);
+    cta_contract_body<T, TC, G>(p1, L, y, T1, ktab);
+    cta_contract_body<T, TC, G>(p2, T1, A, T2, ktab);
+    cta_contract_body<T, TC, G>(p3, T2, R, out, ktab);
   }
 }
 
@@ -261,7 +261,7 @@ struct CtaSolveStats {
   int cycles, inner, status;
 };
 
-template <typename TI, bool TC>
+template <typename TI, bool TC, bool G = TC>
 __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                       const double* L64, const double* A64, const double* R64, double* T1_64,
                                       double* T2_64, const TI* Li, const TI* Ai, const TI* Ri, TI* T1i, TI* T2i,
@@ -276,30 +276,30 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
   double* yv = gv + m + 1;       // m
   double* h1 = yv + m;           // m+2
   double* h2 = h1 + m + 2;       // m+2
-  __shared__ double s_res_g[kGroups<TC>];
-  __shared__ int s_flag_g[kGroups<TC>];
-  __shared__ float s_cf_g[kGroups<TC>][kWideDotsMax + 2];  // Gram-Schmidt / correction coefficients in TI (TC path)
-  double& s_res = s_res_g[gidx<TC>()];
-  int& s_flag = s_flag_g[gidx<TC>()];
-  float* s_cf = s_cf_g[gidx<TC>()];
-  const int tid = gtid<TC>(), nt = gsize<TC>();
+  __shared__ double s_res_g[kGroups<G>];
+  __shared__ int s_flag_g[kGroups<G>];
+  __shared__ float s_cf_g[kGroups<G>][kWideDotsMax + 2];  // Gram-Schmidt / correction coefficients in TI (TC path)
+  double& s_res = s_res_g[gidx<G>()];
+  int& s_flag = s_flag_g[gidx<G>()];
+  float* s_cf = s_cf_g[gidx<G>()];
+  const int tid = gtid<G>(), nt = gsize<G>();
   CtaSolveStats out{1.0, 0, 0, ST_OK};
   // the tensor-core kernel runs one CTA per SM: its vector loops use every
   // thread, keep several loads in flight and avoid per-element FP64 work
   constexpr bool kWide = TC && std::is_same<TI, float>::value;
   auto dots = [&](int nv, const TI* wv, double* o) {
     if constexpr (kWide)
-      cta_dots_wide<TI, TC>(V, N, nv, wv, o);
+      cta_dots_wide<TI, G>(V, N, nv, wv, o);
     else
-      cta_dots<TI, TC>(V, N, nv, wv, o);
+      cta_dots<TI, G>(V, N, nv, wv, o);
   };
 
   double fs = 0.0;
   for (int64_t e = tid; e < N; e += nt) fs += f[e] * f[e];
-  const double fnorm = sqrt(cta_sum<TC>(fs));
+  const double fnorm = sqrt(cta_sum<G>(fs));
   if (!(fnorm > 0.0)) {
     for (int64_t e = tid; e < N; e += nt) x[e] = 0.0;
-    gsync<TC>();
+    gsync<G>();
     out.rel = 0.0;
     if (!(fnorm == 0.0)) out.status = ST_NONFINITE;
     return out;
@@ -309,17 +309,17 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
     double rs = 0.0;
     if (oz) {
       // FP64-accurate residual with the products on the BF16 tensor cores
-      cta_contract_f64<TC>(p1, L64, (const double*)x, T1_64, oz);
-      cta_contract_f64<TC>(p2, (const double*)T1_64, A64, T2_64, oz);
-      cta_contract_f64<TC>(p3, (const double*)T2_64, R64, r, oz);
+      cta_contract_f64<TC, G>(p1, L64, (const double*)x, T1_64, oz);
+      cta_contract_f64<TC, G>(p2, (const double*)T1_64, A64, T2_64, oz);
+      cta_contract_f64<TC, G>(p3, (const double*)T2_64, R64, r, oz);
       for (int64_t e = tid; e < N; e += nt) {
         const double re = f[e] - r[e];
         r[e] = re;
         rs += re * re;
       }
     } else {
-      cta_contract_body<double, TC>(p1, L64, (const double*)x, T1_64);
-      cta_contract_body<double, TC>(p2, (const double*)T1_64, A64, T2_64);
+      cta_contract_body<double, TC, G>(p1, L64, (const double*)x, T1_64);
+      cta_contract_body<double, TC, G>(p2, (const double*)T1_64, A64, T2_64);
       for (int64_t e = tid; e < N; e += nt) {
         int64_t ao, bo, co;
         contract_offsets(p3, e, ao, bo, co);
@@ -328,7 +328,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         rs += re * re;
       }
     }
-    const double rho = sqrt(cta_sum<TC>(rs));
+    const double rho = sqrt(cta_sum<G>(rs));
     *cyc_res += clock64() - c0;
     const long long c1 = clock64();
     out.rel = rho / fnorm;
@@ -345,11 +345,11 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       gv[0] = 1.0;
       for (int i = 1; i <= m; ++i) gv[i] = 0.0;
     }
-    gsync<TC>();
+    gsync<G>();
     int jj = 0;
     for (int j = 0; j < m; ++j) {
       const long long ca0 = clock64();
-      cta_apply<TI, TC>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
+      cta_apply<TI, TC, G>(p1, p2, p3, Li, Ai, Ri, V + (int64_t)j * N, T1i, T2i, w, oz ? oz->ktab : nullptr,
                         oz ? oz->tc : nullptr);
       *cyc_apply += clock64() - ca0;
       dots(j + 1, w, h1);
@@ -371,7 +371,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
           TI* vn = V + (int64_t)(j + 1) * N;
           if constexpr (kWide) {
             for (int q = tid; q <= j; q += nt) s_cf[q] = (float)h1[q];
-            gsync<TC>();
+            gsync<G>();
             for (int64_t e = tid; e < N; e += nt) {
               TI acc = w[e];
 #pragma unroll 4
@@ -392,7 +392,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
           for (int q = 0; q <= j; ++q) acc -= (TI)h1[q] * V[(int64_t)q * N + e];
           w[e] = acc;
         }
-        gsync<TC>();
+        gsync<G>();
         dots(j + 1, w, h2);
         hn2 = h2[j + 1];
         for (int q = 0; q <= j; ++q) hn2 -= h2[q] * h2[q];
@@ -432,7 +432,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         s_res = fabs(gv[j + 1]);
         s_flag = (hn <= 1e-300) ? 1 : 0;
       }
-      gsync<TC>();
+      gsync<G>();
       jj = j + 1;
       ++out.inner;
       if (s_res <= target || s_flag) break;
@@ -452,7 +452,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       }
       s_flag = bad;
     }
-    gsync<TC>();
+    gsync<G>();
     if (s_flag) {
       out.status = ST_SINGULAR;
       return out;
@@ -461,7 +461,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
       // the correction V y is FP32-accurate by construction: sum it in FP32,
       // one FP64 FMA per element adds it to the FP64 solution
       for (int q = tid; q < jj; q += nt) s_cf[q] = (float)yv[q];
-      gsync<TC>();
+      gsync<G>();
       for (int64_t e = tid; e < N; e += nt) {
         float acc = 0.f;
 #pragma unroll 4
@@ -475,7 +475,7 @@ __device__ __noinline__ CtaSolveStats cta_gmres_ir(const Contraction& p1, const 
         x[e] += rho * acc;
       }
     }
-    gsync<TC>();
+    gsync<G>();
     *cyc_inner += clock64() - c1;
   }
   return out;
@@ -575,8 +575,10 @@ __device__ __noinline__ void cta_sym_eig(double* H, double* Z, int n, int ld) {
   }
 }
 
-// Ritz vectors kept by a thick restart of the CTA Lanczos
+// Ritz vectors kept by a thick restart of the CTA Lanczos, and the restarts
+// from a single Ritz vector tried before the thick ones
 constexpr int kLanczosKeep = 8;
+constexpr int kPlainRestarts = 3;
 
 struct CtaEigStats {
   double theta, res;
@@ -586,7 +588,7 @@ struct CtaEigStats {
 // TI: arithmetic of the operator, basis and products (double, or float for
 // the first stage of the mixed-precision eigensolve).  x (in: start vector,
 // out: Ritz vector) and all scalars stay FP64.
-template <typename TI, bool G = false>
+template <typename TI, bool TC = false, bool G = TC>
 __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                                const TI* L, const TI* A, const TI* R, TI* T1, TI* T2, double* x,
                                                TI* V, TI* w, int64_t N, int m, int mode, double sigma,
@@ -636,9 +638,9 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
       if constexpr (std::is_same<TI, double>::value) {
         if (oz) {
           // FP64-accurate products on the tensor cores (emulated FP64)
-          cta_contract_f64<G>(p1, L, V + (int64_t)j * N, T1, oz);
-          cta_contract_f64<G>(p2, T1, A, T2, oz);
-          cta_contract_f64<G>(p3, T2, R, w, oz);
+          cta_contract_f64<TC, G>(p1, L, V + (int64_t)j * N, T1, oz);
+          cta_contract_f64<TC, G>(p2, T1, A, T2, oz);
+          cta_contract_f64<TC, G>(p3, T2, R, w, oz);
         } else {
           cta_apply<TI, G>(p1, p2, p3, L, A, R, V + (int64_t)j * N, T1, T2, w);
         }
@@ -717,7 +719,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
       }
     }
     if (!thick) {
-      if (s_conv || out.restarts >= max_restarts || !can_thick || nT < mm) {
+      if (s_conv || out.restarts >= max_restarts || !can_thick || nT < mm || out.restarts < kPlainRestarts) {
         // Ritz vector of the tridiagonal matrix
         for (int64_t e = tid; e < N; e += nt) {
           double acc = 0.0;
@@ -726,7 +728,9 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
         }
         gsync<G>();
         if (s_conv || out.restarts >= max_restarts || nT < mm) break;
-        // a basis too small for thick restarts: restart from the Ritz vector
+        // restart from the Ritz vector (bases too small for thick restarts,
+        // and the first restarts: most slow local solves converge within a
+        // few of them, checked every four steps)
         ++out.restarts;
         double s2 = 0.0;
         for (int64_t e = tid; e < N; e += nt) s2 += x[e] * x[e];
@@ -735,7 +739,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
         gsync<G>();
         continue;
       }
-      thick = true;  // the first cycle did not converge: thick restarts from here on
+      thick = true;  // still not converged: thick restarts from here on
     }
     // Projected matrix of the cycle: kept Ritz values on the diagonal, their
     // couplings to V[kk] (arrow), the cycle's tridiagonal part; its
@@ -835,7 +839,7 @@ __device__ __noinline__ CtaEigStats cta_lanczos(const Contraction& p1, const Con
 // scipy.linalg.eigh with b), |x| = 1 otherwise (scipy.linalg.eig with b).
 // ---------------------------------------------------------------------------
 
-template <bool G>
+template <bool TC, bool G = TC>
 __device__ __noinline__ CtaEigStats cta_glanczos(const Contraction& p1, const Contraction& p2, const Contraction& p3,
                                                 const Contraction& q1, const Contraction& q2, const Contraction& q3,
                                                 const double* L, const double* A, const double* R,
@@ -859,14 +863,14 @@ __device__ __noinline__ CtaEigStats cta_glanczos(const Contraction& p1, const Co
   const int tid = gtid<G>(), nt = gsize<G>(), lane = tid & 31, warp = tid >> 5;
   CtaEigStats out{0.0, 0.0, 0, 0, ST_OK};
   auto applyA = [&](const double* src, double* dst) {
-    cta_contract_f64<G>(p1, L, src, T1, oz);
-    cta_contract_f64<G>(p2, T1, A, T2, oz);
-    cta_contract_f64<G>(p3, T2, R, dst, oz);
+    cta_contract_f64<TC, G>(p1, L, src, T1, oz);
+    cta_contract_f64<TC, G>(p2, T1, A, T2, oz);
+    cta_contract_f64<TC, G>(p3, T2, R, dst, oz);
   };
   auto applyB = [&](const double* src, double* dst) {
-    cta_contract_f64<G>(q1, LB, src, T1, oz);
-    cta_contract_f64<G>(q2, T1, B, T2, oz);
-    cta_contract_f64<G>(q3, T2, RB, dst, oz);
+    cta_contract_f64<TC, G>(q1, LB, src, T1, oz);
+    cta_contract_f64<TC, G>(q2, T1, B, T2, oz);
+    cta_contract_f64<TC, G>(q3, T2, RB, dst, oz);
   };
   // B-normalise v (its image Bv computed into bv); false if v^T B v is not positive
   auto bnormalise = [&](double* v, double* bv) {
@@ -907,7 +911,7 @@ __device__ __noinline__ CtaEigStats cta_glanczos(const Contraction& p1, const Co
       for (int64_t e = tid; e < N; e += nt) y[e] = 0.0;
       gsync<G>();
       long long c0 = 0, c1 = 0, c2 = 0;
-      const CtaSolveStats gs = cta_gmres_ir<double, G>(q1, q2, q3, LB, B, RB, T1, T2, LB, B, RB, T1, T2, w, y, gr, gV,
+      const CtaSolveStats gs = cta_gmres_ir<double, TC, G>(q1, q2, q3, LB, B, RB, T1, T2, LB, B, RB, T1, T2, w, y, gr, gV,
                                                        gw, N, (int)(N < mg ? N : mg), 60, 1e-13, 0.0, smg, nullptr,
                                                        &c0, &c1, &c2);
       *inner_its += gs.inner;
@@ -1026,9 +1030,9 @@ __device__ __noinline__ CtaEigStats cta_glanczos(const Contraction& p1, const Co
 
 // QR of a core; with a shared-memory region (the group's tensor-core tiles,
 // idle between GEMMs) large enough for the matrix, in shared memory.
-template <bool G = false>
+template <bool G = false, bool SH = G>
 __device__ __noinline__ void cta_qr(const QrArgs& q, unsigned char* shm = nullptr, int64_t shm_doubles = 0) {
-  if constexpr (G) {  // only the tensor-core kernel's groups have such a region
+  if constexpr (SH) {  // only the tensor-core kernels have such a region
     const int64_t k = q.rows < q.cols ? q.rows : q.cols;
     if (shm && q.rows * q.cols <= shm_doubles && k <= kQrSharedMaxK) {
       cta_householder_qr_shared<G>(q, reinterpret_cast<double*>(shm));
@@ -1114,7 +1118,7 @@ __device__ Scratch scratch_of(const BatchArgs& a, int slot) {
   return s;
 }
 
-template <bool TC>
+template <bool TC, bool G = TC>
 __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratch& S, double* sm) {
   const BatchInst& I = a.inst[j];
   const int d = I.d;
@@ -1132,16 +1136,16 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   const int64_t* Rt_off = L_off + d;
   const int64_t* Lb_off = Rt_off + d;
   const int64_t* Rb_off = Lb_off + d;
-  __shared__ int64_t r_g[kGroups<TC>][kMaxOrderB + 1];
-  int64_t* r = r_g[gidx<TC>()];
-  const int tid = gtid<TC>();
-  for (int i = tid; i <= d; i += gsize<TC>()) r[i] = cap[i];
-  gsync<TC>();
+  __shared__ int64_t r_g[kGroups<G>][kMaxOrderB + 1];
+  int64_t* r = r_g[gidx<G>()];
+  const int tid = gtid<G>();
+  for (int i = tid; i <= d; i += gsize<G>()) r[i] = cap[i];
+  gsync<G>();
   // the group's tensor-core tiles hold the QR factorisations between GEMMs;
   // in mixed precision the gauge pushes run as emulated FP64 on tcgen05 (on
   // the warp-MMA kernel they stay native)
   unsigned char* qsh = S.oz.tc ? S.oz.tc->tiles : nullptr;
-  constexpr int64_t qcap = kTcSmemBytes / 8;
+  constexpr int64_t qcap = TcCfg<G>::kSmemBytes / 8;
   const OzScratch* ozp = (TC && a.prec == 1) ? &S.oz : nullptr;
   auto X = [&](int i) { return I.X + X_off[i]; };
   auto L = [&](int i) { return I.L + L_off[i]; };
@@ -1181,15 +1185,15 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_qr<TC>(q, qsh, qcap);
+      cta_qr<G, TC>(q, qsh, qcap);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
-      cta_contract_f64<TC>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb, ozp);
+      cta_contract_f64<TC, G>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb, ozp);
       cur = outb;
       cur_left = rx0[i - 1];
       cur_right = k;
     }
-    cta_copy<TC>(X(0), cur, n[0] * cur_right);
+    cta_copy<G>(X(0), cur, n[0] * cur_right);
   }
   lap(0);
 
@@ -1199,19 +1203,19 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         Rt(i)[0] = 1.0;
         Rb(i)[0] = 1.0;
       }
-      gsync<TC>();
+      gsync<G>();
       return;
     }
     const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
     Contraction q1, q2, q3;
     desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
     const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
-    cta_contract_f64<TC>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
-    cta_contract_f64<TC>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
-    cta_contract_f64<TC>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
+    cta_contract_f64<TC, G>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
+    cta_contract_f64<TC, G>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
+    cta_contract_f64<TC, G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
-    cta_contract<double, TC>(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
-    cta_contract<double, TC>(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
+    cta_contract<double, G>(desc_vec_u_right(aa, nn, ss, rb[i + 2]), (const double*)X(i + 1), (const double*)Rb(i + 1), S.U);
+    cta_contract<double, G>(desc_vec_right(aa, nn, rb[i + 1], rb[i + 2]), B(i + 1), (const double*)S.U, Rb(i));
     lap(1);
   };
   auto left = [&](int i) {
@@ -1220,25 +1224,25 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         L(i)[0] = 1.0;
         Lb(i)[0] = 1.0;
       }
-      gsync<TC>();
+      gsync<G>();
       return;
     }
     const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
     const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
-    cta_contract_f64<TC>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
-    cta_contract_f64<TC>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
-    cta_contract_f64<TC>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
+    cta_contract_f64<TC, G>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
+    cta_contract_f64<TC, G>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
+    cta_contract_f64<TC, G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
-    cta_contract<double, TC>(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
-    cta_contract<double, TC>(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
+    cta_contract<double, G>(desc_vec_u_left(aa, nn, rb[i - 1], rb[i]), (const double*)Lb(i - 1), B(i - 1), S.U);
+    cta_contract<double, G>(desc_vec_left(aa, nn, ss, rb[i]), (const double*)S.U, (const double*)X(i - 1), Lb(i));
     lap(1);
   };
   auto solve = [&](int i) {
     const int64_t aa = r[i], nn = n[i], ss = r[i + 1], N = aa * nn * ss;
-    cta_contract<double, TC>(desc_vec_u_left(aa, nn, rb[i], rb[i + 1]), (const double*)Lb(i), B(i), S.U);
-    cta_contract<double, TC>(desc_micro_f(aa, nn, ss, rb[i + 1]), (const double*)S.U, (const double*)Rb(i), S.f);
+    cta_contract<double, G>(desc_vec_u_left(aa, nn, rb[i], rb[i + 1]), (const double*)Lb(i), B(i), S.U);
+    cta_contract<double, G>(desc_micro_f(aa, nn, ss, rb[i + 1]), (const double*)S.U, (const double*)Rb(i), S.f);
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i], R[i + 1], &p1, &p2, &p3);
     const int m = (int)(N < a.m ? N : a.m);
@@ -1246,13 +1250,13 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     lap(2);
     long long cr = 0, ci = 0, capp = 0;
     if (a.prec == 1) {
-      cta_to_float<TC>(S.Lf, L(i), aa * R[i] * aa);
-      cta_to_float<TC>(S.Rf, Rt(i), ss * R[i + 1] * ss);
-      cta_to_float<TC>(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
-      st = cta_gmres_ir<float, TC>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
+      cta_to_float<G>(S.Lf, L(i), aa * R[i] * aa);
+      cta_to_float<G>(S.Rf, Rt(i), ss * R[i + 1] * ss);
+      cta_to_float<G>(S.Af, A(i), R[i] * nn * nn * R[i + 1]);
+      st = cta_gmres_ir<float, TC, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, S.Lf, S.Af, S.Rf, S.T1f, S.T2f, S.f, X(i),
                                S.r, S.Vf, S.wf, N, m, 30, a.tol, 1e-5, sm, &S.oz, &cr, &ci, &capp);
     } else {
-      st = cta_gmres_ir<double, TC>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
+      st = cta_gmres_ir<double, TC, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, L(i), A(i), Rt(i), S.T1, S.T2, S.f, X(i),
                                 S.r, S.V, S.w, N, m, 60, a.tol, 0.0, sm, nullptr, &cr, &ci, &capp);
     }
     ph[3] += cr;
@@ -1284,13 +1288,13 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_qr<TC>(q, qsh, qcap);
+        cta_qr<G, TC>(q, qsh, qcap);
         fl64 += qr_fl((double)(aa * nn), (double)ss);
         const int64_t qq = n[i + 1] * r[i + 2];
-        cta_contract_f64<TC>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0, ozp);
-        cta_copy<TC>(X(i + 1), S.tmp0, k * qq);
+        cta_contract_f64<TC, G>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0, ozp);
+        cta_copy<G>(X(i + 1), S.tmp0, k * qq);
         if (tid == 0) r[i + 1] = k;
-        gsync<TC>();
+        gsync<G>();
         lap(5);
       }
     }
@@ -1300,13 +1304,13 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_qr<TC>(q, qsh, qcap);
+        cta_qr<G, TC>(q, qsh, qcap);
         fl64 += qr_fl((double)ns, (double)aa);
         const int64_t p = r[i - 1] * n[i - 1];
-        cta_contract_f64<TC>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0, ozp);
-        cta_copy<TC>(X(i - 1), S.tmp0, p * k);
+        cta_contract_f64<TC, G>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0, ozp);
+        cta_copy<G>(X(i - 1), S.tmp0, p * k);
         if (tid == 0) r[i] = k;
-        gsync<TC>();
+        gsync<G>();
         lap(5);
       }
     }
@@ -1315,7 +1319,7 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
   int64_t off = 0;
   for (int i = 0; i < d; ++i) {
     const int64_t cnt = r[i] * n[i] * r[i + 1];
-    for (int64_t e = tid; e < cnt; e += gsize<TC>()) I.out[off + e] = X(i)[e];
+    for (int64_t e = tid; e < cnt; e += gsize<G>()) I.out[off + e] = X(i)[e];
     off += cnt;
   }
   if (tid == 0) {
@@ -1335,14 +1339,14 @@ __device__ __noinline__ void batch_solve(const BatchArgs& a, int j, const Scratc
     I.report[19 + d] = S.oz.tc ? (double)(S.oz.tc->fallbacks - fb0) : 0.0;
     I.report[20 + d] = (double)inner_apply;
   }
-  signal_done<TC>(I.done);
+  signal_done<G>(I.done);
 }
 
 // ---------------------------------------------------------------------------
 // one eigenproblem instance (evp.py:17-179, symmetric, number_ev == 1)
 // ---------------------------------------------------------------------------
 
-template <bool G = false>
+template <bool TC = false, bool G = TC>
 __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch& S, double* sm) {
   const BatchInst& I = a.inst[j];
   const int d = I.d;
@@ -1372,7 +1376,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
   auto Xo = [&](int i) { return I.Xopt + X_off[i]; };
   const OzScratch* oz = a.prec == 1 ? &S.oz : nullptr;
   unsigned char* qsh = S.oz.tc ? S.oz.tc->tiles : nullptr;
-  constexpr int64_t qcap = kTcSmemBytes / 8;
+  constexpr int64_t qcap = TcCfg<G>::kSmemBytes / 8;
   auto L = [&](int i) { return I.L + L_off[i]; };
   auto Rt = [&](int i) { return I.Rt + Rt_off[i]; };
   auto A = [&](int i) { return I.op + op_off[i]; };
@@ -1392,7 +1396,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     for (int i = d - 1; i >= 1; --i) {
       const int64_t ns = n[i] * cur_right, k = cur_left < ns ? cur_left : ns;
       QrArgs q{cur, 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, cur_left, 1, nullptr, S.qwork};
-      cta_qr<G>(q, qsh, qcap);
+      cta_qr<G, TC>(q, qsh, qcap);
       const int64_t p = rx0[i - 1] * n[i - 1];
       double* outb = (i & 1) ? S.tmp1 : S.tmp0;
       cta_contract<double, G>(desc_push_right(p, cur_left, k), I.x0 + x0_off[i - 1], S.rbuf, outb);
@@ -1414,15 +1418,15 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     const int64_t aa = r[i + 1], nn = n[i + 1], ss = r[i + 2];
     Contraction q1, q2, q3;
     desc_right(aa, nn, ss, R[i + 1], R[i + 2], &q1, &q2, &q3);
-    cta_contract_f64<G>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
-    cta_contract_f64<G>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
-    cta_contract_f64<G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
+    cta_contract_f64<TC, G>(q1, (const double*)Rt(i + 1), (const double*)X(i + 1), S.T1, oz);
+    cta_contract_f64<TC, G>(q2, (const double*)S.T1, A(i + 1), S.T2, oz);
+    cta_contract_f64<TC, G>(q3, (const double*)X(i + 1), (const double*)S.T2, Rt(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i + 1], (double)R[i + 2]);
     if (gevp) {  // evp.py:314-329
       desc_right(aa, nn, ss, rb[i + 1], rb[i + 2], &q1, &q2, &q3);
-      cta_contract_f64<G>(q1, (const double*)RB(i + 1), (const double*)X(i + 1), S.T1, oz);
-      cta_contract_f64<G>(q2, (const double*)S.T1, Bg(i + 1), S.T2, oz);
-      cta_contract_f64<G>(q3, (const double*)X(i + 1), (const double*)S.T2, RB(i), oz);
+      cta_contract_f64<TC, G>(q1, (const double*)RB(i + 1), (const double*)X(i + 1), S.T1, oz);
+      cta_contract_f64<TC, G>(q2, (const double*)S.T1, Bg(i + 1), S.T2, oz);
+      cta_contract_f64<TC, G>(q3, (const double*)X(i + 1), (const double*)S.T2, RB(i), oz);
       fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)rb[i + 1], (double)rb[i + 2]);
     }
   };
@@ -1438,15 +1442,15 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     const int64_t aa = r[i - 1], nn = n[i - 1], ss = r[i];
     Contraction p1, p2, p3;
     desc_apply(aa, nn, ss, R[i - 1], R[i], &p1, &p2, &p3);
-    cta_contract_f64<G>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
-    cta_contract_f64<G>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
-    cta_contract_f64<G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
+    cta_contract_f64<TC, G>(p1, (const double*)L(i - 1), (const double*)X(i - 1), S.T1, oz);
+    cta_contract_f64<TC, G>(p2, (const double*)S.T1, A(i - 1), S.T2, oz);
+    cta_contract_f64<TC, G>(desc_left_p3(aa, nn, ss, R[i]), (const double*)S.T2, (const double*)X(i - 1), L(i), oz);
     fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)R[i - 1], (double)R[i]);
     if (gevp) {  // evp.py:272-287
       desc_apply(aa, nn, ss, rb[i - 1], rb[i], &p1, &p2, &p3);
-      cta_contract_f64<G>(p1, (const double*)LB(i - 1), (const double*)X(i - 1), S.T1, oz);
-      cta_contract_f64<G>(p2, (const double*)S.T1, Bg(i - 1), S.T2, oz);
-      cta_contract_f64<G>(desc_left_p3(aa, nn, ss, rb[i]), (const double*)S.T2, (const double*)X(i - 1), LB(i), oz);
+      cta_contract_f64<TC, G>(p1, (const double*)LB(i - 1), (const double*)X(i - 1), S.T1, oz);
+      cta_contract_f64<TC, G>(p2, (const double*)S.T1, Bg(i - 1), S.T2, oz);
+      cta_contract_f64<TC, G>(desc_left_p3(aa, nn, ss, rb[i]), (const double*)S.T2, (const double*)X(i - 1), LB(i), oz);
       fl64 += apply_fl((double)aa, (double)nn, (double)ss, (double)rb[i - 1], (double)rb[i]);
     }
   };
@@ -1465,14 +1469,14 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
     if (gevp) {
       Contraction g1, g2, g3;
       desc_apply(aa, nn, ss, rb[i], rb[i + 1], &g1, &g2, &g3);
-      st = cta_glanczos<G>(p1, p2, p3, g1, g2, g3, L(i), A(i), Rt(i), LB(i), Bg(i), RB(i), S.T1, S.T2, X(i), S.V,
+      st = cta_glanczos<TC, G>(p1, p2, p3, g1, g2, g3, L(i), A(i), Rt(i), LB(i), Bg(i), RB(i), S.T1, S.T2, X(i), S.V,
                            S.BV, S.w, S.gy, S.gV, S.gr, S.gw, N, m, a.m, I.mode, I.sigma, kBatchEvpRestarts,
                            a.tol_evp, sm, sm + batch_lanczos_doubles(a.m_evp), oz, &ginner);
       if (st.status != ST_OK && evp_status == ST_OK) evp_status = st.status;
     } else {
       // thick restarts use the group's idle tile memory (tensor-core kernel) or
       // the QR work area for the projected matrix and its eigenvectors
-      st = cta_lanczos<double, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m, I.mode, I.sigma,
+      st = cta_lanczos<double, TC, G>(p1, p2, p3, L(i), A(i), Rt(i), S.T1, S.T2, X(i), S.V, S.w, N, m, I.mode, I.sigma,
                                   kBatchEvpRestarts, a.tol_evp, sm, oz, qsh ? (double*)qsh : S.qwork);
     }
     theta = st.theta;
@@ -1495,7 +1499,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
         solve(i);
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], k = aa * nn < ss ? aa * nn : ss;
         QrArgs q{X(i), ss, 1, X(i), k, 1, S.rbuf, ss, 1, aa * nn, ss, 0, nullptr, S.qwork};
-        cta_qr<G>(q, qsh, qcap);
+        cta_qr<G, TC>(q, qsh, qcap);
         const int64_t qq = n[i + 1] * r[i + 2];
         cta_contract<double, G>(desc_push_left(k, ss, qq), (const double*)S.rbuf, (const double*)X(i + 1), S.tmp0);
         cta_copy<G>(X(i + 1), S.tmp0, k * qq);
@@ -1509,7 +1513,7 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
       if (i > 0) {
         const int64_t aa = r[i], nn = n[i], ss = r[i + 1], ns = nn * ss, k = aa < ns ? aa : ns;
         QrArgs q{X(i), 1, ns, X(i), 1, ns, S.rbuf, 1, k, ns, aa, 0, nullptr, S.qwork};
-        cta_qr<G>(q, qsh, qcap);
+        cta_qr<G, TC>(q, qsh, qcap);
         const int64_t p = r[i - 1] * n[i - 1];
         cta_contract<double, G>(desc_push_right(p, aa, k), (const double*)X(i - 1), (const double*)S.rbuf, S.tmp0);
         cta_copy<G>(X(i - 1), S.tmp0, p * k);
@@ -1560,9 +1564,10 @@ __device__ __noinline__ void batch_evp(const BatchArgs& a, int j, const Scratch&
 }
 
 // Take the CTA's tensor memory (all threads of the CTA): warp 0 allocates the
-// SM's 512 columns once, each of the `groups` groups gets kTcTmemCols of them
-// and its own completion barrier and operand tiles (tiles + g * tile_stride).
-__device__ __forceinline__ void tc_begin(TcState* tc, int groups, unsigned char* tiles, size_t tile_stride) {
+// SM's 512 columns once, each of the `groups` groups gets `cols` of them and
+// its own completion barrier and operand tiles (tiles + g * tile_stride).
+__device__ __forceinline__ void tc_begin(TcState* tc, int groups, uint32_t cols, unsigned char* tiles,
+                                         size_t tile_stride) {
   __shared__ uint32_t s_tmem;
   if ((threadIdx.x >> 5) == 0) umma::tmem_alloc(&s_tmem, kTcCtaTmemCols);
   umma::fence_before_sync();
@@ -1570,7 +1575,7 @@ __device__ __forceinline__ void tc_begin(TcState* tc, int groups, unsigned char*
   umma::fence_after_sync();
   if (threadIdx.x < (unsigned)groups) {
     TcState& t = tc[threadIdx.x];
-    t.tmem = s_tmem + kTcTmemCols * threadIdx.x;  // column offset in the low half
+    t.tmem = s_tmem + cols * threadIdx.x;  // column offset in the low half
     t.tiles = tiles + tile_stride * threadIdx.x;
     t.phase = 0;
     t.status = ST_OK;
@@ -1598,10 +1603,13 @@ __device__ __forceinline__ void tc_end(TcState* tc, int groups) {
 __host__ __device__ inline size_t tc_tiles_offset(size_t before) { return (before + 1023) / 1024 * 1024; }
 
 // Dynamic shared memory of one group: GMRES / Lanczos scalars, the
-// contraction-offset table, and (tensor-core variant) the operand tiles.
+// contraction-offset table, and (tensor-core variants) the operand tiles.
+// use_tc: 0 no tensor memory, 1 two solves per CTA, 2 one solve per CTA.
 __host__ __device__ size_t batch_group_smem_bytes(int m, int m_evp, int use_tc, int gevp) {
   const size_t base = batch_smem_scalar_bytes(m, m_evp, gevp) + sizeof(int) * 2 * kTcMaxK;
-  return use_tc ? tc_tiles_offset(base) + kTcSmemBytes : base;
+  if (use_tc == 1) return tc_tiles_offset(base) + TcCfg<true>::kSmemBytes;
+  if (use_tc == 2) return tc_tiles_offset(base) + TcCfg<false>::kSmemBytes;
+  return base;
 }
 
 // The persistent loop of both kernel variants.  Each group (the whole CTA, or
@@ -1610,27 +1618,27 @@ __host__ __device__ size_t batch_group_smem_bytes(int m, int m_evp, int use_tc, 
 // UseTc the CTA holds all TMEM columns for its whole life (allocated here,
 // released on the way out whatever happened); its GEMM-shaped FP32 and
 // emulated-FP64 contractions then run on tcgen05.
-template <bool UseTc>
+template <bool UseTc, bool G = UseTc>
 __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
   extern __shared__ __align__(1024) unsigned char smraw[];
-  constexpr int NG = kGroups<UseTc>;
+  constexpr int NG = kGroups<G>;
   __shared__ int s_j[NG];
   __shared__ TcState s_tc[NG];
-  const int g = gidx<UseTc>();
+  const int g = gidx<G>();
   const int gevp = a.sizes.Ng > 0 ? 1 : 0;
-  const size_t gbytes = batch_group_smem_bytes(a.m, a.m_evp, UseTc ? 1 : 0, gevp);
+  const size_t gbytes = batch_group_smem_bytes(a.m, a.m_evp, UseTc ? (G ? 1 : 2) : 0, gevp);
   unsigned char* mine = smraw + gbytes * g;
   double* sm = reinterpret_cast<double*>(mine);
   Scratch S = scratch_of(a, (int)blockIdx.x * NG + g);
   const size_t scal = batch_smem_scalar_bytes(a.m, a.m_evp, gevp);
   S.oz.ktab = reinterpret_cast<int*>(mine + scal);
   if constexpr (UseTc) {
-    tc_begin(s_tc, NG, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK), gbytes);
+    tc_begin(s_tc, NG, TcCfg<G>::kTmemCols, smraw + tc_tiles_offset(scal + sizeof(int) * 2 * kTcMaxK), gbytes);
     S.oz.tc = &s_tc[g];
   }
   bool first = true;
   for (;;) {
-    if (gtid<UseTc>() == 0) {
+    if (gtid<G>() == 0) {
       // every group's first request is fixed: requests 0 .. grid-1 (the
       // largest, in the host's order) go to distinct CTAs, the next grid pair
       // with them in reverse order (largest with smallest); later ones come
@@ -1639,14 +1647,14 @@ __device__ __forceinline__ void batch_kernel_body(const BatchArgs& a) {
       s_j[g] = first ? ((g & 1) ? (g + 1) * grid - 1 - b : g * grid + b) : NG * grid + atomicAdd(a.next, 1);
     }
     first = false;
-    gsync<UseTc>();
+    gsync<G>();
     const int j = s_j[g];
-    gsync<UseTc>();
+    gsync<G>();
     if (j >= a.count) break;
     if (a.inst[j].kind != 0)
-      batch_evp<UseTc>(a, j, S, sm);
+      batch_evp<UseTc, G>(a, j, S, sm);
     else
-      batch_solve<UseTc>(a, j, S, sm);
+      batch_solve<UseTc, G>(a, j, S, sm);
   }
   if constexpr (UseTc) tc_end(s_tc, NG);
 }
@@ -1656,9 +1664,16 @@ __global__ void __launch_bounds__(kBatchThreads, kBatchMinBlocks) batch_sle_kern
   batch_kernel_body<false>(a);
 }
 
-// mixed precision on tcgen05: one CTA per SM holding all of its tensor memory
+// mixed precision on tcgen05: one CTA per SM holding all of its tensor memory,
+// two solves side by side (one per 256-thread group)
 __global__ void __launch_bounds__(kBatchThreadsTc, kBatchMinBlocksTc) batch_sle_tc_kernel(BatchArgs a) {
-  batch_kernel_body<true>(a);
+  batch_kernel_body<true, true>(a);
+}
+
+// the same with one solve on all 512 threads: faster per solve, for batches
+// with fewer requests than two per SM
+__global__ void __launch_bounds__(kTcCtaThreads, kBatchMinBlocksTc) batch_sle_tc1_kernel(BatchArgs a) {
+  batch_kernel_body<true, false>(a);
 }
 
 void oz_need_site(BatchSizes& z, int64_t a, int64_t n, int64_t s, int64_t R0, int64_t R1) {
@@ -1696,7 +1711,7 @@ __global__ void __launch_bounds__(kGroupThreads) apply_f64emu_tc_kernel(Contract
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ TcState s_tc;
   oz.ktab = reinterpret_cast<int*>(smraw);
-  tc_begin(&s_tc, 1, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK), 0);
+  tc_begin(&s_tc, 1, TcCfg<true>::kTmemCols, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK), 0);
   oz.tc = &s_tc;
   cta_contract_f64<true>(p1, L, y, T1, &oz);
   cta_contract_f64<true>(p2, T1, A, T2, &oz);
@@ -1736,7 +1751,7 @@ cudaError_t launch_apply_f64emu(int64_t a, int64_t n, int64_t s, int64_t R0, int
   Contraction p1, p2, p3;
   desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
   if (use_tc) {
-    const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + kTcSmemBytes;
+    const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + TcCfg<true>::kSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(apply_f64emu_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     apply_f64emu_tc_kernel<<<1, kGroupThreads, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out, oz);
@@ -1763,7 +1778,7 @@ __global__ void __launch_bounds__(kGroupThreads) apply_f32_tc_kernel(Contraction
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ TcState s_tc;
   int* ktab = reinterpret_cast<int*>(smraw);
-  tc_begin(&s_tc, 1, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK), 0);
+  tc_begin(&s_tc, 1, TcCfg<true>::kTmemCols, smraw + tc_tiles_offset(sizeof(int) * 2 * kTcMaxK), 0);
   cta_apply<float, true>(p1, p2, p3, L, A, R, y, T1, T2, out, ktab, &s_tc);
   tc_end(&s_tc, 1);
 }
@@ -1774,7 +1789,7 @@ cudaError_t launch_apply_f32(int64_t a, int64_t n, int64_t s, int64_t R0, int64_
   Contraction p1, p2, p3;
   desc_apply(a, n, s, R0, R1, &p1, &p2, &p3);
   if (use_tc) {
-    const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + kTcSmemBytes;
+    const size_t smem = tc_tiles_offset(sizeof(int) * 2 * kTcMaxK) + TcCfg<true>::kSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(apply_f32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     apply_f32_tc_kernel<<<1, kGroupThreads, smem, st>>>(p1, p2, p3, L, A, R, y, T1, T2, out);
@@ -1797,10 +1812,16 @@ __host__ __device__ size_t batch_smem_scalar_bytes(int m, int m_evp, int gevp) {
 }
 
 size_t batch_smem_bytes(int m, int m_evp, int use_tc, int gevp) {
-  return batch_group_smem_bytes(m, m_evp, use_tc, gevp) * (use_tc ? kGroups<true> : 1);
+  return batch_group_smem_bytes(m, m_evp, use_tc, gevp) * batch_solves_per_cta(use_tc);
 }
 
-int batch_solves_per_cta(int use_tc) { return use_tc ? kGroups<true> : 1; }
+int batch_solves_per_cta(int use_tc) { return use_tc == 1 ? kGroups<true> : 1; }
+
+static const void* batch_kernel_fn(int use_tc) {
+  if (use_tc == 1) return (const void*)batch_sle_tc_kernel;
+  if (use_tc == 2) return (const void*)batch_sle_tc1_kernel;
+  return (const void*)batch_sle_kernel;
+}
 
 int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
   const int m = mg > m_evp ? mg : m_evp;
@@ -1811,13 +1832,13 @@ int64_t batch_scratch_stride(const BatchSizes& z, int mg, int m_evp) {
          r(2 * z.oz_a) + r(2 * z.oz_b) + r(4 * z.oz_r) + r(4 * z.oz_c);
 }
 
-int batch_threads(int use_tc) { return use_tc ? kBatchThreadsTc : kBatchThreads; }
+int batch_threads(int use_tc) { return use_tc == 1 ? kBatchThreadsTc : (use_tc == 2 ? kTcCtaThreads : kBatchThreads); }
 
 // Resident CTAs per SM of the kernel variant; *err (if given) receives the
 // first CUDA error of the query (the result is then 1).
 int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err, int gevp) {
   const size_t smem = batch_smem_bytes(m, m_evp, use_tc, gevp);
-  const void* fn = use_tc ? (const void*)batch_sle_tc_kernel : (const void*)batch_sle_kernel;
+  const void* fn = batch_kernel_fn(use_tc);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int occ = 0;
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, batch_threads(use_tc), smem);
@@ -1834,11 +1855,13 @@ int batch_blocks_per_sm(int m, int m_evp, int use_tc, cudaError_t* err, int gevp
 
 cudaError_t launch_batch_sle(const BatchArgs& a, int grid, cudaStream_t st) {
   const size_t smem = batch_smem_bytes(a.m, a.m_evp, a.use_tc, a.sizes.Ng > 0 ? 1 : 0);
-  const void* fn = a.use_tc ? (const void*)batch_sle_tc_kernel : (const void*)batch_sle_kernel;
+  const void* fn = batch_kernel_fn(a.use_tc);
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  if (a.use_tc)
+  if (a.use_tc == 1)
     batch_sle_tc_kernel<<<grid, kBatchThreadsTc, smem, st>>>(a);
+  else if (a.use_tc == 2)
+    batch_sle_tc1_kernel<<<grid, kTcCtaThreads, smem, st>>>(a);
   else
     batch_sle_kernel<<<grid, kBatchThreads, smem, st>>>(a);
   ++launch_counter();

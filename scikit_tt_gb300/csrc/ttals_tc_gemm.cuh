@@ -30,34 +30,40 @@
 namespace ttals {
 
 // A kernel that contains tcgen05 instructions runs one CTA per SM.  That CTA
-// runs two independent solves, one per thread group (kGroupThreads threads,
-// ttals_device.cuh); each group holds half of the SM's 512 TMEM columns and
-// its own operand tiles, and drains its accumulators with two 128-lane
-// sub-groups side by side.  All functions here work on the calling group.
-constexpr int kTcThreads = kGroupThreads;        // threads of one group
-constexpr int kTcGroups = kTcThreads / 128;      // 128-lane drain sub-groups of a group
+// either runs two independent solves, one per thread group (G = true:
+// kGroupThreads threads, ttals_device.cuh), each holding half of the SM's 512
+// TMEM columns and its own operand tiles, or one solve on all of it (G =
+// false: the whole 512-thread CTA).  A group drains its accumulators with
+// 128-lane sub-groups side by side.  All functions here work on the calling
+// group.
 constexpr int kTcM = 128;                        // rows per tile (TMEM lanes)
 constexpr int kTcKC = 32;                        // contraction elements per staged chunk
-constexpr int kTcOzNT = 16 * kTcGroups;          // columns per emulated-FP64 tile: 16 per drain sub-group
 constexpr int kTcOzDrain = 2;                    // chunks accumulated in TMEM between drains (64 steps)
-constexpr int kTcF32NT = 128;                    // columns per 3xTF32 tile
-constexpr uint32_t kTcTmemCols = 256;            // TMEM columns held by one group
 constexpr uint32_t kTcCtaTmemCols = 512;         // TMEM columns allocated by the CTA (all of the SM's)
-constexpr int kTcTileBytes = 64 * 1024;          // operand tiles of one group
-// per-tile index tables after the tiles: operand offset, output offset and
-// exponent of each row (kTcM) and column (kTcF32NT) of the current tile
-constexpr int kTcTabBytes = 3 * 4 * (kTcM + kTcF32NT);
-constexpr int kTcSmemBytes = kTcTileBytes + (kTcTabBytes + 1023) / 1024 * 1024;
+constexpr int kTcCtaThreads = 512;               // threads of a tensor-core CTA
 
-static_assert(kOzSlices * kTcOzNT <= (int)kTcTmemCols, "level accumulators must fit the CTA's TMEM");
-static_assert(kTcF32NT <= (int)kTcTmemCols, "3xTF32 accumulator must fit the CTA's TMEM");
-static_assert(kOzSlices * kTcM * kTcKC * 2 + kOzSlices * kTcOzNT * kTcKC * 2 <= kTcTileBytes, "Ozaki tiles");
-static_assert(2 * kTcM * kTcKC * 4 + 2 * kTcF32NT * kTcKC * 4 <= kTcTileBytes, "3xTF32 tiles");
+template <bool G>
+struct TcCfg {
+  static constexpr int kThreads = G ? kGroupThreads : kTcCtaThreads;  // threads of the group
+  static constexpr int kSub = kThreads / 128;                          // 128-lane drain sub-groups
+  static constexpr int kOzNT = 16 * kSub;       // columns per emulated-FP64 tile: 16 per sub-group
+  static constexpr int kF32NT = G ? 128 : 256;  // columns per 3xTF32 tile
+  static constexpr uint32_t kTmemCols = G ? 256 : 512;  // TMEM columns of the group
+  static constexpr int kTileBytes = G ? 64 * 1024 : 96 * 1024;  // operand tiles of the group
+  // per-tile index tables after the tiles: operand offset, output offset and
+  // exponent of each row (kTcM) and column (kF32NT) of the current tile
+  static constexpr int kTabBytes = 3 * 4 * (kTcM + kF32NT);
+  static constexpr int kSmemBytes = kTileBytes + (kTabBytes + 1023) / 1024 * 1024;
+  static_assert(kOzSlices * kOzNT <= (int)kTmemCols, "level accumulators must fit the group's TMEM");
+  static_assert(kF32NT <= (int)kTmemCols, "3xTF32 accumulator must fit the group's TMEM");
+  static_assert(kOzSlices * kTcM * kTcKC * 2 + kOzSlices * kOzNT * kTcKC * 2 <= kTileBytes, "Ozaki tiles");
+  static_assert(2 * kTcM * kTcKC * 4 + 2 * kF32NT * kTcKC * 4 <= kTileBytes, "3xTF32 tiles");
+};
 
 // Per-group tensor-core state (lives in shared memory).
 struct TcState {
-  unsigned char* tiles;  // kTcSmemBytes, 1024-byte aligned: operand tiles, then the index tables
-  uint32_t tmem;         // TMEM base of the group's kTcTmemCols columns
+  unsigned char* tiles;  // TcCfg::kSmemBytes, 1024-byte aligned: operand tiles, then the index tables
+  uint32_t tmem;         // TMEM base of the group's TcCfg::kTmemCols columns
   uint32_t phase;        // parity of the next MMA completion
   int status;            // ST_OK; ST_TIMEOUT once a completion wait gave up (no further MMAs)
   uint64_t bar;          // mbarrier signalled by tcgen05.commit
@@ -70,9 +76,10 @@ struct TcTables {
   int *rop, *rco, *rex;  // rows: operand offset (-1 beyond the matrix), output offset, exponent
   int *cop, *cco, *cex;  // columns: the same
 };
+template <bool G>
 __device__ __forceinline__ TcTables tc_tables(const TcState& tc) {
-  int* t = reinterpret_cast<int*>(tc.tiles + kTcTileBytes);
-  return TcTables{t, t + kTcM, t + 2 * kTcM, t + 3 * kTcM, t + 3 * kTcM + kTcF32NT, t + 3 * kTcM + 2 * kTcF32NT};
+  int* t = reinterpret_cast<int*>(tc.tiles + TcCfg<G>::kTileBytes);
+  return TcTables{t, t + kTcM, t + 2 * kTcM, t + 3 * kTcM, t + 3 * kTcM + TcCfg<G>::kF32NT, t + 3 * kTcM + 2 * TcCfg<G>::kF32NT};
 }
 
 // int64 fixed point v * 2^e -> FP64, by bit manipulation (round to nearest even).
@@ -106,9 +113,10 @@ __device__ __forceinline__ double tc_i64_to_f64(long long v, int e) {
 }
 
 // Contraction-offset tables koffA / koffB of c (smem, 2 * kTcMaxK ints).
+template <bool G>
 __device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
   const int K = (int)c.ktotal;
-  for (int kk = gtid<true>(); kk < K; kk += gsize<true>()) {
+  for (int kk = gtid<G>(); kk < K; kk += gsize<G>()) {
     int rem = kk, oa = 0, ob = 0;
     for (int q = c.nk - 1; q >= 0; --q) {
       const int iq = rem % c.k_dim[q];
@@ -123,8 +131,9 @@ __device__ __forceinline__ void tc_k_tables(const Contraction& c, int* ktab) {
 
 // Decode rows [r0, r0 + cnt) of an axis set once per tile: operand offset
 // (-1 for rows >= valid) and output offset.
+template <bool G>
 __device__ __forceinline__ void tc_axis_table(const GemmAxes& ax, int r0, int cnt, int valid, int* op, int* co) {
-  for (int i = gtid<true>(); i < cnt; i += gsize<true>()) {
+  for (int i = gtid<G>(); i < cnt; i += gsize<G>()) {
     int o = -1, c = 0;
     if (r0 + i < valid) gemm_axes_offsets(ax, r0 + i, o, c);
     op[i] = o;
@@ -135,10 +144,11 @@ __device__ __forceinline__ void tc_axis_table(const GemmAxes& ax, int r0, int cn
 // E[i] with |x| < 2^E[i] over the contraction of table row i; flags
 // non-finite values.  One warp takes 8 rows at a time with its lanes along
 // the contraction (8 independent loads in flight per lane).
+template <bool G>
 __device__ __forceinline__ void tc_table_exponents(const double* __restrict__ src, const int* koff, int K,
                                                    const int* op, int cnt, int* E, int* bad) {
   constexpr int kRows = 8;
-  const int lane = gtid<true>() & 31, warp = gtid<true>() >> 5, nw = gsize<true>() >> 5;
+  const int lane = gtid<G>() & 31, warp = gtid<G>() >> 5, nw = gsize<G>() >> 5;
   for (int ib = warp * kRows; ib < cnt; ib += nw * kRows) {
     int o[kRows];
     unsigned long long amax[kRows];
@@ -179,12 +189,13 @@ __device__ __forceinline__ void tc_table_exponents(const double* __restrict__ sr
 // at base + p * slice_bytes); rows with op < 0 and k >= K are zero.  One work
 // item = one row x 8 contraction steps (one 16-byte core-matrix row per slice);
 // consecutive threads take consecutive rows.
+template <bool G>
 __device__ __forceinline__ void tc_oz_stage(const double* __restrict__ src, const int* koff, int K, int k0,
                                             const int* op, const int* E, int rows, unsigned char* base,
                                             uint32_t slice_bytes) {
   constexpr int kbytes = kTcKC * 2;
   const int items = rows * (kTcKC / 8);
-  for (int it = gtid<true>(); it < items; it += gsize<true>()) {
+  for (int it = gtid<G>(); it < items; it += gsize<G>()) {
     const int cc = it / rows, r = it - cc * rows;
     const int o = op[r];
     uint32_t w[kOzSlices][4];
@@ -220,99 +231,104 @@ struct TcWaiter {
   uint32_t phase;
   int* fail;  // shared flag, cleared at the start of the call
 };
+template <bool G>
 __device__ __forceinline__ TcWaiter tc_waiter_begin(TcState& tc) {
   __shared__ int s_fail[2];
-  int* f = &s_fail[gidx<true>()];
-  if (gtid<true>() == 0) *f = 0;
+  int* f = &s_fail[gidx<G>()];
+  if (gtid<G>() == 0) *f = 0;
   return TcWaiter{tc.phase, f};
 }
 // Wait for the MMAs committed last (all threads); false (status set) if the wait gave up.
+template <bool G>
 __device__ __forceinline__ bool tc_wait(TcState& tc, TcWaiter& w) {
   if (!umma::mbar_wait(&tc.bar, w.phase)) *w.fail = 1;
   w.phase ^= 1u;
-  gsync<true>();
+  gsync<G>();
   umma::fence_after_sync();
   if (*w.fail) {
-    if (gtid<true>() == 0) tc.status = ST_TIMEOUT;
+    if (gtid<G>() == 0) tc.status = ST_TIMEOUT;
     return false;
   }
   return true;
 }
 // End of a GEMM call: the parity of the next completion goes back to the state.
+template <bool G>
 __device__ __forceinline__ void tc_waiter_end(TcState& tc, const TcWaiter& w) {
-  gsync<true>();
-  if (gtid<true>() == 0) tc.phase = w.phase;
-  gsync<true>();
+  gsync<G>();
+  if (gtid<G>() == 0) tc.phase = w.phase;
+  gsync<G>();
 }
 
 // shared-memory operand writes -> visible to the tensor cores; TMEM reads done
+template <bool G>
 __device__ __forceinline__ void tc_publish() {
   umma::fence_smem_to_async();
   umma::fence_before_sync();
-  gsync<true>();
+  gsync<G>();
   umma::fence_after_sync();
 }
 
 // C = contraction(A, B) with FP64-level accuracy; false when not GEMM-shaped,
 // non-finite, or the tensor cores are unusable (the caller then runs the FP64
 // SIMT path, which overwrites whatever was written).
+template <bool G>
 __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const double* __restrict__ A,
                                                const double* __restrict__ B, double* __restrict__ C,
                                                const OzScratch& z, int* ktab, TcState& tc) {
   (void)z;
   GemmAxes rows, cols;
-  // a group of kTcThreads threads: kTcGroups 128-thread sub-groups, each draining 16 of the tile's columns
+  // a group of TcCfg::kThreads threads: kSub 128-thread sub-groups, each draining 16 of the tile's columns
   if (tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
   __shared__ int s_bad_g[2];
-  int& s_bad = s_bad_g[gidx<true>()];
-  if (gtid<true>() == 0) s_bad = 0;
-  tc_k_tables(c, ktab);
+  int& s_bad = s_bad_g[gidx<G>()];
+  if (gtid<G>() == 0) s_bad = 0;
+  tc_k_tables<G>(c, ktab);
   const int* koffA = ktab;
   const int* koffB = ktab + kTcMaxK;
-  const TcTables T = tc_tables(tc);
-  constexpr uint32_t a_slice = kTcM * kTcKC * 2, b_slice = kTcOzNT * kTcKC * 2;
+  const TcTables T = tc_tables<G>(tc);
+  constexpr uint32_t a_slice = kTcM * kTcKC * 2, b_slice = TcCfg<G>::kOzNT * kTcKC * 2;
   constexpr uint32_t sbo = (kTcKC * 2 / 16) * 128;
   unsigned char* ta = tc.tiles;
   unsigned char* tb = tc.tiles + kOzSlices * a_slice;
   const int nK = (K + kTcKC - 1) / kTcKC;
   const int nwin = (nK + kTcOzDrain - 1) / kTcOzDrain;
   const int sh = nwin <= 1 ? 0 : 32 - __clz(nwin - 1);  // 2^sh >= windows: the int64 sum cannot overflow
-  const int warp = gtid<true>() >> 5, lane = gtid<true>() & 31, q4 = warp & 3;
+  const int warp = gtid<G>() >> 5, lane = gtid<G>() & 31, q4 = warp & 3;
   const int hh = warp >> 2;  // this thread's 16-column block of the tile
   const int rl = 32 * q4 + lane;  // this thread's row of the tile (TMEM lane)
-  TcWaiter wt = tc_waiter_begin(tc);
-  const bool one_n = N <= kTcOzNT;  // column tables and exponents stay valid across row tiles
+  TcWaiter wt = tc_waiter_begin<G>(tc);
+  const bool one_n = N <= TcCfg<G>::kOzNT;  // column tables and exponents stay valid across row tiles
   for (int m0 = 0; m0 < M; m0 += kTcM) {
     const bool cols_now = one_n && m0 == 0;  // the single column tile, decoded once
-    tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
-    if (cols_now) tc_axis_table(cols, 0, (N + 15) & ~15, N, T.cop, T.cco);
-    gsync<true>();
-    tc_table_exponents(A, koffA, K, T.rop, kTcM, T.rex, &s_bad);
-    if (cols_now) tc_table_exponents(B, koffB, K, T.cop, (N + 15) & ~15, T.cex, &s_bad);
-    for (int n0 = 0; n0 < N; n0 += kTcOzNT) {
-      const int ncols = N - n0 < kTcOzNT ? N - n0 : kTcOzNT;
+    tc_axis_table<G>(rows, m0, kTcM, M, T.rop, T.rco);
+    if (cols_now) tc_axis_table<G>(cols, 0, (N + 15) & ~15, N, T.cop, T.cco);
+    gsync<G>();
+    tc_table_exponents<G>(A, koffA, K, T.rop, kTcM, T.rex, &s_bad);
+    if (cols_now) tc_table_exponents<G>(B, koffB, K, T.cop, (N + 15) & ~15, T.cex, &s_bad);
+    for (int n0 = 0; n0 < N; n0 += TcCfg<G>::kOzNT) {
+      const int ncols = N - n0 < TcCfg<G>::kOzNT ? N - n0 : TcCfg<G>::kOzNT;
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtBF16, kTcM, ntile);
       if (!one_n) {
-        gsync<true>();  // the previous tile's store has read the column tables
-        tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
-        gsync<true>();
-        tc_table_exponents(B, koffB, K, T.cop, ntile, T.cex, &s_bad);
+        gsync<G>();  // the previous tile's store has read the column tables
+        tc_axis_table<G>(cols, n0, ntile, N, T.cop, T.cco);
+        gsync<G>();
+        tc_table_exponents<G>(B, koffB, K, T.cop, ntile, T.cex, &s_bad);
       }
-      gsync<true>();
+      gsync<G>();
       if (s_bad) {
-        tc_waiter_end(tc, wt);
+        tc_waiter_end<G>(tc, wt);
         return false;
       }
       long long acc[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) acc[j] = 0;
       for (int kc = 0; kc < nK; ++kc) {
-        if (nK > 1 || n0 == 0) tc_oz_stage(A, koffA, K, kc * kTcKC, T.rop, T.rex, kTcM, ta, a_slice);
-        tc_oz_stage(B, koffB, K, kc * kTcKC, T.cop, T.cex, ntile, tb, b_slice);
-        tc_publish();
-        if (gtid<true>() == 0) {
+        if (nK > 1 || n0 == 0) tc_oz_stage<G>(A, koffA, K, kc * kTcKC, T.rop, T.rex, kTcM, ta, a_slice);
+        tc_oz_stage<G>(B, koffB, K, kc * kTcKC, T.cop, T.cex, ntile, tb, b_slice);
+        tc_publish<G>();
+        if (gtid<G>() == 0) {
           const bool wstart = (kc % kTcOzDrain) == 0;
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
           uint64_t da[kOzSlices], db[kOzSlices];
@@ -329,18 +345,18 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
               for (int q = 0; q < kOzSlices - p; ++q) {
                 // the start-address field counts 16-byte units: +16 per 256-byte K step
                 const uint32_t acc_in = (wstart && ks == 0 && p == 0) ? 0u : 1u;
-                umma::mma_f16(umma::taddr(tc.tmem, 0, (p + q) * kTcOzNT), da[p] + 16u * ks, db[q] + 16u * ks, id,
+                umma::mma_f16(umma::taddr(tc.tmem, 0, (p + q) * TcCfg<G>::kOzNT), da[p] + 16u * ks, db[q] + 16u * ks, id,
                               acc_in);
               }
           umma::commit(&tc.bar);
         }
-        if (!tc_wait(tc, wt)) return false;
+        if (!tc_wait<G>(tc, wt)) return false;
         if ((kc % kTcOzDrain) == kTcOzDrain - 1 || kc == nK - 1) {
           if (hh * 16 < ntile) {  // warp-uniform
 #pragma unroll
             for (int L = 0; L < kOzSlices; ++L) {
               uint32_t v[16];
-              umma::ld16(umma::taddr(tc.tmem, 32 * q4, L * kTcOzNT + hh * 16), v);
+              umma::ld16(umma::taddr(tc.tmem, 32 * q4, L * TcCfg<G>::kOzNT + hh * 16), v);
               umma::ld_wait();
               const int lsh = 8 * (kOzSlices - 1 - L) - sh;
 #pragma unroll
@@ -363,21 +379,22 @@ __device__ __forceinline__ bool cta_gemm_oz_tc(const Contraction& c, const doubl
           if (cl < ncols) C[cr + T.cco[cl]] = tc_i64_to_f64(acc[j], er + T.cex[cl]);
         }
       }
-      gsync<true>();
+      gsync<G>();
     }
   }
-  tc_waiter_end(tc, wt);
+  tc_waiter_end<G>(tc, wt);
   return true;
 }
 
 // Rows [0, rows) of the tile (operand offsets op) x contraction [k0, k0 + kTcKC)
 // of an FP32 operand as TF32 head and tail tiles (hi at base, lo at
 // base + half_bytes); rows with op < 0 and k >= K are zero.
+template <bool G>
 __device__ __forceinline__ void tc_tf32_stage(const float* __restrict__ src, const int* koff, int K, int k0,
                                               const int* op, int rows, unsigned char* base, uint32_t half_bytes) {
   constexpr int kbytes = kTcKC * 4;
   const int items = rows * (kTcKC / 4);
-  for (int it = gtid<true>(); it < items; it += gsize<true>()) {
+  for (int it = gtid<G>(); it < items; it += gsize<G>()) {
     const int cc = it / rows, r = it - cc * rows;
     const int o = op[r];
     uint32_t hi[4] = {0u, 0u, 0u, 0u}, lo[4] = {0u, 0u, 0u, 0u};
@@ -402,39 +419,40 @@ __device__ __forceinline__ void tc_tf32_stage(const float* __restrict__ src, con
 
 // C = contraction(A, B) in FP32 (3xTF32) on the tensor cores; false when not
 // GEMM-shaped or the tensor cores are unusable.
+template <bool G>
 __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const float* __restrict__ A,
                                                  const float* __restrict__ B, float* __restrict__ C, int* ktab,
                                                  TcState& tc) {
   GemmAxes rows, cols;
   if (tc.status != ST_OK || !gemm_split(c, rows, cols)) return false;
   const int M = rows.total, N = cols.total, K = (int)c.ktotal;
-  tc_k_tables(c, ktab);
+  tc_k_tables<G>(c, ktab);
   const int* koffA = ktab;
   const int* koffB = ktab + kTcMaxK;
-  const TcTables T = tc_tables(tc);
-  constexpr uint32_t a_half = kTcM * kTcKC * 4, b_half = kTcF32NT * kTcKC * 4;
+  const TcTables T = tc_tables<G>(tc);
+  constexpr uint32_t a_half = kTcM * kTcKC * 4, b_half = TcCfg<G>::kF32NT * kTcKC * 4;
   constexpr uint32_t sbo = (kTcKC * 4 / 16) * 128;
   unsigned char* ta = tc.tiles;
   unsigned char* tb = tc.tiles + 2 * a_half;
   const int nK = (K + kTcKC - 1) / kTcKC;
-  const int warp = gtid<true>() >> 5, lane = gtid<true>() & 31, q4 = warp & 3;
-  const int halves = gsize<true>() >> 7, grp = warp >> 2;
+  const int warp = gtid<G>() >> 5, lane = gtid<G>() & 31, q4 = warp & 3;
+  const int halves = gsize<G>() >> 7, grp = warp >> 2;
   const int rl = 32 * q4 + lane;
-  TcWaiter wt = tc_waiter_begin(tc);
-  const bool one_n = N <= kTcF32NT;
+  TcWaiter wt = tc_waiter_begin<G>(tc);
+  const bool one_n = N <= TcCfg<G>::kF32NT;
   for (int m0 = 0; m0 < M; m0 += kTcM) {
-    tc_axis_table(rows, m0, kTcM, M, T.rop, T.rco);
-    for (int n0 = 0; n0 < N; n0 += kTcF32NT) {
-      const int ncols = N - n0 < kTcF32NT ? N - n0 : kTcF32NT;
+    tc_axis_table<G>(rows, m0, kTcM, M, T.rop, T.rco);
+    for (int n0 = 0; n0 < N; n0 += TcCfg<G>::kF32NT) {
+      const int ncols = N - n0 < TcCfg<G>::kF32NT ? N - n0 : TcCfg<G>::kF32NT;
       const int ntile = (ncols + 15) & ~15;
       const uint32_t id = umma::idesc(umma::kFmtTF32, kTcM, ntile);
-      if (!one_n || m0 == 0) tc_axis_table(cols, n0, ntile, N, T.cop, T.cco);
-      gsync<true>();
+      if (!one_n || m0 == 0) tc_axis_table<G>(cols, n0, ntile, N, T.cop, T.cco);
+      gsync<G>();
       for (int kc = 0; kc < nK; ++kc) {
-        if (nK > 1 || n0 == 0) tc_tf32_stage(A, koffA, K, kc * kTcKC, T.rop, kTcM, ta, a_half);
-        tc_tf32_stage(B, koffB, K, kc * kTcKC, T.cop, ntile, tb, b_half);
-        tc_publish();
-        if (gtid<true>() == 0) {
+        if (nK > 1 || n0 == 0) tc_tf32_stage<G>(A, koffA, K, kc * kTcKC, T.rop, kTcM, ta, a_half);
+        tc_tf32_stage<G>(B, koffB, K, kc * kTcKC, T.cop, ntile, tb, b_half);
+        tc_publish<G>();
+        if (gtid<G>() == 0) {
           const uint32_t a0 = umma::smem_u32(ta), b0 = umma::smem_u32(tb);
           const uint32_t d = umma::taddr(tc.tmem, 0, 0);
           const uint64_t ah = umma::sdesc(a0, 128, sbo), al = umma::sdesc(a0 + a_half, 128, sbo);
@@ -448,7 +466,7 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
           }
           umma::commit(&tc.bar);
         }
-        if (!tc_wait(tc, wt)) return false;
+        if (!tc_wait<G>(tc, wt)) return false;
       }
       const bool live = T.rop[rl] >= 0;
       const int cr = T.rco[rl];
@@ -466,10 +484,10 @@ __device__ __forceinline__ bool cta_gemm_tf32_tc(const Contraction& c, const flo
         }
       }
       umma::fence_before_sync();
-      gsync<true>();
+      gsync<G>();
     }
   }
-  tc_waiter_end(tc, wt);
+  tc_waiter_end<G>(tc, wt);
   return true;
 }
 

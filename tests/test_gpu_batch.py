@@ -81,9 +81,10 @@ def test_batch_many_instances_more_than_sms():
 
 def test_batch_autotuner_tries_each_variant_then_keeps_the_fastest():
     """The engine's autotuner: per workload bucket the first mixed-precision
-    batches run the tcgen05 kernel, the warp-MMA kernel at full occupancy and
-    at one CTA per SM less (each solving its batch in full), then it keeps
-    the fastest by kernel time per solve; a fixed variant is honoured."""
+    batches run the tcgen05 kernel with two solves per CTA and with one, the
+    warp-MMA kernel at full occupancy and at one CTA per SM less (each solving
+    its batch in full), then it keeps the fastest by kernel time per solve; a
+    fixed variant is honoured."""
     from scikit_tt_gb300 import _lib
     from scikit_tt_gb300.solvers import sle
     lib, ctx = _lib.load(), _lib.context()
@@ -95,16 +96,19 @@ def test_batch_autotuner_tries_each_variant_then_keeps_the_fastest():
     try:
         # a bucket no other test uses: seven instances of the fourth shape
         probs7 = [probs[3]] * 7
-        for _ in range(4):
+        for _ in range(5):
             sols, st = sle.als_batch(probs7, repeats=1, precision='mixed', tol=1e-10)
-            seen.append((st['batch_tensor_cores'], st['batch_ctas_per_sm'], st['solver_ms']))
-            assert O.stable_rel_diff(sols[0].cores, refs[3]) < 1e-8
-        variants = [(t, c) for t, c, _ in seen[:3]]
-        assert variants[0][0] == 1 and variants[1][0] == 0 and variants[2][0] == 0
-        assert variants[2][1] == variants[1][1] - 1
-        best = min(range(3), key=lambda k: seen[k][2])
-        assert (seen[3][0], seen[3][1]) == variants[best]
-        _lib.check(lib.ttals_set_batch_variant(ctx, 1))
+            seen.append((st['batch_tensor_cores'], st['batch_ctas_per_sm'], st['batch_solves_per_cta'],
+                         st['solver_ms']))
+            for sol in sols:
+                assert O.stable_rel_diff(sol.cores, refs[3]) < 1e-8
+        variants = [v[:3] for v in seen[:4]]
+        # tcgen05 with two solves per CTA, with one, then the warp-MMA kernel at full occupancy and one less
+        assert variants[0] == (1, 1, 2) and variants[1] == (1, 1, 1)
+        assert variants[2][0] == 0 and variants[3][0] == 0 and variants[3][1] == variants[2][1] - 1
+        best = min(range(4), key=lambda k: seen[k][3])
+        assert seen[4][:3] == variants[best]
+        _lib.check(lib.ttals_set_batch_variant(ctx, 2))
         sols, st = sle.als_batch(probs, repeats=1, precision='mixed', tol=1e-10)
         assert st['batch_tensor_cores'] == 0
         for sol, ref in zip(sols, refs):
