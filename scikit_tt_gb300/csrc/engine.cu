@@ -1616,7 +1616,7 @@ std::string tune_key(const BatchPlan& P) {
 
 // trial: the plan may try an untested candidate (synchronous batches, which
 // time themselves); otherwise (serving jobs, size queries) it takes the
-// bucket's fastest candidate once known, else the warp-MMA kernel at full occupancy.
+// bucket's fastest candidate once known, else a guess by batch width.
 BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int prec, double tol, bool trial = false) {
   require(count >= 1, TTALS_ERR_ARG, "count must be >= 1");
   require(reqs != nullptr, TTALS_ERR_ARG, "null request array");
@@ -1758,10 +1758,16 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     } else {
       const ttals_ctx::Tune& t = c->tune[tune_key(P)];
       if (t.trials < (int)cand.size()) {
-        // untested bucket outside a timed batch: the warp-MMA kernel at full occupancy
-        int plain = 0;
-        while (plain + 1 < (int)cand.size() && cand[plain].use_tc != 0) ++plain;
-        pick = trial ? t.trials : plain;
+        // untested bucket outside a timed batch (serving jobs): the variant
+        // measured fastest for its batch width -- tcgen05 with two solves per
+        // CTA once the batch fills two per SM, with one below that; the
+        // warp-MMA kernel at full occupancy without tensor cores
+        int guess = 0;
+        const int want = count >= 2 * c->num_sms ? 1 : 2;
+        while (guess + 1 < (int)cand.size() && cand[guess].use_tc != want &&
+               !(cand[guess].use_tc == 0 && cand[guess].less == 0))
+          ++guess;
+        pick = trial ? t.trials : guess;
       } else {
         for (int k = 1; k < (int)cand.size(); ++k)
           if (t.ms[k] < t.ms[pick]) pick = k;
