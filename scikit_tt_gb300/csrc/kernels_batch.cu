@@ -194,9 +194,8 @@ __device__ __forceinline__ void cta_dots(const T* V, int64_t N, int nvec, const 
       s1 += xv[e + 32] * w[e + 32];
     }
     if (e < N) s0 += xv[e] * w[e];
-    double s = (double)s0 + (double)s1;
-    s = warp_sum(s);
-    if (lane == 0) out[kk] = s;
+    const T st = warp_sum(s0 + s1);
+    if (lane == 0) out[kk] = (double)st;
   }
   gsync<G>();
 }
@@ -223,9 +222,12 @@ __device__ __noinline__ void cta_dots_wide(const T* V, int64_t N, int nvec, cons
       s3 += xv[e + 3 * nt] * w[e + 3 * nt];
     }
     for (; e < N; e += nt) s0 += xv[e] * w[e];
-    double sd = ((double)s0 + (double)s1) + ((double)s2 + (double)s3);
+    // FP32 vectors reduce in FP32 within the warp (no per-lane conversions
+    // to FP64, whose pipe runs two FMAs per clock per SM); the warps' sums
+    // are added in FP64
+    T sd = (s0 + s1) + (s2 + s3);
     sd = warp_sum(sd);
-    if (lane == 0) part[warp][kk] = sd;
+    if (lane == 0) part[warp][kk] = (double)sd;
   }
   gsync<G>();
   for (int kk = tid; kk <= nvec; kk += nt) {
