@@ -27,6 +27,8 @@ def main():
     ap.add_argument('--count', type=int, default=1)
     ap.add_argument('--tol', type=float, default=0.0)
     ap.add_argument('--batch', type=int, default=0, help='solve this many seeded instances in one batch launch')
+    ap.add_argument('--variant', type=int, default=-1,
+                    help='launch variant of batched calls (ttals_set_batch_variant; -1: autotuned)')
     a = ap.parse_args()
     kw = {}
     if a.d:
@@ -53,6 +55,8 @@ def main():
     w = wl.laplace_sle(**kw) if a.workload == 'laplace' else wl.coupled_sle(**kw)
     rep = a.repeats or w.repeats
     if a.batch:
+        from . import _lib
+        _lib.check(_lib.load().ttals_set_batch_variant(_lib.context(), a.variant))
         build = wl.laplace_sle if a.workload == 'laplace' else wl.coupled_sle
         probs = []
         for j in range(a.batch):
