@@ -366,6 +366,15 @@ def other_workloads(lib, ctx, args):
     out['ising_d48_r64'] = {'dropin_fp64_ms': evp.last_stats['device_ms'], 'eigenvalue': val,
                             'abs_err_vs_exact': abs(val - e0), 'sweeps': its,
                             'lanczos_iterations': evp.last_stats['krylov_iterations']}
+    # the same eigenproblem in mixed precision: one request of the batch engine, whose mixed
+    # eigensolves run their products as emulated FP64 on the tensor cores (one SM)
+    from scikit_tt_gb300.serving import Request, solve_batch
+    rq = Request('evp', w3.op, w3.x0, repeats=w3.repeats, sigma=w3.sigma)
+    stq = solve_batch([rq], precision='mixed')
+    out['ising_d48_r64']['mixed_batch_request'] = {
+        'eigenvalue': rq.value, 'abs_err_vs_exact': abs(rq.value - e0), 'abs_diff_vs_fp64_dropin': abs(rq.value - val),
+        'device_ms': stq['device_ms'], 'sweeps': rq.iterations, 'max_local_residual': stq['max_local_residual'],
+        'what': 'one request on one SM (the batch engine), mixed precision'}
     # two-site TDVP, Ising d=16 g=1.2 from a rank-4 state, ranks <= 16, imaginary-time steps of 0.05
     # with exact local exponentials; the oracle runs the first two steps for time and parity
     from scikit_tt_gb300.solvers import ode

@@ -175,7 +175,8 @@ int ttals_batch_slots(ttals_ctx* ctx, int32_t* slots);
 
 /* Launch variant of the batched calls (ttals_sle_als_batch, ttals_solve_batch,
  * ttals_submit).  -1 (default): autotuned -- per workload bucket (precision,
- * request kinds, largest local system, stack and operator core) the first
+ * request kinds, largest local system, stack and operator core, and whether
+ * the batch holds two requests per SM) the first
  * batches try each candidate once (every one of them solves its batch in
  * full), later ones use the fastest by kernel time per solve.  Candidates,
  * mixed precision: 0 tensor-core kernel (one CTA per SM running two requests

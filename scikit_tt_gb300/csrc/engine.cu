@@ -1605,13 +1605,16 @@ std::vector<BatchVariant> batch_candidates(int prec) {
   return v;
 }
 
-// Bucket of a planned batch for the autotuner: precision, request kinds and
-// the largest per-site sizes (local unknowns, stack, operator core).
-std::string tune_key(const BatchPlan& P) {
+// Bucket of a planned batch for the autotuner: precision, request kinds, the
+// largest per-site sizes (local unknowns, stack, operator core) and whether
+// the batch fills two requests per SM (the best variant differs: measured,
+// tcgen05 with two solves per CTA for full batches, with one below that).
+std::string tune_key(const ttals_ctx* c, const BatchPlan& P) {
   int evp = 0;
   for (const auto& I : P.in) evp |= I.kind;
+  const bool wide = (int64_t)P.in.size() >= 2 * (int64_t)c->num_sms;
   return std::to_string(P.prec) + "|" + std::to_string(evp) + "|" + std::to_string(P.z.N) + "|" +
-         std::to_string(P.z.stack) + "|" + std::to_string(P.z.opcore);
+         std::to_string(P.z.stack) + "|" + std::to_string(P.z.opcore) + (wide ? "|wide" : "|narrow");
 }
 
 // trial: the plan may try an untested candidate (synchronous batches, which
@@ -1756,7 +1759,7 @@ BatchPlan plan_batch(ttals_ctx* c, int count, const ttals_request* reqs, int pre
     if (c->batch_variant >= 0) {
       pick = std::min<int>(c->batch_variant, (int)cand.size() - 1);
     } else {
-      const ttals_ctx::Tune& t = c->tune[tune_key(P)];
+      const ttals_ctx::Tune& t = c->tune[tune_key(c, P)];
       if (t.trials < (int)cand.size()) {
         // untested bucket outside a timed batch (serving jobs): the variant
         // measured fastest for its batch width -- tcgen05 with two solves per
@@ -2017,7 +2020,7 @@ void run_batch_sync(ttals_ctx* c, int count, const ttals_request* reqs, int prec
   CK(cudaEventElapsedTime(&kms, k0, k1));
   CK(cudaEventElapsedTime(&tms, c->ev0, c->ev1));
   if (c->batch_variant < 0) {
-    ttals_ctx::Tune& t = c->tune[tune_key(P)];
+    ttals_ctx::Tune& t = c->tune[tune_key(c, P)];
     if (t.trials < (int)batch_candidates(prec).size() && P.variant == t.trials) {
       t.ms[t.trials] = (double)kms / count;
       ++t.trials;
