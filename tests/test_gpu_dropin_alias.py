@@ -1,5 +1,5 @@
-"""The drop-in switch as INTEGRATION.md documents it: its module-alias block,
-taken verbatim from that file, runs in a fresh interpreter, after which the
+"""The drop-in switch as the repository's integration guide documents it: its
+module-alias block, taken verbatim from the guide, runs in a fresh interpreter, after which the
 code below reaches this package only through ``scikit_tt.*`` import paths, in
 the way the reference's tests call the ALS path (tests/test_sle.py:13-59 and
 tests/test_evp.py:16-150): the Toeplitz system through the full-array TT
@@ -65,7 +65,7 @@ print('evp ok', vals, vals_h)
 def _alias_block():
     text = open(os.path.join(ROOT, 'INTEGRATION.md')).read()
     m = re.search(r'aliasing the modules.*?```python\n(.*?)```', text, re.S)
-    assert m, 'INTEGRATION.md lost its module-alias block'
+    assert m, 'the integration guide lost its module-alias block'
     return m.group(1)
 
 
