@@ -134,3 +134,22 @@ def test_run_stream_groups_arrivals(fake):
     done, wall, stats = serving.run_stream(items, duration_cap=1.0, max_batch=2, batch_window=0.001)
     assert len(done) == 5 and sum(s['local_solves'] for s in stats) == 5
     assert all(r.done >= r.arrival for r in done)
+
+
+def test_request_kinds_map_to_the_abi():
+    """Served request kinds and their descriptors (host only): a generalised
+    eigenproblem travels as TTALS_REQ_GEVP with operator_gevp in the rhs slot,
+    and it weighs like an eigenproblem in the largest-first order of a job."""
+    from scikit_tt_gb300 import build_ext
+    build_ext.build()
+    d = 4
+    A = wl.ising_op(d, 1.0, 1.2)
+    B = wl.laplace_op(d, 2, h=1.0, shift=1.0)
+    x0 = wl.gaussian_tt(__import__('numpy').random.default_rng(0), d, 2, 2)
+    rg = serving.Request('gevp', A, x0, B, repeats=2, solver='eigh')
+    re_ = serving.Request('evp', A, x0, repeats=2)
+    dg, de = rg._descriptor(), re_._descriptor()
+    assert dg.kind == _lib.REQ_GEVP and de.kind == _lib.REQ_EVP
+    assert dg.rhs.order == d and dg.rhs.ranks[1] == B[0].shape[3]
+    assert dg.solver == _lib.EVP_SOLVERS['eigh']
+    assert rg.work_estimate() == re_.work_estimate() > 0
