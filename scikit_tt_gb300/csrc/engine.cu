@@ -1487,8 +1487,13 @@ void run_arr(ttals_ctx* c, int d, const int64_t* nb, int64_t m, const double* th
       const Ax kc[1] = {{m, kq, 1, 0}};
       CK(launch_contract<double>(desc_make(1, oc, 1, kc), L.A, yk, L.cv, 1.0, 0.0, s_));
       int* kdev = reinterpret_cast<int*>(L.kept);
-      CK(launch_svd_trunc(L.Rb, kq, N, 0, rcond, 0, L.sw, L.cb, L.sb, kdev, E.status, s_));
-      CK(launch_lstsq_combine(L.cb, L.sb, L.cv, kq, N, kdev, L.X[i], s_));
+      int* fast = kdev + 1;  // the triangular solve sufficed: SVD and combination return at once
+      if (kq == N)
+        CK(launch_lstsq_tri(L.Rb, L.cv, N, rcond, L.cb, L.X[i], fast, s_));
+      else
+        CK(cudaMemsetAsync(fast, 0, sizeof(int), s_));
+      CK(launch_svd_trunc(L.Rb, kq, N, 0, rcond, 0, L.sw, L.cb, L.sb, kdev, E.status, s_, fast));
+      CK(launch_lstsq_combine(L.cb, L.sb, L.cv, kq, N, kdev, L.X[i], s_, fast));
       if (forward) {
         QrArgs f{L.X[i], s, 1, L.X[i], std::min(a * nn, s), 1, L.rq, s, 1, a * nn, s, 0, nullptr, L.qw};
         CK(launch_qr_fast(f, s_));

@@ -262,9 +262,11 @@ struct SvdK {
   float* W32;        // FP32 copies for the preconditioning sweeps
   float* V32;
   int in_smem;       // bits: 1 W, 2 W32, 4 Vr, 8 V32 in dynamic shared memory (in that order)
+  const int* skip;   // nonzero *skip: the factorisation is not needed (return at once); may be null
 };
 
 __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
+  if (a.skip && *a.skip) return;
   extern __shared__ double s_dyn[];
   __shared__ int s_a[kTrMaxGram / 2], s_b[kTrMaxGram / 2];
   __shared__ double s_sig[kTrMaxGram];
@@ -588,7 +590,9 @@ __global__ void __launch_bounds__(kTrThreads) svd_trunc_kernel(SvdK a) {
 // singular values, c = Q^T y:  x = V S^-1 U^T c = (S V^T)^T S^-2 (U^T c).
 // U: kq x r (row-major, leading dimension r), SVt: r x N.  One CTA.
 __global__ void __launch_bounds__(1024) lstsq_combine_kernel(const double* U, const double* SVt, const double* c,
-                                                              int64_t kq, int64_t N, const int* kept, double* x) {
+                                                              int64_t kq, int64_t N, const int* kept, double* x,
+                                                              const int* skip) {
+  if (skip && *skip) return;
   __shared__ double w[kTrMaxGram];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int r = *kept;
@@ -609,9 +613,85 @@ __global__ void __launch_bounds__(1024) lstsq_combine_kernel(const double* U, co
 }
 
 cudaError_t launch_lstsq_combine(const double* U, const double* SVt, const double* c, int64_t kq, int64_t N,
-                                 const int* kept, double* x, cudaStream_t st) {
+                                 const int* kept, double* x, cudaStream_t st, const int* skip) {
   if (std::min(kq, N) > kTrMaxGram) return cudaErrorInvalidValue;
-  lstsq_combine_kernel<<<1, 1024, 0, st>>>(U, SVt, c, kq, N, kept, x);
+  lstsq_combine_kernel<<<1, 1024, 0, st>>>(U, SVt, c, kq, N, kept, x, skip);
+  ++launch_counter();
+  return cudaGetLastError();
+}
+
+// Least squares through the triangular factor when that is safe: R (N x N,
+// upper triangular, row-major) from the QR of the m x N micro matrix (m >= N)
+// and c = Q^T y.  gelss (scipy.linalg.lstsq as regression.py:487 calls it)
+// treats singular values below rcond * s_max as zero; when
+// ||R||_F ||R^-1||_F <= 1e-2 / rcond no singular value is that small, and when
+// it is also <= 1e5 the two solutions agree to rounding, so x = R^-1 c.  R^-1
+// is formed column by column (thread j back-substitutes e_j) into Z (N x N);
+// *fast = 1 then and x is written, else *fast = 0 and the SVD path solves.
+__global__ void __launch_bounds__(1024) lstsq_tri_kernel(const double* R, const double* c, int64_t N, double rcond,
+                                                          double* Z, double* x, int* fast) {
+  __shared__ double rinv[kTrMaxGram];
+  __shared__ double red[32];
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  auto block_sum = [&](double v) {
+    v = warp_sum(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += red[w];
+    __syncthreads();
+    return t;
+  };
+  if (tid == 0) s_ok = 1;
+  __syncthreads();
+  for (int64_t i = tid; i < N; i += nt) {
+    const double d = R[i * N + i];
+    if (!(fabs(d) > 0.0) || !isfinite(d)) s_ok = 0;
+    rinv[i] = 1.0 / d;
+  }
+  __syncthreads();
+  if (!s_ok) {
+    if (tid == 0) *fast = 0;
+    return;
+  }
+  double sr = 0.0;
+  for (int64_t e = tid; e < N * N; e += nt) {
+    const int64_t i = e / N, k = e - i * N;
+    if (k >= i) sr += R[e] * R[e];
+  }
+  sr = block_sum(sr);
+  for (int64_t j = tid; j < N; j += nt) {
+    Z[j * N + j] = rinv[j];
+    for (int64_t i = j - 1; i >= 0; --i) {
+      double acc = 0.0;
+      for (int64_t k = i + 1; k <= j; ++k) acc += R[i * N + k] * Z[k * N + j];
+      Z[i * N + j] = -acc * rinv[i];
+    }
+  }
+  __syncthreads();
+  double sz = 0.0;
+  for (int64_t e = tid; e < N * N; e += nt) {
+    const int64_t i = e / N, k = e - i * N;
+    if (k >= i) sz += Z[e] * Z[e];
+  }
+  sz = block_sum(sz);
+  const double kf = sqrt(sr) * sqrt(sz);
+  const int ok = isfinite(kf) && kf <= 1e5 && kf * rcond <= 1e-2;
+  if (ok) {
+    for (int64_t i = tid; i < N; i += nt) {
+      double acc = 0.0;
+      for (int64_t k = i; k < N; ++k) acc += Z[i * N + k] * c[k];
+      x[i] = acc;
+    }
+  }
+  if (tid == 0) *fast = ok;
+}
+
+cudaError_t launch_lstsq_tri(const double* R, const double* c, int64_t N, double rcond, double* Z, double* x,
+                             int* fast, cudaStream_t st) {
+  if (N > kTrMaxGram || N < 1) return cudaErrorInvalidValue;
+  lstsq_tri_kernel<<<1, 1024, 0, st>>>(R, c, N, rcond, Z, x, fast);
   ++launch_counter();
   return cudaGetLastError();
 }
@@ -624,7 +704,8 @@ size_t svd_trunc_work_doubles(int64_t p, int64_t q) {
 }
 
 cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
-                             double* work, double* core, double* r, int* kept, int* status, cudaStream_t st) {
+                             double* work, double* core, double* r, int* kept, int* status, cudaStream_t st,
+                             const int* skip) {
   const int64_t n = p < q ? p : q, rows = p > q ? p : q;
   if (n > kTrMaxGram || n < 1) return cudaErrorInvalidValue;
   // the dots read W at every rotation step: W first, then V if both fit
@@ -641,7 +722,7 @@ cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, do
   double* w32 = work + rows * n + n * n;
   double* v32 = w32 + (rows * n + 1) / 2;
   SvdK a{M,    p,    q, side, threshold, max_rank, work, work + rows * n, core, r, kept, status,
-         reinterpret_cast<float*>(w32), reinterpret_cast<float*>(v32), in_smem};
+         reinterpret_cast<float*>(w32), reinterpret_cast<float*>(v32), in_smem, skip};
   if (in_smem) {
     cudaError_t e = cudaFuncSetAttribute(svd_trunc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSvdSmemMax);

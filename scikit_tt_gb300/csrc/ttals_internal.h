@@ -155,11 +155,16 @@ cudaError_t launch_trunc_basis(const double* M, int64_t p, int64_t q, int tr_k, 
 // -> side 0: core = U (p x k), r = S V^T (k x q); side 1: core = V^T, r = U S
 size_t svd_trunc_work_doubles(int64_t p, int64_t q);
 cudaError_t launch_svd_trunc(const double* M, int64_t p, int64_t q, int side, double threshold, int64_t max_rank,
-                             double* work, double* core, double* r, int* kept, int* status, cudaStream_t st);
+                             double* work, double* core, double* r, int* kept, int* status, cudaStream_t st,
+                             const int* skip = nullptr);
 
 // x = V S^-1 U^T c from the truncated SVD of R (kernels_evp.cu, least squares)
 cudaError_t launch_lstsq_combine(const double* U, const double* SVt, const double* c, int64_t kq, int64_t N,
-                                 const int* kept, double* x, cudaStream_t st);
+                                 const int* kept, double* x, cudaStream_t st, const int* skip = nullptr);
+// x = R^-1 c when the square triangular R is safely invertible for gelss's
+// rcond (kernels_evp.cu); *fast = 1 then (the SVD path is skipped), else 0
+cudaError_t launch_lstsq_tri(const double* R, const double* c, int64_t N, double rcond, double* Z, double* x,
+                             int* fast, cudaStream_t st);
 
 // failure-detection probe (kernels_basic.cu): bounded wait on *flag leaving 0
 cudaError_t launch_wait_probe(const unsigned* flag, unsigned limit, int* status, cudaStream_t st);
