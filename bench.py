@@ -114,6 +114,62 @@ def site_sizes(w):
     return sizes
 
 
+def stack_update_flops(w, op_rank=4):
+    """Algorithmic FP64-class flops of every operator-stack update of one
+    solve of the coupled workload, in the batch kernel's order (initial right
+    stacks, then per sweep a left update before each forward local solve and a
+    right update before each backward one) and with its rank rule: the
+    three-contraction update 2 a^2 R n s + 2 a s n^2 R R' + 2 a n s^2 R' per
+    site (sle.py:194-219, 250-276)."""
+    d, n = w.meta['d'], w.meta['n']
+    R = [1] + [op_rank] * (d - 1) + [1]
+    r = [1] + [w.meta['x_rank']] * (d - 1) + [1]
+    for i in range(d - 1, 0, -1):
+        r[i] = min(r[i], n * r[i + 1])
+    fl = lambda a, s_, R0, R1: 2 * a * a * R0 * n * s_ + 2 * a * s_ * n * n * R0 * R1 + 2 * a * n * s_ * s_ * R1
+    tot = 0.0
+    for i in range(d - 2, -1, -1):                 # right(i) for i < d - 1
+        tot += fl(r[i + 1], r[i + 2], R[i + 1], R[i + 2])
+    for _ in range(w.repeats):
+        for i in range(d):
+            if i > 0:
+                tot += fl(r[i - 1], r[i], R[i - 1], R[i])
+            if i < d - 1:
+                r[i + 1] = min(r[i] * n, r[i + 1])
+        for i in range(d - 1, -1, -1):
+            if i < d - 1:
+                tot += fl(r[i + 1], r[i + 2], R[i + 1], R[i + 2])
+            if i > 0:
+                r[i] = min(r[i], n * r[i + 1])
+    return tot
+
+
+def stack_phase_tensor(w, st, nreq, sm_mhz, bf16_peak_tflops, sms):
+    """Tensor-pipe fraction of the mixed kernel's stack phase: each FP64-class
+    stack flop is 21 BF16 slice products on the tensor pipe (six-slice
+    emulation, slice pairs p + q < 6); the phase's seconds per solve come from
+    the kernel's per-request phase counters (SM cycles, summed over the
+    launch's ``nreq`` requests) at the sampled SM clock; an SM runs
+    solves_per_cta x ctas_per_sm solves at once, all counted as in the phase
+    (an upper bound).  None when an input is missing."""
+    try:
+        cyc = float(list(st.phase_cycles)[1]) / nreq
+        if not (cyc > 0 and sm_mhz and sm_mhz > 0):
+            return None
+        t = cyc / (sm_mhz * 1e6)
+        fl = stack_update_flops(w)
+        per_sm = max(1, int(st.batch_solves_per_cta)) * max(1, int(st.batch_ctas_per_sm))
+        rate = per_sm * 21.0 * fl / t
+        peak = bf16_peak_tflops * 1e12 / sms
+        return {'fp64_class_gflop_per_solve': fl / 1e9, 'tensor_gflop_per_solve': 21.0 * fl / 1e9,
+                'phase_s_per_solve': t, 'tensor_tflops_per_sm': rate / 1e12, 'frac': rate / peak,
+                'what': 'stack updates only: 21 BF16 slice products per FP64-class flop over the stack '
+                        'phase of the kernel\'s own cycle counters, per SM against the measured BF16 peak '
+                        '/ SMs (all resident solves counted as in the phase: an upper bound)'}
+    except Exception:
+        return None
+
+
 LU_CAP = 8192   # dense LU timed on the leading LU_CAP x LU_CAP block, scaled by (N / LU_CAP)^3 (larger N only)
 
 
@@ -690,6 +746,8 @@ def main_gpu(args):
                      'achieved_fp64_class_gflops': ach64, 'achieved_fp32_gflops': ach32,
                      'fp64_fma_peak_gflops': p64.value, 'fp32_fma_peak_gflops': p32.value,
                      'avg_launch_ms': sm_.solver_ms,
+                     'stack_phase': stack_phase_tensor(inst[0], sm_, B, clk.summary().get('sm_mhz'), bf16_peak,
+                                                       sms),
                      'plain_fp64_engine': {'achieved_gflops': plain_ach64, 'peak_gflops': p64.value,
                                            'frac': plain_ach64 / p64.value, 'bound': 'fp64 pipe',
                                            'peak_source': 'FP64 FMA-chain microbenchmark (ttals_measure_peaks)'}},
